@@ -1,0 +1,279 @@
+/*
+ * osgpu.h -- C ABI of the GB300 (sm_103a) propagation library.
+ *
+ * This is the drop-in boundary for the optics-studio hot path: every entry
+ * point is what the Rust FFI crate behind optics-core / optics-inverse
+ * binds.  Plain C: status-int returns, plain pointers and sizes, no
+ * exceptions cross the boundary.  Field samples are interleaved {re, im}
+ * doubles in the reference's row-major layout (index iy*nx + ix), i.e.
+ * `Vec<Complex64>::as_ptr()` of `optics_core::field::Field` viewed as
+ * `const double*` (reference src/field.rs:99-105).
+ *
+ * Threading: calls are serialised internally on one stream per device.
+ * Status codes map 1:1 onto the reference's error variants (see the
+ * OSGPU_E_* list); on failure osgpu_last_error() holds a message.
+ */
+#ifndef OSGPU_H
+#define OSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  OSGPU_OK = 0,
+  /* PropagationError / FresnelError / FraunhoferError / RayleighSommerfeldError
+   * (src/propagation/asm.rs:219-250, fresnel.rs:225-254, fraunhofer.rs:259-282,
+   * rayleigh_sommerfeld.rs:197-223) */
+  OSGPU_E_INVALID_DISTANCE = 1,
+  OSGPU_E_INVALID_WAVELENGTH = 2,
+  OSGPU_E_INVALID_MEDIUM = 3,
+  OSGPU_E_EMPTY_GRID = 4,
+  OSGPU_E_NON_FINITE_SAMPLE = 5,
+  OSGPU_E_ALIASING_RISK = 6,
+  OSGPU_E_REGIME_VIOLATION = 7,
+  /* OpticsError (src/element.rs:62-230) */
+  OSGPU_E_INVALID_APERTURE = 20,
+  OSGPU_E_OUTSIDE_FIELD = 21,
+  OSGPU_E_INVALID_AXIS = 22,
+  OSGPU_E_INVALID_FOCAL = 23,
+  OSGPU_E_INVALID_ORIENTATION = 24,
+  OSGPU_E_INVALID_PHASE = 25,
+  OSGPU_E_INVALID_GRID = 26,
+  OSGPU_E_INVALID_GRID_PITCH = 27,
+  OSGPU_E_INVALID_GRATING = 28,
+  /* InverseError (crates/optics-inverse/src/error.rs:11-85) */
+  OSGPU_E_WRONG_DIMENSION = 40,
+  OSGPU_E_NOT_FINITE = 41,
+  OSGPU_E_OUT_OF_BOUNDS = 42,
+  OSGPU_E_RENDER = 43,
+  /* library conditions with no reference counterpart */
+  OSGPU_E_UNSUPPORTED = 100, /* size beyond the kernels' shared-memory plan */
+  OSGPU_E_CUDA = 101,
+  OSGPU_E_BAD_ARGUMENT = 102,
+  OSGPU_E_NO_DEVICE = 103,
+  OSGPU_E_OUT_OF_MEMORY = 104
+};
+
+/* Arithmetic of a propagation.  F64 is the plain path (parity <= 1e-12 with
+ * the f64 reference); F32 computes the FFTs and multiplies in complex64 with
+ * FP64-derived phase tables. */
+enum { OSGPU_F64 = 0, OSGPU_F32 = 1 };
+
+/* Device buffer element type for the *_device entry points. */
+enum { OSGPU_C128 = 0, OSGPU_C64 = 1 };
+
+/* Grid of one BandField: Field dims/pitch + BandField wavelength
+ * (src/field.rs:99-105, 287-290). */
+typedef struct {
+  uint64_t nx, ny;
+  double dx, dy;
+  double lambda;
+} osgpu_grid;
+
+/* ------------------------------------------------------------ ASM engine */
+/* AsmConfig (src/propagation/asm.rs:101-137). */
+typedef struct {
+  double padding;
+  int32_t band_limited;
+  int32_t strict;
+  double max_padding;
+  double medium;
+} osgpu_asm_config;
+
+/* SamplingReport (src/propagation/asm.rs:145-179). */
+typedef struct {
+  double lambda, medium, z;
+  uint64_t nx, ny;
+  double dx, dy;
+  double requested_padding, used_padding;
+  uint64_t nx_pad, ny_pad;
+  double band_limit_fx, band_limit_fy;
+  double max_phase_step_x, max_phase_step_y;
+  int32_t nyquist_ok;
+} osgpu_asm_report;
+
+/* asm::sampling_report (asm.rs:418-420): diagnostics at cfg->padding. */
+int osgpu_asm_sampling_report(const osgpu_grid* g, double z, const osgpu_asm_config* cfg,
+                              osgpu_asm_report* out);
+
+/* asm::propagate (asm.rs:438-538).  in/out: host complex128, nx*ny samples
+ * (may alias).  `report` (optional) receives the report the propagation ran
+ * on (also filled on OSGPU_E_ALIASING_RISK).  z == 0 copies in to out. */
+int osgpu_asm_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                        const osgpu_asm_config* cfg, int32_t precision,
+                        osgpu_asm_report* report);
+
+/* Device-resident form: d_in/d_out are device buffers of `dtype`
+ * (OSGPU_C128 -> f64 engine, OSGPU_C64 -> f32 engine), `stream` a
+ * cudaStream_t (NULL: the library stream).  Asynchronous; the NonFinite
+ * check is folded into the first pass and reported by osgpu_sync_status. */
+int osgpu_asm_propagate_device(const void* d_in, void* d_out, int32_t dtype,
+                               const osgpu_grid* g, double z, const osgpu_asm_config* cfg,
+                               void* stream, osgpu_asm_report* report);
+
+/* -------------------------------------------------------- Fresnel engine */
+/* FresnelConfig (src/propagation/fresnel.rs:99-123). */
+typedef struct {
+  double padding;
+  int32_t strict;
+  double max_padding;
+} osgpu_fresnel_config;
+
+/* FresnelSamplingReport (fresnel.rs:130-170). */
+typedef struct {
+  double lambda, z;
+  uint64_t nx, ny;
+  double dx, dy;
+  double requested_padding, used_padding;
+  uint64_t nx_pad, ny_pad;
+  double max_phase_step_x, max_phase_step_y;
+  int32_t nyquist_ok;
+  double max_kernel_step_x, max_kernel_step_y;
+  int32_t kernel_nyquist_ok;
+  double max_phase_error_vs_asm;
+  int32_t paraxial_ok;
+} osgpu_fresnel_report;
+
+int osgpu_fresnel_sampling_report(const osgpu_grid* g, double z, const osgpu_fresnel_config* cfg,
+                                  osgpu_fresnel_report* out);
+/* fresnel::propagate (transfer-function form, fresnel.rs:430-509). */
+int osgpu_fresnel_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                            const osgpu_fresnel_config* cfg, int32_t precision,
+                            osgpu_fresnel_report* report);
+/* fresnel::propagate_convolution (fresnel.rs:531-590). */
+int osgpu_fresnel_propagate_convolution(const double* in, double* out, const osgpu_grid* g,
+                                        double z, const osgpu_fresnel_config* cfg,
+                                        int32_t precision, osgpu_fresnel_report* report);
+
+/* ----------------------------------------------------- Fraunhofer engine */
+/* FraunhoferConfig (src/propagation/fraunhofer.rs:118-171).  has_* select
+ * the Option<_> fields. */
+typedef struct {
+  int32_t strict;
+  double max_n_f;
+  int32_t has_source_pos;
+  double source_x, source_y;
+  int32_t has_aperture_extent;
+  double aperture_extent;
+} osgpu_fraunhofer_config;
+
+/* FraunhoferReport (fraunhofer.rs:177-213). */
+typedef struct {
+  double lambda, z;
+  uint64_t nx, ny;
+  double dx, dy;
+  double dx_out, dy_out;
+  double n_f_x, n_f_y;
+  double source_x, source_y;
+  double extent_used;
+  int32_t extent_is_aperture;
+  double quad_phase_error_rad;
+  double max_n_f;
+  int32_t regime_ok;
+} osgpu_fraunhofer_report;
+
+int osgpu_fraunhofer_regime_report(const osgpu_grid* g, double z,
+                                   const osgpu_fraunhofer_config* cfg,
+                                   osgpu_fraunhofer_report* out);
+/* fraunhofer::propagate (fraunhofer.rs:364-443).  The output lives on the
+ * far-field grid: same dims, pitch (report->dx_out, report->dy_out). */
+int osgpu_fraunhofer_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                               const osgpu_fraunhofer_config* cfg, int32_t precision,
+                               osgpu_fraunhofer_report* report);
+
+/* ------------------------------------------- Rayleigh-Sommerfeld engine */
+/* RayleighSommerfeldConfig (rayleigh_sommerfeld.rs:95-116). */
+typedef struct {
+  double padding;
+  int32_t strict;
+} osgpu_rs_config;
+
+/* RayleighSommerfeldSamplingReport (rayleigh_sommerfeld.rs:123-160). */
+typedef struct {
+  double lambda, z;
+  uint64_t nx, ny;
+  double dx, dy;
+  double padding;
+  uint64_t nx_pad, ny_pad;
+  double max_kernel_step_x, max_kernel_step_y;
+  int32_t kernel_nyquist_ok;
+  double max_phase_error_vs_fresnel;
+  int32_t paraxial_ok;
+} osgpu_rs_report;
+
+int osgpu_rs_sampling_report(const osgpu_grid* g, double z, const osgpu_rs_config* cfg,
+                             osgpu_rs_report* out);
+/* rayleigh_sommerfeld::propagate (rayleigh_sommerfeld.rs:384-442). */
+int osgpu_rs_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                       const osgpu_rs_config* cfg, int32_t precision, osgpu_rs_report* report);
+
+/* --------------------------------------------------------------- elements */
+enum {
+  OSGPU_EL_ELLIPTICAL_APERTURE = 1, /* element.rs:635-790 */
+  OSGPU_EL_RECTANGULAR_APERTURE = 2, /* element.rs:817-929 */
+  OSGPU_EL_THIN_LENS = 3,            /* element.rs:965-1154 */
+  OSGPU_EL_PHASE_MASK_SAMPLED = 4,   /* element.rs:1321-1484 */
+  OSGPU_EL_BLAZED_GRATING = 5        /* element.rs:1519-1703 */
+};
+/* ClearAperture (element.rs:384-408) */
+enum { OSGPU_STOP_FIELD = 0, OSGPU_STOP_CIRCLE = 1, OSGPU_STOP_ELLIPSE = 2, OSGPU_STOP_RECT = 3 };
+
+/* One thin element at a plane.  Host-side closures of the reference
+ * (ThinLens f(lambda), analytic PhaseMask) are evaluated by the caller:
+ * `focal` is f(band lambda); an analytic PhaseMask is passed as its lattice
+ * sampled on the field grid. */
+typedef struct {
+  int32_t kind;
+  int32_t stop;          /* clear aperture of lens / mask / grating */
+  double a, b;           /* semi-axes (ellipse), half-widths (rect) or stop extents */
+  double orientation;    /* radians (wrapped into [0, 2pi) as Angle::new) */
+  double center_x, center_y;
+  double focal;          /* thin lens: f(lambda) */
+  double period, depth;  /* blazed grating */
+  const double* lattice; /* sampled phase, row-major lny x lnx, host memory */
+  uint64_t lnx, lny;
+  double ldx, ldy;
+} osgpu_element;
+
+/* Element::apply of each element in order (pointwise transmission). */
+int osgpu_apply_elements(const double* in, double* out, const osgpu_grid* g,
+                         const osgpu_element* els, int32_t n_els, int32_t precision);
+
+/* --------------------------------------------------------------- beamline */
+/* One Beamline step (src/beamline.rs:52-99): elements applied at the plane,
+ * then a propagation of z_after through `medium` (skipped when 0). */
+typedef struct {
+  const osgpu_element* elements;
+  int32_t n_elements;
+  double z_after;
+  double medium;
+} osgpu_step;
+
+/* Beamline::trace with the ASM engine closure (observe.rs:195-210 form:
+ * AsmConfig with the step's medium).  Each plane costs one fused pass set:
+ * elements are applied inside the first FFT pass.  `reports` (optional)
+ * receives one report per step (zeroed for z_after == 0). */
+int osgpu_beamline_trace(const double* in, double* out, const osgpu_grid* g,
+                         const osgpu_step* steps, int32_t n_steps, const osgpu_asm_config* cfg,
+                         int32_t precision, osgpu_asm_report* reports);
+
+/* ---------------------------------------------------------------- runtime */
+int osgpu_init(int32_t device);
+/* Copies the last error message (NUL-terminated, truncated to len). */
+int osgpu_last_error(char* buf, size_t len);
+/* Waits for the library stream; returns a pending device-side status
+ * (e.g. OSGPU_E_NON_FINITE_SAMPLE from an asynchronous call). */
+int osgpu_sync_status(void);
+const char* osgpu_version(void);
+/* Number of kernel launches issued by the library since load. */
+uint64_t osgpu_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OSGPU_H */

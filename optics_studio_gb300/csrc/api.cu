@@ -1,0 +1,824 @@
+// C ABI (include/osgpu.h) over the sm_103a propagation kernels.
+//
+// Host control flow per call: reference-identical validation and sampling
+// analysis (host_analysis.cpp) -> device plan (axis plans, twiddle tables,
+// workspace) -> kernels on the library stream.  The sample finiteness scan
+// that the reference runs on the CPU before propagating
+// (src/propagation/asm.rs:458) is folded into the first pass on the GPU;
+// only on an error path that the reference would rank after it does the
+// host scan the input itself.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "../../include/osgpu.h"
+#include "host_analysis.h"
+#include "prop_kernels.cuh"
+
+using namespace osgpu;
+
+namespace {
+
+const double PI = 3.14159265358979323846;
+const size_t kMaxSmem = 232448;  // sm_103a opt-in shared memory per block
+
+thread_local char t_err[1024] = "";
+
+void set_err(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(t_err, sizeof(t_err), fmt, ap);
+  va_end(ap);
+}
+
+struct Context {
+  std::recursive_mutex mu;
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  int* d_status = nullptr;
+  std::map<std::pair<int, int>, void*> tw;  // (n, is_double) -> twiddle table
+};
+
+Context& ctx() {
+  static Context c;
+  return c;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  set_err("%s: %s", where, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? OSGPU_E_OUT_OF_MEMORY : OSGPU_E_CUDA;
+}
+
+#define CK(call)                                        \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+int ensure_init(Context& c) {
+  if (c.device >= 0) return OSGPU_OK;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    set_err("no CUDA device visible");
+    return OSGPU_E_NO_DEVICE;
+  }
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaSetDevice(dev));
+  CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  CK(cudaMalloc(&c.d_status, sizeof(int)));
+  CK(cudaMemset(c.d_status, 0, sizeof(int)));
+  cudaMemPool_t pool;
+  CK(cudaDeviceGetDefaultMemPool(&pool, dev));
+  uint64_t thr = UINT64_MAX;
+  CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  c.device = dev;
+  return OSGPU_OK;
+}
+
+// Stream-ordered device buffer (pool allocator; freed at scope exit).
+struct DBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), s(o.s) { o.p = nullptr; }
+  ~DBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  cudaError_t alloc(size_t bytes, cudaStream_t st) {
+    s = st;
+    return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+  }
+};
+
+int get_tw(Context& c, int n, int is_d, const void** out) {
+  auto key = std::make_pair(n, is_d);
+  auto it = c.tw.find(key);
+  if (it != c.tw.end()) {
+    *out = it->second;
+    return OSGPU_OK;
+  }
+  void* p = nullptr;
+  CK(cudaMalloc(&p, (size_t)(n > 0 ? n : 1) * (is_d ? 16 : 8)));
+  CK(launch_twiddles(p, n, is_d, c.stream));
+  c.tw[key] = p;
+  *out = p;
+  return OSGPU_OK;
+}
+
+// Device element list + uploaded lattices (kept alive for the call).
+struct Elements {
+  ElementList list;
+  std::vector<DBuf> lattices;
+};
+
+int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid& g,
+                   Elements& E) {
+  std::memset(&E.list, 0, sizeof(E.list));
+  if (n < 0 || (n > 0 && els == nullptr)) {
+    set_err("bad element list");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  if (n > kMaxElements) {
+    set_err("at most %d elements per plane", kMaxElements);
+    return OSGPU_E_UNSUPPORTED;
+  }
+  for (int i = 0; i < n; ++i) {
+    DevElement d;
+    char msg[512] = "";
+    int st = element_check(els[i], g, g.lambda, d, msg, sizeof(msg));
+    if (st) {
+      set_err("element %d: %s (status %d)", i, msg, st);
+      return st;
+    }
+    if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED) {
+      const size_t bytes = (size_t)els[i].lnx * els[i].lny * sizeof(double);
+      DBuf b;
+      CK(b.alloc(bytes, c.stream));
+      CK(cudaMemcpyAsync(b.p, els[i].lattice, bytes, cudaMemcpyHostToDevice, c.stream));
+      d.lat = reinterpret_cast<const double*>(b.p);
+      E.lattices.push_back(std::move(b));
+    }
+    E.list.el[E.list.count++] = d;
+  }
+  return OSGPU_OK;
+}
+
+bool host_all_finite(const double* p, size_t n_doubles) {
+  for (size_t i = 0; i < n_doubles; ++i)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+struct PropJob {
+  int engine;
+  osgpu_grid g;
+  double z;
+  uint64_t Px, Py;
+  double medium;
+  int band_limited;
+  double lim_x, lim_y;
+  ElementList els;
+  const void* d_in;
+  int in_c128;
+  void* d_out;
+  int out_c128;
+  float* d_int;
+  double* d_int64;
+  int conj_h;
+};
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <typename T>
+int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
+  const int is_d = sizeof(T) == 8;
+  const size_t es = is_d ? 16 : 8;
+  PropArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nx = (int)j.g.nx;
+  a.ny = (int)j.g.ny;
+  a.dx = j.g.dx;
+  a.dy = j.g.dy;
+  a.ax = make_axis(a.nx, (int)j.Px);
+  a.ay = make_axis(a.ny, (int)j.Py);
+  if (a.ax.nst < 0 || a.ay.nst < 0) {
+    set_err("padded length has too many prime factors");
+    return OSGPU_E_UNSUPPORTED;
+  }
+  if (smem_passA_bytes(a.ax, is_d, 1) > kMaxSmem || smem_passB_bytes(a.ay, is_d) > kMaxSmem ||
+      (2 * ((size_t)a.ax.m + 1) + (size_t)a.ax.n) * es > kMaxSmem) {
+    set_err("grid %dx%d (sub-FFT %d x %d) exceeds the shared-memory plan of this build",
+            a.nx, a.ny, a.ax.m, a.ay.m);
+    return OSGPU_E_UNSUPPORTED;
+  }
+  a.in = j.d_in;
+  a.in_c128 = j.in_c128;
+  a.out = j.d_out;
+  a.out_c128 = j.out_c128;
+  a.out_intensity = j.d_int;
+  a.out_intensity64 = j.d_int64;
+  a.els = j.els;
+  a.engine = j.engine;
+  a.status = c.d_status;
+  a.lam = j.g.lambda;
+  a.z = j.z;
+  a.scale = 1.0 / ((double)j.Px * (double)j.Py);
+  a.conj_h = j.conj_h;
+  int rc;
+  if ((rc = get_tw(c, a.ax.m, is_d, &a.tw_mx))) return rc;
+  if ((rc = get_tw(c, a.ay.m, is_d, &a.tw_my))) return rc;
+  a.tw_Px = a.tw_mx;
+  a.tw_Py = a.tw_my;
+  if (a.ax.r > 1 && (rc = get_tw(c, (int)j.Px, is_d, &a.tw_Px))) return rc;
+  if (a.ay.r > 1 && (rc = get_tw(c, (int)j.Py, is_d, &a.tw_Py))) return rc;
+
+  const size_t Px = j.Px, Py = j.Py, ny = j.g.ny;
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off += align256(bytes);
+    return o;
+  };
+  const size_t o_work = carve(Px * ny * es);
+  size_t o_fxv = 0, o_fyv = 0, o_Ex = 0, o_Ey = 0, o_cah = 0, o_cal = 0, o_sa = 0, o_bh = 0,
+         o_bl = 0, o_km = 0, o_hx = 0, o_hy = 0, o_tmp = 0, o_ks = 0;
+  const bool tf = (j.engine == ENG_ASM || j.engine == ENG_FRESNEL_TF);
+  if (tf) {
+    o_fxv = carve(Px * 8);
+    o_fyv = carve(Py * 8);
+    o_Ex = carve(Px * 8);
+    o_Ey = carve(Py * 8);
+    o_cah = carve(Px * 4);
+    o_cal = carve(Px * 4);
+    o_sa = carve(Px * 4);
+    o_bh = carve(Py * 4);
+    o_bl = carve(Py * 4);
+    o_km = carve(Px * 4);
+  } else if (j.engine == ENG_KSEP) {
+    o_hx = carve(Px * es);
+    o_hy = carve(Py * es);
+    o_tmp = carve(2 * (Px + Py) * 16);
+  } else if (j.engine == ENG_KSPEC) {
+    o_ks = carve(Px * Py * es);
+    o_tmp = carve((2 * Px * Py + Px + Py) * 16);
+  }
+  DBuf ws;
+  CK(ws.alloc(off, st));
+  char* base = reinterpret_cast<char*>(ws.p);
+  a.work = base + o_work;
+  if (tf) {
+    a.fxv = reinterpret_cast<const double*>(base + o_fxv);
+    a.fyv = reinterpret_cast<const double*>(base + o_fyv);
+    a.Ex = reinterpret_cast<const float2*>(base + o_Ex);
+    a.Ey = reinterpret_cast<const float2*>(base + o_Ey);
+    a.ca_hi = reinterpret_cast<const float*>(base + o_cah);
+    a.ca_lo = reinterpret_cast<const float*>(base + o_cal);
+    a.sa = reinterpret_cast<const float*>(base + o_sa);
+    a.b_hi = reinterpret_cast<const float*>(base + o_bh);
+    a.b_lo = reinterpret_cast<const float*>(base + o_bl);
+    a.kmax = reinterpret_cast<const int*>(base + o_km);
+    if (j.engine == ENG_ASM) {
+      const double lam_n = j.g.lambda / j.medium;
+      a.lam_n = lam_n;
+      a.kz = (2.0 * PI / lam_n) * j.z;
+      a.band_limited = j.band_limited;
+      a.lim_x = j.lim_x;
+      a.lim_y = j.lim_y;
+      a.h_mode = is_d ? 0
+                      : asm_f32_split_ok(j.g, j.z, j.medium, j.Px, j.Py, j.band_limited != 0,
+                                         j.lim_x, j.lim_y);
+    } else {
+      a.kz = (2.0 * PI / j.g.lambda) * j.z;
+      a.cfr = PI * j.g.lambda * j.z;
+      a.h_mode = is_d ? 0 : 1;
+    }
+    a.Kf = (float)a.kz;
+    CK(launch_asm_prep<T>(a, nullptr, st));
+  } else if (j.engine == ENG_KSEP) {
+    a.hx = base + o_hx;
+    a.hy = base + o_hy;
+    CK(launch_fresnel_ksep<T>(a, base + o_hx, base + o_hy, base + o_tmp, st));
+  } else if (j.engine == ENG_KSPEC) {
+    PropArgs b = a;
+    b.ax = make_axis((int)Px, (int)Px);
+    b.ay = make_axis((int)Py, (int)Py);
+    if (b.ax.nst < 0 || b.ay.nst < 0 || smem_passA_bytes(b.ax, 1, 1) > kMaxSmem ||
+        smem_passB_bytes(b.ay, 1) > kMaxSmem) {
+      set_err("kernel-spectrum build of %zux%zu exceeds the shared-memory plan", Px, Py);
+      return OSGPU_E_UNSUPPORTED;
+    }
+    CK(launch_rs_kspec<T>(b, base + o_ks, base + o_tmp, st));
+    a.kspec = base + o_ks;
+  }
+  CK(launch_passA<T>(a, st));
+  CK(launch_passB<T>(a, st));
+  CK(launch_passC<T>(a, st));
+  return OSGPU_OK;
+}
+
+int run_prop_dispatch(Context& c, const PropJob& j, int f32, cudaStream_t st) {
+  return f32 ? run_prop<float>(c, j, st) : run_prop<double>(c, j, st);
+}
+
+// Upload host complex128 input, run `fn(d_in, d_out)`, download output, map
+// the device status.
+template <typename F>
+int host_call(Context& c, const double* in, double* out, size_t n, F&& fn) {
+  cudaStream_t st = c.stream;
+  DBuf din, dout;
+  CK(din.alloc(n * 16, st));
+  CK(dout.alloc(n * 16, st));
+  CK(cudaMemcpyAsync(din.p, in, n * 16, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), st));
+  int rc = fn(din.p, dout.p);
+  if (rc) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  CK(cudaMemcpyAsync(out, dout.p, n * 16, cudaMemcpyDeviceToHost, st));
+  int status = 0;
+  CK(cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (status) {
+    set_err("field contains non-finite samples");
+    return OSGPU_E_NON_FINITE_SAMPLE;
+  }
+  return OSGPU_OK;
+}
+
+int check_grid(const osgpu_grid* g) {
+  if (!g) {
+    set_err("null grid");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  return OSGPU_OK;
+}
+
+int check_precision(int32_t p) {
+  if (p != OSGPU_F64 && p != OSGPU_F32) {
+    set_err("precision must be OSGPU_F64 or OSGPU_F32");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  return OSGPU_OK;
+}
+
+// Identity / error-path helper: scan host input first, as the reference does.
+int identity_copy(const double* in, double* out, size_t n) {
+  if (!host_all_finite(in, 2 * n)) {
+    set_err("field contains non-finite samples");
+    return OSGPU_E_NON_FINITE_SAMPLE;
+  }
+  if (out != in) std::memmove(out, in, n * 16);
+  return OSGPU_OK;
+}
+
+int scan_then(const double* in, size_t n, int code) {
+  if (in && !host_all_finite(in, 2 * n)) {
+    set_err("field contains non-finite samples");
+    return OSGPU_E_NON_FINITE_SAMPLE;
+  }
+  return code;
+}
+
+template <typename T>
+int run_fraun(Context& c, const osgpu_grid& g, double z, const osgpu_fraunhofer_report& r,
+              const ElementList& els, const void* d_in, int in_c128, void* d_out, int out_c128,
+              float* d_int, int adjoint, cudaStream_t st) {
+  const int is_d = sizeof(T) == 8;
+  const size_t es = is_d ? 16 : 8;
+  FraunArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nx = (int)g.nx;
+  a.ny = (int)g.ny;
+  a.dx = g.dx;
+  a.dy = g.dy;
+  a.ax = make_axis(a.nx, a.nx);
+  a.ay = make_axis(a.ny, a.ny);
+  if (a.ax.nst < 0 || a.ay.nst < 0 || 2 * ((size_t)a.ax.m + 1) * es > kMaxSmem ||
+      2 * (size_t)a.ay.m * es > kMaxSmem) {
+    set_err("Fraunhofer grid %dx%d exceeds the shared-memory plan", a.nx, a.ny);
+    return OSGPU_E_UNSUPPORTED;
+  }
+  int rc;
+  if ((rc = get_tw(c, a.ax.m, is_d, &a.tw_mx))) return rc;
+  if ((rc = get_tw(c, a.ay.m, is_d, &a.tw_my))) return rc;
+  DBuf ws;
+  CK(ws.alloc((size_t)a.nx * a.ny * es, st));
+  a.work = ws.p;
+  a.in = d_in;
+  a.in_c128 = in_c128;
+  a.out = d_out;
+  a.out_c128 = out_c128;
+  a.out_intensity = d_int;
+  a.els = els;
+  a.lam = g.lambda;
+  a.z = z;
+  a.k = 2.0 * PI / g.lambda;
+  a.xs = r.source_x;
+  a.ys = r.source_y;
+  a.f_s = r.source_x / (g.lambda * z);
+  a.g_s = r.source_y / (g.lambda * z);
+  a.dxo = r.dx_out;
+  a.dyo = r.dy_out;
+  a.cxc = ((double)g.nx - 1.0) / 2.0;
+  a.cyc = ((double)g.ny - 1.0) / 2.0;
+  // quad = e^{ikz} / (i lam z), num_complex division order (fraunhofer.rs:420)
+  const double kz = a.k * z;
+  const double cre = std::cos(kz), cim = std::sin(kz);
+  const double dre = 0.0 * z, dim = g.lambda * z;
+  const double ns = dre * dre + dim * dim;
+  a.quad_re = (cre * dre + cim * dim) / ns;
+  a.quad_im = (cim * dre - cre * dim) / ns;
+  a.adjoint = adjoint;
+  a.status = c.d_status;
+  CK(launch_fraunhofer<T>(a, st));
+  return OSGPU_OK;
+}
+
+void fill_asm_job(PropJob& j, const osgpu_grid& g, double z, const osgpu_asm_report& r,
+                  const osgpu_asm_config& cfg) {
+  std::memset(&j, 0, sizeof(j));
+  j.engine = ENG_ASM;
+  j.g = g;
+  j.z = z;
+  j.Px = r.nx_pad;
+  j.Py = r.ny_pad;
+  j.medium = cfg.medium;
+  j.band_limited = cfg.band_limited;
+  j.lim_x = r.band_limit_fx;
+  j.lim_y = r.band_limit_fy;
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+int osgpu_init(int32_t device) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if (c.device >= 0) return OSGPU_OK;
+  if (device >= 0) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  }
+  return ensure_init(c);
+}
+
+int osgpu_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return OSGPU_E_BAD_ARGUMENT;
+  std::snprintf(buf, len, "%s", t_err);
+  return OSGPU_OK;
+}
+
+const char* osgpu_version(void) { return "osgpu 0.1 (sm_103a)"; }
+
+uint64_t osgpu_launch_count(void) { return (uint64_t)launch_count(); }
+
+int osgpu_sync_status(void) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc = ensure_init(c);
+  if (rc) return rc;
+  int status = 0;
+  CK(cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream));
+  if (status) {
+    set_err("field contains non-finite samples");
+    return OSGPU_E_NON_FINITE_SAMPLE;
+  }
+  return OSGPU_OK;
+}
+
+// ------------------------------------------------------------------ ASM
+
+int osgpu_asm_sampling_report(const osgpu_grid* g, double z, const osgpu_asm_config* cfg,
+                              osgpu_asm_report* out) {
+  if (!g || !cfg || !out) return OSGPU_E_BAD_ARGUMENT;
+  asm_analyze(*g, z, *cfg, cfg->padding, *out);
+  return OSGPU_OK;
+}
+
+int osgpu_asm_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                        const osgpu_asm_config* cfg, int32_t precision,
+                        osgpu_asm_report* report) {
+  int rc;
+  if ((rc = check_grid(g)) || (rc = check_precision(precision))) return rc;
+  if (!cfg || !in || !out) return OSGPU_E_BAD_ARGUMENT;
+  osgpu_asm_report r;
+  rc = asm_resolve(*g, z, *cfg, r);
+  if (report) *report = r;
+  const size_t n = g->nx * g->ny;
+  if (rc == -1) return identity_copy(in, out, n);
+  if (rc == OSGPU_E_ALIASING_RISK) {
+    set_err("sampling criteria not met (ASM transfer function undersampled)");
+    return scan_then(in, n, rc);
+  }
+  if (rc) {
+    set_err("invalid ASM propagation arguments (status %d)", rc);
+    return rc;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  return host_call(c, in, out, n, [&](const void* din, void* dout) {
+    PropJob j;
+    fill_asm_job(j, *g, z, r, *cfg);
+    j.d_in = din;
+    j.in_c128 = 1;
+    j.d_out = dout;
+    j.out_c128 = 1;
+    return run_prop_dispatch(c, j, precision == OSGPU_F32, c.stream);
+  });
+}
+
+int osgpu_asm_propagate_device(const void* d_in, void* d_out, int32_t dtype,
+                               const osgpu_grid* g, double z, const osgpu_asm_config* cfg,
+                               void* stream, osgpu_asm_report* report) {
+  int rc;
+  if ((rc = check_grid(g))) return rc;
+  if (!cfg || !d_in || !d_out || (dtype != OSGPU_C128 && dtype != OSGPU_C64))
+    return OSGPU_E_BAD_ARGUMENT;
+  osgpu_asm_report r;
+  rc = asm_resolve(*g, z, *cfg, r);
+  if (report) *report = r;
+  if (rc > 0) return rc;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int e0 = ensure_init(c);
+  if (e0) return e0;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const size_t es = dtype == OSGPU_C128 ? 16 : 8;
+  if (rc == -1) {
+    if (d_out != d_in) CK(cudaMemcpyAsync(d_out, d_in, g->nx * g->ny * es, cudaMemcpyDeviceToDevice, st));
+    return OSGPU_OK;
+  }
+  PropJob j;
+  fill_asm_job(j, *g, z, r, *cfg);
+  j.d_in = d_in;
+  j.in_c128 = dtype == OSGPU_C128;
+  j.d_out = d_out;
+  j.out_c128 = dtype == OSGPU_C128;
+  return run_prop_dispatch(c, j, dtype == OSGPU_C64, st);
+}
+
+// -------------------------------------------------------------- Fresnel
+
+int osgpu_fresnel_sampling_report(const osgpu_grid* g, double z, const osgpu_fresnel_config* cfg,
+                                  osgpu_fresnel_report* out) {
+  if (!g || !cfg || !out) return OSGPU_E_BAD_ARGUMENT;
+  fresnel_analyze(*g, z, *cfg, cfg->padding, *out);
+  return OSGPU_OK;
+}
+
+static int fresnel_common(const double* in, double* out, const osgpu_grid* g, double z,
+                          const osgpu_fresnel_config* cfg, int32_t precision,
+                          osgpu_fresnel_report* report, int conv) {
+  int rc;
+  if ((rc = check_grid(g)) || (rc = check_precision(precision))) return rc;
+  if (!cfg || !in || !out) return OSGPU_E_BAD_ARGUMENT;
+  osgpu_fresnel_report r;
+  rc = conv ? fresnel_resolve_conv(*g, z, *cfg, r) : fresnel_resolve_tf(*g, z, *cfg, r);
+  if (report) *report = r;
+  const size_t n = g->nx * g->ny;
+  if (rc == -1) return identity_copy(in, out, n);
+  if (rc == OSGPU_E_ALIASING_RISK) {
+    set_err("sampling criteria not met (Fresnel %s)", conv ? "kernel" : "transfer function");
+    return scan_then(in, n, rc);
+  }
+  if (rc) {
+    set_err("invalid Fresnel propagation arguments (status %d)", rc);
+    return rc;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  return host_call(c, in, out, n, [&](const void* din, void* dout) {
+    PropJob j;
+    std::memset(&j, 0, sizeof(j));
+    j.engine = conv ? ENG_KSEP : ENG_FRESNEL_TF;
+    j.g = *g;
+    j.z = z;
+    j.Px = r.nx_pad;
+    j.Py = r.ny_pad;
+    j.medium = 1.0;
+    j.d_in = din;
+    j.in_c128 = 1;
+    j.d_out = dout;
+    j.out_c128 = 1;
+    return run_prop_dispatch(c, j, precision == OSGPU_F32, c.stream);
+  });
+}
+
+int osgpu_fresnel_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                            const osgpu_fresnel_config* cfg, int32_t precision,
+                            osgpu_fresnel_report* report) {
+  return fresnel_common(in, out, g, z, cfg, precision, report, 0);
+}
+
+int osgpu_fresnel_propagate_convolution(const double* in, double* out, const osgpu_grid* g,
+                                        double z, const osgpu_fresnel_config* cfg,
+                                        int32_t precision, osgpu_fresnel_report* report) {
+  return fresnel_common(in, out, g, z, cfg, precision, report, 1);
+}
+
+// ----------------------------------------------------------- Fraunhofer
+
+int osgpu_fraunhofer_regime_report(const osgpu_grid* g, double z,
+                                   const osgpu_fraunhofer_config* cfg,
+                                   osgpu_fraunhofer_report* out) {
+  if (!g || !cfg || !out) return OSGPU_E_BAD_ARGUMENT;
+  fraunhofer_report(*g, z, *cfg, *out);
+  return OSGPU_OK;
+}
+
+int osgpu_fraunhofer_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                               const osgpu_fraunhofer_config* cfg, int32_t precision,
+                               osgpu_fraunhofer_report* report) {
+  int rc;
+  if ((rc = check_grid(g)) || (rc = check_precision(precision))) return rc;
+  if (!cfg || !in || !out) return OSGPU_E_BAD_ARGUMENT;
+  osgpu_fraunhofer_report r;
+  rc = fraunhofer_resolve(*g, z, *cfg, r);
+  if (report) *report = r;
+  const size_t n = g->nx * g->ny;
+  if (rc == OSGPU_E_REGIME_VIOLATION) {
+    set_err("far-field regime criteria not met");
+    return scan_then(in, n, rc);
+  }
+  if (rc) {
+    set_err("invalid Fraunhofer propagation arguments (status %d)", rc);
+    return rc;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  return host_call(c, in, out, n, [&](const void* din, void* dout) {
+    ElementList none;
+    std::memset(&none, 0, sizeof(none));
+    return precision == OSGPU_F32
+               ? run_fraun<float>(c, *g, z, r, none, din, 1, dout, 1, nullptr, 0, c.stream)
+               : run_fraun<double>(c, *g, z, r, none, din, 1, dout, 1, nullptr, 0, c.stream);
+  });
+}
+
+// ----------------------------------------------------- Rayleigh-Sommerfeld
+
+int osgpu_rs_sampling_report(const osgpu_grid* g, double z, const osgpu_rs_config* cfg,
+                             osgpu_rs_report* out) {
+  if (!g || !cfg || !out) return OSGPU_E_BAD_ARGUMENT;
+  rs_analyze(*g, z, cfg->padding, *out);
+  return OSGPU_OK;
+}
+
+int osgpu_rs_propagate(const double* in, double* out, const osgpu_grid* g, double z,
+                       const osgpu_rs_config* cfg, int32_t precision, osgpu_rs_report* report) {
+  int rc;
+  if ((rc = check_grid(g)) || (rc = check_precision(precision))) return rc;
+  if (!cfg || !in || !out) return OSGPU_E_BAD_ARGUMENT;
+  osgpu_rs_report r;
+  rc = rs_resolve(*g, z, *cfg, r);
+  if (report) *report = r;
+  const size_t n = g->nx * g->ny;
+  if (rc == OSGPU_E_ALIASING_RISK) {
+    set_err("sampling criteria not met (RS kernel undersampled)");
+    return scan_then(in, n, rc);
+  }
+  if (rc) {
+    set_err("invalid RS propagation arguments (status %d)", rc);
+    return rc;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  return host_call(c, in, out, n, [&](const void* din, void* dout) {
+    PropJob j;
+    std::memset(&j, 0, sizeof(j));
+    j.engine = ENG_KSPEC;
+    j.g = *g;
+    j.z = z;
+    j.Px = r.nx_pad;
+    j.Py = r.ny_pad;
+    j.medium = 1.0;
+    j.d_in = din;
+    j.in_c128 = 1;
+    j.d_out = dout;
+    j.out_c128 = 1;
+    return run_prop_dispatch(c, j, precision == OSGPU_F32, c.stream);
+  });
+}
+
+// ------------------------------------------------------------- elements
+
+int osgpu_apply_elements(const double* in, double* out, const osgpu_grid* g,
+                         const osgpu_element* els, int32_t n_els, int32_t precision) {
+  int rc;
+  if ((rc = check_grid(g)) || (rc = check_precision(precision))) return rc;
+  if (!in || !out) return OSGPU_E_BAD_ARGUMENT;
+  if (g->nx == 0 || g->ny == 0) return OSGPU_E_EMPTY_GRID;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  Elements E;
+  if ((rc = build_elements(c, els, n_els, *g, E))) return rc;
+  const size_t n = g->nx * g->ny;
+  return host_call(c, in, out, n, [&](const void* din, void* dout) {
+    cudaError_t e = precision == OSGPU_F32
+                        ? launch_apply_elements<float>(din, 1, dout, 1, E.list, (int)g->nx,
+                                                       (int)g->ny, g->dx, g->dy, nullptr, c.stream)
+                        : launch_apply_elements<double>(din, 1, dout, 1, E.list, (int)g->nx,
+                                                        (int)g->ny, g->dx, g->dy, nullptr,
+                                                        c.stream);
+    return e == cudaSuccess ? OSGPU_OK : cuda_fail(e, "apply_elements");
+  });
+}
+
+// ------------------------------------------------------------- beamline
+
+int osgpu_beamline_trace(const double* in, double* out, const osgpu_grid* g,
+                         const osgpu_step* steps, int32_t n_steps, const osgpu_asm_config* cfg,
+                         int32_t precision, osgpu_asm_report* reports) {
+  int rc;
+  if ((rc = check_grid(g)) || (rc = check_precision(precision))) return rc;
+  if (!cfg || !in || !out || n_steps < 0 || (n_steps > 0 && !steps)) return OSGPU_E_BAD_ARGUMENT;
+  const size_t n = g->nx * g->ny;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  // Validate every step in trace order (beamline.rs:109-127): element
+  // errors, then the engine's; the first failure wins.
+  std::vector<Elements> E(n_steps > 0 ? n_steps : 1);
+  std::vector<osgpu_asm_report> R(n_steps > 0 ? n_steps : 1);
+  int first_prop = -1;
+  for (int s = 0; s < n_steps; ++s) {
+    if ((rc = build_elements(c, steps[s].elements, steps[s].n_elements, *g, E[s]))) {
+      if (first_prop >= 0 && first_prop < s) rc = scan_then(in, n, rc);
+      return rc;
+    }
+    std::memset(&R[s], 0, sizeof(R[s]));
+    if (steps[s].z_after != 0.0) {
+      osgpu_asm_config sc = *cfg;
+      sc.medium = steps[s].medium;
+      rc = asm_resolve(*g, steps[s].z_after, sc, R[s]);
+      if (rc > 0) {
+        if (rc == OSGPU_E_ALIASING_RISK || (first_prop >= 0 && first_prop < s))
+          rc = scan_then(in, n, rc);
+        set_err("beamline step %d: propagation failed (status %d)", s, rc);
+        if (reports) reports[s] = R[s];
+        return rc;
+      }
+      if (first_prop < 0) first_prop = s;
+    }
+    if (reports) reports[s] = R[s];
+  }
+  return host_call(c, in, out, n, [&](const void* din, void* dout) -> int {
+    const int f32 = precision == OSGPU_F32;
+    // Working buffer in the engine precision; the first pass reads din.
+    ElementList pending;
+    std::memset(&pending, 0, sizeof(pending));
+    const void* src = din;
+    int src_c128 = 1;
+    DBuf cur;
+    const size_t es = f32 ? 8 : 16;
+    cudaError_t e = cur.alloc(n * es, c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "alloc");
+    for (int s = 0; s < n_steps; ++s) {
+      for (int q = 0; q < E[s].list.count; ++q) {
+        if (pending.count == kMaxElements) {
+          e = f32 ? launch_apply_elements<float>(src, src_c128, cur.p, 0, pending, (int)g->nx,
+                                                 (int)g->ny, g->dx, g->dy, nullptr, c.stream)
+                  : launch_apply_elements<double>(src, src_c128, cur.p, 1, pending, (int)g->nx,
+                                                  (int)g->ny, g->dx, g->dy, nullptr, c.stream);
+          if (e != cudaSuccess) return cuda_fail(e, "apply_elements");
+          src = cur.p;
+          src_c128 = !f32;
+          pending.count = 0;
+        }
+        pending.el[pending.count++] = E[s].list.el[q];
+      }
+      if (steps[s].z_after != 0.0) {
+        osgpu_asm_config sc = *cfg;
+        sc.medium = steps[s].medium;
+        PropJob j;
+        fill_asm_job(j, *g, steps[s].z_after, R[s], sc);
+        j.els = pending;
+        j.d_in = src;
+        j.in_c128 = src_c128;
+        j.d_out = cur.p;
+        j.out_c128 = !f32;
+        int r2 = run_prop_dispatch(c, j, f32, c.stream);
+        if (r2) return r2;
+        src = cur.p;
+        src_c128 = !f32;
+        pending.count = 0;
+      }
+    }
+    if (pending.count > 0 || src == din) {
+      e = f32 ? launch_apply_elements<float>(src, src_c128, dout, 1, pending, (int)g->nx,
+                                             (int)g->ny, g->dx, g->dy, nullptr, c.stream)
+              : launch_apply_elements<double>(src, src_c128, dout, 1, pending, (int)g->nx,
+                                              (int)g->ny, g->dx, g->dy, nullptr, c.stream);
+      if (e != cudaSuccess) return cuda_fail(e, "apply_elements");
+    } else {
+      e = f32 ? launch_apply_elements<float>(src, 0, dout, 1, pending, (int)g->nx, (int)g->ny,
+                                             g->dx, g->dy, nullptr, c.stream)
+              : cudaMemcpyAsync(dout, src, n * 16, cudaMemcpyDeviceToDevice, c.stream);
+      if (e != cudaSuccess) return cuda_fail(e, "copy out");
+    }
+    return OSGPU_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// Plain structs shared by the host planner and the sm_103a kernels.
+//
+// Layouts in HBM:
+//   field      row-major ny x nx complex (index iy*nx + ix), interleaved
+//              {re, im}; complex128 for the f64 engine, complex64 for f32.
+//   spectrum   "column-major" scratch Px x ny: element (kx, iy) at
+//              kx*ld + iy, so a spectral column is contiguous (pass B reads
+//              and writes it with unit stride).
+#pragma once
+#include <cstdint>
+#include <vector_types.h>
+
+namespace osgpu {
+
+constexpr int kMaxStages = 20;
+constexpr int kMaxElements = 8;
+
+// One axis of a padded transform: support n (field samples), padded
+// length P = r*m, sub-FFT length m (m | P, m >= n), Stockham radices of m.
+struct AxisPlan {
+  int n;
+  int P;
+  int m;
+  int r;
+  int nst;
+  int radix[kMaxStages];
+};
+
+enum EngineKind : int {
+  ENG_ASM = 0,          // exact angular spectrum (on-the-fly H)
+  ENG_FRESNEL_TF = 1,   // Fresnel transfer function (on-the-fly H)
+  ENG_KSPEC = 2,        // precomputed kernel spectrum (Fresnel conv, RS)
+  ENG_KSEP = 3,         // separable kernel spectrum Hx[kx]*Hy[ky] (Fresnel conv)
+  ENG_IDENTITY = 4,     // spectrum untouched (used to build 2D FFTs)
+};
+
+enum ElementKind : int {
+  EL_ELLIPSE = 1,   // EllipticalAperture (element predicate b2 x^2 + a2 y^2 > a2 b2)
+  EL_RECT = 2,      // RectangularAperture
+  EL_LENS = 3,      // ThinLens with a clear-aperture stop
+  EL_PHASE = 4,     // PhaseMask::sampled (bilinear lattice) with a stop
+  EL_GRATING = 5,   // BlazedGrating with a stop
+};
+
+enum StopKind : int { STOP_FIELD = 0, STOP_CIRCLE = 1, STOP_ELLIPSE = 2, STOP_RECT = 3 };
+
+// Device-side element: everything in FP64 plus optional f32 fast tables.
+struct DevElement {
+  int kind;
+  int stop;        // stop of lens / mask / grating
+  double a, b;     // semi-axes, half-widths or stop half-extents (m)
+  double psi, cpsi, spsi;
+  double cx, cy;
+  double k;        // 2 pi / lambda (lens)
+  double f;        // focal length at this band (lens)
+  double inv_period, depth;  // grating
+  const double* lat;         // sampled phase lattice (device, row-major lny x lnx)
+  int lnx, lny;
+  double ldx, ldy;
+  int lat_is_grid;           // lattice == field grid, psi == 0, center == 0
+  // f32 fast tables (null when the element needs the per-sample FP64 path)
+  const int2* span;          // per row inclusive [lo, hi] of the transmitting set
+  const float2* tabx;        // per column factor (lens / grating)
+  const float2* taby;        // per row factor (lens)
+  const float* latf;         // f32 copy of the lattice when lat_is_grid
+};
+
+struct ElementList {
+  int count;
+  int fast;  // 1: every element has f32 tables (f32 engine only)
+  DevElement el[kMaxElements];
+};
+
+}  // namespace osgpu

@@ -1,0 +1,951 @@
+// Propagation passes for sm_103a: table prep, pass A (row FFTs + element
+// fusion), pass B (column FFT -> transfer function -> inverse column FFT),
+// pass C (inverse row FFTs + crop), plus kernel-spectrum builds and the
+// two-pass Fraunhofer transform.
+//
+// Pruned padded transform along one axis (support n, padded P = r*m):
+//   X[r q + s] = DFT_m( x[j] W_P^{s j} )[q]          (j < n, zero to m)
+//   y[j]       = sum_s W_P^{-s j} IDFT_m( Y[r q + s] )[j]   (j < n)
+// The centred embed offset of the reference cancels against the centred
+// crop (a circular shift of the input by o followed by a shift of the
+// output by -o leaves a circular convolution unchanged), so the support
+// starts at index 0 here.
+#include <cstdio>
+#include "prop_kernels.cuh"
+#include "fft_smem.cuh"
+
+namespace osgpu {
+
+constexpr int kThreads = 256;
+constexpr size_t kSmemBudgetRows = 100 * 1024;
+
+static unsigned long long g_launches = 0;
+unsigned long long launch_count() { return g_launches; }
+#define COUNT_LAUNCH() (++g_launches)
+
+__device__ __forceinline__ bool nonfinite2(double a, double b) { return !isfinite(a) || !isfinite(b); }
+
+// ---------------------------------------------------------------- helpers
+
+template <typename T>
+__device__ __forceinline__ cx<T> load_in(const void* p, int in_c128, size_t idx) {
+  if (in_c128) {
+    double2 v = reinterpret_cast<const double2*>(p)[idx];
+    return mkc<cx<T>>((T)v.x, (T)v.y);
+  }
+  float2 v = reinterpret_cast<const float2*>(p)[idx];
+  return mkc<cx<T>>((T)v.x, (T)v.y);
+}
+
+template <typename T>
+__device__ __forceinline__ void store_out(void* p, int out_c128, size_t idx, cx<T> v) {
+  if (out_c128) {
+    double2 w; w.x = (double)v.x; w.y = (double)v.y;
+    reinterpret_cast<double2*>(p)[idx] = w;
+  } else {
+    float2 w; w.x = (float)v.x; w.y = (float)v.y;
+    reinterpret_cast<float2*>(p)[idx] = w;
+  }
+}
+
+// fftfreq value k/(n d) with negative wrap (reference propagation/fft.rs:115-126).
+__device__ __forceinline__ double fftfreq_d(int k, int n, double d) {
+  double kk = (k <= (n - 1) / 2) ? (double)k : (double)k - (double)n;
+  return __ddiv_rn(kk, __dmul_rn((double)n, d));
+}
+
+// Origin-centred coordinate (i - (n-1)/2) d (reference field.rs:216-221).
+__device__ __forceinline__ double coord_d(int i, int n, double d) {
+  return __dmul_rn(__dsub_rn((double)i, ((double)n - 1.0) / 2.0), d);
+}
+
+// Element-frame rotation (reference element.rs:557-560), no FMA contraction.
+__device__ __forceinline__ void to_frame(double x, double y, double c, double s, double& fx,
+                                         double& fy) {
+  fx = __dadd_rn(__dmul_rn(c, x), __dmul_rn(s, y));
+  fy = __dadd_rn(__dmul_rn(-s, x), __dmul_rn(c, y));
+}
+
+// ClearAperture::contains (reference element.rs:476-488).
+__device__ __forceinline__ bool stop_contains(int kind, double a, double b, double x, double y) {
+  switch (kind) {
+    case STOP_CIRCLE:
+      return __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)) <= __dmul_rn(a, a);
+    case STOP_ELLIPSE: {
+      double a2 = __dmul_rn(a, a), b2 = __dmul_rn(b, b);
+      return __dadd_rn(__dmul_rn(__dmul_rn(b2, x), x), __dmul_rn(__dmul_rn(a2, y), y)) <=
+             __dmul_rn(a2, b2);
+    }
+    case STOP_RECT:
+      return fabs(x) <= a && fabs(y) <= b;
+    default:
+      return true;
+  }
+}
+
+// SampledPhase::at, bilinear, zero outside the span (reference element.rs:1189-1207).
+__device__ double lattice_at(const DevElement& e, double x, double y) {
+  double gx = __dadd_rn(__ddiv_rn(x, e.ldx), ((double)e.lnx - 1.0) / 2.0);
+  double gy = __dadd_rn(__ddiv_rn(y, e.ldy), ((double)e.lny - 1.0) / 2.0);
+  double lx = (double)e.lnx - 1.0, ly = (double)e.lny - 1.0;
+  if (gx < 0.0 || gx > lx || gy < 0.0 || gy > ly) return 0.0;
+  int i0 = (int)floor(gx), j0 = (int)floor(gy);
+  int i1 = min(i0 + 1, e.lnx - 1), j1 = min(j0 + 1, e.lny - 1);
+  double tx = __dsub_rn(gx, (double)i0), ty = __dsub_rn(gy, (double)j0);
+  const double* v = e.lat;
+  double v00 = v[(size_t)j0 * e.lnx + i0], v10 = v[(size_t)j0 * e.lnx + i1];
+  double v01 = v[(size_t)j1 * e.lnx + i0], v11 = v[(size_t)j1 * e.lnx + i1];
+  double A = __dadd_rn(v00, __dmul_rn(__dsub_rn(v10, v00), tx));
+  double B = __dadd_rn(v01, __dmul_rn(__dsub_rn(v11, v01), tx));
+  return __dadd_rn(A, __dmul_rn(__dsub_rn(B, A), ty));
+}
+
+__device__ __forceinline__ void cmul_phase(double& re, double& im, double phi) {
+  double s, c;
+  sincos(phi, &s, &c);
+  double r2 = re * c - im * s;
+  double i2 = re * s + im * c;
+  re = r2;
+  im = i2;
+}
+
+// Per-sample FP64 evaluation of every element at sample (ix, iy), in the
+// reference's operation order (element.rs:754-790, 900-929, 1115-1154,
+// 1443-1484, 1668-1703).  Elements apply in list order.
+__device__ void apply_elements_exact(const ElementList& L, int ix, int iy, int nx, int ny,
+                                     double dx, double dy, double& re, double& im) {
+  const double x = coord_d(ix, nx, dx);
+  const double y = coord_d(iy, ny, dy);
+  for (int q = 0; q < L.count; ++q) {
+    const DevElement& e = L.el[q];
+    const double xr = __dsub_rn(x, e.cx), yr = __dsub_rn(y, e.cy);
+    double fx, fy;
+    to_frame(xr, yr, e.cpsi, e.spsi, fx, fy);
+    switch (e.kind) {
+      case EL_ELLIPSE: {
+        double a2 = __dmul_rn(e.a, e.a), b2 = __dmul_rn(e.b, e.b);
+        double lhs = __dadd_rn(__dmul_rn(__dmul_rn(b2, fx), fx), __dmul_rn(__dmul_rn(a2, fy), fy));
+        if (lhs > __dmul_rn(a2, b2)) { re = 0.0; im = 0.0; }
+        break;
+      }
+      case EL_RECT:
+        if (fabs(fx) > e.a || fabs(fy) > e.b) { re = 0.0; im = 0.0; }
+        break;
+      case EL_LENS: {
+        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+        double r2 = __dadd_rn(__dmul_rn(xr, xr), __dmul_rn(yr, yr));
+        double phase = __ddiv_rn(__dmul_rn(-e.k, r2), __dmul_rn(2.0, e.f));
+        cmul_phase(re, im, phase);
+        break;
+      }
+      case EL_PHASE: {
+        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+        cmul_phase(re, im, lattice_at(e, fx, fy));
+        break;
+      }
+      case EL_GRATING: {
+        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+        double u = __dmul_rn(fx, e.inv_period);
+        double phi = __dmul_rn(e.depth, __dsub_rn(u, floor(u)));
+        cmul_phase(re, im, phi);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ cx<T> apply_elements(const ElementList& L, int ix, int iy, int nx,
+                                                int ny, double dx, double dy, cx<T> v) {
+  double re = (double)v.x, im = (double)v.y;
+  apply_elements_exact(L, ix, iy, nx, ny, dx, dy, re, im);
+  return mkc<cx<T>>((T)re, (T)im);
+}
+
+// ----------------------------------------------------------------- tables
+
+__global__ void k_twiddles(void* dst, int n, int is_double) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  // W_n^k = e^{-2 pi i k / n}; sincospi on the exact ratio 2k/n.
+  double s, c;
+  sincospi(2.0 * (double)k / (double)n, &s, &c);
+  if (is_double) {
+    reinterpret_cast<double2*>(dst)[k] = make_double2(c, -s);
+  } else {
+    reinterpret_cast<float2*>(dst)[k] = make_float2((float)c, (float)-s);
+  }
+}
+
+cudaError_t launch_twiddles(void* dst, int n, int is_double, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  COUNT_LAUNCH();
+  k_twiddles<<<(n + 255) / 256, 256, 0, st>>>(dst, n, is_double);
+  return cudaGetLastError();
+}
+
+// Per-axis tables for the transfer function.  fxv/fyv always; the f32
+// split tables when h_mode == 1:
+//   ASM: phi = K sqrt(1-s), s = a + b, a = (lam_n fx)^2, b = (lam_n fy)^2
+//        = K + [-K a/2 - K a^2/8] + [-K b/2 - K b^2/8] + [-K a b/4] - K tau(s)
+//        with tau(s) = s^3 (3+q) / (8 (1+q)^3), q = sqrt(1-s).
+//   The bracketed separable terms and e^{iK} are evaluated in FP64 into Ex/Ey;
+//   the cross term -K a b/4 runs in double-float; tau in f32.
+//   kmax[kx] is the largest |k_y| whose bin the reference keeps (evanescent
+//   and band-limit tests evaluated in FP64 exactly as asm.rs:505-522).
+//   Fresnel TF: Ex = e^{i (kz - c fx^2)} * scale, Ey = e^{-i c fy^2}.
+__global__ void k_axis_prep(PropArgs a, double* fxv, double* fyv, float2* Ex, float2* Ey,
+                            float* ca_hi, float* ca_lo, float* sa, float* b_hi, float* b_lo,
+                            int* kmax) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Px = a.ax.P, Py = a.ay.P;
+  const double K = a.kz;
+  if (i < Px) {
+    const double fx = fftfreq_d(i, Px, a.dx);
+    fxv[i] = fx;
+    if (a.h_mode == 1) {
+      if (a.engine == ENG_ASM) {
+        const double al = a.lam_n * fx;
+        const double aa = al * al;
+        const double phx = K - K * aa * 0.5 - K * aa * aa * 0.125;
+        double s, c;
+        sincos(phx, &s, &c);
+        Ex[i] = make_float2((float)(c * a.scale), (float)(s * a.scale));
+        const double ca = -K * aa * 0.25;
+        const float h = (float)ca;
+        ca_hi[i] = h;
+        ca_lo[i] = (float)(ca - (double)h);
+        sa[i] = (float)aa;
+        // kmax: exact reference predicate, monotone in |k_y|.
+        int km = -1;
+        if (!(a.band_limited && fabs(fx) > a.lim_x)) {
+          const double axx = __dmul_rn(a.lam_n, fx);
+          const double t1 = __dsub_rn(1.0, __dmul_rn(axx, axx));
+          auto ok = [&](int kk) {
+            double fy = __ddiv_rn((double)kk, __dmul_rn((double)Py, a.dy));
+            if (a.band_limited && fabs(fy) > a.lim_y) return false;
+            double ayy = __dmul_rn(a.lam_n, fy);
+            return !(__dsub_rn(t1, __dmul_rn(ayy, ayy)) < 0.0);
+          };
+          if (ok(0)) {
+            int lo = 0, hi = Py / 2;
+            if (ok(hi)) {
+              lo = hi;
+            } else {
+              while (hi - lo > 1) {
+                int mid = (lo + hi) / 2;
+                if (ok(mid)) lo = mid; else hi = mid;
+              }
+            }
+            km = lo;
+          }
+        }
+        kmax[i] = km;
+      } else if (a.engine == ENG_FRESNEL_TF) {
+        const double ph = a.kz - a.cfr * (fx * fx);
+        double s, c;
+        sincos(ph, &s, &c);
+        Ex[i] = make_float2((float)(c * a.scale), (float)(s * a.scale));
+      }
+    }
+  }
+  if (i < Py) {
+    const double fy = fftfreq_d(i, Py, a.dy);
+    fyv[i] = fy;
+    if (a.h_mode == 1) {
+      if (a.engine == ENG_ASM) {
+        const double bl = a.lam_n * fy;
+        const double bb = bl * bl;
+        const double phy = -K * bb * 0.5 - K * bb * bb * 0.125;
+        double s, c;
+        sincos(phy, &s, &c);
+        Ey[i] = make_float2((float)c, (float)s);
+        const float h = (float)bb;
+        b_hi[i] = h;
+        b_lo[i] = (float)(bb - (double)h);
+      } else if (a.engine == ENG_FRESNEL_TF) {
+        const double ph = -a.cfr * (fy * fy);
+        double s, c;
+        sincos(ph, &s, &c);
+        Ey[i] = make_float2((float)c, (float)s);
+      }
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_asm_prep(const PropArgs& a, void* tables, cudaStream_t st) {
+  (void)tables;
+  const int n = max(a.ax.P, a.ay.P);
+  COUNT_LAUNCH();
+  k_axis_prep<<<(n + 127) / 128, 128, 0, st>>>(
+      a, const_cast<double*>(a.fxv), const_cast<double*>(a.fyv), const_cast<float2*>(a.Ex),
+      const_cast<float2*>(a.Ey), const_cast<float*>(a.ca_hi), const_cast<float*>(a.ca_lo),
+      const_cast<float*>(a.sa), const_cast<float*>(a.b_hi), const_cast<float*>(a.b_lo),
+      const_cast<int*>(a.kmax));
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- pass A
+
+size_t smem_passA_bytes(const AxisPlan& ax, int is_double, int rows) {
+  const size_t es = is_double ? 16 : 8;
+  const size_t ld = (size_t)ax.m + 1;
+  return (2 * ld + (ax.r > 1 ? (size_t)ax.n : 0)) * rows * es;
+}
+
+int rows_per_cta(const AxisPlan& ax, int is_double) {
+  int rows = 16;
+  while (rows > 1 && smem_passA_bytes(ax, is_double, rows) > kSmemBudgetRows) rows /= 2;
+  return rows;
+}
+
+// Row forward transforms of the n input rows (elements fused), written to
+// the column-major spectrum scratch W[kx * ny + iy].
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_passA(PropArgs a, int rows) {
+  using V = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = a.ax.m, r = a.ax.r, P = a.ax.P, nx = a.nx, ny = a.ny;
+  const int ld = m + 1;
+  V* bufA = reinterpret_cast<V*>(smem_raw);
+  V* bufB = bufA + (size_t)rows * ld;
+  V* xin = bufB + (size_t)rows * ld;  // staged input rows when r > 1
+  const int row0 = blockIdx.x * rows;
+  const V* twm = reinterpret_cast<const V*>(a.tw_mx);
+  const V* twP = reinterpret_cast<const V*>(a.tw_Px);
+  V* W = reinterpret_cast<V*>(a.work);
+  const V zero = mkc<V>((T)0, (T)0);
+
+  if (r > 1) {
+    for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
+      const int i = e / nx, j = e - i * nx, iy = row0 + i;
+      V v = zero;
+      if (iy < ny) {
+        v = load_in<T>(a.in, a.in_c128, (size_t)iy * nx + j);
+        if (a.status && nonfinite2((double)v.x, (double)v.y)) atomicOr(a.status, 1);
+        if (a.els.count) v = apply_elements<T>(a.els, j, iy, nx, ny, a.dx, a.dy, v);
+      }
+      xin[(size_t)i * nx + j] = v;
+    }
+    __syncthreads();
+  }
+  for (int s = 0; s < r; ++s) {
+    for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
+      const int i = e / m, j = e - i * m, iy = row0 + i;
+      V v = zero;
+      if (iy < ny && j < nx) {
+        if (r > 1) {
+          v = xin[(size_t)i * nx + j];
+          if (s > 0) v = cmul(v, twP[(int)(((long long)s * j) % P)]);
+        } else {
+          v = load_in<T>(a.in, a.in_c128, (size_t)iy * nx + j);
+          if (a.status && nonfinite2((double)v.x, (double)v.y)) atomicOr(a.status, 1);
+          if (a.els.count) v = apply_elements<T>(a.els, j, iy, nx, ny, a.dx, a.dy, v);
+        }
+      }
+      bufA[(size_t)i * ld + j] = v;
+    }
+    __syncthreads();
+    V* res = stockham<T, false>(bufA, bufB, m, rows, ld, a.ax, twm);
+    for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
+      const int i = e % rows, q = e / rows, iy = row0 + i;
+      if (iy < ny) W[(size_t)(r * q + s) * ny + iy] = res[(size_t)i * ld + q];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+cudaError_t launch_passA(const PropArgs& a, cudaStream_t st) {
+  const int is_d = sizeof(T) == 8;
+  const int rows = rows_per_cta(a.ax, is_d);
+  const size_t smem = smem_passA_bytes(a.ax, is_d, rows);
+  cudaError_t e = cudaFuncSetAttribute(k_passA<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((a.ny + rows - 1) / rows);
+  COUNT_LAUNCH();
+  k_passA<T><<<grid, kThreads, smem, st>>>(a, rows);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- pass B
+
+size_t smem_passB_bytes(const AxisPlan& ay, int is_double) {
+  const size_t es = is_double ? 16 : 8;
+  return (2 * (size_t)ay.m + 2 * (size_t)ay.n) * es;
+}
+
+template <typename T>
+__device__ __forceinline__ cx<T> transfer_exact(const PropArgs& a, double fx, double fy) {
+  using V = cx<T>;
+  double ph;
+  if (a.engine == ENG_ASM) {
+    if (a.band_limited && (fabs(fx) > a.lim_x || fabs(fy) > a.lim_y)) return mkc<V>((T)0, (T)0);
+    const double axx = __dmul_rn(a.lam_n, fx), ayy = __dmul_rn(a.lam_n, fy);
+    const double sv = __dsub_rn(__dsub_rn(1.0, __dmul_rn(axx, axx)), __dmul_rn(ayy, ayy));
+    if (sv < 0.0) return mkc<V>((T)0, (T)0);
+    ph = __dmul_rn(a.kz, __dsqrt_rn(sv));
+  } else {  // ENG_FRESNEL_TF
+    ph = __dsub_rn(a.kz, __dmul_rn(a.cfr, __dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy))));
+  }
+  double s, c;
+  sincos(ph, &s, &c);
+  return mkc<V>((T)(c * a.scale), (T)(s * a.scale));
+}
+
+// One CTA per spectral column kx: pruned forward column FFT, transfer
+// function, pruned inverse column FFT; the column is rewritten in place.
+// fwd_only: forward transform only, result (all Py bins) written to `dst`.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_passB(PropArgs a, int fwd_only, void* dst) {
+  using V = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int my = a.ay.m, ry = a.ay.r, Py = a.ay.P, ny = a.ny;
+  const int kx = blockIdx.x;
+  V* buf0 = reinterpret_cast<V*>(smem_raw);
+  V* buf1 = buf0 + my;
+  V* col = buf1 + my;
+  V* acc = col + ny;
+  const V* twm = reinterpret_cast<const V*>(a.tw_my);
+  const V* twP = reinterpret_cast<const V*>(a.tw_Py);
+  V* W = reinterpret_cast<V*>(a.work) + (size_t)kx * ny;
+  const V zero = mkc<V>((T)0, (T)0);
+
+  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+    col[j] = W[j];
+    acc[j] = zero;
+  }
+  // Per-column transfer-function data.
+  double fx = 0.0;
+  float2 exc = make_float2(0.f, 0.f);
+  float cah = 0.f, cal = 0.f, sac = 0.f;
+  int kmc = -1;
+  if (!fwd_only) {
+    if (a.h_mode == 0 && (a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF)) fx = a.fxv[kx];
+    if (a.h_mode == 1 && (a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF)) {
+      exc = a.Ex[kx];
+      if (a.engine == ENG_ASM) {
+        cah = a.ca_hi[kx];
+        cal = a.ca_lo[kx];
+        sac = a.sa[kx];
+        kmc = a.kmax[kx];
+      }
+    }
+  }
+  __syncthreads();
+  for (int t = 0; t < ry; ++t) {
+    for (int j = threadIdx.x; j < my; j += blockDim.x) {
+      V v = zero;
+      if (j < ny) {
+        v = col[j];
+        if (t > 0) v = cmul(v, twP[(int)(((long long)t * j) % Py)]);
+      }
+      buf0[j] = v;
+    }
+    __syncthreads();
+    V* res = stockham<T, false>(buf0, buf1, my, 1, my, a.ay, twm);
+    if (fwd_only) {
+      V* D = reinterpret_cast<V*>(dst) + (size_t)kx * Py;
+      for (int p = threadIdx.x; p < my; p += blockDim.x) D[ry * p + t] = cscale(res[p], (T)a.scale);
+      __syncthreads();
+      continue;
+    }
+    for (int p = threadIdx.x; p < my; p += blockDim.x) {
+      const int ky = ry * p + t;
+      V h;
+      if (a.engine == ENG_KSPEC) {
+        h = reinterpret_cast<const V*>(a.kspec)[(size_t)kx * Py + ky];
+        if (a.conj_h) h.y = -h.y;
+      } else if (a.engine == ENG_KSEP) {
+        h = cmul(reinterpret_cast<const V*>(a.hx)[kx], reinterpret_cast<const V*>(a.hy)[ky]);
+        if (a.conj_h) h.y = -h.y;
+      } else if (a.engine == ENG_IDENTITY) {
+        h = mkc<V>((T)a.scale, (T)0);
+      } else if (a.h_mode == 0) {
+        h = transfer_exact<T>(a, fx, a.fyv[ky]);
+      } else if (a.engine == ENG_FRESNEL_TF) {
+        const float2 ey = a.Ey[ky];
+        h = mkc<V>((T)(exc.x * ey.x - exc.y * ey.y), (T)(exc.x * ey.y + exc.y * ey.x));
+      } else {
+        const int kk = (ky <= (Py - 1) / 2) ? ky : ky - Py;
+        if (abs(kk) > kmc) {
+          h = zero;
+        } else {
+          const float bh = a.b_hi[ky], blo = a.b_lo[ky];
+          const float s = sac + bh;
+          const float q = sqrtf(fmaxf(1.f - s, 0.f));
+          const float opq = 1.f + q;
+          const float tau = a.Kf * (s * s * s) * (3.f + q) / (8.f * opq * opq * opq);
+          const float pr = cah * bh;
+          const float er = fmaf(cah, bh, -pr);
+          const float corr = er + (cah * blo + cal * bh);
+          const float nq = rintf(pr * 0.159154943091895336f);
+          float rr = fmaf(-nq, 6.28125f, pr);
+          rr = fmaf(-nq, 1.93530717958647692e-3f, rr);
+          const float th = rr + (corr - tau);
+          float sn, cs;
+          __sincosf(th, &sn, &cs);
+          const float2 ey = a.Ey[ky];
+          const float hr = exc.x * ey.x - exc.y * ey.y;
+          const float hi = exc.x * ey.y + exc.y * ey.x;
+          h = mkc<V>((T)(hr * cs - hi * sn), (T)(hr * sn + hi * cs));
+        }
+      }
+      res[p] = cmul(res[p], h);
+    }
+    __syncthreads();
+    V* other = (res == buf0) ? buf1 : buf0;
+    V* res2 = stockham<T, true>(res, other, my, 1, my, a.ay, twm);
+    for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+      V v = res2[j];
+      if (t > 0) v = cmulc(v, twP[(int)(((long long)t * j) % Py)]);
+      acc[j] = cadd(acc[j], v);
+    }
+    __syncthreads();
+  }
+  if (!fwd_only) {
+    for (int j = threadIdx.x; j < ny; j += blockDim.x) W[j] = acc[j];
+  }
+}
+
+template <typename T>
+static cudaError_t launch_passB_impl(const PropArgs& a, int fwd_only, void* dst, cudaStream_t st) {
+  const int is_d = sizeof(T) == 8;
+  const size_t smem = smem_passB_bytes(a.ay, is_d);
+  cudaError_t e = cudaFuncSetAttribute(k_passB<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  COUNT_LAUNCH();
+  k_passB<T><<<a.ax.P, kThreads, smem, st>>>(a, fwd_only, dst);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_passB(const PropArgs& a, cudaStream_t st) {
+  return launch_passB_impl<T>(a, 0, nullptr, st);
+}
+
+// ---------------------------------------------------------------- pass C
+
+// Inverse row transforms + crop: out[iy][j] = sum_s W_Px^{-s j} IDFT_m(Z_s)[j].
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_passC(PropArgs a, int rows) {
+  using V = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = a.ax.m, r = a.ax.r, P = a.ax.P, nx = a.nx, ny = a.ny;
+  const int ld = m + 1;
+  V* bufA = reinterpret_cast<V*>(smem_raw);
+  V* bufB = bufA + (size_t)rows * ld;
+  V* acc = bufB + (size_t)rows * ld;
+  const int row0 = blockIdx.x * rows;
+  const V* twm = reinterpret_cast<const V*>(a.tw_mx);
+  const V* twP = reinterpret_cast<const V*>(a.tw_Px);
+  const V* W = reinterpret_cast<const V*>(a.work);
+
+  for (int s = 0; s < r; ++s) {
+    for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
+      const int i = e % rows, q = e / rows, iy = row0 + i;
+      bufA[(size_t)i * ld + q] =
+          (iy < ny) ? W[(size_t)(r * q + s) * ny + iy] : mkc<V>((T)0, (T)0);
+    }
+    __syncthreads();
+    V* res = stockham<T, true>(bufA, bufB, m, rows, ld, a.ax, twm);
+    for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
+      const int i = e / nx, j = e - i * nx;
+      V v = res[(size_t)i * ld + j];
+      if (s > 0) v = cmulc(v, twP[(int)(((long long)s * j) % P)]);
+      if (r > 1) {
+        if (s == 0) acc[(size_t)i * nx + j] = v;
+        else acc[(size_t)i * nx + j] = cadd(acc[(size_t)i * nx + j], v);
+      } else {
+        acc[(size_t)i * nx + j] = v;
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
+    const int i = e / nx, j = e - i * nx, iy = row0 + i;
+    if (iy >= ny) continue;
+    const V v = acc[(size_t)i * nx + j];
+    const size_t o = (size_t)iy * nx + j;
+    if (a.status && nonfinite2((double)v.x, (double)v.y)) atomicOr(a.status, 2);
+    if (a.out) store_out<T>(a.out, a.out_c128, o, v);
+    if (a.out_intensity) a.out_intensity[o] = (float)((double)v.x * v.x + (double)v.y * v.y);
+    if (a.out_intensity64) a.out_intensity64[o] = (double)v.x * v.x + (double)v.y * v.y;
+  }
+}
+
+static size_t smem_passC_bytes(const AxisPlan& ax, int is_double, int rows) {
+  const size_t es = is_double ? 16 : 8;
+  return (2 * ((size_t)ax.m + 1) + (size_t)ax.n) * rows * es;
+}
+
+template <typename T>
+cudaError_t launch_passC(const PropArgs& a, cudaStream_t st) {
+  const int is_d = sizeof(T) == 8;
+  int rows = 16;
+  while (rows > 1 && smem_passC_bytes(a.ax, is_d, rows) > kSmemBudgetRows) rows /= 2;
+  const size_t smem = smem_passC_bytes(a.ax, is_d, rows);
+  cudaError_t e = cudaFuncSetAttribute(k_passC<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  COUNT_LAUNCH();
+  k_passC<T><<<(a.ny + rows - 1) / rows, kThreads, smem, st>>>(a, rows);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------ kernel spectra
+
+// DFT-order coordinate (reference fresnel.rs:322-328).
+__device__ __forceinline__ double dft_coord(int i, int n, double d) {
+  return (i <= n / 2) ? __dmul_rn((double)i, d) : __dmul_rn(__dsub_rn((double)i, (double)n), d);
+}
+
+// Direct length-n DFT of one row (used for the two 1-D chirp spectra of the
+// separable Fresnel kernel; O(n^2) once per (lambda, z, grid)).
+__global__ void k_chirp_dft(int n, double d, double A, const double2* tw, double2* out,
+                            double pre_re, double pre_im) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double sr = 0.0, si = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const double x = dft_coord(j, n, d);
+    double s, c;
+    sincos(__dmul_rn(A, __dmul_rn(x, x)), &s, &c);
+    const double2 w = tw[(int)(((long long)j * k) % n)];
+    sr += c * w.x - s * w.y;
+    si += c * w.y + s * w.x;
+  }
+  out[k] = make_double2(sr * pre_re - si * pre_im, sr * pre_im + si * pre_re);
+}
+
+template <typename T>
+__global__ void k_cast_c128(const double2* src, void* dst, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = src[i];
+  if (sizeof(T) == 8) reinterpret_cast<double2*>(dst)[i] = v;
+  else reinterpret_cast<float2*>(dst)[i] = make_float2((float)v.x, (float)v.y);
+}
+
+// hx[kx] = pref * scale * DFT(e^{i A x^2}), hy[ky] = DFT(e^{i A y^2}),
+// A = pi / (lam z); the product is the 2-D spectrum of the sampled kernel
+// h = pref e^{i pi (x^2+y^2)/(lam z)} (reference fresnel.rs:312-338).
+template <typename T>
+cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp, cudaStream_t st) {
+  // tmp: (Px + Py) double2 twiddles + (Px + Py) double2 results
+  const int Px = a.ax.P, Py = a.ay.P;
+  double2* twx = reinterpret_cast<double2*>(tmp);
+  double2* twy = twx + Px;
+  double2* ox = twy + Py;
+  double2* oy = ox + Px;
+  cudaError_t e = launch_twiddles(twx, Px, 1, st);
+  if (e != cudaSuccess) return e;
+  e = launch_twiddles(twy, Py, 1, st);
+  if (e != cudaSuccess) return e;
+  const double A = M_PI / (a.lam * a.z);
+  // pref = e^{ikz}/(i lam z) * dx dy, folded with the 1/(Px Py) scale.
+  const double k = 2.0 * M_PI / a.lam;
+  const double kz = k * a.z;
+  const double lz = a.lam * a.z;
+  // e^{ikz} / (i lz) = (cos + i sin) * (-i / lz) = (sin / lz) - i (cos / lz)
+  const double pr = sin(kz) / lz * (a.dx * a.dy) * a.scale;
+  const double pi_ = -cos(kz) / lz * (a.dx * a.dy) * a.scale;
+  COUNT_LAUNCH();
+  k_chirp_dft<<<(Px + 127) / 128, 128, 0, st>>>(Px, a.dx, A, twx, ox, pr, pi_);
+  COUNT_LAUNCH();
+  k_chirp_dft<<<(Py + 127) / 128, 128, 0, st>>>(Py, a.dy, A, twy, oy, 1.0, 0.0);
+  COUNT_LAUNCH();
+  k_cast_c128<T><<<(Px + 255) / 256, 256, 0, st>>>(ox, hx, Px);
+  COUNT_LAUNCH();
+  k_cast_c128<T><<<(Py + 255) / 256, 256, 0, st>>>(oy, hy, Py);
+  return cudaGetLastError();
+}
+
+// RS-I kernel samples in DFT order, dx dy folded in (reference
+// rayleigh_sommerfeld.rs:228-235, 277-301).
+__global__ void k_rs_kernel(int Px, int Py, double dx, double dy, double lam, double z,
+                            double2* h) {
+  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (idx >= (size_t)Px * Py) return;
+  const int ix = (int)(idx % Px), iy = (int)(idx / Px);
+  const double x = dft_coord(ix, Px, dx), y = dft_coord(iy, Py, dy);
+  const double k = __ddiv_rn(2.0 * M_PI, lam);
+  const double sg = z > 0.0 ? 1.0 : -1.0;
+  const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+  const double amp = __ddiv_rn(fabs(z), __dmul_rn(__dmul_rn(2.0 * M_PI, r), r));
+  const double ob_re = __ddiv_rn(1.0, r), ob_im = -sg * k;
+  double s, c;
+  sincos(__dmul_rn(__dmul_rn(sg, k), r), &s, &c);
+  // amp * obliquity * e^{i s k r} * (dx dy)
+  const double pr = amp * ob_re, pi_ = amp * ob_im;
+  const double w = __dmul_rn(dx, dy);
+  h[idx] = make_double2((pr * c - pi_ * s) * w, (pr * s + pi_ * c) * w);
+}
+
+template <typename T>
+cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStream_t st) {
+  // tmp64 holds: h (Px*Py double2) then the column-major work (Px*Py double2)
+  // then twiddles (Px + Py double2); `a` carries full-support axis plans.
+  const int Px = a.ax.P, Py = a.ay.P;
+  double2* h = reinterpret_cast<double2*>(tmp64);
+  double2* work = h + (size_t)Px * Py;
+  double2* twx = work + (size_t)Px * Py;
+  double2* twy = twx + Px;
+  cudaError_t e = launch_twiddles(twx, Px, 1, st);
+  if (e != cudaSuccess) return e;
+  e = launch_twiddles(twy, Py, 1, st);
+  if (e != cudaSuccess) return e;
+  const size_t n = (size_t)Px * Py;
+  COUNT_LAUNCH();
+  k_rs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Px, Py, a.dx, a.dy, a.lam, a.z, h);
+  PropArgs b = a;
+  b.nx = Px;
+  b.ny = Py;
+  b.in = h;
+  b.in_c128 = 1;
+  b.work = work;
+  b.tw_mx = twx;
+  b.tw_Px = twx;
+  b.tw_my = twy;
+  b.tw_Py = twy;
+  b.els.count = 0;
+  b.engine = ENG_IDENTITY;
+  e = launch_passA<double>(b, st);
+  if (e != cudaSuccess) return e;
+  double2* spec = reinterpret_cast<double2*>(h);  // reuse h as the f64 spectrum
+  e = launch_passB_impl<double>(b, 1, spec, st);
+  if (e != cudaSuccess) return e;
+  COUNT_LAUNCH();
+  k_cast_c128<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(spec, kspec, n);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ Fraunhofer
+
+// Pass FA: offset-DFT pre-phase and off-axis ramp (reference
+// fraunhofer.rs:396-412), then forward row FFTs into column-major scratch.
+// Adjoint mode: input is the far-field grid; rows carry conj(post * chirp *
+// quad) dx dy (and the mirror), followed by inverse row FFTs.
+template <typename T>
+__device__ __forceinline__ void fraun_pre(const FraunArgs& a, int ix, int iy, double& re,
+                                          double& im) {
+  const double cy = a.cyc, cx = a.cxc;
+  const double eta = __dmul_rn(__dsub_rn((double)iy, cy), a.dy);
+  const double xi = __dmul_rn(__dsub_rn((double)ix, cx), a.dx);
+  const double py = __ddiv_rn(__dmul_rn(__dmul_rn(2.0 * M_PI, cy), (double)iy), (double)a.ny);
+  const double ry = __dmul_rn(__dmul_rn(2.0 * M_PI, a.g_s), eta);
+  const double px = __dmul_rn(2.0 * M_PI, __dadd_rn(__ddiv_rn(__dmul_rn(cx, (double)ix), (double)a.nx),
+                                                    __dmul_rn(a.f_s, xi)));
+  double s1, c1, s2, c2, s3, c3;
+  sincos(py, &s1, &c1);
+  sincos(ry, &s2, &c2);
+  sincos(px, &s3, &c3);
+  // pre = pre_y * ramp_y * pre_x
+  double ar = c1 * c2 - s1 * s2, ai = c1 * s2 + s1 * c2;
+  double br = ar * c3 - ai * s3, bi = ar * s3 + ai * c3;
+  if (a.adjoint) bi = -bi;
+  const double r2 = re * br - im * bi, i2 = re * bi + im * br;
+  re = r2;
+  im = i2;
+}
+
+// Output factor quad * chirp * post * (dx dy) for output sample (ix, iy)
+// with source bin (mx, my) (reference fraunhofer.rs:421-438).
+__device__ __forceinline__ void fraun_post(const FraunArgs& a, int ix, int iy, int mx, int my,
+                                           double& fr, double& fi) {
+  const double cy = a.cyc, cx = a.cxc;
+  const double dyp = __dsub_rn(__dmul_rn(__dsub_rn((double)iy, cy), a.dyo), a.ys);
+  const double dxp = __dsub_rn(__dmul_rn(__dsub_rn((double)ix, cx), a.dxo), a.xs);
+  const double py = __ddiv_rn(__dmul_rn(__dmul_rn(2.0 * M_PI, cy), __dsub_rn((double)my, cy)), (double)a.ny);
+  const double px = __ddiv_rn(__dmul_rn(__dmul_rn(2.0 * M_PI, cx), __dsub_rn((double)mx, cx)), (double)a.nx);
+  const double ch = __ddiv_rn(__dmul_rn(M_PI, __dadd_rn(__dmul_rn(dxp, dxp), __dmul_rn(dyp, dyp))),
+                              __dmul_rn(a.lam, a.z));
+  double s1, c1, s2, c2, s3, c3;
+  sincos(py, &s1, &c1);
+  sincos(px, &s2, &c2);
+  sincos(ch, &s3, &c3);
+  // quad * chirp
+  double qr = a.quad_re * c3 - a.quad_im * s3, qi = a.quad_re * s3 + a.quad_im * c3;
+  // * post_y * post_x
+  double pr = c1 * c2 - s1 * s2, pi_ = c1 * s2 + s1 * c2;
+  double tr = qr * pr - qi * pi_, ti = qr * pi_ + qi * pr;
+  const double w = __dmul_rn(a.dx, a.dy);
+  fr = tr * w;
+  fi = ti * w;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_fraunA(FraunArgs a, int rows) {
+  using V = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = a.ax.m, nx = a.nx, ny = a.ny;
+  const int ld = m + 1;
+  V* bufA = reinterpret_cast<V*>(smem_raw);
+  V* bufB = bufA + (size_t)rows * ld;
+  const int row0 = blockIdx.x * rows;
+  const V* twm = reinterpret_cast<const V*>(a.tw_mx);
+  V* W = reinterpret_cast<V*>(a.work);
+  const double sgn = a.z > 0.0 ? 1.0 : -1.0;
+  for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
+    const int i = e / m, j = e - i * m, iy = row0 + i;
+    double re = 0.0, im = 0.0;
+    int pos = j;
+    if (iy < ny) {
+      V v = load_in<T>(a.in, a.in_c128, (size_t)iy * nx + j);
+      re = (double)v.x;
+      im = (double)v.y;
+      if (a.status && nonfinite2(re, im)) atomicOr(a.status, 1);
+      if (!a.adjoint) {
+        if (a.els.count) apply_elements_exact(a.els, j, iy, nx, ny, a.dx, a.dy, re, im);
+        fraun_pre<T>(a, j, iy, re, im);
+      } else {
+        // adjoint: far-field sample (ix = j, iy) came from DFT bin (mx, my);
+        // multiply conj(factor) and place it at its bin index mx.
+        const int mx = (int)rint(sgn * ((double)j - a.cxc) + a.cxc);
+        const int my = (int)rint(sgn * ((double)iy - a.cyc) + a.cyc);
+        double fr, fi;
+        fraun_post(a, j, iy, mx, my, fr, fi);
+        const double r2 = re * fr + im * fi, i2 = im * fr - re * fi;  // * conj(f)
+        re = r2;
+        im = i2;
+        pos = mx;
+      }
+    }
+    bufA[(size_t)i * ld + pos] = mkc<V>((T)re, (T)im);
+  }
+  __syncthreads();
+  V* res = a.adjoint ? stockham<T, true>(bufA, bufB, m, rows, ld, a.ax, twm)
+                     : stockham<T, false>(bufA, bufB, m, rows, ld, a.ax, twm);
+  // adjoint: the DFT index of this row is the source bin mx(ix); scatter so
+  // that W[mx][my] holds the row.  Forward: identity placement.
+  for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
+    const int i = e % rows, q = e / rows, iy = row0 + i;
+    if (iy >= ny) continue;
+    int dst_row = iy;
+    if (a.adjoint) dst_row = (int)rint(sgn * ((double)iy - a.cyc) + a.cyc);
+    W[(size_t)q * ny + dst_row] = res[(size_t)i * ld + q];
+  }
+}
+
+// Pass FB: forward column FFT over y, then the output factor and mirror
+// (forward), or inverse column FFT and conj(pre) (adjoint).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_fraunB(FraunArgs a) {
+  using V = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int my = a.ay.m, ny = a.ny, nx = a.nx;
+  const int kx = blockIdx.x;
+  V* buf0 = reinterpret_cast<V*>(smem_raw);
+  V* buf1 = buf0 + my;
+  const V* twm = reinterpret_cast<const V*>(a.tw_my);
+  const V* W = reinterpret_cast<const V*>(a.work) + (size_t)kx * ny;
+  for (int j = threadIdx.x; j < my; j += blockDim.x) buf0[j] = W[j];
+  __syncthreads();
+  V* res = a.adjoint ? stockham<T, true>(buf0, buf1, my, 1, my, a.ay, twm)
+                     : stockham<T, false>(buf0, buf1, my, 1, my, a.ay, twm);
+  const double sgn = a.z > 0.0 ? 1.0 : -1.0;
+  for (int p = threadIdx.x; p < my; p += blockDim.x) {
+    V v = res[p];
+    double re = (double)v.x, im = (double)v.y;
+    int ox, oy;
+    if (!a.adjoint) {
+      // bin (mx = kx, my = p) lands on output (ix, iy) with mx = sgn (ix - c) + c
+      const int ix = (int)rint(sgn * ((double)kx - a.cxc) + a.cxc);
+      const int iy = (int)rint(sgn * ((double)p - a.cyc) + a.cyc);
+      double fr, fi;
+      fraun_post(a, ix, iy, kx, p, fr, fi);
+      const double r2 = fr * re - fi * im, i2 = fr * im + fi * re;
+      re = r2;
+      im = i2;
+      ox = ix;
+      oy = iy;
+    } else {
+      // spatial sample (ix = kx, iy = p): multiply conj(pre)
+      fraun_pre<T>(a, kx, p, re, im);
+      ox = kx;
+      oy = p;
+    }
+    const size_t o = (size_t)oy * nx + ox;
+    const V w = mkc<V>((T)re, (T)im);
+    if (a.status && nonfinite2(re, im)) atomicOr(a.status, 2);
+    if (a.out) store_out<T>(a.out, a.out_c128, o, w);
+    if (a.out_intensity) a.out_intensity[o] = (float)(re * re + im * im);
+  }
+}
+
+template <typename T>
+cudaError_t launch_fraunhofer(const FraunArgs& a, cudaStream_t st) {
+  const int is_d = sizeof(T) == 8;
+  const size_t es = is_d ? 16 : 8;
+  int rows = 16;
+  while (rows > 1 && 2 * ((size_t)a.ax.m + 1) * rows * es > kSmemBudgetRows) rows /= 2;
+  size_t smem = 2 * ((size_t)a.ax.m + 1) * rows * es;
+  cudaError_t e = cudaFuncSetAttribute(k_fraunA<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  COUNT_LAUNCH();
+  k_fraunA<T><<<(a.ny + rows - 1) / rows, kThreads, smem, st>>>(a, rows);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  smem = 2 * (size_t)a.ay.m * es;
+  e = cudaFuncSetAttribute(k_fraunB<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  COUNT_LAUNCH();
+  k_fraunB<T><<<a.nx, kThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------ element kernel
+
+template <typename T>
+__global__ void k_apply_elements(const void* in, int in_c128, void* out, int out_c128,
+                                 ElementList els, int nx, int ny, double dx, double dy,
+                                 int* status) {
+  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (idx >= (size_t)nx * ny) return;
+  const int ix = (int)(idx % nx), iy = (int)(idx / nx);
+  cx<T> v = load_in<T>(in, in_c128, idx);
+  v = apply_elements<T>(els, ix, iy, nx, ny, dx, dy, v);
+  if (status && nonfinite2((double)v.x, (double)v.y)) atomicOr(status, 2);
+  store_out<T>(out, out_c128, idx, v);
+}
+
+template <typename T>
+cudaError_t launch_apply_elements(const void* in, int in_c128, void* out, int out_c128,
+                                  const ElementList& els, int nx, int ny, double dx, double dy,
+                                  int* status, cudaStream_t st) {
+  const size_t n = (size_t)nx * ny;
+  COUNT_LAUNCH();
+  k_apply_elements<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, in_c128, out, out_c128,
+                                                                    els, nx, ny, dx, dy, status);
+  return cudaGetLastError();
+}
+
+// -------------------------------------------------------- instantiations
+
+template cudaError_t launch_apply_elements<float>(const void*, int, void*, int, const ElementList&,
+                                                  int, int, double, double, int*, cudaStream_t);
+template cudaError_t launch_apply_elements<double>(const void*, int, void*, int, const ElementList&,
+                                                   int, int, double, double, int*, cudaStream_t);
+
+template cudaError_t launch_asm_prep<float>(const PropArgs&, void*, cudaStream_t);
+template cudaError_t launch_asm_prep<double>(const PropArgs&, void*, cudaStream_t);
+template cudaError_t launch_passA<float>(const PropArgs&, cudaStream_t);
+template cudaError_t launch_passA<double>(const PropArgs&, cudaStream_t);
+template cudaError_t launch_passB<float>(const PropArgs&, cudaStream_t);
+template cudaError_t launch_passB<double>(const PropArgs&, cudaStream_t);
+template cudaError_t launch_passC<float>(const PropArgs&, cudaStream_t);
+template cudaError_t launch_passC<double>(const PropArgs&, cudaStream_t);
+template cudaError_t launch_fraunhofer<float>(const FraunArgs&, cudaStream_t);
+template cudaError_t launch_fraunhofer<double>(const FraunArgs&, cudaStream_t);
+template cudaError_t launch_fresnel_ksep<float>(const PropArgs&, void*, void*, void*, cudaStream_t);
+template cudaError_t launch_fresnel_ksep<double>(const PropArgs&, void*, void*, void*, cudaStream_t);
+template cudaError_t launch_rs_kspec<float>(const PropArgs&, void*, void*, cudaStream_t);
+template cudaError_t launch_rs_kspec<double>(const PropArgs&, void*, void*, cudaStream_t);
+
+}  // namespace osgpu

@@ -1,0 +1,107 @@
+// Kernel argument blocks and host launchers for the propagation passes.
+#pragma once
+#include <cuda_runtime.h>
+#include "osgpu_types.h"
+
+namespace osgpu {
+
+// Everything the three propagation passes need for one propagation.
+// Pointers are device pointers.  `T` is the arithmetic type (float/double);
+// complex buffers are float2/double2 (input/output may be complex128 while
+// the engine computes in f32: see in_c128/out_c128).
+struct PropArgs {
+  int nx, ny;
+  double dx, dy;
+  AxisPlan ax, ay;
+  const void* in;      // field in, row-major ny x nx
+  int in_c128;
+  void* out;           // field out, row-major ny x nx
+  int out_c128;
+  float* out_intensity;  // optional |u|^2 (f32) of the output, row-major
+  double* out_intensity64;
+  void* work;          // Px x ny spectrum scratch (column-major)
+  const void* tw_mx;   // m-point twiddles (x)
+  const void* tw_Px;   // P-point twiddles (x), used when r > 1
+  const void* tw_my;
+  const void* tw_Py;
+  ElementList els;
+  // transfer function
+  int engine;
+  int h_mode;          // 0 exact per-bin FP64, 1 f32 split tables
+  double lam, lam_n, z, kz;   // kz = (2 pi / lam_n) * z  (ASM) or (2 pi/lam)*z (Fresnel)
+  double cfr;          // Fresnel: (pi * lam) * z
+  int band_limited;
+  double lim_x, lim_y;
+  double scale;        // 1 / (Px * Py)
+  int conj_h;          // 1: use conj(H) (adjoint of a kernel-spectrum engine)
+  // per-axis tables produced by the prep kernel
+  const double* fxv;   // fftfreq(Px, dx)
+  const double* fyv;   // fftfreq(Py, dy)
+  const float2* Ex;    // f32 split: per-column factor (includes e^{i kz} and scale)
+  const float2* Ey;    // per-row factor
+  const float* ca_hi;  // -kz a/4 (double-float)
+  const float* ca_lo;
+  const float* sa;     // a = (lam_n fx)^2
+  const float* b_hi;   // b = (lam_n fy)^2 (double-float)
+  const float* b_lo;
+  const int* kmax;     // per column: largest unmasked |k_y| (-1: column masked)
+  float Kf;            // kz as f32 (for the small residual term)
+  // kernel spectra
+  const void* kspec;   // ENG_KSPEC: column-major Px x Py spectrum (type of engine)
+  const void* hx;      // ENG_KSEP: per-column spectrum factor (includes prefactor, scale)
+  const void* hy;      // ENG_KSEP: per-row spectrum factor
+  int* status;         // bit 0: non-finite input sample, bit 1: non-finite output
+};
+
+// Fraunhofer arguments (no padding; two passes).
+struct FraunArgs {
+  int nx, ny;
+  double dx, dy;
+  AxisPlan ax, ay;
+  const void* in;
+  int in_c128;
+  void* out;
+  int out_c128;
+  float* out_intensity;
+  void* work;
+  const void* tw_mx;
+  const void* tw_my;
+  ElementList els;
+  double lam, z, k;
+  double xs, ys, f_s, g_s;
+  double dxo, dyo;
+  double cxc, cyc;     // (n-1)/2
+  double quad_re, quad_im;  // e^{ikz}/(i lam z)
+  int adjoint;         // 1: exact adjoint of the forward operator
+  int* status;
+};
+
+template <typename T> cudaError_t launch_asm_prep(const PropArgs& a, void* tables, cudaStream_t st);
+template <typename T> cudaError_t launch_passA(const PropArgs& a, cudaStream_t st);
+template <typename T> cudaError_t launch_passB(const PropArgs& a, cudaStream_t st);
+template <typename T> cudaError_t launch_passC(const PropArgs& a, cudaStream_t st);
+template <typename T> cudaError_t launch_fraunhofer(const FraunArgs& a, cudaStream_t st);
+
+cudaError_t launch_twiddles(void* dst, int n, int is_double, cudaStream_t st);
+// Separable Fresnel-convolution kernel spectrum: fills hx (Px) and hy (Py).
+template <typename T>
+cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp, cudaStream_t st);
+// Rayleigh-Sommerfeld kernel spectrum, column-major Px x Py, built in f64
+// and stored as T.
+template <typename T>
+cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStream_t st);
+
+// Standalone element application (Element::apply chain, no propagation).
+template <typename T>
+cudaError_t launch_apply_elements(const void* in, int in_c128, void* out, int out_c128,
+                                  const ElementList& els, int nx, int ny, double dx, double dy,
+                                  int* status, cudaStream_t st);
+
+// Kernel launches issued by the library since load.
+unsigned long long launch_count();
+
+size_t smem_passA_bytes(const AxisPlan& ax, int is_double, int rows);
+size_t smem_passB_bytes(const AxisPlan& ay, int is_double);
+int rows_per_cta(const AxisPlan& ax, int is_double);
+
+}  // namespace osgpu

@@ -1,0 +1,159 @@
+"""CPU tests of the C ABI: the library builds and exports every symbol of
+include/osgpu.h, and its host-side analysis (which picks the padded grid and
+fills the reports) matches the f64 oracle bit for bit.  No GPU needed."""
+
+import ctypes
+import math
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+import optics_studio_gb300 as og
+from optics_studio_gb300 import _ffi
+from optics_studio_gb300.field import BandField
+from optics_studio_gb300.propagation import asm as gasm, fresnel as gfr, fraunhofer as gfh
+from optics_studio_gb300.propagation import rayleigh_sommerfeld as grs
+from oracle import asm as oasm, fresnel as ofr, fraunhofer as ofh, rs as ors, field as ofield
+
+HEADER = pathlib.Path(__file__).resolve().parents[1] / "include" / "osgpu.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(osgpu_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = og.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 17
+    for s in syms:
+        assert hasattr(L, s), s
+    bound = {n for n, _, _ in _ffi.SIGNATURES}
+    assert set(syms) == bound
+
+
+def test_struct_layouts_match_header_sizes():
+    # sizes implied by the header's field lists (natural alignment, x86-64/aarch64)
+    assert ctypes.sizeof(_ffi.Grid) == 40
+    assert ctypes.sizeof(_ffi.AsmConfigC) == 32
+    assert ctypes.sizeof(_ffi.ElementC) == 112
+
+
+GEOMS = [
+    # (nx, ny, dx, dy, lam, z, padding, band_limited, strict, max_padding, medium)
+    (512, 512, 2e-6, 2e-6, 633e-9, 10e-3, 2.0, True, True, 8.0, 1.0),
+    (2048, 2048, 3e-6, 3e-6, 450e-9, 0.1, 2.0, True, True, 8.0, 1.0),
+    (2048, 2048, 3e-6, 3e-6, 650e-9, 1e-3, 2.0, True, True, 8.0, 1.0),
+    (64, 64, 1e-6, 1e-6, 500e-9, 7.68e-4, 1.0, False, True, 8.0, 1.0),
+    (32, 32, 1e-6, 1e-6, 500e-9, 0.5, 2.0, False, False, 8.0, 1.5),
+    (45, 37, 4e-6, 5e-6, 532e-9, -2e-3, 1.5, True, True, 8.0, 1.3),
+    (1536, 1536, 20e-6, 20e-6, 500e-9, 40.0, 2.0, True, True, 8.0, 1.0),
+]
+
+
+@pytest.mark.parametrize("geom", GEOMS)
+def test_asm_sampling_report_matches_oracle(geom):
+    nx, ny, dx, dy, lam, z, pad, bl, strict, mp, med = geom
+    cfg = gasm.AsmConfig(pad, bl, strict, mp, med)
+    gb = BandField(np.zeros((1, 1), complex), dx, dy, lam)
+    grid = _ffi.Grid(nx, ny, dx, dy, lam)
+    rep = _ffi.AsmReportC()
+    assert og.lib().osgpu_asm_sampling_report(grid, z, cfg.c(), rep) == 0
+    ob = ofield.BandField(np.zeros((ny, nx), complex), dx, dy, lam)
+    oref = oasm.sampling_report(ob, z, oasm.AsmConfig(pad, bl, strict, mp, med))
+    assert (rep.nx_pad, rep.ny_pad) == oref.padded_dims
+    for a, b in [(rep.band_limit_fx, oref.band_limit_fx), (rep.band_limit_fy, oref.band_limit_fy),
+                 (rep.max_phase_step_x, oref.max_phase_step_x),
+                 (rep.max_phase_step_y, oref.max_phase_step_y)]:
+        assert a == b
+    assert bool(rep.nyquist_ok) == oref.nyquist_ok
+
+
+@pytest.mark.parametrize("geom", GEOMS)
+def test_asm_densification_ladder_matches_oracle(geom):
+    """The padded grid the propagation runs on (asm.rs:465-479) — resolved on
+    the host before any device work, so it is observable without a GPU."""
+    nx, ny, dx, dy, lam, z, pad, bl, strict, mp, med = geom
+    cfg = gasm.AsmConfig(pad, bl, strict, mp, med)
+    ob = ofield.BandField(np.zeros((ny, nx), complex), dx, dy, lam)
+    try:
+        oref = oasm.resolve_report(ob, z, oasm.AsmConfig(pad, bl, strict, mp, med))
+        want = 0
+    except oasm.PropagationError as e:
+        oref = e.report
+        want = 6
+    rep = _ffi.AsmReportC()
+    buf = np.zeros((ny, nx), complex)
+    code = og.lib().osgpu_asm_propagate(buf.ctypes.data_as(_ffi.c_double_p),
+                                        buf.ctypes.data_as(_ffi.c_double_p),
+                                        _ffi.Grid(nx, ny, dx, dy, lam), z, cfg.c(), 0, rep)
+    if want == 6:
+        assert code == 6
+    else:
+        assert code in (0, 103)  # 103 = no device here
+    assert (rep.nx_pad, rep.ny_pad) == oref.padded_dims
+    assert rep.used_padding == oref.used_padding
+
+
+@pytest.mark.parametrize("z", [50e-3, 200e-3, -5e-3, 1e-4])
+def test_fresnel_report_matches_oracle(z):
+    for pad in (1.0, 2.0, 3.5):
+        cfg = gfr.FresnelConfig(pad, True, 8.0)
+        ob = ofield.BandField(np.zeros((100, 120), complex), 4e-6, 3e-6, 532e-9)
+        rep = _ffi.FresnelReportC()
+        og.lib().osgpu_fresnel_sampling_report(_ffi.Grid(120, 100, 4e-6, 3e-6, 532e-9), z,
+                                               cfg.c(), rep)
+        o = ofr.sampling_report(ob, z, ofr.FresnelConfig(pad, True, 8.0))
+        assert (rep.nx_pad, rep.ny_pad) == o.padded_dims
+        assert rep.max_phase_step_x == o.max_phase_step_x
+        assert rep.max_kernel_step_y == o.max_kernel_step_y
+        assert rep.max_phase_error_vs_asm == o.max_phase_error_vs_asm
+        assert bool(rep.kernel_nyquist_ok) == o.kernel_nyquist_ok
+
+
+def test_fraunhofer_and_rs_reports_match_oracle():
+    ob = ofield.BandField(np.zeros((31, 33), complex), 10e-6, 12e-6, 633e-9)
+    for cfgp in [gfh.FraunhoferConfig(), gfh.FraunhoferConfig(True, 0.1, (1e-5, -2e-5), None),
+                 gfh.FraunhoferConfig(False, 1.0, None, 2e-4)]:
+        rep = _ffi.FraunhoferReportC()
+        og.lib().osgpu_fraunhofer_regime_report(_ffi.Grid(33, 31, 10e-6, 12e-6, 633e-9), -0.3,
+                                                cfgp.c(), rep)
+        o = ofh.regime_report(ob, -0.3, ofh.FraunhoferConfig(cfgp.strict, cfgp.max_n_f,
+                                                             cfgp.source_pos,
+                                                             cfgp.aperture_extent))
+        assert (rep.dx_out, rep.dy_out) == o.output_pitch
+        assert (rep.n_f_x, rep.n_f_y) == (o.n_f_x, o.n_f_y)
+        assert bool(rep.regime_ok) == o.regime_ok and rep.extent_used == o.extent_used
+    rr = _ffi.RsReportC()
+    og.lib().osgpu_rs_sampling_report(_ffi.Grid(33, 31, 10e-6, 12e-6, 633e-9), 5e-3,
+                                      grs.RayleighSommerfeldConfig().c(), rr)
+    o = ors.sampling_report(ob, 5e-3, ors.RayleighSommerfeldConfig())
+    assert (rr.max_kernel_step_x, rr.max_phase_error_vs_fresnel) == (
+        o.max_kernel_step_x, o.max_phase_error_vs_fresnel)
+
+
+def test_host_validation_errors_without_device():
+    L = og.lib()
+    buf = np.zeros((8, 8), complex)
+    p = buf.ctypes.data_as(_ffi.c_double_p)
+    g = _ffi.Grid(8, 8, 20e-6, 20e-6, 500e-9)
+    assert L.osgpu_asm_propagate(p, p, g, float("nan"), gasm.AsmConfig().c(), 0, None) == 1
+    assert L.osgpu_asm_propagate(p, p, g, 1e-3, gasm.AsmConfig(medium=0.0).c(), 0, None) == 3
+    assert L.osgpu_asm_propagate(p, p, _ffi.Grid(8, 8, 20e-6, 20e-6, -1.0), 1e-3,
+                                 gasm.AsmConfig().c(), 0, None) == 2
+    assert L.osgpu_fraunhofer_propagate(p, p, g, 0.0, gfh.FraunhoferConfig().c(), 0, None) == 1
+    assert L.osgpu_rs_propagate(p, p, g, 0.0, grs.RayleighSommerfeldConfig().c(), 0, None) == 1
+    # z == 0 is the identity (asm.rs:461-463) and needs no device; NaN is still rejected
+    src = np.arange(64, dtype=float).reshape(8, 8) + 0j
+    out = np.zeros_like(src)
+    assert L.osgpu_asm_propagate(src.ctypes.data_as(_ffi.c_double_p),
+                                 out.ctypes.data_as(_ffi.c_double_p), g, 0.0,
+                                 gasm.AsmConfig().c(), 0, None) == 0
+    assert np.array_equal(out, src)
+    src[3, 3] = np.nan
+    assert L.osgpu_asm_propagate(src.ctypes.data_as(_ffi.c_double_p),
+                                 out.ctypes.data_as(_ffi.c_double_p), g, 0.0,
+                                 gasm.AsmConfig().c(), 0, None) == 5
