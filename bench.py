@@ -1,0 +1,392 @@
+"""Benchmark of the propagation hot path on one GB300 (or N replicas).
+
+Workload (the 2048^2 batched BandField beamline): 32 wavelengths uniform
+450-650 nm, each a 2048 x 2048 complex64 field (dx = 3 um, unit plane wave)
+through [16-level random DOE phase (seeded), square aperture 5 mm, thin lens
+f = 100 mm, ASM z = 100 mm] with the default AsmConfig (strict densification
+gives a 8192 x 8192 padded grid for every band).  One step = the whole
+32-band batch, device resident, through osgpu_beamline_trace_batch_device.
+Metric: propagations (band-planes) per second.
+
+Also reported: the same batch on the plain FP64 path, end-to-end throughput
+through the reference-facing host-buffer C ABI (osgpu_beamline_trace with
+pinned complex128 buffers, copies inside the timed region), the roofline of
+the dominant kernel (CUDA events recorded by the library on the launching
+stream), SM clocks sampled during the timed region, and a bounded CPU
+baseline (the f64 oracle restatement, one band, one thread).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank runs its own 32-band batch (weak scaling, no
+collective on the data path); rank 0 prints one JSON line.
+"""
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 2048
+DX = 3e-6
+NBANDS = 32
+LAMS = np.linspace(450e-9, 650e-9, NBANDS)
+Z = 0.1
+F_LENS = 0.1
+HALF_AP = 2.5e-3
+LEVELS = 16
+SEED = 1234
+METRIC = "2048^2 ASM propagations/s (batched BandField beamline, FP32)"
+WORKLOAD = ("32 bands 450-650 nm x 2048^2, dx 3 um, [16-level DOE, square aperture 5 mm, "
+            "thin lens f 100 mm, ASM z 100 mm], padded 8192^2")
+
+
+def doe_lattice():
+    rng = np.random.default_rng(SEED)
+    return np.floor(rng.uniform(0, LEVELS, (N, N))) * (2 * math.pi / LEVELS)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[3:7]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_items(og, ffi, d_in, d_out, lattice_handle, keep):
+    """One osgpu_trace_item per band: DOE -> aperture -> lens -> ASM z."""
+    items = (ffi.TraceItemC * NBANDS)()
+    for b in range(NBANDS):
+        doe = ffi.ElementC(4, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+                           C.cast(C.c_void_p(lattice_handle), ffi.c_double_p), N, N, DX, DX, 1)
+        ap = ffi.ElementC(2, 0, HALF_AP, HALF_AP, 0, 0, 0, 0, 0, 0, None, 0, 0, 0, 0, 0)
+        lens = ffi.ElementC(3, 0, 0, 0, 0, 0, 0, F_LENS, 0, 0, None, 0, 0, 0, 0, 0)
+        e1 = (ffi.ElementC * 1)(doe)
+        e2 = (ffi.ElementC * 1)(ap)
+        e3 = (ffi.ElementC * 1)(lens)
+        steps = (ffi.StepC * 3)(ffi.StepC(e1, 1, 0.0, 1.0), ffi.StepC(e2, 1, 0.0, 1.0),
+                                ffi.StepC(e3, 1, Z, 1.0))
+        keep.extend([e1, e2, e3, steps])
+        items[b] = ffi.TraceItemC(d_in[b], d_out[b], ffi.Grid(N, N, DX, DX, float(LAMS[b])),
+                                  steps, 3)
+    return items
+
+
+def run_batch(og, ffi, items, dtype, stream):
+    cfg = ffi.AsmConfigC(2.0, 1, 1, 8.0, 1.0)
+    code = og.lib().osgpu_beamline_trace_batch_device(items, NBANDS, cfg, dtype, stream, None, 0)
+    ffi.check(code)
+
+
+def cpu_baseline_band0():
+    """Bounded CPU sample: band 0 through the f64 oracle, one thread."""
+    from oracle import field as ofield, element as oel, beamline as obl, asm as oasm
+    lat = doe_lattice()
+    t0 = time.perf_counter()
+    b = ofield.plane_wave(0.0, 0.0, 1.0, N, N, DX, DX, float(LAMS[0]))
+    bl = obl.Beamline()
+    bl.push(oel.PhaseMask.sampled(lat, (N, N), (DX, DX)), 0.0)
+    bl.push(oel.RectangularAperture((HALF_AP, HALF_AP)), 0.0)
+    bl.push(oel.ThinLens.fixed(F_LENS), Z)
+    out = bl.trace(b, obl.asm_engine(oasm.AsmConfig()))
+    dt = time.perf_counter() - t0
+    return out.samples, dt
+
+
+def reference_arm(args):
+    """--impl reference: the f64 oracle port on all usable host cores, one
+    band per worker process per step (spawned processes, no GPU)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    try:
+        with open("/proc/meminfo") as f:
+            kb = int([ln for ln in f if ln.startswith("MemAvailable")][0].split()[1])
+        mem_workers = max(1, int(kb / 1024 / 1024 // 8))  # ~8 GB per band at P = 8192
+    except (OSError, IndexError, ValueError):
+        mem_workers = 4
+    workers = max(1, min(cores, mem_workers, NBANDS))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_worker, range(workers))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            pool.map(_ref_worker, range(workers))
+        dt = time.perf_counter() - t0
+    props = workers * args.steps
+    val = props / dt
+    line = {"metric": METRIC, "value": val, "unit": "propagations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": f"{workers} bands, one per worker process"},
+            "cpu_baseline": {"value": val, "unit": "propagations/s", "cores": workers,
+                             "kind": "port",
+                             "sample": f"{workers} of the 32 bands per step, f64 oracle "
+                                       f"(numpy/pocketfft) restatement, one process per band"},
+            "e2e": {"value": val, "unit": "propagations/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _ref_worker(i):
+    sys.path.insert(0, ROOT)
+    _, dt = cpu_baseline_band0()
+    return dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import _ffi as ffi
+    L = og.lib()
+    ffi.check(L.osgpu_init(local))
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    lat = doe_lattice()
+    handle = C.c_void_p()
+    ffi.check(L.osgpu_lattice_create(lat.ctypes.data_as(ffi.c_double_p), N, N, C.byref(handle)))
+
+    # device-resident batch: inputs (unit plane wave) and outputs, complex64
+    fin = torch.ones((NBANDS, N, N), dtype=torch.complex64, device="cuda")
+    fout = torch.empty_like(fin)
+    d_in = [fin[b].data_ptr() for b in range(NBANDS)]
+    d_out = [fout[b].data_ptr() for b in range(NBANDS)]
+    keep = []
+    items = make_items(og, ffi, d_in, d_out, handle.value, keep)
+
+    for _ in range(args.warmup):
+        run_batch(og, ffi, items, ffi.C64, sptr)
+    torch.cuda.synchronize()
+    ffi.check(L.osgpu_sync_status())
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = L.osgpu_launch_count()
+    ffi.check(L.osgpu_profile_begin())
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        run_batch(og, ffi, items, ffi.C64, sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_total = e0.elapsed_time(e1)
+    stats = (ffi.KernelStatC * 16)()
+    nst = C.c_int32()
+    ffi.check(L.osgpu_profile_end(stats, 16, C.byref(nst)))
+    launches = L.osgpu_launch_count() - launches0
+    clk = clocks.stop()
+    ffi.check(L.osgpu_sync_status())
+
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = NBANDS * world / (ms_step / 1e3)
+
+    kstats = {}
+    for i in range(nst.value):
+        s = stats[i]
+        kstats[s.name.decode()] = {"launches": int(s.launches), "total_ms": s.total_ms,
+                                   "bytes": s.bytes}
+    dom = max(kstats.items(), key=lambda kv: kv[1]["total_ms"])
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f).get("hbm_gbs", peak))
+        peak_src = "measured"
+    dname, d = dom
+    per_launch_bytes = d["bytes"] / d["launches"]
+    per_launch_ms = d["total_ms"] / d["launches"]
+    achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+    all_bytes = sum(v["bytes"] for v in kstats.values())
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(dname)
+
+    line = {"metric": METRIC, "value": value, "unit": "propagations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "bands_per_gpu": NBANDS, "grid": N, "padded": 8192,
+                       "l2": "inputs larger than L2 (1 GiB field batch + 134 MB spectrum per band)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_src,
+                         "bytes_per_launch": per_launch_bytes,
+                         "ms_per_launch": per_launch_ms},
+            "kernels": kstats,
+            "whole_step_hbm_gbs": all_bytes / args.steps / (ms_step / 1e3) / 1e9,
+            "clocks": clk, "gpu_launches": int(launches)}
+
+    # plain FP64 path on the same batch (device resident complex128)
+    if not args.no_f64 and rank == 0:
+        nb64 = 8
+        fin64 = torch.ones((nb64, N, N), dtype=torch.complex128, device="cuda")
+        fout64 = torch.empty_like(fin64)
+        k2 = []
+        it64 = make_items(og, ffi, [fin64[i % nb64].data_ptr() for i in range(NBANDS)],
+                          [fout64[i % nb64].data_ptr() for i in range(NBANDS)], handle.value, k2)
+        sub = (ffi.TraceItemC * nb64)(*[it64[i * (NBANDS // nb64)] for i in range(nb64)])
+        cfg = ffi.AsmConfigC(2.0, 1, 1, 8.0, 1.0)
+        ffi.check(L.osgpu_beamline_trace_batch_device(sub, nb64, cfg, ffi.C128, sptr, None, 0))
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ffi.check(L.osgpu_beamline_trace_batch_device(sub, nb64, cfg, ffi.C128, sptr, None, 0))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        v64 = nb64 / (ms64 / 1e3)
+        line["f64_plain"] = {"value": v64, "unit": "propagations/s",
+                             "sample": f"{nb64} of the 32 bands, complex128 resident"}
+        line["speedup_vs_f64"] = value / world / v64
+        del fin64, fout64
+
+    # end to end through the reference-facing host-buffer ABI
+    if not args.no_e2e:
+        host_in = torch.ones((NBANDS, N, N), dtype=torch.complex128).pin_memory()
+        host_out = torch.empty((NBANDS, N, N), dtype=torch.complex128).pin_memory()
+        cfg = ffi.AsmConfigC(2.0, 1, 1, 8.0, 1.0)
+
+        def e2e_step():
+            for b in range(NBANDS):
+                it = items[b]
+                code = L.osgpu_beamline_trace(
+                    C.cast(C.c_void_p(host_in[b].data_ptr()), ffi.c_double_p),
+                    C.cast(C.c_void_p(host_out[b].data_ptr()), ffi.c_double_p),
+                    C.byref(it.grid), it.steps, 3, cfg, ffi.F32, None)
+                ffi.check(code)
+
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        nrep = max(1, min(args.steps, 3))
+        for _ in range(nrep):
+            e2e_step()
+        dt = (time.perf_counter() - t0) / nrep
+        barrier()
+        line["e2e"] = {"value": NBANDS * world / dt, "unit": "propagations/s",
+                       "h2d_bytes_per_step": NBANDS * N * N * 16,
+                       "d2h_bytes_per_step": NBANDS * N * N * 16,
+                       "api": "osgpu_beamline_trace (host complex128, pinned), f32 engine"}
+
+    # accuracy of band 0 against the f64 oracle + bounded CPU baseline
+    if rank == 0 and not args.no_cpu_baseline:
+        ref, dt_cpu = cpu_baseline_band0()
+        got = fout[0].cpu().numpy().astype(np.complex128)
+        line["rel_l2_vs_oracle_band0"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        line["cpu_baseline"] = {"value": 1.0 / dt_cpu, "unit": "propagations/s", "cores": 1,
+                                "kind": "port",
+                                "sample": "band 0 (450 nm) of the batch: 2048^2 DOE + aperture + "
+                                          "lens + ASM at 8192^2, f64 oracle (numpy), 1 thread"}
+    L.osgpu_lattice_destroy(handle)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -235,10 +235,22 @@ typedef struct {
   double center_x, center_y;
   double focal;          /* thin lens: f(lambda) */
   double period, depth;  /* blazed grating */
-  const double* lattice; /* sampled phase, row-major lny x lnx, host memory */
+  const double* lattice; /* sampled phase, row-major lny x lnx */
   uint64_t lnx, lny;
   double ldx, ldy;
+  int32_t lattice_on_device; /* 0: `lattice` is host memory (scanned for non-finite
+                                values as PhaseMask::sampled does, then uploaded);
+                                1: device memory, used in place (the caller owns the
+                                finiteness guarantee) */
 } osgpu_element;
+
+/* Device copy of a sampled phase lattice, created once (PhaseMask::sampled,
+ * element.rs:1321-1368: the lattice is scanned for non-finite values here,
+ * OSGPU_E_INVALID_PHASE).  `*handle` is a device pointer to the f64 lattice
+ * usable as osgpu_element.lattice with lattice_on_device = 1; the library
+ * also keeps an f32 copy for the f32 engine.  Destroy when no call uses it. */
+int osgpu_lattice_create(const double* host, uint64_t lnx, uint64_t lny, void** handle);
+int osgpu_lattice_destroy(void* handle);
 
 /* Element::apply of each element in order (pointwise transmission). */
 int osgpu_apply_elements(const double* in, double* out, const osgpu_grid* g,
@@ -261,6 +273,40 @@ typedef struct {
 int osgpu_beamline_trace(const double* in, double* out, const osgpu_grid* g,
                          const osgpu_step* steps, int32_t n_steps, const osgpu_asm_config* cfg,
                          int32_t precision, osgpu_asm_report* reports);
+
+/* Batched, device-resident Beamline::trace with the ASM engine: one item per
+ * band (or independent propagation).  d_in/d_out are device fields of
+ * `dtype` (may alias); items may differ in grid size, wavelength, distances
+ * and elements.  Asynchronous on `stream` (NULL: the library stream); a
+ * non-finite input is reported by osgpu_sync_status.  `reports` (optional)
+ * receives n_items * reports_stride reports, item-major. */
+typedef struct {
+  const void* d_in;
+  void* d_out;
+  osgpu_grid grid;
+  const osgpu_step* steps;
+  int32_t n_steps;
+} osgpu_trace_item;
+
+int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_items,
+                                      const osgpu_asm_config* cfg, int32_t dtype, void* stream,
+                                      osgpu_asm_report* reports, int32_t reports_stride);
+
+/* --------------------------------------------------------------- profiling */
+/* Per-kernel-class CUDA-event timing on the launching stream.  Between
+ * osgpu_profile_begin and osgpu_profile_end every pass launch is bracketed by
+ * events; _end synchronises and returns, per class, the launch count, total
+ * device time and the algorithmic bytes those launches move (reads of the
+ * inputs they must read + writes of their outputs). */
+typedef struct {
+  char name[32];
+  uint64_t launches;
+  double total_ms;
+  double bytes;
+} osgpu_kernel_stat;
+
+int osgpu_profile_begin(void);
+int osgpu_profile_end(osgpu_kernel_stat* out, int32_t max_out, int32_t* n_out);
 
 /* ---------------------------------------------------------------- runtime */
 int osgpu_init(int32_t device);

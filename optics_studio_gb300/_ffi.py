@@ -92,12 +92,22 @@ class ElementC(C.Structure):
                 ("orientation", C.c_double), ("center_x", C.c_double), ("center_y", C.c_double),
                 ("focal", C.c_double), ("period", C.c_double), ("depth", C.c_double),
                 ("lattice", c_double_p), ("lnx", C.c_uint64), ("lny", C.c_uint64),
-                ("ldx", C.c_double), ("ldy", C.c_double)]
+                ("ldx", C.c_double), ("ldy", C.c_double), ("lattice_on_device", C.c_int32)]
 
 
 class StepC(C.Structure):
     _fields_ = [("elements", C.POINTER(ElementC)), ("n_elements", C.c_int32),
                 ("z_after", C.c_double), ("medium", C.c_double)]
+
+
+class TraceItemC(C.Structure):
+    _fields_ = [("d_in", C.c_void_p), ("d_out", C.c_void_p), ("grid", Grid),
+                ("steps", C.POINTER(StepC)), ("n_steps", C.c_int32)]
+
+
+class KernelStatC(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double),
+                ("bytes", C.c_double)]
 
 
 # (name, restype, argtypes) for every symbol of include/osgpu.h
@@ -138,6 +148,14 @@ SIGNATURES = [
     ("osgpu_beamline_trace", C.c_int,
      [c_double_p, c_double_p, C.POINTER(Grid), C.POINTER(StepC), C.c_int32,
       C.POINTER(AsmConfigC), C.c_int32, C.POINTER(AsmReportC)]),
+    ("osgpu_beamline_trace_batch_device", C.c_int,
+     [C.POINTER(TraceItemC), C.c_int32, C.POINTER(AsmConfigC), C.c_int32, C.c_void_p,
+      C.POINTER(AsmReportC), C.c_int32]),
+    ("osgpu_lattice_create", C.c_int,
+     [c_double_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("osgpu_lattice_destroy", C.c_int, [C.c_void_p]),
+    ("osgpu_profile_begin", C.c_int, []),
+    ("osgpu_profile_end", C.c_int, [C.POINTER(KernelStatC), C.c_int32, C.POINTER(C.c_int32)]),
 ]
 
 _lib = None

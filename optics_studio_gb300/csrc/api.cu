@@ -38,12 +38,28 @@ void set_err(const char* fmt, ...) {
   va_end(ap);
 }
 
+// Per-kernel-class event timing (osgpu_profile_begin/end).
+struct ProfRec {
+  int cls;
+  cudaEvent_t a, b;
+  double bytes;
+};
+enum { PC_PREP = 0, PC_ELEMENTS, PC_APPLY, PC_PASS_A, PC_PASS_B, PC_PASS_C, PC_KSPEC, PC_FRAUN,
+       PC_N };
+const char* kProfNames[PC_N] = {"prep_tables", "element_tables", "element_apply",
+                                "pass_a_rows", "pass_b_columns", "pass_c_rows",
+                                "kernel_spectrum", "fraunhofer"};
+
 struct Context {
   std::recursive_mutex mu;
   int device = -1;
   cudaStream_t stream = nullptr;
   int* d_status = nullptr;
   std::map<std::pair<int, int>, void*> tw;  // (n, is_double) -> twiddle table
+  bool profiling = false;
+  std::vector<ProfRec> prof;
+  std::vector<cudaEvent_t> event_pool;
+  std::map<const void*, float*> lattices;  // osgpu_lattice_create handle -> f32 copy
 };
 
 Context& ctx() {
@@ -100,6 +116,42 @@ struct DBuf {
   }
 };
 
+cudaEvent_t pool_event(Context& c) {
+  if (!c.event_pool.empty()) {
+    cudaEvent_t e = c.event_pool.back();
+    c.event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets one launch group with events when profiling.
+struct ProfScope {
+  Context& c;
+  cudaStream_t st;
+  int cls;
+  double bytes;
+  cudaEvent_t a = nullptr;
+  ProfScope(Context& c_, cudaStream_t st_, int cls_, double bytes_)
+      : c(c_), st(st_), cls(cls_), bytes(bytes_) {
+    if (c.profiling) {
+      a = pool_event(c);
+      cudaEventRecord(a, st);
+    }
+  }
+  ~ProfScope() {
+    if (c.profiling && a) {
+      cudaEvent_t b = pool_event(c);
+      cudaEventRecord(b, st);
+      c.prof.push_back(ProfRec{cls, a, b, bytes});
+    }
+  }
+};
+
+// Twiddle tables are cached per (n, precision) and shared by every stream:
+// the first build is synchronised so later users on any stream see it.
 int get_tw(Context& c, int n, int is_d, const void** out) {
   auto key = std::make_pair(n, is_d);
   auto it = c.tw.find(key);
@@ -110,15 +162,18 @@ int get_tw(Context& c, int n, int is_d, const void** out) {
   void* p = nullptr;
   CK(cudaMalloc(&p, (size_t)(n > 0 ? n : 1) * (is_d ? 16 : 8)));
   CK(launch_twiddles(p, n, is_d, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
   c.tw[key] = p;
   *out = p;
   return OSGPU_OK;
 }
 
-// Device element list + uploaded lattices (kept alive for the call).
+// Device element list + uploaded lattices and fast tables (kept alive for
+// the call; freed stream-ordered).
 struct Elements {
   ElementList list;
   std::vector<DBuf> lattices;
+  DBuf tables;
 };
 
 int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid& g,
@@ -140,7 +195,9 @@ int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid
       set_err("element %d: %s (status %d)", i, msg, st);
       return st;
     }
-    if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED) {
+    if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED && els[i].lattice_on_device) {
+      d.lat = els[i].lattice;
+    } else if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED) {
       const size_t bytes = (size_t)els[i].lnx * els[i].lny * sizeof(double);
       DBuf b;
       CK(b.alloc(bytes, c.stream));
@@ -151,6 +208,39 @@ int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid
     E.list.el[E.list.count++] = d;
   }
   return OSGPU_OK;
+}
+
+// f32 engine: build the FP64-derived fast tables of every element of `L`
+// for grid `g`; L.fast = 1 when all elements qualify (orientation 0).
+int build_fast_tables(Context& c, ElementList& L, const osgpu_grid& g, DBuf& keep,
+                      cudaStream_t st) {
+  L.fast = 0;
+  if (L.count == 0) return OSGPU_OK;
+  size_t bytes = 0;
+  for (int q = 0; q < L.count; ++q) {
+    if (L.el[q].psi != 0.0) return OSGPU_OK;
+    bytes += element_tables_bytes(L.el[q], (int)g.nx, (int)g.ny);
+  }
+  CK(keep.alloc(bytes, st));
+  ProfScope ps(c, st, PC_ELEMENTS, 0.0);
+  char* p = reinterpret_cast<char*>(keep.p);
+  for (int q = 0; q < L.count; ++q) {
+    DevElement& e = L.el[q];
+    auto hit = c.lattices.find(e.lat);
+    e.latf = (e.kind == EL_PHASE && hit != c.lattices.end()) ? hit->second : nullptr;
+    CK(launch_element_tables(e, (int)g.nx, (int)g.ny, g.dx, g.dy, p, st));
+    p += element_tables_bytes(e, (int)g.nx, (int)g.ny);
+  }
+  L.fast = 1;
+  return OSGPU_OK;
+}
+
+// Algorithmic bytes of the lattice reads of one plane's elements.
+double element_bytes(const ElementList& L, int f32) {
+  double b = 0;
+  for (int q = 0; q < L.count; ++q)
+    if (L.el[q].kind == EL_PHASE) b += (double)L.el[q].lnx * L.el[q].lny * (f32 ? 4 : 8);
+  return b;
 }
 
 bool host_all_finite(const double* p, size_t n_doubles) {
@@ -283,10 +373,12 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
       a.h_mode = is_d ? 0 : 1;
     }
     a.Kf = (float)a.kz;
+    ProfScope ps(c, st, PC_PREP, 0.0);
     CK(launch_asm_prep<T>(a, nullptr, st));
   } else if (j.engine == ENG_KSEP) {
     a.hx = base + o_hx;
     a.hy = base + o_hy;
+    ProfScope ps(c, st, PC_KSPEC, 0.0);
     CK(launch_fresnel_ksep<T>(a, base + o_hx, base + o_hy, base + o_tmp, st));
   } else if (j.engine == ENG_KSPEC) {
     PropArgs b = a;
@@ -297,12 +389,27 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
       set_err("kernel-spectrum build of %zux%zu exceeds the shared-memory plan", Px, Py);
       return OSGPU_E_UNSUPPORTED;
     }
+    ProfScope ps(c, st, PC_KSPEC, 0.0);
     CK(launch_rs_kspec<T>(b, base + o_ks, base + o_tmp, st));
     a.kspec = base + o_ks;
   }
-  CK(launch_passA<T>(a, st));
-  CK(launch_passB<T>(a, st));
-  CK(launch_passC<T>(a, st));
+  const double nin = (double)j.g.nx * j.g.ny, nsp = (double)Px * ny;
+  {
+    ProfScope ps(c, st, PC_PASS_A,
+                 nin * (j.in_c128 ? 16 : 8) + nsp * es + element_bytes(j.els, !is_d));
+    CK(launch_passA<T>(a, st));
+  }
+  {
+    ProfScope ps(c, st, PC_PASS_B,
+                 2 * nsp * es + (j.engine == ENG_KSPEC ? (double)Px * Py * es : 0.0));
+    CK(launch_passB<T>(a, st));
+  }
+  {
+    const double ob = (j.d_out ? (j.out_c128 ? 16 : 8) : 0) + (j.d_int ? 4 : 0) +
+                      (j.d_int64 ? 8 : 0);
+    ProfScope ps(c, st, PC_PASS_C, nsp * es + nin * ob);
+    CK(launch_passC<T>(a, st));
+  }
   return OSGPU_OK;
 }
 
@@ -421,6 +528,7 @@ int run_fraun(Context& c, const osgpu_grid& g, double z, const osgpu_fraunhofer_
   a.quad_im = (cim * dre - cre * dim) / ns;
   a.adjoint = adjoint;
   a.status = c.d_status;
+  ProfScope ps(c, st, PC_FRAUN, (double)a.nx * a.ny * (es + 2 * es + es));
   CK(launch_fraunhofer<T>(a, st));
   return OSGPU_OK;
 }
@@ -472,9 +580,9 @@ int osgpu_sync_status(void) {
   int rc = ensure_init(c);
   if (rc) return rc;
   int status = 0;
-  CK(cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  CK(cudaStreamSynchronize(c.stream));
-  CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream));
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemset(c.d_status, 0, sizeof(int)));
   if (status) {
     set_err("field contains non-finite samples");
     return OSGPU_E_NON_FINITE_SAMPLE;
@@ -713,8 +821,11 @@ int osgpu_apply_elements(const double* in, double* out, const osgpu_grid* g,
   if ((rc = ensure_init(c))) return rc;
   Elements E;
   if ((rc = build_elements(c, els, n_els, *g, E))) return rc;
+  if (precision == OSGPU_F32 && (rc = build_fast_tables(c, E.list, *g, E.tables, c.stream)))
+    return rc;
   const size_t n = g->nx * g->ny;
   return host_call(c, in, out, n, [&](const void* din, void* dout) {
+    ProfScope ps(c, c.stream, PC_APPLY, (double)n * 32);
     cudaError_t e = precision == OSGPU_F32
                         ? launch_apply_elements<float>(din, 1, dout, 1, E.list, (int)g->nx,
                                                        (int)g->ny, g->dx, g->dy, nullptr, c.stream)
@@ -725,7 +836,160 @@ int osgpu_apply_elements(const double* in, double* out, const osgpu_grid* g,
   });
 }
 
+int osgpu_lattice_create(const double* host, uint64_t lnx, uint64_t lny, void** handle) {
+  if (!host || !handle) return OSGPU_E_BAD_ARGUMENT;
+  if (lnx == 0 || lny == 0) return OSGPU_E_INVALID_GRID;
+  const size_t n = lnx * lny;
+  for (size_t k = 0; k < n; ++k)
+    if (!std::isfinite(host[k])) {
+      set_err("lattice value %zu is not finite", k);
+      return OSGPU_E_INVALID_PHASE;
+    }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc = ensure_init(c);
+  if (rc) return rc;
+  void* d64 = nullptr;
+  float* d32 = nullptr;
+  CK(cudaMalloc(&d64, n * sizeof(double)));
+  CK(cudaMalloc(reinterpret_cast<void**>(&d32), n * sizeof(float)));
+  std::vector<float> h32(n);
+  for (size_t k = 0; k < n; ++k) h32[k] = (float)host[k];
+  CK(cudaMemcpy(d64, host, n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d32, h32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  c.lattices[d64] = d32;
+  *handle = d64;
+  return OSGPU_OK;
+}
+
+int osgpu_lattice_destroy(void* handle) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  auto it = c.lattices.find(handle);
+  if (it == c.lattices.end()) return OSGPU_E_BAD_ARGUMENT;
+  CK(cudaDeviceSynchronize());
+  cudaFree(it->second);
+  cudaFree(handle);
+  c.lattices.erase(it);
+  return OSGPU_OK;
+}
+
 // ------------------------------------------------------------- beamline
+
+}  // extern "C"
+
+namespace {
+
+// Validates every step of one beamline in trace order (beamline.rs:109-127):
+// element errors, then the engine's; the first failure wins.  Builds the
+// device element lists (and the f32 fast tables) and the per-step reports.
+int prepare_trace(Context& c, const double* host_in, size_t n, const osgpu_grid& g,
+                  const osgpu_step* steps, int n_steps, const osgpu_asm_config& cfg, int f32,
+                  std::vector<Elements>& E, std::vector<osgpu_asm_report>& R, cudaStream_t st) {
+  E.clear();
+  E.resize(n_steps > 0 ? n_steps : 0);
+  R.assign(n_steps > 0 ? n_steps : 0, osgpu_asm_report());
+  int first_prop = -1;
+  for (int s = 0; s < n_steps; ++s) {
+    int rc = build_elements(c, steps[s].elements, steps[s].n_elements, g, E[s]);
+    if (rc) {
+      if (first_prop >= 0 && first_prop < s) rc = scan_then(host_in, n, rc);
+      return rc;
+    }
+    if (f32 && (rc = build_fast_tables(c, E[s].list, g, E[s].tables, st))) return rc;
+    std::memset(&R[s], 0, sizeof(R[s]));
+    if (steps[s].z_after != 0.0) {
+      osgpu_asm_config sc = cfg;
+      sc.medium = steps[s].medium;
+      rc = asm_resolve(g, steps[s].z_after, sc, R[s]);
+      if (rc > 0) {
+        if (rc == OSGPU_E_ALIASING_RISK || (first_prop >= 0 && first_prop < s))
+          rc = scan_then(host_in, n, rc);
+        set_err("beamline step %d: propagation failed (status %d)", s, rc);
+        return rc;
+      }
+      if (first_prop < 0) first_prop = s;
+    }
+  }
+  return OSGPU_OK;
+}
+
+// Runs one prepared beamline on the device: elements of consecutive planes
+// are merged and fused into the first pass of the propagation that follows
+// them; trailing elements run as one element kernel.
+int run_trace(Context& c, const void* d_in, int in_c128, void* d_out, int out_c128,
+              const osgpu_grid& g, const osgpu_step* steps, int n_steps, std::vector<Elements>& E,
+              const std::vector<osgpu_asm_report>& R, const osgpu_asm_config& cfg, int f32,
+              cudaStream_t st) {
+  const size_t n = g.nx * g.ny;
+  const size_t es = f32 ? 8 : 16;
+  DBuf work;
+  CK(work.alloc(n * es, st));
+  int last_prop = -1;
+  for (int s = 0; s < n_steps; ++s)
+    if (steps[s].z_after != 0.0) last_prop = s;
+  bool tail_elements = false;
+  for (int s = last_prop + 1; s < n_steps; ++s)
+    if (E[s].list.count) tail_elements = true;
+
+  auto apply = [&](const void* src, int src_c, void* dst, int dst_c, const ElementList& L) {
+    ProfScope ps(c, st, PC_APPLY, (double)n * ((src_c ? 16 : 8) + (dst_c ? 16 : 8)));
+    cudaError_t e =
+        f32 ? launch_apply_elements<float>(src, src_c, dst, dst_c, L, (int)g.nx, (int)g.ny, g.dx,
+                                           g.dy, c.d_status, st)
+            : launch_apply_elements<double>(src, src_c, dst, dst_c, L, (int)g.nx, (int)g.ny,
+                                            g.dx, g.dy, c.d_status, st);
+    return e == cudaSuccess ? OSGPU_OK : cuda_fail(e, "apply_elements");
+  };
+
+  const void* src = d_in;
+  int src_c = in_c128;
+  ElementList pending;
+  std::memset(&pending, 0, sizeof(pending));
+  bool pending_fast = true;
+  int rc;
+  for (int s = 0; s < n_steps; ++s) {
+    for (int q = 0; q < E[s].list.count; ++q) {
+      if (pending.count == kMaxElements) {
+        pending.fast = f32 && pending_fast;
+        if ((rc = apply(src, src_c, work.p, !f32, pending))) return rc;
+        src = work.p;
+        src_c = !f32;
+        pending.count = 0;
+        pending_fast = true;
+      }
+      pending.el[pending.count++] = E[s].list.el[q];
+      pending_fast = pending_fast && E[s].list.fast;
+    }
+    if (steps[s].z_after != 0.0) {
+      osgpu_asm_config sc = cfg;
+      sc.medium = steps[s].medium;
+      PropJob j;
+      fill_asm_job(j, g, steps[s].z_after, R[s], sc);
+      pending.fast = f32 && pending_fast;
+      j.els = pending;
+      j.d_in = src;
+      j.in_c128 = src_c;
+      const bool final_write = (s == last_prop && !tail_elements);
+      j.d_out = final_write ? d_out : work.p;
+      j.out_c128 = final_write ? out_c128 : !f32;
+      if ((rc = run_prop_dispatch(c, j, f32, st))) return rc;
+      src = j.d_out;
+      src_c = j.out_c128;
+      pending.count = 0;
+      pending_fast = true;
+    }
+  }
+  if (pending.count > 0 || src != d_out) {
+    pending.fast = f32 && pending_fast;
+    if ((rc = apply(src, src_c, d_out, out_c128, pending))) return rc;
+  }
+  return OSGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
 
 int osgpu_beamline_trace(const double* in, double* out, const osgpu_grid* g,
                          const osgpu_step* steps, int32_t n_steps, const osgpu_asm_config* cfg,
@@ -733,92 +997,106 @@ int osgpu_beamline_trace(const double* in, double* out, const osgpu_grid* g,
   int rc;
   if ((rc = check_grid(g)) || (rc = check_precision(precision))) return rc;
   if (!cfg || !in || !out || n_steps < 0 || (n_steps > 0 && !steps)) return OSGPU_E_BAD_ARGUMENT;
+  if (g->nx == 0 || g->ny == 0) return OSGPU_E_EMPTY_GRID;
   const size_t n = g->nx * g->ny;
   Context& c = ctx();
   std::lock_guard<std::recursive_mutex> lk(c.mu);
   if ((rc = ensure_init(c))) return rc;
-  // Validate every step in trace order (beamline.rs:109-127): element
-  // errors, then the engine's; the first failure wins.
-  std::vector<Elements> E(n_steps > 0 ? n_steps : 1);
-  std::vector<osgpu_asm_report> R(n_steps > 0 ? n_steps : 1);
-  int first_prop = -1;
-  for (int s = 0; s < n_steps; ++s) {
-    if ((rc = build_elements(c, steps[s].elements, steps[s].n_elements, *g, E[s]))) {
-      if (first_prop >= 0 && first_prop < s) rc = scan_then(in, n, rc);
+  const int f32 = precision == OSGPU_F32;
+  std::vector<Elements> E;
+  std::vector<osgpu_asm_report> R;
+  rc = prepare_trace(c, in, n, *g, steps, n_steps, *cfg, f32, E, R, c.stream);
+  if (reports)
+    for (int s = 0; s < n_steps && s < (int)R.size(); ++s) reports[s] = R[s];
+  if (rc) {
+    cudaStreamSynchronize(c.stream);
+    return rc;
+  }
+  return host_call(c, in, out, n, [&](const void* din, void* dout) {
+    return run_trace(c, din, 1, dout, 1, *g, steps, n_steps, E, R, *cfg, f32, c.stream);
+  });
+}
+
+int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_items,
+                                      const osgpu_asm_config* cfg, int32_t dtype, void* stream,
+                                      osgpu_asm_report* reports, int32_t reports_stride) {
+  if (!items || n_items < 0 || !cfg || (dtype != OSGPU_C128 && dtype != OSGPU_C64))
+    return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f32 = dtype == OSGPU_C64;
+  const int c128 = dtype == OSGPU_C128;
+  for (int i = 0; i < n_items; ++i) {
+    const osgpu_trace_item& it = items[i];
+    if (!it.d_in || !it.d_out || it.n_steps < 0 || (it.n_steps > 0 && !it.steps))
+      return OSGPU_E_BAD_ARGUMENT;
+    if (it.grid.nx == 0 || it.grid.ny == 0) return OSGPU_E_EMPTY_GRID;
+    std::vector<Elements> E;
+    std::vector<osgpu_asm_report> R;
+    rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, st);
+    if (reports && reports_stride > 0)
+      for (int s = 0; s < it.n_steps && s < reports_stride && s < (int)R.size(); ++s)
+        reports[(size_t)i * reports_stride + s] = R[s];
+    if (rc) {
+      set_err("batch item %d: %s", i, t_err);
       return rc;
     }
-    std::memset(&R[s], 0, sizeof(R[s]));
-    if (steps[s].z_after != 0.0) {
-      osgpu_asm_config sc = *cfg;
-      sc.medium = steps[s].medium;
-      rc = asm_resolve(*g, steps[s].z_after, sc, R[s]);
-      if (rc > 0) {
-        if (rc == OSGPU_E_ALIASING_RISK || (first_prop >= 0 && first_prop < s))
-          rc = scan_then(in, n, rc);
-        set_err("beamline step %d: propagation failed (status %d)", s, rc);
-        if (reports) reports[s] = R[s];
-        return rc;
-      }
-      if (first_prop < 0) first_prop = s;
-    }
-    if (reports) reports[s] = R[s];
+    if ((rc = run_trace(c, it.d_in, c128, it.d_out, c128, it.grid, it.steps, it.n_steps, E, R,
+                        *cfg, f32, st)))
+      return rc;
   }
-  return host_call(c, in, out, n, [&](const void* din, void* dout) -> int {
-    const int f32 = precision == OSGPU_F32;
-    // Working buffer in the engine precision; the first pass reads din.
-    ElementList pending;
-    std::memset(&pending, 0, sizeof(pending));
-    const void* src = din;
-    int src_c128 = 1;
-    DBuf cur;
-    const size_t es = f32 ? 8 : 16;
-    cudaError_t e = cur.alloc(n * es, c.stream);
-    if (e != cudaSuccess) return cuda_fail(e, "alloc");
-    for (int s = 0; s < n_steps; ++s) {
-      for (int q = 0; q < E[s].list.count; ++q) {
-        if (pending.count == kMaxElements) {
-          e = f32 ? launch_apply_elements<float>(src, src_c128, cur.p, 0, pending, (int)g->nx,
-                                                 (int)g->ny, g->dx, g->dy, nullptr, c.stream)
-                  : launch_apply_elements<double>(src, src_c128, cur.p, 1, pending, (int)g->nx,
-                                                  (int)g->ny, g->dx, g->dy, nullptr, c.stream);
-          if (e != cudaSuccess) return cuda_fail(e, "apply_elements");
-          src = cur.p;
-          src_c128 = !f32;
-          pending.count = 0;
-        }
-        pending.el[pending.count++] = E[s].list.el[q];
-      }
-      if (steps[s].z_after != 0.0) {
-        osgpu_asm_config sc = *cfg;
-        sc.medium = steps[s].medium;
-        PropJob j;
-        fill_asm_job(j, *g, steps[s].z_after, R[s], sc);
-        j.els = pending;
-        j.d_in = src;
-        j.in_c128 = src_c128;
-        j.d_out = cur.p;
-        j.out_c128 = !f32;
-        int r2 = run_prop_dispatch(c, j, f32, c.stream);
-        if (r2) return r2;
-        src = cur.p;
-        src_c128 = !f32;
-        pending.count = 0;
-      }
+  return OSGPU_OK;
+}
+
+// ------------------------------------------------------------ profiling
+
+int osgpu_profile_begin(void) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc = ensure_init(c);
+  if (rc) return rc;
+  for (auto& r : c.prof) {
+    c.event_pool.push_back(r.a);
+    c.event_pool.push_back(r.b);
+  }
+  c.prof.clear();
+  c.profiling = true;
+  return OSGPU_OK;
+}
+
+int osgpu_profile_end(osgpu_kernel_stat* out, int32_t max_out, int32_t* n_out) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc = ensure_init(c);
+  if (rc) return rc;
+  c.profiling = false;
+  CK(cudaDeviceSynchronize());
+  osgpu_kernel_stat agg[PC_N];
+  std::memset(agg, 0, sizeof(agg));
+  for (auto& r : c.prof) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    agg[r.cls].launches += 1;
+    agg[r.cls].total_ms += ms;
+    agg[r.cls].bytes += r.bytes;
+    c.event_pool.push_back(r.a);
+    c.event_pool.push_back(r.b);
+  }
+  c.prof.clear();
+  int k = 0;
+  for (int q = 0; q < PC_N; ++q) {
+    if (!agg[q].launches) continue;
+    if (out && k < max_out) {
+      out[k] = agg[q];
+      std::snprintf(out[k].name, sizeof(out[k].name), "%s", kProfNames[q]);
     }
-    if (pending.count > 0 || src == din) {
-      e = f32 ? launch_apply_elements<float>(src, src_c128, dout, 1, pending, (int)g->nx,
-                                             (int)g->ny, g->dx, g->dy, nullptr, c.stream)
-              : launch_apply_elements<double>(src, src_c128, dout, 1, pending, (int)g->nx,
-                                              (int)g->ny, g->dx, g->dy, nullptr, c.stream);
-      if (e != cudaSuccess) return cuda_fail(e, "apply_elements");
-    } else {
-      e = f32 ? launch_apply_elements<float>(src, 0, dout, 1, pending, (int)g->nx, (int)g->ny,
-                                             g->dx, g->dy, nullptr, c.stream)
-              : cudaMemcpyAsync(dout, src, n * 16, cudaMemcpyDeviceToDevice, c.stream);
-      if (e != cudaSuccess) return cuda_fail(e, "copy out");
-    }
-    return OSGPU_OK;
-  });
+    ++k;
+  }
+  if (n_out) *n_out = k;
+  return OSGPU_OK;
 }
 
 }  // extern "C"

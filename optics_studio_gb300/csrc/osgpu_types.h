@@ -57,17 +57,18 @@ struct DevElement {
   const double* lat;         // sampled phase lattice (device, row-major lny x lnx)
   int lnx, lny;
   double ldx, ldy;
-  int lat_is_grid;           // lattice == field grid, psi == 0, center == 0
-  // f32 fast tables (null when the element needs the per-sample FP64 path)
-  const int2* span;          // per row inclusive [lo, hi] of the transmitting set
-  const float2* tabx;        // per column factor (lens / grating)
-  const float2* taby;        // per row factor (lens)
-  const float* latf;         // f32 copy of the lattice when lat_is_grid
+  // f32 fast tables (psi == 0 elements; built by launch_element_tables).
+  const int2* span;          // per row inclusive [lo, hi] of the transmitting set (lo > hi: none)
+  const float2* tabx;        // per column factor (lens x part, grating)
+  const float2* taby;        // per row factor (lens y part)
+  const float* latf;         // f32 copy of the phase lattice
+  const int4* bilx;          // per column bilinear lookup (i0, i1, bits of tx, inside)
+  const int4* bily;          // per row bilinear lookup (j0, j1, bits of ty, inside)
 };
 
 struct ElementList {
   int count;
-  int fast;  // 1: every element has f32 tables (f32 engine only)
+  int fast;  // 1: every element carries f32 fast tables (f32 engine only)
   DevElement el[kMaxElements];
 };
 

@@ -156,12 +156,235 @@ __device__ void apply_elements_exact(const ElementList& L, int ix, int iy, int n
   }
 }
 
+// f32 fast path: every element has psi == 0 and tables built in FP64 by
+// k_element_tables, so the per-sample work is table lookups plus one
+// sincosf for a phase lattice.  Decisions (stops, lattice span) are the
+// reference's exact FP64 decisions, precomputed per row / column.
+__device__ __forceinline__ float2 apply_elements_fast(const ElementList& L, int ix, int iy,
+                                                      float2 v) {
+  for (int q = 0; q < L.count; ++q) {
+    const DevElement& e = L.el[q];
+    if (e.span) {
+      const int2 sp = e.span[iy];
+      if (ix < sp.x || ix > sp.y) return make_float2(0.f, 0.f);
+    }
+    switch (e.kind) {
+      case EL_LENS: {
+        const float2 a = e.tabx[ix], b = e.taby[iy];
+        const float2 t = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
+        break;
+      }
+      case EL_GRATING: {
+        const float2 t = e.tabx[ix];
+        v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
+        break;
+      }
+      case EL_PHASE: {
+        const int4 bx = e.bilx[ix], by = e.bily[iy];
+        float phi = 0.f;
+        if (bx.w && by.w) {
+          const float tx = __int_as_float(bx.z), ty = __int_as_float(by.z);
+          const float* r0 = e.latf + (size_t)by.x * e.lnx;
+          const float* r1 = e.latf + (size_t)by.y * e.lnx;
+          const float v00 = r0[bx.x], v10 = r0[bx.y], v01 = r1[bx.x], v11 = r1[bx.y];
+          const float A = v00 + (v10 - v00) * tx;
+          const float B = v01 + (v11 - v01) * tx;
+          phi = A + (B - A) * ty;
+        }
+        float sn, cs;
+        sincosf(phi, &sn, &cs);
+        v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+  return v;
+}
+
 template <typename T>
 __device__ __forceinline__ cx<T> apply_elements(const ElementList& L, int ix, int iy, int nx,
                                                 int ny, double dx, double dy, cx<T> v) {
+  if (sizeof(T) == 4 && L.fast) {
+    float2 w = make_float2((float)v.x, (float)v.y);
+    w = apply_elements_fast(L, ix, iy, w);
+    return mkc<cx<T>>((T)w.x, (T)w.y);
+  }
   double re = (double)v.x, im = (double)v.y;
   apply_elements_exact(L, ix, iy, nx, ny, dx, dy, re, im);
   return mkc<cx<T>>((T)re, (T)im);
+}
+
+// Transmitting-set predicate of one element with psi == 0 (frame
+// coordinates are then exactly (xr, yr)); same FP64 expressions as
+// apply_elements_exact.
+__device__ bool el_inside_psi0(const DevElement& e, double xr, double yr) {
+  switch (e.kind) {
+    case EL_ELLIPSE: {
+      double a2 = __dmul_rn(e.a, e.a), b2 = __dmul_rn(e.b, e.b);
+      double lhs = __dadd_rn(__dmul_rn(__dmul_rn(b2, xr), xr), __dmul_rn(__dmul_rn(a2, yr), yr));
+      return !(lhs > __dmul_rn(a2, b2));
+    }
+    case EL_RECT:
+      return !(fabs(xr) > e.a || fabs(yr) > e.b);
+    default:
+      return stop_contains(e.stop, e.a, e.b, xr, yr);
+  }
+}
+
+// Per-row spans, per-axis factors and bilinear lookups for one element.
+// Along a row the predicate depends on |fl(x - cx)| monotonically, so the
+// transmitting set is an interval around the column nearest cx; it is
+// found by binary search with the exact predicate.
+__global__ void k_element_tables(DevElement e, int nx, int ny, double dx, double dy, int2* span,
+                                 float2* tabx, float2* taby, int4* bilx, int4* bily) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (span && i < ny) {
+    const double yr = __dsub_rn(coord_d(i, ny, dy), e.cy);
+    auto xr_of = [&](int ix) { return __dsub_rn(coord_d(ix, nx, dx), e.cx); };
+    auto inside = [&](int ix) { return el_inside_psi0(e, xr_of(ix), yr); };
+    int ic = (int)rint(e.cx / dx + ((double)nx - 1.0) / 2.0);
+    ic = max(0, min(nx - 1, ic));
+    for (int d = -2; d <= 2; ++d) {
+      const int j = ic + d;
+      if (j >= 0 && j < nx && fabs(xr_of(j)) < fabs(xr_of(ic))) ic = j;
+    }
+    int2 sp = make_int2(1, 0);
+    if (inside(ic)) {
+      int lo, hi;
+      if (inside(0)) {
+        lo = 0;
+      } else {
+        int a = 0, b = ic;
+        while (b - a > 1) {
+          const int mid = (a + b) / 2;
+          if (inside(mid)) b = mid; else a = mid;
+        }
+        lo = b;
+      }
+      if (inside(nx - 1)) {
+        hi = nx - 1;
+      } else {
+        int a = ic, b = nx - 1;
+        while (b - a > 1) {
+          const int mid = (a + b) / 2;
+          if (inside(mid)) a = mid; else b = mid;
+        }
+        hi = a;
+      }
+      sp = make_int2(lo, hi);
+    }
+    span[i] = sp;
+  }
+  if (i < nx) {
+    const double xr = __dsub_rn(coord_d(i, nx, dx), e.cx);
+    if (tabx && e.kind == EL_LENS) {
+      double s, c;
+      sincos(__ddiv_rn(__dmul_rn(-e.k, __dmul_rn(xr, xr)), __dmul_rn(2.0, e.f)), &s, &c);
+      tabx[i] = make_float2((float)c, (float)s);
+    }
+    if (tabx && e.kind == EL_GRATING) {
+      const double u = __dmul_rn(xr, e.inv_period);
+      double s, c;
+      sincos(__dmul_rn(e.depth, __dsub_rn(u, floor(u))), &s, &c);
+      tabx[i] = make_float2((float)c, (float)s);
+    }
+    if (bilx) {
+      const double g = __dadd_rn(__ddiv_rn(xr, e.ldx), ((double)e.lnx - 1.0) / 2.0);
+      const bool ok = !(g < 0.0 || g > (double)e.lnx - 1.0);
+      int i0 = 0, i1 = 0;
+      float t = 0.f;
+      if (ok) {
+        i0 = (int)floor(g);
+        i1 = min(i0 + 1, e.lnx - 1);
+        t = (float)__dsub_rn(g, (double)i0);
+      }
+      bilx[i] = make_int4(i0, i1, __float_as_int(t), ok ? 1 : 0);
+    }
+  }
+  if (i < ny) {
+    const double yr = __dsub_rn(coord_d(i, ny, dy), e.cy);
+    if (taby && e.kind == EL_LENS) {
+      double s, c;
+      sincos(__ddiv_rn(__dmul_rn(-e.k, __dmul_rn(yr, yr)), __dmul_rn(2.0, e.f)), &s, &c);
+      taby[i] = make_float2((float)c, (float)s);
+    }
+    if (bily) {
+      const double g = __dadd_rn(__ddiv_rn(yr, e.ldy), ((double)e.lny - 1.0) / 2.0);
+      const bool ok = !(g < 0.0 || g > (double)e.lny - 1.0);
+      int j0 = 0, j1 = 0;
+      float t = 0.f;
+      if (ok) {
+        j0 = (int)floor(g);
+        j1 = min(j0 + 1, e.lny - 1);
+        t = (float)__dsub_rn(g, (double)j0);
+      }
+      bily[i] = make_int4(j0, j1, __float_as_int(t), ok ? 1 : 0);
+    }
+  }
+}
+
+__global__ void k_cast_f64_f32(const double* src, float* dst, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+
+size_t element_tables_bytes(const DevElement& e, int nx, int ny) {
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t b = al((size_t)ny * sizeof(int2));
+  if (e.kind == EL_LENS || e.kind == EL_GRATING) b += al((size_t)nx * sizeof(float2));
+  if (e.kind == EL_LENS) b += al((size_t)ny * sizeof(float2));
+  if (e.kind == EL_PHASE)
+    b += al((size_t)nx * sizeof(int4)) + al((size_t)ny * sizeof(int4)) +
+         al((size_t)e.lnx * e.lny * sizeof(float));
+  return b;
+}
+
+cudaError_t launch_element_tables(DevElement& e, int nx, int ny, double dx, double dy,
+                                  void* scratch, cudaStream_t st) {
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* p = reinterpret_cast<char*>(scratch);
+  const bool has_span = (e.kind == EL_ELLIPSE || e.kind == EL_RECT || e.stop != STOP_FIELD);
+  int2* span = reinterpret_cast<int2*>(p);
+  p += al((size_t)ny * sizeof(int2));
+  float2 *tx = nullptr, *ty = nullptr;
+  int4 *bx = nullptr, *by = nullptr;
+  float* lf = nullptr;
+  if (e.kind == EL_LENS || e.kind == EL_GRATING) {
+    tx = reinterpret_cast<float2*>(p);
+    p += al((size_t)nx * sizeof(float2));
+  }
+  if (e.kind == EL_LENS) {
+    ty = reinterpret_cast<float2*>(p);
+    p += al((size_t)ny * sizeof(float2));
+  }
+  if (e.kind == EL_PHASE) {
+    bx = reinterpret_cast<int4*>(p);
+    p += al((size_t)nx * sizeof(int4));
+    by = reinterpret_cast<int4*>(p);
+    p += al((size_t)ny * sizeof(int4));
+    if (e.latf) {
+      lf = const_cast<float*>(e.latf);  // f32 copy kept with the lattice handle
+    } else {
+      lf = reinterpret_cast<float*>(p);
+      const size_t n = (size_t)e.lnx * e.lny;
+      COUNT_LAUNCH();
+      k_cast_f64_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(e.lat, lf, n);
+    }
+  }
+  const int n = max(nx, ny);
+  COUNT_LAUNCH();
+  k_element_tables<<<(n + 127) / 128, 128, 0, st>>>(e, nx, ny, dx, dy, has_span ? span : nullptr,
+                                                    tx, ty, bx, by);
+  e.span = has_span ? span : nullptr;
+  e.tabx = tx;
+  e.taby = ty;
+  e.bilx = bx;
+  e.bily = by;
+  e.latf = lf;
+  return cudaGetLastError();
 }
 
 // ----------------------------------------------------------------- tables

@@ -97,6 +97,12 @@ cudaError_t launch_apply_elements(const void* in, int in_c128, void* out, int ou
                                   const ElementList& els, int nx, int ny, double dx, double dy,
                                   int* status, cudaStream_t st);
 
+// f32 fast element tables (psi == 0 elements): bytes of scratch needed and
+// the build; fills e.span / tabx / taby / bilx / bily / latf.
+size_t element_tables_bytes(const DevElement& e, int nx, int ny);
+cudaError_t launch_element_tables(DevElement& e, int nx, int ny, double dx, double dy,
+                                  void* scratch, cudaStream_t st);
+
 // Kernel launches issued by the library since load.
 unsigned long long launch_count();
 

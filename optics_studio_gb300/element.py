@@ -71,7 +71,7 @@ def _desc(kind, stop=STOP_FIELD, a=0.0, b=0.0, psi=0.0, center=(0.0, 0.0), focal
           depth=0.0, lattice=None, lnx=0, lny=0, ldx=0.0, ldy=0.0):
     lp = ptr(lattice) if lattice is not None else None
     return _ffi.ElementC(kind, stop, a, b, psi, center[0], center[1], focal, period, depth, lp,
-                         lnx, lny, ldx, ldy)
+                         lnx, lny, ldx, ldy, 0)
 
 
 class EllipticalAperture(Element):

@@ -39,7 +39,7 @@ def test_struct_layouts_match_header_sizes():
     # sizes implied by the header's field lists (natural alignment, x86-64/aarch64)
     assert ctypes.sizeof(_ffi.Grid) == 40
     assert ctypes.sizeof(_ffi.AsmConfigC) == 32
-    assert ctypes.sizeof(_ffi.ElementC) == 112
+    assert ctypes.sizeof(_ffi.ElementC) == 120
 
 
 GEOMS = [

@@ -1,0 +1,91 @@
+"""Batched, device-resident beamline traces (osgpu_beamline_trace_batch_device)
+against the f64 oracle: ragged grid sizes, wavelengths and distances in one
+call, complex64 (f32 engine, <= 1e-5) and complex128 (f64 engine, <= 1e-12)."""
+
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import optics_studio_gb300 as og
+from optics_studio_gb300 import _ffi as ffi
+from oracle import asm as oasm, field as ofield, element as oel, beamline as obl
+
+from _util import rel_l2
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+ITEMS = [  # n, dx, lam, z, lens f, aperture half-width
+    (64, 4e-6, 450e-9, 1e-3, 0.05, 100e-6),
+    (96, 3e-6, 550e-9, 4e-3, 0.08, 120e-6),
+    (48, 5e-6, 650e-9, -2e-3, 0.03, 90e-6),
+]
+
+
+def oracle_item(n, dx, lam, z, f, half, lat, u):
+    b = ofield.BandField(u, dx, dx, lam)
+    bl = obl.Beamline()
+    bl.push(oel.PhaseMask.sampled(lat, (n, n), (dx, dx)), 0.0)
+    bl.push(oel.RectangularAperture((half, half)), 0.0)
+    bl.push(oel.ThinLens.fixed(f), z)
+    return bl.trace(b, obl.asm_engine(oasm.AsmConfig())).samples
+
+
+@pytest.mark.parametrize("dtype,tol", [(ffi.C64, 1e-5), (ffi.C128, 1e-12)])
+def test_batch_device_ragged_matches_oracle(dtype, tol):
+    L = og.lib()
+    tdt = torch.complex64 if dtype == ffi.C64 else torch.complex128
+    rng = np.random.default_rng(7)
+    keep, items, refs, outs, handles = [], [], [], [], []
+    arr = (ffi.TraceItemC * len(ITEMS))()
+    for i, (n, dx, lam, z, f, half) in enumerate(ITEMS):
+        lat = np.floor(rng.uniform(0, 16, (n, n))) * (2 * math.pi / 16)
+        u = np.exp(1j * rng.uniform(0, 0.3, (n, n)))
+        refs.append(oracle_item(n, dx, lam, z, f, half, lat, u))
+        h = C.c_void_p()
+        ffi.check(L.osgpu_lattice_create(lat.ctypes.data_as(ffi.c_double_p), n, n, C.byref(h)))
+        handles.append(h)
+        tin = torch.from_numpy(u).to(device="cuda", dtype=tdt)
+        tout = torch.empty_like(tin)
+        outs.append(tout)
+        doe = ffi.ElementC(4, 0, 0, 0, 0, 0, 0, 0, 0, 0, C.cast(h, ffi.c_double_p), n, n, dx, dx, 1)
+        ap = ffi.ElementC(2, 0, half, half, 0, 0, 0, 0, 0, 0, None, 0, 0, 0, 0, 0)
+        lens = ffi.ElementC(3, 0, 0, 0, 0, 0, 0, f, 0, 0, None, 0, 0, 0, 0, 0)
+        e1, e2, e3 = (ffi.ElementC * 1)(doe), (ffi.ElementC * 1)(ap), (ffi.ElementC * 1)(lens)
+        steps = (ffi.StepC * 3)(ffi.StepC(e1, 1, 0.0, 1.0), ffi.StepC(e2, 1, 0.0, 1.0),
+                                ffi.StepC(e3, 1, z, 1.0))
+        keep += [tin, e1, e2, e3, steps]
+        arr[i] = ffi.TraceItemC(tin.data_ptr(), tout.data_ptr(), ffi.Grid(n, n, dx, dx, lam),
+                                steps, 3)
+    reps = (ffi.AsmReportC * (3 * len(ITEMS)))()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ffi.check(L.osgpu_beamline_trace_batch_device(arr, len(ITEMS), ffi.AsmConfigC(2, 1, 1, 8, 1),
+                                                  dtype, stream, reps, 3))
+    torch.cuda.synchronize()
+    ffi.check(L.osgpu_sync_status())
+    for i, ref in enumerate(refs):
+        got = outs[i].cpu().numpy().astype(np.complex128)
+        assert rel_l2(got, ref) <= tol, (i, rel_l2(got, ref))
+        assert reps[3 * i + 2].nx_pad >= ITEMS[i][0]
+    for h in handles:
+        ffi.check(L.osgpu_lattice_destroy(h))
+
+
+def test_profile_reports_kernel_classes():
+    L = og.lib()
+    n = 64
+    u = torch.ones((n, n), dtype=torch.complex64, device="cuda")
+    out = torch.empty_like(u)
+    ffi.check(L.osgpu_profile_begin())
+    ffi.check(L.osgpu_asm_propagate_device(u.data_ptr(), out.data_ptr(), ffi.C64,
+                                           ffi.Grid(n, n, 5e-6, 5e-6, 500e-9), 1e-3,
+                                           ffi.AsmConfigC(2, 1, 1, 8, 1), None, None))
+    stats = (ffi.KernelStatC * 16)()
+    k = C.c_int32()
+    ffi.check(L.osgpu_profile_end(stats, 16, C.byref(k)))
+    names = {stats[i].name.decode() for i in range(k.value)}
+    assert {"pass_a_rows", "pass_b_columns", "pass_c_rows"} <= names
+    for i in range(k.value):
+        assert stats[i].total_ms >= 0 and stats[i].launches >= 1
