@@ -231,8 +231,13 @@ def main():
     from optics_studio_gb300 import _ffi as ffi
     L = og.lib()
     ffi.check(L.osgpu_init(local))
-    stream = torch.cuda.current_stream()
+    # An explicit stream: the legacy default stream has handle 0, which the C
+    # ABI reads as "the library's own stream", so torch events on it would
+    # not bracket the library's kernels.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = C.c_void_p(stream.cuda_stream)
+    assert sptr.value, "need a non-default CUDA stream"
 
     lat = doe_lattice()
     handle = C.c_void_p()

@@ -235,7 +235,7 @@ typedef struct {
   double center_x, center_y;
   double focal;          /* thin lens: f(lambda) */
   double period, depth;  /* blazed grating */
-  const double* lattice; /* sampled phase, row-major lny x lnx */
+  const void* lattice;   /* sampled phase (double), row-major lny x lnx */
   uint64_t lnx, lny;
   double ldx, ldy;
   int32_t lattice_on_device; /* 0: `lattice` is host memory (scanned for non-finite

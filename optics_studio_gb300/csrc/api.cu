@@ -177,7 +177,7 @@ struct Elements {
 };
 
 int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid& g,
-                   Elements& E) {
+                   Elements& E, cudaStream_t st) {
   std::memset(&E.list, 0, sizeof(E.list));
   if (n < 0 || (n > 0 && els == nullptr)) {
     set_err("bad element list");
@@ -190,18 +190,18 @@ int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid
   for (int i = 0; i < n; ++i) {
     DevElement d;
     char msg[512] = "";
-    int st = element_check(els[i], g, g.lambda, d, msg, sizeof(msg));
-    if (st) {
-      set_err("element %d: %s (status %d)", i, msg, st);
-      return st;
+    int est = element_check(els[i], g, g.lambda, d, msg, sizeof(msg));
+    if (est) {
+      set_err("element %d: %s (status %d)", i, msg, est);
+      return est;
     }
     if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED && els[i].lattice_on_device) {
-      d.lat = els[i].lattice;
+      d.lat = reinterpret_cast<const double*>(els[i].lattice);
     } else if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED) {
       const size_t bytes = (size_t)els[i].lnx * els[i].lny * sizeof(double);
       DBuf b;
-      CK(b.alloc(bytes, c.stream));
-      CK(cudaMemcpyAsync(b.p, els[i].lattice, bytes, cudaMemcpyHostToDevice, c.stream));
+      CK(b.alloc(bytes, st));
+      CK(cudaMemcpyAsync(b.p, els[i].lattice, bytes, cudaMemcpyHostToDevice, st));
       d.lat = reinterpret_cast<const double*>(b.p);
       E.lattices.push_back(std::move(b));
     }
@@ -820,7 +820,7 @@ int osgpu_apply_elements(const double* in, double* out, const osgpu_grid* g,
   std::lock_guard<std::recursive_mutex> lk(c.mu);
   if ((rc = ensure_init(c))) return rc;
   Elements E;
-  if ((rc = build_elements(c, els, n_els, *g, E))) return rc;
+  if ((rc = build_elements(c, els, n_els, *g, E, c.stream))) return rc;
   if (precision == OSGPU_F32 && (rc = build_fast_tables(c, E.list, *g, E.tables, c.stream)))
     return rc;
   const size_t n = g->nx * g->ny;
@@ -891,7 +891,7 @@ int prepare_trace(Context& c, const double* host_in, size_t n, const osgpu_grid&
   R.assign(n_steps > 0 ? n_steps : 0, osgpu_asm_report());
   int first_prop = -1;
   for (int s = 0; s < n_steps; ++s) {
-    int rc = build_elements(c, steps[s].elements, steps[s].n_elements, g, E[s]);
+    int rc = build_elements(c, steps[s].elements, steps[s].n_elements, g, E[s], st);
     if (rc) {
       if (first_prop >= 0 && first_prop < s) rc = scan_then(host_in, n, rc);
       return rc;

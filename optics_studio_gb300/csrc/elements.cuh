@@ -1,0 +1,166 @@
+// Element transmissions evaluated on the device (shared by the generic
+// and the register-FFT passes).
+#pragma once
+#include <cuda_runtime.h>
+#include "osgpu_types.h"
+
+namespace osgpu {
+
+// fftfreq value k/(n d) with negative wrap (reference propagation/fft.rs:115-126).
+static __device__ __forceinline__ double fftfreq_d(int k, int n, double d) {
+  double kk = (k <= (n - 1) / 2) ? (double)k : (double)k - (double)n;
+  return __ddiv_rn(kk, __dmul_rn((double)n, d));
+}
+
+// Origin-centred coordinate (i - (n-1)/2) d (reference field.rs:216-221).
+static __device__ __forceinline__ double coord_d(int i, int n, double d) {
+  return __dmul_rn(__dsub_rn((double)i, ((double)n - 1.0) / 2.0), d);
+}
+
+// Element-frame rotation (reference element.rs:557-560), no FMA contraction.
+static __device__ __forceinline__ void to_frame(double x, double y, double c, double s, double& fx,
+                                         double& fy) {
+  fx = __dadd_rn(__dmul_rn(c, x), __dmul_rn(s, y));
+  fy = __dadd_rn(__dmul_rn(-s, x), __dmul_rn(c, y));
+}
+
+// ClearAperture::contains (reference element.rs:476-488).
+static __device__ __forceinline__ bool stop_contains(int kind, double a, double b, double x, double y) {
+  switch (kind) {
+    case STOP_CIRCLE:
+      return __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)) <= __dmul_rn(a, a);
+    case STOP_ELLIPSE: {
+      double a2 = __dmul_rn(a, a), b2 = __dmul_rn(b, b);
+      return __dadd_rn(__dmul_rn(__dmul_rn(b2, x), x), __dmul_rn(__dmul_rn(a2, y), y)) <=
+             __dmul_rn(a2, b2);
+    }
+    case STOP_RECT:
+      return fabs(x) <= a && fabs(y) <= b;
+    default:
+      return true;
+  }
+}
+
+// SampledPhase::at, bilinear, zero outside the span (reference element.rs:1189-1207).
+static __device__ double lattice_at(const DevElement& e, double x, double y) {
+  double gx = __dadd_rn(__ddiv_rn(x, e.ldx), ((double)e.lnx - 1.0) / 2.0);
+  double gy = __dadd_rn(__ddiv_rn(y, e.ldy), ((double)e.lny - 1.0) / 2.0);
+  double lx = (double)e.lnx - 1.0, ly = (double)e.lny - 1.0;
+  if (gx < 0.0 || gx > lx || gy < 0.0 || gy > ly) return 0.0;
+  int i0 = (int)floor(gx), j0 = (int)floor(gy);
+  int i1 = min(i0 + 1, e.lnx - 1), j1 = min(j0 + 1, e.lny - 1);
+  double tx = __dsub_rn(gx, (double)i0), ty = __dsub_rn(gy, (double)j0);
+  const double* v = e.lat;
+  double v00 = v[(size_t)j0 * e.lnx + i0], v10 = v[(size_t)j0 * e.lnx + i1];
+  double v01 = v[(size_t)j1 * e.lnx + i0], v11 = v[(size_t)j1 * e.lnx + i1];
+  double A = __dadd_rn(v00, __dmul_rn(__dsub_rn(v10, v00), tx));
+  double B = __dadd_rn(v01, __dmul_rn(__dsub_rn(v11, v01), tx));
+  return __dadd_rn(A, __dmul_rn(__dsub_rn(B, A), ty));
+}
+
+static __device__ __forceinline__ void cmul_phase(double& re, double& im, double phi) {
+  double s, c;
+  sincos(phi, &s, &c);
+  double r2 = re * c - im * s;
+  double i2 = re * s + im * c;
+  re = r2;
+  im = i2;
+}
+
+// Per-sample FP64 evaluation of every element at sample (ix, iy), in the
+// reference's operation order (element.rs:754-790, 900-929, 1115-1154,
+// 1443-1484, 1668-1703).  Elements apply in list order.
+static __device__ void apply_elements_exact(const ElementList& L, int ix, int iy, int nx, int ny,
+                                     double dx, double dy, double& re, double& im) {
+  const double x = coord_d(ix, nx, dx);
+  const double y = coord_d(iy, ny, dy);
+  for (int q = 0; q < L.count; ++q) {
+    const DevElement& e = L.el[q];
+    const double xr = __dsub_rn(x, e.cx), yr = __dsub_rn(y, e.cy);
+    double fx, fy;
+    to_frame(xr, yr, e.cpsi, e.spsi, fx, fy);
+    switch (e.kind) {
+      case EL_ELLIPSE: {
+        double a2 = __dmul_rn(e.a, e.a), b2 = __dmul_rn(e.b, e.b);
+        double lhs = __dadd_rn(__dmul_rn(__dmul_rn(b2, fx), fx), __dmul_rn(__dmul_rn(a2, fy), fy));
+        if (lhs > __dmul_rn(a2, b2)) { re = 0.0; im = 0.0; }
+        break;
+      }
+      case EL_RECT:
+        if (fabs(fx) > e.a || fabs(fy) > e.b) { re = 0.0; im = 0.0; }
+        break;
+      case EL_LENS: {
+        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+        double r2 = __dadd_rn(__dmul_rn(xr, xr), __dmul_rn(yr, yr));
+        double phase = __ddiv_rn(__dmul_rn(-e.k, r2), __dmul_rn(2.0, e.f));
+        cmul_phase(re, im, phase);
+        break;
+      }
+      case EL_PHASE: {
+        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+        cmul_phase(re, im, lattice_at(e, fx, fy));
+        break;
+      }
+      case EL_GRATING: {
+        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+        double u = __dmul_rn(fx, e.inv_period);
+        double phi = __dmul_rn(e.depth, __dsub_rn(u, floor(u)));
+        cmul_phase(re, im, phi);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
+// f32 fast path: every element has psi == 0 and tables built in FP64 by
+// k_element_tables, so the per-sample work is table lookups plus one
+// sincosf for a phase lattice.  Decisions (stops, lattice span) are the
+// reference's exact FP64 decisions, precomputed per row / column.
+static __device__ __forceinline__ float2 apply_elements_fast(const ElementList& L, int ix, int iy,
+                                                      float2 v) {
+  for (int q = 0; q < L.count; ++q) {
+    const DevElement& e = L.el[q];
+    if (e.span) {
+      const int2 sp = e.span[iy];
+      if (ix < sp.x || ix > sp.y) return make_float2(0.f, 0.f);
+    }
+    switch (e.kind) {
+      case EL_LENS: {
+        const float2 a = e.tabx[ix], b = e.taby[iy];
+        const float2 t = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
+        break;
+      }
+      case EL_GRATING: {
+        const float2 t = e.tabx[ix];
+        v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
+        break;
+      }
+      case EL_PHASE: {
+        const int4 bx = e.bilx[ix], by = e.bily[iy];
+        float phi = 0.f;
+        if (bx.w && by.w) {
+          const float tx = __int_as_float(bx.z), ty = __int_as_float(by.z);
+          const float* r0 = e.latf + (size_t)by.x * e.lnx;
+          const float* r1 = e.latf + (size_t)by.y * e.lnx;
+          const float v00 = r0[bx.x], v10 = r0[bx.y], v01 = r1[bx.x], v11 = r1[bx.y];
+          const float A = v00 + (v10 - v00) * tx;
+          const float B = v01 + (v11 - v01) * tx;
+          phi = A + (B - A) * ty;
+        }
+        float sn, cs;
+        sincosf(phi, &sn, &cs);
+        v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+  return v;
+}
+
+
+}  // namespace osgpu

@@ -1,0 +1,198 @@
+// Register-resident Stockham FFT for power-of-two lengths M in [256, 4096],
+// f32 complex.  T = M/16 threads cooperate on one transform; every thread
+// owns one radix-16 butterfly per stage and holds 16 points in registers:
+//   on entry  v[q] = x[tid + T q]      on exit  v[q] = X[tid + T q]
+// (same layout both ways, so a forward and an inverse transform chain
+// without reshuffling).  Stages: floor(log16 M) radix-16 stages plus a final
+// radix-2/4/8 stage when log2 M is not a multiple of 4.  Between stages the
+// data goes through shared memory once (padded index i + i/16 to keep the
+// transposed stage-0 store conflict free): 2 exchanges for M = 512..4096.
+//
+// Stage (Ns = product of earlier radices, radix R, butterfly j, k = j mod Ns):
+//   v[q] = src[j + q M/R] * W_{Ns R}^{q k};  v = DFT_R(v);
+//   dst[(j - k) R + k + q Ns] = v[q]
+// Twiddles W_M^t come from a table tw[t] = e^{-2 pi i t / M} (conjugated for
+// the inverse).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace osgpu {
+namespace regfft {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <bool INV> __device__ __forceinline__ float2 rot(float2 a) {  // * (-i) fwd, * (+i) inv
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+template <bool INV> __device__ __forceinline__ float2 twiddle(float2 a, float2 w) {
+  return INV ? cmulc(a, w) : cmul(a, w);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft2(float2& a, float2& b) {
+  float2 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  float2 b0 = cadd(a0, a2), b1 = csub(a0, a2);
+  float2 b2 = cadd(a1, a3), b3 = rot<INV>(csub(a1, a3));
+  a0 = cadd(b0, b2);
+  a2 = csub(b0, b2);
+  a1 = cadd(b1, b3);
+  a3 = csub(b1, b3);
+}
+
+// multiply by W8^1 = e^{-i pi/4} (fwd) or its conjugate (inv)
+template <bool INV> __device__ __forceinline__ float2 w8_1(float2 a) {
+  const float h = 0.70710678118654752f;
+  return INV ? make_float2(h * (a.x - a.y), h * (a.x + a.y))
+             : make_float2(h * (a.x + a.y), h * (a.y - a.x));
+}
+// multiply by W8^3 (fwd) or conjugate (inv)
+template <bool INV> __device__ __forceinline__ float2 w8_3(float2 a) {
+  const float h = 0.70710678118654752f;
+  return INV ? make_float2(-h * (a.x + a.y), h * (a.x - a.y))
+             : make_float2(h * (a.y - a.x), -h * (a.x + a.y));
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft8(float2* v) {
+  // v[0..7] -> DFT_8 in natural order
+  dft4<INV>(v[0], v[2], v[4], v[6]);
+  dft4<INV>(v[1], v[3], v[5], v[7]);
+  // evens E0..E3 at v0,v2,v4,v6 ; odds O0..O3 at v1,v3,v5,v7
+  float2 o1 = w8_1<INV>(v[3]);
+  float2 o2 = rot<INV>(v[5]);
+  float2 o3 = w8_3<INV>(v[7]);
+  float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1];
+  v[0] = cadd(e0, o0);
+  v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1);
+  v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2);
+  v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3);
+  v[7] = csub(e3, o3);
+}
+
+// In-place DFT_16 of v[0..15] (natural order in and out): 16 = 4 x 4,
+// n = 4 n1 + n2, k = k1 + 4 k2.
+template <bool INV>
+__device__ __forceinline__ void dft16(float2* v) {
+  const float c1 = 0.92387953251128676f, s1 = 0.38268343236508977f;
+  const float h = 0.70710678118654752f;
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4<INV>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
+  // slot n2 + 4 k1 holds Y[n2][k1]; twiddle W16^{n2 k1}
+  // W16^1 = (c1, -s1), W16^2 = (h, -h), W16^3 = (s1, -c1), W16^4 = -i,
+  // W16^6 = (-h, -h), W16^9 = (-c1, s1)... (conjugates for the inverse)
+  const float sg = INV ? -1.f : 1.f;
+  v[5] = cmul(v[5], make_float2(c1, -sg * s1));   // n2=1,k1=1 : W^1
+  v[9] = cmul(v[9], make_float2(h, -sg * h));     // n2=1,k1=2 : W^2
+  v[13] = cmul(v[13], make_float2(s1, -sg * c1)); // n2=1,k1=3 : W^3
+  v[6] = cmul(v[6], make_float2(h, -sg * h));     // n2=2,k1=1 : W^2
+  v[10] = rot<INV>(v[10]);                        // n2=2,k1=2 : W^4
+  v[14] = cmul(v[14], make_float2(-h, -sg * h));  // n2=2,k1=3 : W^6
+  v[7] = cmul(v[7], make_float2(s1, -sg * c1));   // n2=3,k1=1 : W^3
+  v[11] = cmul(v[11], make_float2(-h, -sg * h));  // n2=3,k1=2 : W^6
+  v[15] = cmul(v[15], make_float2(-c1, sg * s1)); // n2=3,k1=3 : W^9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+  // slot k2 + 4 k1 holds X[k1 + 4 k2]: transpose the 4x4 index (register renaming)
+  float2 t;
+  t = v[1]; v[1] = v[4]; v[4] = t;
+  t = v[2]; v[2] = v[8]; v[8] = t;
+  t = v[3]; v[3] = v[12]; v[12] = t;
+  t = v[6]; v[6] = v[9]; v[9] = t;
+  t = v[7]; v[7] = v[13]; v[13] = t;
+  t = v[11]; v[11] = v[14]; v[14] = t;
+}
+
+__device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
+
+constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
+
+template <int M> struct Plan {
+  static constexpr int T = M / 16;
+  static constexpr int E = ilog2(M);
+  static constexpr int N16 = E / 4;          // radix-16 stages
+  static constexpr int RF = 1 << (E % 4);    // final radix (1: none)
+  static constexpr int SMEM = M + M / 16;    // padded elements per buffer
+};
+
+// One transform of length M by the T = M/16 threads with local index tid.
+// s0/s1: two padded shared buffers of Plan<M>::SMEM float2 owned by this
+// transform.  Contains __syncthreads: every thread of the block must call it.
+template <int M, bool INV>
+__device__ __forceinline__ void fft(float2 (&v)[16], float2* s0, float2* s1,
+                                    const float2* __restrict__ tw, int tid) {
+  using P = Plan<M>;
+  constexpr int T = P::T;
+  // stage 0: radix 16, Ns = 1, butterfly j = tid, k = 0
+  dft16<INV>(v);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) s0[pad(16 * tid + q)] = v[q];
+  __syncthreads();
+  float2* src = s0;
+  float2* dst = s1;
+  int Ns = 16;
+  // middle radix-16 stages (all but the last if it is radix 16)
+  constexpr int mid16 = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;
+#pragma unroll
+  for (int st = 0; st < mid16; ++st) {
+    const int k = tid & (Ns - 1);
+    const int tstride = M / (Ns * 16);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = src[pad(tid + T * q)];
+#pragma unroll
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], __ldg(&tw[q * k * tstride]));
+    dft16<INV>(v);
+    const int base = (tid - k) * 16 + k;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) dst[pad(base + q * Ns)] = v[q];
+    __syncthreads();
+    float2* tmp = src; src = dst; dst = tmp;
+    Ns *= 16;
+  }
+  if (P::RF == 1) {
+    // last stage radix 16 with Ns = M/16 = T: k = tid, output X[tid + T q]
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = src[pad(tid + T * q)];
+#pragma unroll
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], __ldg(&tw[q * tid]));
+    dft16<INV>(v);
+  } else {
+    // last stage radix RF, Ns = M/RF; butterflies j = tid + T i, i < 16/RF
+    constexpr int RF = P::RF;
+    constexpr int NB = 16 / RF;
+    constexpr int NSF = M / RF;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const int j = tid + T * i;
+      float2 u[RF];
+#pragma unroll
+      for (int q = 0; q < RF; ++q) u[q] = src[pad(j + q * NSF)];
+#pragma unroll
+      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], __ldg(&tw[q * j]));
+      if (RF == 2) dft2<INV>(u[0], u[1]);
+      if (RF == 4) dft4<INV>(u[0], u[1], u[2], u[3]);
+      if (RF == 8) dft8<INV>(u);
+      // output index j + q NSF = tid + T (i + q NB)
+#pragma unroll
+      for (int q = 0; q < RF; ++q) v[i + q * NB] = u[q];
+    }
+  }
+}
+
+}  // namespace regfft
+}  // namespace osgpu

@@ -396,9 +396,15 @@ int element_check(const osgpu_element& e, const osgpu_grid& g, double lambda, De
       if (e.lnx == 0 || e.lny == 0 || e.lattice == nullptr) return OSGPU_E_INVALID_GRID;
       if (!std::isfinite(e.ldx) || e.ldx <= 0.0 || !std::isfinite(e.ldy) || e.ldy <= 0.0)
         return OSGPU_E_INVALID_GRID_PITCH;
-      const uint64_t n = e.lnx * e.lny;
-      for (uint64_t k = 0; k < n; ++k)
-        if (!std::isfinite(e.lattice[k])) return OSGPU_E_INVALID_PHASE;
+      // A host lattice is scanned here, as PhaseMask::sampled does; a device
+      // lattice (lattice_on_device) was scanned when it was created and is
+      // never dereferenced on the host.
+      if (!e.lattice_on_device) {
+        const double* lat = reinterpret_cast<const double*>(e.lattice);
+        const uint64_t n = e.lnx * e.lny;
+        for (uint64_t k = 0; k < n; ++k)
+          if (!std::isfinite(lat[k])) return OSGPU_E_INVALID_PHASE;
+      }
       int st = stop_check();
       if (st) return st;
       d.lnx = (int)e.lnx;

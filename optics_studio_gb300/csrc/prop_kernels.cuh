@@ -103,6 +103,13 @@ size_t element_tables_bytes(const DevElement& e, int nx, int ny);
 cudaError_t launch_element_tables(DevElement& e, int nx, int ny, double dx, double dy,
                                   void* scratch, cudaStream_t st);
 
+// Register-FFT f32 passes (prop_fast.cu) for power-of-two sub-FFT lengths
+// in [256, 4096]; the generic launchers route to them.
+bool reg_fft_size(int m);
+cudaError_t launch_passA_reg(const PropArgs& a, cudaStream_t st);
+cudaError_t launch_passB_reg(const PropArgs& a, cudaStream_t st);
+cudaError_t launch_passC_reg(const PropArgs& a, cudaStream_t st);
+
 // Kernel launches issued by the library since load.
 unsigned long long launch_count();
 

@@ -218,3 +218,53 @@ def test_beamline_trace_fused_matches_oracle(prec, tol):
     gbl.push(gel.ThinLens.fixed(0.05), 5e-3)
     out = gbl.trace(to_gpu_band(ob), AsmEngine(gasm.AsmConfig(), prec))
     assert rel_l2(out.samples, ref.samples) <= tol
+
+
+REG_CASES = [
+    # ny, nx, dx, lam, z, cfg  (sub-FFT lengths 256..2048: the register-FFT passes)
+    (256, 256, 3e-6, 500e-9, 0.02, oasm.AsmConfig()),
+    (256, 512, 2e-6, 633e-9, -4e-3, oasm.AsmConfig(2.0, True, True, 8.0, 1.3)),
+    (512, 512, 3e-6, 450e-9, 0.05, oasm.AsmConfig(2.0, False, False, 8.0, 1.0)),
+    (1024, 1024, 4e-6, 532e-9, 0.03, oasm.AsmConfig()),
+]
+
+
+@pytest.mark.parametrize("case", REG_CASES)
+def test_asm_f32_register_fft_sizes(case):
+    ny, nx, dx, lam, z, cfg = case
+    ob = ofield.BandField(rng_field(ny, nx, seed=nx + ny), dx, dx, lam)
+    ref = oasm.propagate(ob, z, cfg)
+    gcfg = gasm.AsmConfig(cfg.padding, cfg.band_limited, cfg.strict, cfg.max_padding, cfg.medium)
+    out = gasm.propagate(to_gpu_band(ob), z, gcfg, "f32")
+    assert rel_l2(out.samples, ref.samples) <= TOL32
+
+
+def test_beamline_f32_register_fft_with_fused_fast_elements():
+    """1024^2 DOE -> square aperture -> lens -> ASM, f32 engine: fast element
+    tables fused into the register-FFT first pass."""
+    n, d, lam = 1024, 4e-6, 532e-9
+    lat = np.floor(np.random.default_rng(8).uniform(0, 16, (n, n))) * (2 * np.pi / 16)
+    ob = ofield.plane_wave(0.0, 0.0, 1.0, n, n, d, d, lam)
+    o = obl.Beamline()
+    o.push(oel.PhaseMask.sampled(lat, (n, n), (d, d)), 0.0)
+    o.push(oel.RectangularAperture((1.5e-3, 1.5e-3)), 0.0)
+    o.push(oel.ThinLens.fixed(0.05), 0.02)
+    ref = o.trace(ob, obl.asm_engine(oasm.AsmConfig()))
+    g = Beamline()
+    g.push(gel.PhaseMask.sampled(lat, (n, n), (d, d)), 0.0)
+    g.push(gel.RectangularAperture((1.5e-3, 1.5e-3)), 0.0)
+    g.push(gel.ThinLens.fixed(0.05), 0.02)
+    out = g.trace(to_gpu_band(ob), AsmEngine(gasm.AsmConfig(), "f32"))
+    assert rel_l2(out.samples, ref.samples) <= TOL32
+
+
+@pytest.mark.parametrize("z", [5e-3, -3e-3])
+def test_fresnel_f32_register_fft(z):
+    ob = ofield.BandField(rng_field(256, 256, seed=21), 8e-6, 8e-6, 633e-9)
+    cfg = ofr.FresnelConfig(strict=False)
+    g = to_gpu_band(ob)
+    gcfg = gfr.FresnelConfig(strict=False)
+    assert rel_l2(gfr.propagate(g, z, gcfg, "f32").samples,
+                  ofr.propagate(ob, z, cfg).samples) <= TOL32
+    assert rel_l2(gfr.propagate_convolution(g, z, gcfg, "f32").samples,
+                  ofr.propagate_convolution(ob, z, cfg).samples) <= TOL32
