@@ -50,6 +50,12 @@ WORKLOAD = ("32 bands 450-650 nm x 2048^2, dx 3 um, [16-level DOE, square apertu
             "thin lens f 100 mm, ASM z 100 mm], padded 8192^2")
 
 
+def set_bands(n):
+    global NBANDS, LAMS
+    NBANDS = n
+    LAMS = np.linspace(450e-9, 650e-9, 32)[:n] if n <= 32 else np.linspace(450e-9, 650e-9, n)
+
+
 def doe_lattice():
     rng = np.random.default_rng(SEED)
     return np.floor(rng.uniform(0, LEVELS, (N, N))) * (2 * math.pi / LEVELS)
@@ -210,7 +216,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--bands", type=int, default=NBANDS,
+                    help="bands per step (profiling runs use a smaller batch)")
     args = ap.parse_args()
+    set_bands(args.bands)
     if args.impl == "reference":
         reference_arm(args)
         return
@@ -327,7 +336,7 @@ def main():
 
     # plain FP64 path on the same batch (device resident complex128)
     if not args.no_f64 and rank == 0:
-        nb64 = 8
+        nb64 = min(8, NBANDS)
         fin64 = torch.ones((nb64, N, N), dtype=torch.complex128, device="cuda")
         fout64 = torch.empty_like(fin64)
         k2 = []

@@ -112,6 +112,9 @@ __global__ void __launch_bounds__(2 * (M / 16), (M <= 2048 ? 2 : 1)) k_passB_reg
 #pragma unroll
   for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
   for (int t = 0; t < ry; ++t) {
+    // W_P^{t j} for j = tid + T q  (t j < ry M = Py, no reduction needed):
+    // W_P^{t tid} (per thread) times W_P^{t T q} (uniform across the CTA)
+    const float2 wb = __ldg(&twP[t * tid]);
     float2 v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
@@ -119,7 +122,7 @@ __global__ void __launch_bounds__(2 * (M / 16), (M <= 2048 ? 2 : 1)) k_passB_reg
       float2 x = make_float2(0.f, 0.f);
       if (j < ny) {
         x = W[j];
-        if (t > 0) x = cmul(x, __ldg(&twP[(int)(((long long)t * j) % Py)]));
+        if (t > 0) x = cmul(x, cmul(wb, __ldg(&twP[t * T * q])));
       }
       v[q] = x;
     }
@@ -149,7 +152,7 @@ __global__ void __launch_bounds__(2 * (M / 16), (M <= 2048 ? 2 : 1)) k_passB_reg
     for (int q = 0; q < 16; ++q) {
       const int j = tid + T * q;
       float2 y = v[q];
-      if (t > 0 && j < ny) y = cmulc(y, __ldg(&twP[(int)(((long long)t * j) % Py)]));
+      if (t > 0 && j < ny) y = cmulc(y, cmul(wb, __ldg(&twP[t * T * q])));
       acc[q] = cadd(acc[q], y);
     }
   }
@@ -200,12 +203,12 @@ __global__ void __launch_bounds__(256, 2) k_passA_reg(PropArgs a, int rows) {
     xin[q] = x;
   }
   for (int s = 0; s < rx; ++s) {
+    const float2 wb = __ldg(&twP[s * tid]);  // s j < rx M = Px
     float2 v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const int j = tid + T * q;
-      v[q] = (s > 0 && j < nx) ? cmul(xin[q], __ldg(&twP[(int)(((long long)s * j) % Px)]))
-                               : xin[q];
+      v[q] = (s > 0 && j < nx) ? cmul(xin[q], cmul(wb, __ldg(&twP[s * T * q]))) : xin[q];
     }
     fft<M, false>(v, s0, s1, twm, tid);
     if (live) {
@@ -241,11 +244,12 @@ __global__ void __launch_bounds__(256, 2) k_passC_reg(PropArgs a, int rows) {
     for (int q = 0; q < 16; ++q)
       v[q] = live ? W[(size_t)(rx * (tid + T * q) + s) * ny + iy] : make_float2(0.f, 0.f);
     fft<M, true>(v, s0, s1, twm, tid);
+    const float2 wb = __ldg(&twP[s * tid]);
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const int j = tid + T * q;
       float2 y = v[q];
-      if (s > 0 && j < nx) y = cmulc(y, __ldg(&twP[(int)(((long long)s * j) % Px)]));
+      if (s > 0 && j < nx) y = cmulc(y, cmul(wb, __ldg(&twP[s * T * q])));
       acc[q] = cadd(acc[q], y);
     }
   }

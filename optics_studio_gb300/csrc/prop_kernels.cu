@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kThreads) k_passA(PropArgs a, int rows) {
       if (iy < ny && j < nx) {
         if (r > 1) {
           v = xin[(size_t)i * nx + j];
-          if (s > 0) v = cmul(v, twP[(int)(((long long)s * j) % P)]);
+          if (s > 0) v = cmul(v, twP[s * j]);
         } else {
           v = load_in<T>(a.in, a.in_c128, (size_t)iy * nx + j);
           if (a.status && nonfinite2((double)v.x, (double)v.y)) atomicOr(a.status, 1);
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(kThreads) k_passB(PropArgs a, int fwd_only, vo
       V v = zero;
       if (j < ny) {
         v = col[j];
-        if (t > 0) v = cmul(v, twP[(int)(((long long)t * j) % Py)]);
+        if (t > 0) v = cmul(v, twP[t * j]);
       }
       buf0[j] = v;
     }
@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(kThreads) k_passB(PropArgs a, int fwd_only, vo
     V* res2 = stockham<T, true>(res, other, my, 1, my, a.ay, twm);
     for (int j = threadIdx.x; j < ny; j += blockDim.x) {
       V v = res2[j];
-      if (t > 0) v = cmulc(v, twP[(int)(((long long)t * j) % Py)]);
+      if (t > 0) v = cmulc(v, twP[t * j]);
       acc[j] = cadd(acc[j], v);
     }
     __syncthreads();
@@ -630,7 +630,7 @@ __global__ void __launch_bounds__(kThreads) k_passC(PropArgs a, int rows) {
     for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
       const int i = e / nx, j = e - i * nx;
       V v = res[(size_t)i * ld + j];
-      if (s > 0) v = cmulc(v, twP[(int)(((long long)s * j) % P)]);
+      if (s > 0) v = cmulc(v, twP[s * j]);
       if (r > 1) {
         if (s == 0) acc[(size_t)i * nx + j] = v;
         else acc[(size_t)i * nx + j] = cadd(acc[(size_t)i * nx + j], v);
