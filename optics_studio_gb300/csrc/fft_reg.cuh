@@ -120,6 +120,15 @@ __device__ __forceinline__ void dft16(float2* v) {
 
 __device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
 
+// Twiddle-table read issued in place: volatile, so the compiler does not
+// merge the forward and inverse transforms' reads of the same entries
+// (which would keep them live in registers from one transform to the next).
+__device__ __forceinline__ float2 twl(const float2* p) {
+  float2 v;
+  asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+}
+
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
 
 template <int M> struct Plan {
@@ -155,7 +164,7 @@ __device__ __forceinline__ void fft(float2 (&v)[16], float2* s0, float2* s1,
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = src[pad(tid + T * q)];
 #pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], __ldg(&tw[q * k * tstride]));
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(&tw[q * k * tstride]));
     dft16<INV>(v);
     const int base = (tid - k) * 16 + k;
 #pragma unroll
@@ -169,7 +178,7 @@ __device__ __forceinline__ void fft(float2 (&v)[16], float2* s0, float2* s1,
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = src[pad(tid + T * q)];
 #pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], __ldg(&tw[q * tid]));
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(&tw[q * tid]));
     dft16<INV>(v);
   } else {
     // last stage radix RF, Ns = M/RF; butterflies j = tid + T i, i < 16/RF
@@ -183,11 +192,147 @@ __device__ __forceinline__ void fft(float2 (&v)[16], float2* s0, float2* s1,
 #pragma unroll
       for (int q = 0; q < RF; ++q) u[q] = src[pad(j + q * NSF)];
 #pragma unroll
-      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], __ldg(&tw[q * j]));
+      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], twl(&tw[q * j]));
       if (RF == 2) dft2<INV>(u[0], u[1]);
       if (RF == 4) dft4<INV>(u[0], u[1], u[2], u[3]);
       if (RF == 8) dft8<INV>(u);
       // output index j + q NSF = tid + T (i + q NB)
+#pragma unroll
+      for (int q = 0; q < RF; ++q) v[i + q * NB] = u[q];
+    }
+  }
+}
+
+// Single-buffer variant: the exchanges of all stages go through one padded
+// buffer (Plan<M>::SMEM float2), at the cost of a barrier before each store.
+// Same register layout and arithmetic as fft().  Every padded index is a
+// per-thread base plus a compile-time offset (T, Ns and M/RF are multiples of
+// 16, so pad(b + 16 c) = pad(b) + 17 c), which keeps the address arithmetic
+// in one register per stage.
+template <int M, bool INV>
+__device__ __forceinline__ void fft1(float2 (&v)[16], float2* buf, const float2* __restrict__ tw,
+                                     int tid) {
+  using P = Plan<M>;
+  constexpr int T = P::T;
+  constexpr int TP = T + T / 16;  // pad(x + T) - pad(x)
+  static_assert(T % 16 == 0, "register FFT needs M >= 256");
+  dft16<INV>(v);
+  __syncthreads();  // earlier readers of buf are done
+  {
+    float2* b0 = buf + 17 * tid;  // pad(16 tid + q) = 17 tid + q
+#pragma unroll
+    for (int q = 0; q < 16; ++q) b0[q] = v[q];
+  }
+  __syncthreads();
+  const float2* bl = buf + (tid + (tid >> 4));  // pad(tid + T q) = pad(tid) + TP q
+  int Ns = 16;
+  constexpr int mid16 = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;
+#pragma unroll
+  for (int st = 0; st < mid16; ++st) {
+    const int k = tid & (Ns - 1);
+    const int tstride = M / (Ns * 16);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
+    __syncthreads();
+#pragma unroll
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(tw + q * k * tstride));
+    dft16<INV>(v);
+    const int base = (tid - k) * 16 + k;
+    float2* bs = buf + (base + (base >> 4));
+    const int NP = Ns + Ns / 16;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) bs[NP * q] = v[q];
+    __syncthreads();
+    Ns *= 16;
+  }
+  if (P::RF == 1) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
+#pragma unroll
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(&tw[q * tid]));
+    dft16<INV>(v);
+  } else {
+    constexpr int RF = P::RF;
+    constexpr int NB = 16 / RF;
+    constexpr int NSF = M / RF;
+    constexpr int FP = NSF + NSF / 16;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const int j = tid + T * i;
+      const float2* bj = bl + TP * i;  // pad(j)
+      float2 u[RF];
+#pragma unroll
+      for (int q = 0; q < RF; ++q) u[q] = bj[FP * q];
+#pragma unroll
+      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], twl(&tw[q * j]));
+      if (RF == 2) dft2<INV>(u[0], u[1]);
+      if (RF == 4) dft4<INV>(u[0], u[1], u[2], u[3]);
+      if (RF == 8) dft8<INV>(u);
+#pragma unroll
+      for (int q = 0; q < RF; ++q) v[i + q * NB] = u[q];
+    }
+  }
+}
+
+// fft1 with the M-entry twiddle table in shared memory (plain loads).
+template <int M, bool INV>
+__device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2* tws, int tid) {
+  using P = Plan<M>;
+  constexpr int T = P::T;
+  constexpr int TP = T + T / 16;
+  static_assert(T % 16 == 0, "register FFT needs M >= 256");
+  dft16<INV>(v);
+  __syncthreads();
+  {
+    float2* b0 = buf + 17 * tid;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) b0[q] = v[q];
+  }
+  __syncthreads();
+  const float2* bl = buf + (tid + (tid >> 4));
+  int Ns = 16;
+  constexpr int mid16 = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;
+#pragma unroll
+  for (int st = 0; st < mid16; ++st) {
+    const int k = tid & (Ns - 1);
+    const int ts = (M / (Ns * 16)) * k;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
+    __syncthreads();
+#pragma unroll
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tws[q * ts]);
+    dft16<INV>(v);
+    const int base = (tid - k) * 16 + k;
+    float2* bs = buf + (base + (base >> 4));
+    const int NP = Ns + Ns / 16;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) bs[NP * q] = v[q];
+    __syncthreads();
+    Ns *= 16;
+  }
+  if (P::RF == 1) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
+#pragma unroll
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tws[q * tid]);
+    dft16<INV>(v);
+  } else {
+    constexpr int RF = P::RF;
+    constexpr int NB = 16 / RF;
+    constexpr int NSF = M / RF;
+    constexpr int FP = NSF + NSF / 16;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const int j = tid + T * i;
+      const float2* bj = bl + TP * i;
+      float2 u[RF];
+#pragma unroll
+      for (int q = 0; q < RF; ++q) u[q] = bj[FP * q];
+#pragma unroll
+      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], tws[q * j]);
+      if (RF == 2) dft2<INV>(u[0], u[1]);
+      if (RF == 4) dft4<INV>(u[0], u[1], u[2], u[3]);
+      if (RF == 8) dft8<INV>(u);
 #pragma unroll
       for (int q = 0; q < RF; ++q) v[i + q * NB] = u[q];
     }

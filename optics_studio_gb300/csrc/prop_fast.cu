@@ -8,6 +8,8 @@
 // Pass B runs one CTA per column pair (kx, Px - kx): the transfer functions
 // of the engines it serves are even in fx and fy, so one shared table of
 // H(kx, |k_y|) for |k_y| <= Py/2 serves all 4 quadrant bins of both columns.
+#include <cstdlib>
+
 #include "fft_reg.cuh"
 #include "prop_kernels.cuh"
 #include "elements.cuh"
@@ -53,57 +55,90 @@ __device__ __forceinline__ float2 h_asm_split(const PropArgs& a, float2 exc, flo
   return make_float2(hr * cs - hi * sn, hr * sn + hi * cs);
 }
 
+// ------------------------------------------------------------ layout
+//
+// One CTA per row (passes A, C) or per spectral column (pass B), G thread
+// groups of T = M/16 threads.  The r sub-transforms of the pruned
+// decomposition are spread over the groups (group g takes s = g, g + G, ...;
+// every group runs the same number of iterations so the barriers inside the
+// FFT match).  Shared memory holds the M-point twiddle table, the staged row
+// or column, one exchange buffer per group, and the pruning twiddles
+// W_P^{s j} = W_P^{s tid} W_P^{s T q} as two small tables.  Passes B and C
+// reduce the groups' partial sums through the exchange buffers.
+
+template <int M, int G>
+struct Lay {
+  static constexpr int T = M / 16;
+  static constexpr int THREADS = G * T;
+  static constexpr int MINB = THREADS >= 512 ? 1 : 512 / THREADS;
+};
+
+__device__ __forceinline__ void load_ptw(float2* tb, float2* tq, const float2* __restrict__ twP, int r,
+                                         int T) {
+  for (int i = threadIdx.x; i < r * T; i += blockDim.x) {
+    const int s = i / T, t = i - s * T;
+    tb[i] = twP[s * t];
+  }
+  for (int i = threadIdx.x; i < r * 16; i += blockDim.x) {
+    const int s = i >> 4, q = i & 15;
+    tq[i] = twP[s * T * q];
+  }
+}
+
 // ---------------------------------------------------------------- pass B
 
-template <int M>
-__global__ void __launch_bounds__(2 * (M / 16), (M <= 2048 ? 2 : 1)) k_passB_reg(PropArgs a, int use_table) {
+template <int M, int G>
+__global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
+    k_passB_v3(PropArgs a, int use_table) {
   constexpr int T = M / 16;
+  constexpr int U = M / 2 + 1;
+  constexpr int SB = Plan<M>::SMEM;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int half = threadIdx.x / T;  // which column of the pair
-  const int tid = threadIdx.x - half * T;
-  float2* s0 = sm + (size_t)half * 2 * Plan<M>::SMEM;
-  float2* s1 = s0 + Plan<M>::SMEM;
-  float2* htab = sm + 4 * Plan<M>::SMEM;
-  const int Px = a.ax.P, Py = a.ay.P, ry = a.ay.r, ny = a.ny;
-  const int p = blockIdx.x;
-  int kx = p;
-  bool active = true;
-  if (half == 1) {
-    // columns 0 and Px/2 have no partner: the second half recomputes column
-    // p and does not store (every thread must reach the FFT barriers)
-    const bool single = (p == 0) || (2 * p == Px);
-    kx = single ? p : Px - p;
-    active = !single;
-  }
+  const int Py = a.ay.P, ry = a.ay.r, ny = a.ny;
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* col = tws + M;
+  float2* bufs = col + M;
+  float2* tb = bufs + G * SB;
+  float2* tq = tb + ry * T;
+  float2* htab = tq + ry * 16;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  const int kx = blockIdx.x;
+  float2* buf = bufs + g * SB;
+  float2* W = reinterpret_cast<float2*>(a.work) + (size_t)kx * ny;
   const float2* twm = reinterpret_cast<const float2*>(a.tw_my);
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Py);
-  float2* W = reinterpret_cast<float2*>(a.work) + (size_t)kx * ny;
 
-  // Column data of kx0 = p (shared by the pair: |fx| is equal).
-  const bool asm_split = (a.engine == ENG_ASM && a.h_mode == 1);
-  const bool fres = (a.engine == ENG_FRESNEL_TF && a.h_mode == 1);
-  float2 exc = make_float2(0.f, 0.f);
-  float cah = 0.f, cal = 0.f, sac = 0.f;
-  int kmc = -1;
-  if (asm_split || fres) exc = a.Ex[p];
-  if (asm_split) {
-    cah = a.ca_hi[p];
-    cal = a.ca_lo[p];
-    sac = a.sa[p];
-    kmc = a.kmax[p];
+  for (int i = threadIdx.x; i < M; i += blockDim.x) {
+    tws[i] = twm[i];
+    col[i] = (i < ny) ? W[i] : make_float2(0.f, 0.f);
   }
-  const int hh = Py / 2;
+  load_ptw(tb, tq, twP, ry, T);
   if (use_table) {
-    for (int k = threadIdx.x; k <= hh; k += blockDim.x) {
+    // H(kx, |k_y|) for |k_y| <= Py/2 (H even in fy), row rr = |k_y| mod ry
+    const bool asm_split = (a.engine == ENG_ASM);
+    const float2 exc = a.Ex[kx];
+    float cah = 0.f, cal = 0.f, sac = 0.f;
+    int kmc = -1;
+    if (asm_split) {
+      cah = a.ca_hi[kx];
+      cal = a.ca_lo[kx];
+      sac = a.sa[kx];
+      kmc = a.kmax[kx];
+    }
+    const int hh = Py / 2;
+    for (int idx = threadIdx.x; idx < ry * U; idx += blockDim.x) {
+      const int rr = idx / U, u = idx - rr * U;
+      const int akk = ry * u + rr;
+      if (akk > hh) continue;
       float2 h;
       if (asm_split) {
-        h = h_asm_split(a, exc, cah, cal, sac, kmc, k, k);
-      } else {  // Fresnel TF: Ex[kx] Ey[ky]
-        const float2 ey = a.Ey[k];
+        h = h_asm_split(a, exc, cah, cal, sac, kmc, akk, akk);
+      } else {
+        const float2 ey = a.Ey[akk];
         h = make_float2(exc.x * ey.x - exc.y * ey.y, exc.x * ey.y + exc.y * ey.x);
       }
-      htab[k] = h;
+      htab[idx] = h;
     }
   }
   __syncthreads();
@@ -111,30 +146,38 @@ __global__ void __launch_bounds__(2 * (M / 16), (M <= 2048 ? 2 : 1)) k_passB_reg
   float2 acc[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
-  for (int t = 0; t < ry; ++t) {
-    // W_P^{t j} for j = tid + T q  (t j < ry M = Py, no reduction needed):
-    // W_P^{t tid} (per thread) times W_P^{t T q} (uniform across the CTA)
-    const float2 wb = __ldg(&twP[t * tid]);
+  const int iters = (ry + G - 1) / G;
+  for (int it = 0; it < iters; ++it) {
+    const int t = g + G * it;
+    const bool valid = t < ry;
+    const int tt = valid ? t : 0;
+    const float2 wb = tb[tt * T + tid];
     float2 v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      const int j = tid + T * q;
-      float2 x = make_float2(0.f, 0.f);
-      if (j < ny) {
-        x = W[j];
-        if (t > 0) x = cmul(x, cmul(wb, __ldg(&twP[t * T * q])));
-      }
+      float2 x = valid ? col[tid + T * q] : make_float2(0.f, 0.f);
+      if (tt > 0) x = cmul(x, cmul(wb, tq[tt * 16 + q]));
       v[q] = x;
     }
-    fft<M, false>(v, s0, s1, twm, tid);
+    fft1s<M, false>(v, buf, tws, tid);
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      const int ky = ry * (tid + T * q) + t;
-      const int kk = (ky <= (Py - 1) / 2) ? ky : ky - Py;
-      const int akk = kk < 0 ? -kk : kk;
+      const int pp = tid + T * q;
+      const int ky = ry * pp + tt;
       float2 h;
       if (use_table) {
-        h = htab[akk];
+        int rr, u;
+        if (ky <= (Py - 1) / 2) {
+          rr = tt;
+          u = pp;
+        } else if (tt == 0) {
+          rr = 0;
+          u = M - pp;
+        } else {
+          rr = ry - tt;
+          u = M - pp - 1;
+        }
+        h = htab[rr * U + u];
       } else if (a.engine == ENG_KSPEC) {
         h = __ldg(reinterpret_cast<const float2*>(a.kspec) + (size_t)kx * Py + ky);
         if (a.conj_h) h.y = -h.y;
@@ -142,52 +185,65 @@ __global__ void __launch_bounds__(2 * (M / 16), (M <= 2048 ? 2 : 1)) k_passB_reg
         h = cmul(__ldg(reinterpret_cast<const float2*>(a.hx) + kx),
                  __ldg(reinterpret_cast<const float2*>(a.hy) + ky));
         if (a.conj_h) h.y = -h.y;
-      } else {  // ENG_IDENTITY
+      } else if (a.engine == ENG_ASM) {  // table did not fit: per bin
+        const int kk = (ky <= (Py - 1) / 2) ? ky : ky - Py;
+        h = h_asm_split(a, a.Ex[kx], a.ca_hi[kx], a.ca_lo[kx], a.sa[kx], a.kmax[kx], ky,
+                        kk < 0 ? -kk : kk);
+      } else if (a.engine == ENG_FRESNEL_TF) {
+        const float2 ex = a.Ex[kx], ey = a.Ey[ky];
+        h = make_float2(ex.x * ey.x - ex.y * ey.y, ex.x * ey.y + ex.y * ey.x);
+      } else {
         h = make_float2((float)a.scale, 0.f);
       }
       v[q] = cmul(v[q], h);
     }
-    fft<M, true>(v, s0, s1, twm, tid);
+    fft1s<M, true>(v, buf, tws, tid);
+    if (valid) {
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int j = tid + T * q;
-      float2 y = v[q];
-      if (t > 0 && j < ny) y = cmulc(y, cmul(wb, __ldg(&twP[t * T * q])));
-      acc[q] = cadd(acc[q], y);
+      for (int q = 0; q < 16; ++q) {
+        float2 y = v[q];
+        if (tt > 0) y = cmulc(y, cmul(wb, tq[tt * 16 + q]));
+        acc[q] = cadd(acc[q], y);
+      }
     }
   }
-  if (active) {
+  // reduce the G partial columns through the exchange buffers
+  __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int j = tid + T * q;
-      if (j < ny) W[j] = acc[q];
-    }
+  for (int q = 0; q < 16; ++q) buf[tid + T * q] = acc[q];
+  __syncthreads();
+  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+    float2 sum = bufs[j];
+#pragma unroll
+    for (int gg = 1; gg < G; ++gg) sum = cadd(sum, bufs[gg * SB + j]);
+    W[j] = sum;
   }
 }
 
 // ---------------------------------------------------------------- pass A
 
-template <int M>
-__global__ void __launch_bounds__(256, 2) k_passA_reg(PropArgs a, int rows) {
+template <int M, int G>
+__global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v3(PropArgs a) {
   constexpr int T = M / 16;
+  constexpr int SB = Plan<M>::SMEM;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int r = threadIdx.x / T;
-  const int tid = threadIdx.x - r * T;
-  float2* s0 = sm + (size_t)r * 2 * Plan<M>::SMEM;
-  float2* s1 = s0 + Plan<M>::SMEM;
-  const int nx = a.nx, ny = a.ny, rx = a.ax.r, Px = a.ax.P;
-  const int iy = blockIdx.x * rows + r;
-  const bool live = iy < ny;
+  const int nx = a.nx, ny = a.ny, rx = a.ax.r;
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* xin = tws + M;
+  float2* bufs = xin + M;
+  float2* tb = bufs + G * SB;
+  float2* tq = tb + rx * T;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  const int iy = blockIdx.x;
+  float2* buf = bufs + g * SB;
   const float2* twm = reinterpret_cast<const float2*>(a.tw_mx);
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   float2* W = reinterpret_cast<float2*>(a.work);
-  float2 xin[16];
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int j = tid + T * q;
+  for (int j = threadIdx.x; j < M; j += blockDim.x) {
+    tws[j] = twm[j];
     float2 x = make_float2(0.f, 0.f);
-    if (live && j < nx) {
+    if (j < nx) {
       x = ld_in(a.in, a.in_c128, (size_t)iy * nx + j);
       if (a.status && (!isfinite(x.x) || !isfinite(x.y))) atomicOr(a.status, 1);
       if (a.els.count) {
@@ -200,18 +256,25 @@ __global__ void __launch_bounds__(256, 2) k_passA_reg(PropArgs a, int rows) {
         }
       }
     }
-    xin[q] = x;
+    xin[j] = x;
   }
-  for (int s = 0; s < rx; ++s) {
-    const float2 wb = __ldg(&twP[s * tid]);  // s j < rx M = Px
+  load_ptw(tb, tq, twP, rx, T);
+  __syncthreads();
+  const int iters = (rx + G - 1) / G;
+  for (int it = 0; it < iters; ++it) {
+    const int s = g + G * it;
+    const bool valid = s < rx;
+    const int ss = valid ? s : 0;
+    const float2 wb = tb[ss * T + tid];
     float2 v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      const int j = tid + T * q;
-      v[q] = (s > 0 && j < nx) ? cmul(xin[q], cmul(wb, __ldg(&twP[s * T * q]))) : xin[q];
+      float2 x = xin[tid + T * q];
+      if (ss > 0) x = cmul(x, cmul(wb, tq[ss * 16 + q]));
+      v[q] = x;
     }
-    fft<M, false>(v, s0, s1, twm, tid);
-    if (live) {
+    fft1s<M, false>(v, buf, tws, tid);
+    if (valid) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) W[(size_t)(rx * (tid + T * q) + s) * ny + iy] = v[q];
     }
@@ -220,45 +283,58 @@ __global__ void __launch_bounds__(256, 2) k_passA_reg(PropArgs a, int rows) {
 
 // ---------------------------------------------------------------- pass C
 
-template <int M>
-__global__ void __launch_bounds__(256, 2) k_passC_reg(PropArgs a, int rows) {
+template <int M, int G>
+__global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v3(PropArgs a) {
   constexpr int T = M / 16;
+  constexpr int SB = Plan<M>::SMEM;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int r = threadIdx.x / T;
-  const int tid = threadIdx.x - r * T;
-  float2* s0 = sm + (size_t)r * 2 * Plan<M>::SMEM;
-  float2* s1 = s0 + Plan<M>::SMEM;
-  const int nx = a.nx, ny = a.ny, rx = a.ax.r, Px = a.ax.P;
-  const int iy = blockIdx.x * rows + r;
-  const bool live = iy < ny;
+  const int nx = a.nx, ny = a.ny, rx = a.ax.r;
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* bufs = tws + M;
+  float2* tb = bufs + G * SB;
+  float2* tq = tb + rx * T;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  const int iy = blockIdx.x;
+  float2* buf = bufs + g * SB;
   const float2* twm = reinterpret_cast<const float2*>(a.tw_mx);
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   const float2* W = reinterpret_cast<const float2*>(a.work);
+  for (int j = threadIdx.x; j < M; j += blockDim.x) tws[j] = twm[j];
+  load_ptw(tb, tq, twP, rx, T);
+  // first gathers before the barrier: they overlap the table loads
+  const int iters = (rx + G - 1) / G;
   float2 acc[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
-  for (int s = 0; s < rx; ++s) {
+  __syncthreads();
+  for (int it = 0; it < iters; ++it) {
+    const int s = g + G * it;
+    const bool valid = s < rx;
+    const int ss = valid ? s : 0;
     float2 v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q)
-      v[q] = live ? W[(size_t)(rx * (tid + T * q) + s) * ny + iy] : make_float2(0.f, 0.f);
-    fft<M, true>(v, s0, s1, twm, tid);
-    const float2 wb = __ldg(&twP[s * tid]);
+      v[q] = valid ? W[(size_t)(rx * (tid + T * q) + s) * ny + iy] : make_float2(0.f, 0.f);
+    fft1s<M, true>(v, buf, tws, tid);
+    if (valid) {
+      const float2 wb = tb[ss * T + tid];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int j = tid + T * q;
-      float2 y = v[q];
-      if (s > 0 && j < nx) y = cmulc(y, cmul(wb, __ldg(&twP[s * T * q])));
-      acc[q] = cadd(acc[q], y);
+      for (int q = 0; q < 16; ++q) {
+        float2 y = v[q];
+        if (ss > 0) y = cmulc(y, cmul(wb, tq[ss * 16 + q]));
+        acc[q] = cadd(acc[q], y);
+      }
     }
   }
-  if (!live) return;
+  __syncthreads();
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int j = tid + T * q;
-    if (j >= nx) continue;
-    const float2 v = acc[q];
+  for (int q = 0; q < 16; ++q) buf[tid + T * q] = acc[q];
+  __syncthreads();
+  for (int j = threadIdx.x; j < nx; j += blockDim.x) {
+    float2 v = bufs[j];
+#pragma unroll
+    for (int gg = 1; gg < G; ++gg) v = cadd(v, bufs[gg * SB + j]);
     const size_t o = (size_t)iy * nx + j;
     if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
     if (a.out) {
@@ -270,45 +346,101 @@ __global__ void __launch_bounds__(256, 2) k_passC_reg(PropArgs a, int rows) {
   }
 }
 
+constexpr size_t kMaxSmemB = 232448;
+
+template <int M, int G>
+size_t smem_v3(int kind, int r, int table) {
+  constexpr int T = M / 16;
+  size_t n = (size_t)M + (size_t)G * Plan<M>::SMEM + (size_t)r * (T + 16);
+  if (kind != 2) n += M;  // staged row (A) or column (B)
+  if (kind == 1 && table) n += (size_t)r * (M / 2 + 1);
+  return n * sizeof(float2);
+}
+
+int env_groups(const char* name, int dflt) {
+  const char* e = getenv(name);
+  if (!e) return dflt;
+  int g = atoi(e);
+  return (g == 1 || g == 2 || g == 4) ? g : dflt;
+}
+
+template <int M, int G>
+cudaError_t launchB_mg(const PropArgs& a, int use_table, cudaStream_t st) {
+  const size_t smem = smem_v3<M, G>(1, a.ay.r, use_table);
+  cudaError_t e = cudaFuncSetAttribute(k_passB_v3<M, G>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  k_passB_v3<M, G><<<a.ax.P, Lay<M, G>::THREADS, smem, st>>>(a, use_table);
+  return cudaGetLastError();
+}
+
+template <int M, int G>
+cudaError_t launchA_mg(const PropArgs& a, cudaStream_t st) {
+  const size_t smem = smem_v3<M, G>(0, a.ax.r, 0);
+  cudaError_t e = cudaFuncSetAttribute(k_passA_v3<M, G>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  k_passA_v3<M, G><<<a.ny, Lay<M, G>::THREADS, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int M, int G>
+cudaError_t launchC_mg(const PropArgs& a, cudaStream_t st) {
+  const size_t smem = smem_v3<M, G>(2, a.ax.r, 0);
+  cudaError_t e = cudaFuncSetAttribute(k_passC_v3<M, G>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  k_passC_v3<M, G><<<a.ny, Lay<M, G>::THREADS, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+// Largest group count <= want (and <= r) whose shared memory fits, with
+// 32..512 threads per CTA (one warp at least; at most 512 so that the
+// 128-register budget of the FFT holds).
 template <int M>
-size_t smem_B() { return (4 * (size_t)Plan<M>::SMEM) * sizeof(float2); }
+int pick_groups(int kind, int r, int table, int want) {
+  constexpr int T = M / 16;
+  int g = want;
+  while (g > r && g > 1) g >>= 1;
+  while (g > 1 && g * T > 512) g >>= 1;
+  if (g * T < 32) g = 32 / T;
+  while (g > 1 && g * T > 32) {
+    const size_t b = g == 4 ? smem_v3<M, 4>(kind, r, table)
+                            : smem_v3<M, 2>(kind, r, table);
+    if (b <= kMaxSmemB) break;
+    g >>= 1;
+  }
+  return g;
+}
 
 template <int M>
 cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
   const bool even = (a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF) && a.h_mode == 1;
-  const int use_table = even ? 1 : 0;
-  const size_t smem = smem_B<M>() + (use_table ? (size_t)(a.ay.P / 2 + 1) * sizeof(float2) : 0);
-  cudaError_t e = cudaFuncSetAttribute(k_passB_reg<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  const int pairs = a.ax.P / 2 + 1;
-  ++launch_counter();
-  k_passB_reg<M><<<pairs, 2 * (M / 16), smem, st>>>(a, use_table);
-  return cudaGetLastError();
+  int table = even ? 1 : 0;
+  if (table && smem_v3<M, 1>(1, a.ay.r, 1) > kMaxSmemB) table = 0;
+  const int g = pick_groups<M>(1, a.ay.r, table, env_groups("OSGPU_GROUPS_B", 4));
+  if (g == 4) return launchB_mg<M, 4>(a, table, st);
+  if (g == 2) return launchB_mg<M, 2>(a, table, st);
+  return launchB_mg<M, 1>(a, table, st);
 }
 
 template <int M>
 cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
-  const int rows = 256 / (M / 16) > 0 ? 256 / (M / 16) : 1;
-  const size_t smem = (size_t)rows * 2 * Plan<M>::SMEM * sizeof(float2);
-  cudaError_t e = cudaFuncSetAttribute(k_passA_reg<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  ++launch_counter();
-  k_passA_reg<M><<<(a.ny + rows - 1) / rows, rows * (M / 16), smem, st>>>(a, rows);
-  return cudaGetLastError();
+  const int g = pick_groups<M>(0, a.ax.r, 0, env_groups("OSGPU_GROUPS_A", 4));
+  if (g == 4) return launchA_mg<M, 4>(a, st);
+  if (g == 2) return launchA_mg<M, 2>(a, st);
+  return launchA_mg<M, 1>(a, st);
 }
 
 template <int M>
 cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
-  const int rows = 256 / (M / 16) > 0 ? 256 / (M / 16) : 1;
-  const size_t smem = (size_t)rows * 2 * Plan<M>::SMEM * sizeof(float2);
-  cudaError_t e = cudaFuncSetAttribute(k_passC_reg<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  ++launch_counter();
-  k_passC_reg<M><<<(a.ny + rows - 1) / rows, rows * (M / 16), smem, st>>>(a, rows);
-  return cudaGetLastError();
+  const int g = pick_groups<M>(2, a.ax.r, 0, env_groups("OSGPU_GROUPS_C", 4));
+  if (g == 4) return launchC_mg<M, 4>(a, st);
+  if (g == 2) return launchC_mg<M, 2>(a, st);
+  return launchC_mg<M, 1>(a, st);
 }
 
 }  // namespace
