@@ -321,7 +321,7 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
   };
   const size_t o_work = carve(Px * ny * es);
   size_t o_fxv = 0, o_fyv = 0, o_Ex = 0, o_Ey = 0, o_cah = 0, o_cal = 0, o_sa = 0, o_bh = 0,
-         o_bl = 0, o_km = 0, o_hx = 0, o_hy = 0, o_tmp = 0, o_ks = 0;
+         o_bl = 0, o_km = 0, o_hx = 0, o_hy = 0, o_tmp = 0, o_ks = 0, o_rt = 0;
   const bool tf = (j.engine == ENG_ASM || j.engine == ENG_FRESNEL_TF);
   if (tf) {
     o_fxv = carve(Px * 8);
@@ -334,6 +334,7 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
     o_bh = carve(Py * 4);
     o_bl = carve(Py * 4);
     o_km = carve(Px * 4);
+    o_rt = carve(Py * 16);
   } else if (j.engine == ENG_KSEP) {
     o_hx = carve(Px * es);
     o_hy = carve(Py * es);
@@ -357,6 +358,7 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
     a.b_hi = reinterpret_cast<const float*>(base + o_bh);
     a.b_lo = reinterpret_cast<const float*>(base + o_bl);
     a.kmax = reinterpret_cast<const int*>(base + o_km);
+    a.rowtab = base + o_rt;
     if (j.engine == ENG_ASM) {
       const double lam_n = j.g.lambda / j.medium;
       a.lam_n = lam_n;

@@ -85,6 +85,29 @@ __device__ __forceinline__ void load_ptw(float2* tb, float2* tq, const float2* _
   }
 }
 
+// h_asm_split with the row data (Ey, b_hi, b_lo) already loaded.
+__device__ __forceinline__ float2 h_asm_split_row(const PropArgs& a, float2 exc, float cah,
+                                                  float cal, float sac, int kmc, int akk,
+                                                  float2 ey, float bh, float blo) {
+  if (akk > kmc) return make_float2(0.f, 0.f);
+  const float s = sac + bh;
+  const float q = sqrtf(fmaxf(1.f - s, 0.f));
+  const float opq = 1.f + q;
+  const float tau = a.Kf * (s * s * s) * (3.f + q) / (8.f * opq * opq * opq);
+  const float pr = cah * bh;
+  const float er = fmaf(cah, bh, -pr);
+  const float corr = er + (cah * blo + cal * bh);
+  const float nq = rintf(pr * 0.159154943091895336f);
+  float rr = fmaf(-nq, 6.28125f, pr);
+  rr = fmaf(-nq, 1.93530717958647692e-3f, rr);
+  const float th = rr + (corr - tau);
+  float sn, cs;
+  __sincosf(th, &sn, &cs);
+  const float hr = exc.x * ey.x - exc.y * ey.y;
+  const float hi = exc.x * ey.y + exc.y * ey.x;
+  return make_float2(hr * cs - hi * sn, hr * sn + hi * cs);
+}
+
 // ---------------------------------------------------------------- pass B
 
 template <int M, int G>
@@ -109,7 +132,10 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
   const float2* twm = reinterpret_cast<const float2*>(a.tw_my);
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Py);
 
-  for (int i = threadIdx.x; i < M; i += blockDim.x) {
+  constexpr int NT = Lay<M, G>::THREADS;
+#pragma unroll
+  for (int k = 0; k < M / NT; ++k) {
+    const int i = threadIdx.x + k * NT;
     tws[i] = twm[i];
     col[i] = (i < ny) ? W[i] : make_float2(0.f, 0.f);
   }
@@ -127,18 +153,31 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
       kmc = a.kmax[kx];
     }
     const int hh = Py / 2;
-    for (int idx = threadIdx.x; idx < ry * U; idx += blockDim.x) {
-      const int rr = idx / U, u = idx - rr * U;
-      const int akk = ry * u + rr;
-      if (akk > hh) continue;
-      float2 h;
-      if (asm_split) {
-        h = h_asm_split(a, exc, cah, cal, sac, kmc, akk, akk);
-      } else {
-        const float2 ey = a.Ey[akk];
-        h = make_float2(exc.x * ey.x - exc.y * ey.y, exc.x * ey.y + exc.y * ey.x);
+    const float4* rt = reinterpret_cast<const float4*>(a.rowtab);
+    constexpr int UNR = 4;
+    for (int base = threadIdx.x; base < ry * U; base += UNR * NT) {
+      float4 rv[UNR];
+      int ak[UNR];
+#pragma unroll
+      for (int k = 0; k < UNR; ++k) {  // issue the loads first
+        const int idx = base + k * NT;
+        const int rr = idx / U, u = idx - rr * U;
+        ak[k] = ry * u + rr;
+        rv[k] = (idx < ry * U && ak[k] <= hh) ? __ldg(rt + ak[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      htab[idx] = h;
+#pragma unroll
+      for (int k = 0; k < UNR; ++k) {
+        const int idx = base + k * NT;
+        if (idx >= ry * U || ak[k] > hh) continue;
+        const float2 ey = make_float2(rv[k].x, rv[k].y);
+        float2 h;
+        if (asm_split) {
+          h = h_asm_split_row(a, exc, cah, cal, sac, kmc, ak[k], ey, rv[k].z, rv[k].w);
+        } else {
+          h = make_float2(exc.x * ey.x - exc.y * ey.y, exc.x * ey.y + exc.y * ey.x);
+        }
+        htab[idx] = h;
+      }
     }
   }
   __syncthreads();
@@ -159,7 +198,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
       if (tt > 0) x = cmul(x, cmul(wb, tq[tt * 16 + q]));
       v[q] = x;
     }
-    fft1s<M, false>(v, buf, tws, tid);
+    fft1s<M, false>(v, buf, tws, tid, 1 + g);
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const int pp = tid + T * q;
@@ -197,7 +236,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
       }
       v[q] = cmul(v[q], h);
     }
-    fft1s<M, true>(v, buf, tws, tid);
+    fft1s<M, true>(v, buf, tws, tid, 1 + g);
     if (valid) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
@@ -240,7 +279,10 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
   const float2* twm = reinterpret_cast<const float2*>(a.tw_mx);
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   float2* W = reinterpret_cast<float2*>(a.work);
-  for (int j = threadIdx.x; j < M; j += blockDim.x) {
+  constexpr int NT = Lay<M, G>::THREADS;
+#pragma unroll
+  for (int k = 0; k < M / NT; ++k) {
+    const int j = threadIdx.x + k * NT;
     tws[j] = twm[j];
     float2 x = make_float2(0.f, 0.f);
     if (j < nx) {
@@ -273,7 +315,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
       if (ss > 0) x = cmul(x, cmul(wb, tq[ss * 16 + q]));
       v[q] = x;
     }
-    fft1s<M, false>(v, buf, tws, tid);
+    fft1s<M, false>(v, buf, tws, tid, 1 + g);
     if (valid) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) W[(size_t)(rx * (tid + T * q) + s) * ny + iy] = v[q];
@@ -300,7 +342,9 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
   const float2* twm = reinterpret_cast<const float2*>(a.tw_mx);
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   const float2* W = reinterpret_cast<const float2*>(a.work);
-  for (int j = threadIdx.x; j < M; j += blockDim.x) tws[j] = twm[j];
+  constexpr int NT = Lay<M, G>::THREADS;
+#pragma unroll
+  for (int k = 0; k < M / NT; ++k) tws[threadIdx.x + k * NT] = twm[threadIdx.x + k * NT];
   load_ptw(tb, tq, twP, rx, T);
   // first gathers before the barrier: they overlap the table loads
   const int iters = (rx + G - 1) / G;
@@ -316,7 +360,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
 #pragma unroll
     for (int q = 0; q < 16; ++q)
       v[q] = valid ? W[(size_t)(rx * (tid + T * q) + s) * ny + iy] : make_float2(0.f, 0.f);
-    fft1s<M, true>(v, buf, tws, tid);
+    fft1s<M, true>(v, buf, tws, tid, 1 + g);
     if (valid) {
       const float2 wb = tb[ss * T + tid];
 #pragma unroll

@@ -267,7 +267,7 @@ cudaError_t launch_twiddles(void* dst, int n, int is_double, cudaStream_t st) {
 //   Fresnel TF: Ex = e^{i (kz - c fx^2)} * scale, Ey = e^{-i c fy^2}.
 __global__ void k_axis_prep(PropArgs a, double* fxv, double* fyv, float2* Ex, float2* Ey,
                             float* ca_hi, float* ca_lo, float* sa, float* b_hi, float* b_lo,
-                            int* kmax) {
+                            int* kmax, float4* rowtab) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int Px = a.ax.P, Py = a.ay.P;
   const double K = a.kz;
@@ -334,11 +334,13 @@ __global__ void k_axis_prep(PropArgs a, double* fxv, double* fyv, float2* Ex, fl
         const float h = (float)bb;
         b_hi[i] = h;
         b_lo[i] = (float)(bb - (double)h);
+        if (rowtab) rowtab[i] = make_float4((float)c, (float)s, h, (float)(bb - (double)h));
       } else if (a.engine == ENG_FRESNEL_TF) {
         const double ph = -a.cfr * (fy * fy);
         double s, c;
         sincos(ph, &s, &c);
         Ey[i] = make_float2((float)c, (float)s);
+        if (rowtab) rowtab[i] = make_float4((float)c, (float)s, 0.f, 0.f);
       }
     }
   }
@@ -353,7 +355,7 @@ cudaError_t launch_asm_prep(const PropArgs& a, void* tables, cudaStream_t st) {
       a, const_cast<double*>(a.fxv), const_cast<double*>(a.fyv), const_cast<float2*>(a.Ex),
       const_cast<float2*>(a.Ey), const_cast<float*>(a.ca_hi), const_cast<float*>(a.ca_lo),
       const_cast<float*>(a.sa), const_cast<float*>(a.b_hi), const_cast<float*>(a.b_lo),
-      const_cast<int*>(a.kmax));
+      const_cast<int*>(a.kmax), reinterpret_cast<float4*>(const_cast<void*>(a.rowtab)));
   return cudaGetLastError();
 }
 

@@ -45,6 +45,7 @@ struct PropArgs {
   const float* b_hi;   // b = (lam_n fy)^2 (double-float)
   const float* b_lo;
   const int* kmax;     // per column: largest unmasked |k_y| (-1: column masked)
+  const void* rowtab;  // f32 split: per row {Ey.x, Ey.y, b_hi, b_lo} packed (float4)
   float Kf;            // kz as f32 (for the small residual term)
   // kernel spectra
   const void* kspec;   // ENG_KSPEC: column-major Px x Py spectrum (type of engine)
