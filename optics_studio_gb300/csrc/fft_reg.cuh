@@ -274,8 +274,9 @@ __device__ __forceinline__ void fft1(float2 (&v)[16], float2* buf, const float2*
   }
 }
 
-// Barrier over the T threads of one group (named barrier `id`, 1..15; id 0
-// is __syncthreads).  T is a multiple of 32.
+// Named barrier `id` (1..15; id 0 is __syncthreads) over `nthreads`
+// threads, which must be whole warps: callers whose groups are narrower than
+// a warp pass one shared id and the CTA's thread count.
 __device__ __forceinline__ void group_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
@@ -284,19 +285,19 @@ __device__ __forceinline__ void group_sync(int id, int nthreads) {
 // per-group barrier, so the groups of a CTA proceed independently.
 template <int M, bool INV>
 __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2* tws, int tid,
-                                      int bar_id) {
+                                      int bar_id, int bar_count) {
   using P = Plan<M>;
   constexpr int T = P::T;
   constexpr int TP = T + T / 16;
   static_assert(T % 16 == 0, "register FFT needs M >= 256");
   dft16<INV>(v);
-  group_sync(bar_id, P::T);
+  group_sync(bar_id, bar_count);
   {
     float2* b0 = buf + 17 * tid;
 #pragma unroll
     for (int q = 0; q < 16; ++q) b0[q] = v[q];
   }
-  group_sync(bar_id, P::T);
+  group_sync(bar_id, bar_count);
   const float2* bl = buf + (tid + (tid >> 4));
   int Ns = 16;
   constexpr int mid16 = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;
@@ -306,7 +307,7 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
     const int ts = (M / (Ns * 16)) * k;
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
-    group_sync(bar_id, P::T);
+    group_sync(bar_id, bar_count);
 #pragma unroll
     for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tws[q * ts]);
     dft16<INV>(v);
@@ -315,7 +316,7 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
     const int NP = Ns + Ns / 16;
 #pragma unroll
     for (int q = 0; q < 16; ++q) bs[NP * q] = v[q];
-    group_sync(bar_id, P::T);
+    group_sync(bar_id, bar_count);
     Ns *= 16;
   }
   if (P::RF == 1) {

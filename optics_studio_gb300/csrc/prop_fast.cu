@@ -126,6 +126,9 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
   float2* htab = tq + ry * 16;
   const int g = threadIdx.x / T;
   const int tid = threadIdx.x - g * T;
+  // per-group barrier when a group is whole warps, else one CTA-wide barrier
+  const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
+  const int BAR_N = (T % 32 == 0) ? T : Lay<M, G>::THREADS;
   const int kx = blockIdx.x;
   float2* buf = bufs + g * SB;
   float2* W = reinterpret_cast<float2*>(a.work) + (size_t)kx * ny;
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
       if (tt > 0) x = cmul(x, cmul(wb, tq[tt * 16 + q]));
       v[q] = x;
     }
-    fft1s<M, false>(v, buf, tws, tid, 1 + g);
+    fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const int pp = tid + T * q;
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
       }
       v[q] = cmul(v[q], h);
     }
-    fft1s<M, true>(v, buf, tws, tid, 1 + g);
+    fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
     if (valid) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
@@ -274,6 +277,9 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
   float2* tq = tb + rx * T;
   const int g = threadIdx.x / T;
   const int tid = threadIdx.x - g * T;
+  // per-group barrier when a group is whole warps, else one CTA-wide barrier
+  const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
+  const int BAR_N = (T % 32 == 0) ? T : Lay<M, G>::THREADS;
   const int iy = blockIdx.x;
   float2* buf = bufs + g * SB;
   const float2* twm = reinterpret_cast<const float2*>(a.tw_mx);
@@ -315,7 +321,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
       if (ss > 0) x = cmul(x, cmul(wb, tq[ss * 16 + q]));
       v[q] = x;
     }
-    fft1s<M, false>(v, buf, tws, tid, 1 + g);
+    fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
     if (valid) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) W[(size_t)(rx * (tid + T * q) + s) * ny + iy] = v[q];
@@ -337,6 +343,9 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
   float2* tq = tb + rx * T;
   const int g = threadIdx.x / T;
   const int tid = threadIdx.x - g * T;
+  // per-group barrier when a group is whole warps, else one CTA-wide barrier
+  const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
+  const int BAR_N = (T % 32 == 0) ? T : Lay<M, G>::THREADS;
   const int iy = blockIdx.x;
   float2* buf = bufs + g * SB;
   const float2* twm = reinterpret_cast<const float2*>(a.tw_mx);
@@ -360,7 +369,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
 #pragma unroll
     for (int q = 0; q < 16; ++q)
       v[q] = valid ? W[(size_t)(rx * (tid + T * q) + s) * ny + iy] : make_float2(0.f, 0.f);
-    fft1s<M, true>(v, buf, tws, tid, 1 + g);
+    fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
     if (valid) {
       const float2 wb = tb[ss * T + tid];
 #pragma unroll
