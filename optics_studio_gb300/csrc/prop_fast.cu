@@ -474,7 +474,7 @@ cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
   const bool even = (a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF) && a.h_mode == 1;
   int table = even ? 1 : 0;
   if (table && smem_v3<M, 1>(1, a.ay.r, 1) > kMaxSmemB) table = 0;
-  const int g = pick_groups<M>(1, a.ay.r, table, env_groups("OSGPU_GROUPS_B", 4));
+  const int g = pick_groups<M>(1, a.ay.r, table, env_groups("OSGPU_GROUPS_B", 2));
   if (g == 4) return launchB_mg<M, 4>(a, table, st);
   if (g == 2) return launchB_mg<M, 2>(a, table, st);
   return launchB_mg<M, 1>(a, table, st);
@@ -482,7 +482,7 @@ cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
 
 template <int M>
 cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
-  const int g = pick_groups<M>(0, a.ax.r, 0, env_groups("OSGPU_GROUPS_A", 4));
+  const int g = pick_groups<M>(0, a.ax.r, 0, env_groups("OSGPU_GROUPS_A", 2));
   if (g == 4) return launchA_mg<M, 4>(a, st);
   if (g == 2) return launchA_mg<M, 2>(a, st);
   return launchA_mg<M, 1>(a, st);
@@ -490,7 +490,7 @@ cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
 
 template <int M>
 cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
-  const int g = pick_groups<M>(2, a.ax.r, 0, env_groups("OSGPU_GROUPS_C", 4));
+  const int g = pick_groups<M>(2, a.ax.r, 0, env_groups("OSGPU_GROUPS_C", 2));
   if (g == 4) return launchC_mg<M, 4>(a, st);
   if (g == 2) return launchC_mg<M, 2>(a, st);
   return launchC_mg<M, 1>(a, st);
