@@ -292,6 +292,26 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
                                       const osgpu_asm_config* cfg, int32_t dtype, void* stream,
                                       osgpu_asm_report* reports, int32_t reports_stride);
 
+/* ------------------------------------------------------- allocation-free */
+/* ASM propagation that allocates no device memory, on any call.  No
+ * counterpart in the reference: it exists for callers that must not have a
+ * library allocate, such as code running during CUDA graph capture,
+ * applications whose device memory is owned by another allocator, and
+ * latency-critical loops that cannot absorb cudaMalloc's synchronisation.
+ * d_in/d_out: caller-owned device complex64 fields (f32 engine); stream: a
+ * cudaStream_t (NULL: the default stream).  All other scratch (spectrum
+ * buffer, transfer-function and twiddle tables) comes from one static
+ * device array of 32 MiB that every GPU loading the library holds until
+ * exit; sizes needing more return OSGPU_E_UNSUPPORTED before any GPU work
+ * (a 1024 x 1024 field at padding 2 fits, 2048 x 2048 padded to 4096 does
+ * not).  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress, with that device current): make it before any
+ * stream capture.  Calls share the array, so calls whose GPU work overlaps
+ * race: serialise them on one stream.  Input finiteness is not checked. */
+int osgpu_asm_propagate_noalloc(const void* d_in, void* d_out, const osgpu_grid* g, double z,
+                                const osgpu_asm_config* cfg, void* stream,
+                                osgpu_asm_report* report);
+
 /* --------------------------------------------------------------- profiling */
 /* Per-kernel-class CUDA-event timing on the launching stream.  Between
  * osgpu_profile_begin and osgpu_profile_end every pass launch is bracketed by

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 # OSGPU_LIB_DIR / OSGPU_NVCC_FLAGS build side-by-side variants (tuning runs).
 OUT_DIR = os.environ.get("OSGPU_LIB_DIR") or os.path.join(HERE, "lib")
 LIB = os.path.join(OUT_DIR, "libosgpu.so")
-SOURCES = ["prop_kernels.cu", "prop_fast.cu", "api.cu", "host_analysis.cpp"]
+SOURCES = ["prop_kernels.cu", "prop_fast.cu", "api.cu", "host_analysis.cpp", "noalloc.cu"]
 HEADERS = ["fft_smem.cuh", "fft_reg.cuh", "elements.cuh", "prop_kernels.cuh", "osgpu_types.h",
            "host_analysis.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

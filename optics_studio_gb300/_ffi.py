@@ -154,6 +154,9 @@ SIGNATURES = [
     ("osgpu_lattice_create", C.c_int,
      [c_double_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]),
     ("osgpu_lattice_destroy", C.c_int, [C.c_void_p]),
+    ("osgpu_asm_propagate_noalloc", C.c_int,
+     [C.c_void_p, C.c_void_p, C.POINTER(Grid), C.c_double, C.POINTER(AsmConfigC), C.c_void_p,
+      C.POINTER(AsmReportC)]),
     ("osgpu_profile_begin", C.c_int, []),
     ("osgpu_profile_end", C.c_int, [C.POINTER(KernelStatC), C.c_int32, C.POINTER(C.c_int32)]),
 ]
