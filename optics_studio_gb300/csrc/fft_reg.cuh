@@ -11,8 +11,8 @@
 // Stage (Ns = product of earlier radices, radix R, butterfly j, k = j mod Ns):
 //   v[q] = src[j + q M/R] * W_{Ns R}^{q k};  v = DFT_R(v);
 //   dst[(j - k) R + k + q Ns] = v[q]
-// Twiddles W_M^t come from a table tw[t] = e^{-2 pi i t / M} (conjugated for
-// the inverse).
+// Twiddles come from a stage-ordered copy of the table e^{-2 pi i t / M}
+// (conjugated for the inverse), TwLay below.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -118,17 +118,6 @@ __device__ __forceinline__ void dft16(float2* v) {
   t = v[11]; v[11] = v[14]; v[14] = t;
 }
 
-__device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
-
-// Twiddle-table read issued in place: volatile, so the compiler does not
-// merge the forward and inverse transforms' reads of the same entries
-// (which would keep them live in registers from one transform to the next).
-__device__ __forceinline__ float2 twl(const float2* p) {
-  float2 v;
-  asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
-  return v;
-}
-
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
 
 template <int M> struct Plan {
@@ -139,138 +128,49 @@ template <int M> struct Plan {
   static constexpr int SMEM = M + M / 16;    // padded elements per buffer
 };
 
-// One transform of length M by the T = M/16 threads with local index tid.
-// s0/s1: two padded shared buffers of Plan<M>::SMEM float2 owned by this
-// transform.  Contains __syncthreads: every thread of the block must call it.
-template <int M, bool INV>
-__device__ __forceinline__ void fft(float2 (&v)[16], float2* s0, float2* s1,
-                                    const float2* __restrict__ tw, int tid) {
+// Twiddle table in stage order, laid out so that the lanes of a warp read
+// consecutive entries (no shared-memory bank conflicts):
+//   middle radix-16 stage st (span Ns = 16^(st+1), butterfly k = tid mod Ns):
+//     entry mid_off(st) + (q-1) Ns + k = W_{16 Ns}^{q k},   q = 1..15
+//   last stage (radix LR = RF, or 16 when log2 M is a multiple of 4; span LS = M/LR,
+//   butterfly j < LS):
+//     entry LAST + (q-1) LS + j = W_M^{q j},                q = 1..LR-1
+// Every entry is a copy of one entry of the M-point table W_M^e, so the
+// values are those of a plain table lookup.  SIZE <= M.
+template <int M> struct TwLay {
   using P = Plan<M>;
-  constexpr int T = P::T;
-  // stage 0: radix 16, Ns = 1, butterfly j = tid, k = 0
-  dft16<INV>(v);
-#pragma unroll
-  for (int q = 0; q < 16; ++q) s0[pad(16 * tid + q)] = v[q];
-  __syncthreads();
-  float2* src = s0;
-  float2* dst = s1;
-  int Ns = 16;
-  // middle radix-16 stages (all but the last if it is radix 16)
-  constexpr int mid16 = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;
-#pragma unroll
-  for (int st = 0; st < mid16; ++st) {
-    const int k = tid & (Ns - 1);
-    const int tstride = M / (Ns * 16);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = src[pad(tid + T * q)];
-#pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(&tw[q * k * tstride]));
-    dft16<INV>(v);
-    const int base = (tid - k) * 16 + k;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) dst[pad(base + q * Ns)] = v[q];
-    __syncthreads();
-    float2* tmp = src; src = dst; dst = tmp;
-    Ns *= 16;
-  }
-  if (P::RF == 1) {
-    // last stage radix 16 with Ns = M/16 = T: k = tid, output X[tid + T q]
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = src[pad(tid + T * q)];
-#pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(&tw[q * tid]));
-    dft16<INV>(v);
-  } else {
-    // last stage radix RF, Ns = M/RF; butterflies j = tid + T i, i < 16/RF
-    constexpr int RF = P::RF;
-    constexpr int NB = 16 / RF;
-    constexpr int NSF = M / RF;
-#pragma unroll
-    for (int i = 0; i < NB; ++i) {
-      const int j = tid + T * i;
-      float2 u[RF];
-#pragma unroll
-      for (int q = 0; q < RF; ++q) u[q] = src[pad(j + q * NSF)];
-#pragma unroll
-      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], twl(&tw[q * j]));
-      if (RF == 2) dft2<INV>(u[0], u[1]);
-      if (RF == 4) dft4<INV>(u[0], u[1], u[2], u[3]);
-      if (RF == 8) dft8<INV>(u);
-      // output index j + q NSF = tid + T (i + q NB)
-#pragma unroll
-      for (int q = 0; q < RF; ++q) v[i + q * NB] = u[q];
-    }
-  }
-}
+  static constexpr int MID = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;  // middle radix-16 stages
+  static constexpr int LR = (P::RF == 1) ? 16 : P::RF;
+  static constexpr int LS = M / LR;
+  __host__ __device__ static constexpr int span(int st) { return st < 0 ? 1 : 16 * span(st - 1); }
+  __host__ __device__ static constexpr int mid_off(int st) { return st <= 0 ? 0 : mid_off(st - 1) + 15 * span(st - 1); }
+  static constexpr int LAST = mid_off(MID);
+  static constexpr int SIZE = LAST + (LR - 1) * LS;
+};
 
-// Single-buffer variant: the exchanges of all stages go through one padded
-// buffer (Plan<M>::SMEM float2), at the cost of a barrier before each store.
-// Same register layout and arithmetic as fft().  Every padded index is a
-// per-thread base plus a compile-time offset (T, Ns and M/RF are multiples of
-// 16, so pad(b + 16 c) = pad(b) + 17 c), which keeps the address arithmetic
-// in one register per stage.
-template <int M, bool INV>
-__device__ __forceinline__ void fft1(float2 (&v)[16], float2* buf, const float2* __restrict__ tw,
-                                     int tid) {
-  using P = Plan<M>;
-  constexpr int T = P::T;
-  constexpr int TP = T + T / 16;  // pad(x + T) - pad(x)
-  static_assert(T % 16 == 0, "register FFT needs M >= 256");
-  dft16<INV>(v);
-  __syncthreads();  // earlier readers of buf are done
-  {
-    float2* b0 = buf + 17 * tid;  // pad(16 tid + q) = 17 tid + q
-#pragma unroll
-    for (int q = 0; q < 16; ++q) b0[q] = v[q];
-  }
-  __syncthreads();
-  const float2* bl = buf + (tid + (tid >> 4));  // pad(tid + T q) = pad(tid) + TP q
-  int Ns = 16;
-  constexpr int mid16 = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;
-#pragma unroll
-  for (int st = 0; st < mid16; ++st) {
-    const int k = tid & (Ns - 1);
-    const int tstride = M / (Ns * 16);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
-    __syncthreads();
-#pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(tw + q * k * tstride));
-    dft16<INV>(v);
-    const int base = (tid - k) * 16 + k;
-    float2* bs = buf + (base + (base >> 4));
-    const int NP = Ns + Ns / 16;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) bs[NP * q] = v[q];
-    __syncthreads();
-    Ns *= 16;
-  }
-  if (P::RF == 1) {
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
-#pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], twl(&tw[q * tid]));
-    dft16<INV>(v);
-  } else {
-    constexpr int RF = P::RF;
-    constexpr int NB = 16 / RF;
-    constexpr int NSF = M / RF;
-    constexpr int FP = NSF + NSF / 16;
-#pragma unroll
-    for (int i = 0; i < NB; ++i) {
-      const int j = tid + T * i;
-      const float2* bj = bl + TP * i;  // pad(j)
-      float2 u[RF];
-#pragma unroll
-      for (int q = 0; q < RF; ++q) u[q] = bj[FP * q];
-#pragma unroll
-      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], twl(&tw[q * j]));
-      if (RF == 2) dft2<INV>(u[0], u[1]);
-      if (RF == 4) dft4<INV>(u[0], u[1], u[2], u[3]);
-      if (RF == 8) dft8<INV>(u);
-#pragma unroll
-      for (int q = 0; q < RF; ++q) v[i + q * NB] = u[q];
+// Fill the stage-ordered table from the M-point table twm[e] = W_M^e
+// (threads t0, t0 + nt, ...).
+template <int M>
+__device__ __forceinline__ void load_stage_twiddles(float2* tws, const float2* __restrict__ twm,
+                                                    int t0, int nt) {
+  using L = TwLay<M>;
+  for (int i = t0; i < L::SIZE; i += nt) {
+    int e;
+    if (i >= L::LAST) {
+      const int r = i - L::LAST;
+      const int q = r / L::LS + 1;
+      e = q * (r - (q - 1) * L::LS);
+    } else {
+      int off = 0, ns = 16;
+      while (i >= off + 15 * ns) {
+        off += 15 * ns;
+        ns *= 16;
+      }
+      const int r = i - off;
+      const int q = r / ns + 1;
+      e = q * (r - (q - 1) * ns) * (M / (16 * ns));
     }
+    tws[i] = __ldg(twm + e);
   }
 }
 
@@ -281,35 +181,41 @@ __device__ __forceinline__ void group_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// fft1 with the M-entry twiddle table in shared memory (plain loads) and a
-// per-group barrier, so the groups of a CTA proceed independently.
+// One transform of length M by the T = M/16 threads with local index tid.
+// buf: one padded shared buffer of Plan<M>::SMEM float2 owned by this
+// transform (padded index i + i/16 keeps the transposed stores conflict
+// free); tws: the stage-ordered twiddle table of TwLay<M> in shared memory.
+// Every padded index is a per-thread base plus a compile-time offset (T, Ns
+// and M/RF are multiples of 16, so pad(b + 16 c) = pad(b) + 17 c).  The
+// barrier (bar_id, bar_count) covers the threads of this transform, so the
+// groups of a CTA proceed independently.
 template <int M, bool INV>
 __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2* tws, int tid,
                                       int bar_id, int bar_count) {
   using P = Plan<M>;
+  using L = TwLay<M>;
   constexpr int T = P::T;
-  constexpr int TP = T + T / 16;
+  constexpr int TP = T + T / 16;  // pad(x + T) - pad(x)
   static_assert(T % 16 == 0, "register FFT needs M >= 256");
   dft16<INV>(v);
-  group_sync(bar_id, bar_count);
+  group_sync(bar_id, bar_count);  // earlier readers of buf are done
   {
-    float2* b0 = buf + 17 * tid;
+    float2* b0 = buf + 17 * tid;  // pad(16 tid + q) = 17 tid + q
 #pragma unroll
     for (int q = 0; q < 16; ++q) b0[q] = v[q];
   }
   group_sync(bar_id, bar_count);
-  const float2* bl = buf + (tid + (tid >> 4));
-  int Ns = 16;
-  constexpr int mid16 = (P::RF == 1) ? P::N16 - 2 : P::N16 - 1;
+  const float2* bl = buf + (tid + (tid >> 4));  // pad(tid + T q) = pad(tid) + TP q
 #pragma unroll
-  for (int st = 0; st < mid16; ++st) {
+  for (int st = 0; st < L::MID; ++st) {
+    const int Ns = L::span(st);
     const int k = tid & (Ns - 1);
-    const int ts = (M / (Ns * 16)) * k;
+    const float2* tk = tws + L::mid_off(st) + k;
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
     group_sync(bar_id, bar_count);
 #pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tws[q * ts]);
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tk[(q - 1) * Ns]);
     dft16<INV>(v);
     const int base = (tid - k) * 16 + k;
     float2* bs = buf + (base + (base >> 4));
@@ -317,31 +223,32 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
 #pragma unroll
     for (int q = 0; q < 16; ++q) bs[NP * q] = v[q];
     group_sync(bar_id, bar_count);
-    Ns *= 16;
   }
+  const float2* tl = tws + L::LAST + tid;
   if (P::RF == 1) {
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
 #pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tws[q * tid]);
+    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tl[(q - 1) * T]);
     dft16<INV>(v);
   } else {
+    // last stage radix RF, span M/RF; butterflies j = tid + T i, i < 16/RF
     constexpr int RF = P::RF;
     constexpr int NB = 16 / RF;
     constexpr int NSF = M / RF;
     constexpr int FP = NSF + NSF / 16;
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
-      const int j = tid + T * i;
-      const float2* bj = bl + TP * i;
+      const float2* bj = bl + TP * i;  // pad(j)
       float2 u[RF];
 #pragma unroll
       for (int q = 0; q < RF; ++q) u[q] = bj[FP * q];
 #pragma unroll
-      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], tws[q * j]);
+      for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], tl[(q - 1) * NSF + T * i]);
       if (RF == 2) dft2<INV>(u[0], u[1]);
       if (RF == 4) dft4<INV>(u[0], u[1], u[2], u[3]);
       if (RF == 8) dft8<INV>(u);
+      // output index j + q NSF = tid + T (i + q NB)
 #pragma unroll
       for (int q = 0; q < RF; ++q) v[i + q * NB] = u[q];
     }

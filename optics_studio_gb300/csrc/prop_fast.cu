@@ -139,9 +139,9 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
 #pragma unroll
   for (int k = 0; k < M / NT; ++k) {
     const int i = threadIdx.x + k * NT;
-    tws[i] = twm[i];
     col[i] = (i < ny) ? W[i] : make_float2(0.f, 0.f);
   }
+  load_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, ry, T);
   if (use_table) {
     // H(kx, |k_y|) for |k_y| <= Py/2 (H even in fy), row rr = |k_y| mod ry
@@ -289,7 +289,6 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
 #pragma unroll
   for (int k = 0; k < M / NT; ++k) {
     const int j = threadIdx.x + k * NT;
-    tws[j] = twm[j];
     float2 x = make_float2(0.f, 0.f);
     if (j < nx) {
       x = ld_in(a.in, a.in_c128, (size_t)iy * nx + j);
@@ -306,6 +305,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
     }
     xin[j] = x;
   }
+  load_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, rx, T);
   __syncthreads();
   const int iters = (rx + G - 1) / G;
@@ -352,8 +352,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   const float2* W = reinterpret_cast<const float2*>(a.work);
   constexpr int NT = Lay<M, G>::THREADS;
-#pragma unroll
-  for (int k = 0; k < M / NT; ++k) tws[threadIdx.x + k * NT] = twm[threadIdx.x + k * NT];
+  load_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, rx, T);
   // first gathers before the barrier: they overlap the table loads
   const int iters = (rx + G - 1) / G;
