@@ -51,6 +51,7 @@ enum {
   OSGPU_E_NOT_FINITE = 41,
   OSGPU_E_OUT_OF_BOUNDS = 42,
   OSGPU_E_RENDER = 43,
+  OSGPU_E_ADJOINT = 44,
   /* library conditions with no reference counterpart */
   OSGPU_E_UNSUPPORTED = 100, /* size beyond the kernels' shared-memory plan */
   OSGPU_E_CUDA = 101,
@@ -241,7 +242,9 @@ typedef struct {
   int32_t lattice_on_device; /* 0: `lattice` is host memory (scanned for non-finite
                                 values as PhaseMask::sampled does, then uploaded);
                                 1: device memory, used in place (the caller owns the
-                                finiteness guarantee) */
+                                finiteness guarantee);
+                                2: device memory holding float (f32 engine only,
+                                orientation 0), used in place */
 } osgpu_element;
 
 /* Device copy of a sampled phase lattice, created once (PhaseMask::sampled,
@@ -291,6 +294,100 @@ typedef struct {
 int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_items,
                                       const osgpu_asm_config* cfg, int32_t dtype, void* stream,
                                       osgpu_asm_report* reports, int32_t reports_stride);
+
+/* ---------------------------------------------------------- inverse loops */
+/* One frame (band x scene) of a render or adjoint batch: the design traced on
+ * the frame's source field with the ASM engine (optics-inverse observe.rs:
+ * 195-210; the carrier's Design is passed as Beamline steps).  Device
+ * buffers use the call's dtype: complex fields of `dtype`, real arrays of
+ * double (OSGPU_C128) or float (OSGPU_C64). */
+typedef struct {
+  osgpu_grid grid;
+  const void* d_source;     /* source field (device) */
+  const osgpu_step* steps;  /* design: elements at each plane, then z_after */
+  int32_t n_steps;
+  void* d_intensity;        /* render: |u|^2 at the detector (NULL: not written) */
+  const void* d_dmdi;       /* push_back: seed dM/dI of this frame (real) */
+  double dmdi_scale;        /* push_back: seed multiplier (1 for a plain seed) */
+  void* const* d_grad;      /* push_back: one dM/dphi accumulator (real, nx*ny) per
+                               element of the design in step order; NULL entries are
+                               skipped, NULL: none.  Frames may share accumulators
+                               (grid_gradient's sum over frames). */
+} osgpu_frame;
+
+/* Forward planes kept between a render and the adjoint sweep (the
+ * checkpoints of push_back's tape): one device allocation reused and grown
+ * across renders.  budget_bytes > 0 caps it; a render whose planes exceed
+ * the cap records nothing and push_back recomputes the forward planes per
+ * frame, as the reference's push_back does (adjoint.rs:158-190). */
+typedef struct osgpu_tape osgpu_tape;
+int osgpu_tape_create(uint64_t budget_bytes, osgpu_tape** out);
+int osgpu_tape_destroy(osgpu_tape* tape);
+uint64_t osgpu_tape_bytes(const osgpu_tape* tape);
+
+/* Renderer::render intensity channel (observe.rs:213-314, one frame per
+ * (band, scene)): forward trace of every frame, |u|^2 of the detector field
+ * into d_intensity; with a tape, the output field of every propagation is
+ * recorded for osgpu_push_back_batch_device.  Asynchronous on `stream`
+ * (NULL: the library stream). */
+int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
+                              const osgpu_asm_config* cfg, int32_t dtype, void* stream,
+                              osgpu_tape* tape, osgpu_asm_report* reports,
+                              int32_t reports_stride);
+
+/* adjoint::push_back per frame (adjoint.rs:140-246), accumulated into the
+ * frames' d_grad (adjoint::grid_gradient's sum, adjoint.rs:268-340):
+ * w = (dmdi * dmdi_scale) U at the detector, then in reverse order the
+ * adjoint propagation A(-z) (asm_adjoint, adjoint.rs:90-92) and at each
+ * element grad += -2 Im(conj(mu) V_after), mu <- conj(t) mu.  The seed
+ * multiply runs inside the first FFT pass of the first adjoint propagation
+ * and each element plane inside the last pass of the propagation before it.
+ * With a valid tape from the render of the same frames the forward planes
+ * are read from it; otherwise they are recomputed.  Asynchronous. */
+int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
+                                 const osgpu_asm_config* cfg, int32_t dtype, void* stream,
+                                 const osgpu_tape* tape);
+
+/* sum |u|^2 of a device field in FP64 (compensated); synchronous. */
+int osgpu_field_power_device(const void* d_field, int32_t dtype, uint64_t n, void* stream,
+                             double* out);
+
+/* Merits over device observations (real_dtype OSGPU_F64 / OSGPU_F32; frames
+ * band-major, scenes inner).  `value` receives the merit (synchronous);
+ * d_seed (optional, same layout as d_obs) receives dM/dI.  Sums run in FP64
+ * with compensation.
+ * Spot-window efficiency (no reference counterpart: the merit of the spot-
+ * array inverse design): M = -sum_f sum_{k in windows} I_f[k] / p_in[f],
+ * p_in host array of n_frames input powers, d_windows a 0/1 byte mask. */
+int osgpu_merit_spot_efficiency_device(const void* d_obs, int32_t real_dtype, int32_t n_frames,
+                                       uint64_t frame_len, const uint8_t* d_windows,
+                                       const double* p_in, void* d_seed, void* stream,
+                                       double* value);
+/* MseToTarget (merit.rs:112-164); band/scene -1 selects all (Selector). */
+int osgpu_merit_mse_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                           int32_t n_scenes, uint64_t frame_len, const double* d_target,
+                           int32_t band, int32_t scene, void* d_seed, void* stream,
+                           double* value);
+/* EncircledEnergyMerit (merit.rs:167-245); a seed request with a
+ * non-positive total returns OSGPU_E_ADJOINT (obs_gradient is None). */
+int osgpu_merit_encircled_energy_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                                        int32_t n_scenes, uint64_t nx, uint64_t ny, double dx,
+                                        double dy, double radius, int32_t band, int32_t scene,
+                                        void* d_seed, void* stream, double* value);
+
+/* Adam update of fd.rs:186-257 (AdamConfig, fd.rs:63-110): optional global
+ * gradient-norm clip, bias-corrected moments, x -= lr_frac (hi - lo) m^ /
+ * (sqrt(v^) + eps), clamp into [lo, hi].  t >= 1 is the step number.  d_x32
+ * (optional) receives a float copy of x (the f32 engine's lattice).
+ * Asynchronous. */
+typedef struct {
+  double lr_frac, beta1, beta2, eps;
+  double clip_norm; /* used when clip != 0 */
+  int32_t clip;
+} osgpu_adam_config;
+int osgpu_adam_step_device(double* d_x, float* d_x32, const void* d_g, int32_t g_real_dtype,
+                           double* d_m, double* d_v, uint64_t n, const osgpu_adam_config* cfg,
+                           int32_t t, double lo, double hi, void* stream);
 
 /* ------------------------------------------------------- allocation-free */
 /* ASM propagation that allocates no device memory, on any call.  No

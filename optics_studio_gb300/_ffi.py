@@ -18,7 +18,7 @@ STATUS_NAMES = {
     20: "InvalidAperture", 21: "OutsideField", 22: "InvalidAxis", 23: "InvalidFocal",
     24: "InvalidOrientation", 25: "InvalidPhase", 26: "InvalidGrid", 27: "InvalidGridPitch",
     28: "InvalidGrating",
-    40: "WrongDimension", 41: "NotFinite", 42: "OutOfBounds", 43: "Render",
+    40: "WrongDimension", 41: "NotFinite", 42: "OutOfBounds", 43: "Render", 44: "Adjoint",
     100: "Unsupported", 101: "Cuda", 102: "BadArgument", 103: "NoDevice", 104: "OutOfMemory",
 }
 F64, F32 = 0, 1
@@ -105,6 +105,17 @@ class TraceItemC(C.Structure):
                 ("steps", C.POINTER(StepC)), ("n_steps", C.c_int32)]
 
 
+class FrameC(C.Structure):
+    _fields_ = [("grid", Grid), ("d_source", C.c_void_p), ("steps", C.POINTER(StepC)),
+                ("n_steps", C.c_int32), ("d_intensity", C.c_void_p), ("d_dmdi", C.c_void_p),
+                ("dmdi_scale", C.c_double), ("d_grad", C.POINTER(C.c_void_p))]
+
+
+class AdamConfigC(C.Structure):
+    _fields_ = [("lr_frac", C.c_double), ("beta1", C.c_double), ("beta2", C.c_double),
+                ("eps", C.c_double), ("clip_norm", C.c_double), ("clip", C.c_int32)]
+
+
 class KernelStatC(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double),
                 ("bytes", C.c_double)]
@@ -154,6 +165,29 @@ SIGNATURES = [
     ("osgpu_lattice_create", C.c_int,
      [c_double_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]),
     ("osgpu_lattice_destroy", C.c_int, [C.c_void_p]),
+    ("osgpu_tape_create", C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("osgpu_tape_destroy", C.c_int, [C.c_void_p]),
+    ("osgpu_tape_bytes", C.c_uint64, [C.c_void_p]),
+    ("osgpu_render_batch_device", C.c_int,
+     [C.POINTER(FrameC), C.c_int32, C.POINTER(AsmConfigC), C.c_int32, C.c_void_p, C.c_void_p,
+      C.POINTER(AsmReportC), C.c_int32]),
+    ("osgpu_push_back_batch_device", C.c_int,
+     [C.POINTER(FrameC), C.c_int32, C.POINTER(AsmConfigC), C.c_int32, C.c_void_p, C.c_void_p]),
+    ("osgpu_field_power_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_uint64, C.c_void_p, C.POINTER(C.c_double)]),
+    ("osgpu_merit_spot_efficiency_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p, c_double_p, C.c_void_p,
+      C.c_void_p, C.POINTER(C.c_double)]),
+    ("osgpu_merit_mse_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p, C.c_int32, C.c_int32,
+      C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    ("osgpu_merit_encircled_energy_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_double,
+      C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+      C.POINTER(C.c_double)]),
+    ("osgpu_adam_step_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64,
+      C.POINTER(AdamConfigC), C.c_int32, C.c_double, C.c_double, C.c_void_p]),
     ("osgpu_asm_propagate_noalloc", C.c_int,
      [C.c_void_p, C.c_void_p, C.POINTER(Grid), C.c_double, C.POINTER(AsmConfigC), C.c_void_p,
       C.POINTER(AsmReportC)]),

@@ -20,6 +20,7 @@
 
 #include "../../include/osgpu.h"
 #include "host_analysis.h"
+#include "inverse_kernels.cuh"
 #include "prop_kernels.cuh"
 
 using namespace osgpu;
@@ -195,7 +196,10 @@ int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid
       set_err("element %d: %s (status %d)", i, msg, est);
       return est;
     }
-    if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED && els[i].lattice_on_device) {
+    if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED && els[i].lattice_on_device == 2) {
+      d.lat = nullptr;  // f32 engine only (checked in prepare_trace)
+      d.latf = reinterpret_cast<const float*>(els[i].lattice);
+    } else if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED && els[i].lattice_on_device) {
       d.lat = reinterpret_cast<const double*>(els[i].lattice);
     } else if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED) {
       const size_t bytes = (size_t)els[i].lnx * els[i].lny * sizeof(double);
@@ -218,7 +222,13 @@ int build_fast_tables(Context& c, ElementList& L, const osgpu_grid& g, DBuf& kee
   if (L.count == 0) return OSGPU_OK;
   size_t bytes = 0;
   for (int q = 0; q < L.count; ++q) {
-    if (L.el[q].psi != 0.0) return OSGPU_OK;
+    if (L.el[q].psi != 0.0) {
+      if (L.el[q].kind == EL_PHASE && !L.el[q].lat) {
+        set_err("an f32 device lattice needs orientation 0");
+        return OSGPU_E_UNSUPPORTED;
+      }
+      return OSGPU_OK;
+    }
     bytes += element_tables_bytes(L.el[q], (int)g.nx, (int)g.ny);
   }
   CK(keep.alloc(bytes, st));
@@ -226,8 +236,10 @@ int build_fast_tables(Context& c, ElementList& L, const osgpu_grid& g, DBuf& kee
   char* p = reinterpret_cast<char*>(keep.p);
   for (int q = 0; q < L.count; ++q) {
     DevElement& e = L.el[q];
-    auto hit = c.lattices.find(e.lat);
-    e.latf = (e.kind == EL_PHASE && hit != c.lattices.end()) ? hit->second : nullptr;
+    if (!(e.kind == EL_PHASE && e.latf && !e.lat)) {  // not a caller-owned f32 lattice
+      auto hit = c.lattices.find(e.lat);
+      e.latf = (e.kind == EL_PHASE && hit != c.lattices.end()) ? hit->second : nullptr;
+    }
     CK(launch_element_tables(e, (int)g.nx, (int)g.ny, g.dx, g.dy, p, st));
     p += element_tables_bytes(e, (int)g.nx, (int)g.ny);
   }
@@ -265,6 +277,14 @@ struct PropJob {
   float* d_int;
   double* d_int64;
   int conj_h;
+  // adjoint hooks (PropArgs::seed*, adj*)
+  const void* seed;
+  int seed_f64;
+  double seed_scale;
+  int adj;
+  const void* adj_uin;
+  int adj_uin_c128;
+  void* adj_grad[kMaxElements];
 };
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -304,6 +324,13 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
   a.z = j.z;
   a.scale = 1.0 / ((double)j.Px * (double)j.Py);
   a.conj_h = j.conj_h;
+  a.seed = j.seed;
+  a.seed_f64 = j.seed_f64;
+  a.seed_scale = j.seed_scale;
+  a.adj = j.adj;
+  a.adj_uin = j.adj_uin;
+  a.adj_uin_c128 = j.adj_uin_c128;
+  for (int q = 0; q < kMaxElements; ++q) a.adj_grad[q] = j.adj_grad[q];
   int rc;
   if ((rc = get_tw(c, a.ax.m, is_d, &a.tw_mx))) return rc;
   if ((rc = get_tw(c, a.ay.m, is_d, &a.tw_my))) return rc;
@@ -396,9 +423,17 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
     a.kspec = base + o_ks;
   }
   const double nin = (double)j.g.nx * j.g.ny, nsp = (double)Px * ny;
+  const double el_bytes = element_bytes(j.els, !is_d);
+  double adj_bytes = 0.0;  // pass C adjoint plane: forward field read + gradient RMW
+  if (j.adj) {
+    adj_bytes = nin * (j.adj_uin_c128 ? 16 : 8) + el_bytes;
+    for (int q = 0; q < j.els.count; ++q)
+      if (j.adj_grad[q]) adj_bytes += 2.0 * nin * (is_d ? 8 : 4);
+  }
   {
+    const double seed_bytes = j.seed ? nin * (j.seed_f64 ? 8 : 4) : 0.0;
     ProfScope ps(c, st, PC_PASS_A,
-                 nin * (j.in_c128 ? 16 : 8) + nsp * es + element_bytes(j.els, !is_d));
+                 nin * (j.in_c128 ? 16 : 8) + nsp * es + (j.adj ? 0.0 : el_bytes) + seed_bytes);
     CK(launch_passA<T>(a, st));
   }
   {
@@ -409,7 +444,7 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
   {
     const double ob = (j.d_out ? (j.out_c128 ? 16 : 8) : 0) + (j.d_int ? 4 : 0) +
                       (j.d_int64 ? 8 : 0);
-    ProfScope ps(c, st, PC_PASS_C, nsp * es + nin * ob);
+    ProfScope ps(c, st, PC_PASS_C, nsp * es + nin * ob + adj_bytes);
     CK(launch_passC<T>(a, st));
   }
   return OSGPU_OK;
@@ -547,6 +582,134 @@ void fill_asm_job(PropJob& j, const osgpu_grid& g, double z, const osgpu_asm_rep
   j.band_limited = cfg.band_limited;
   j.lim_x = r.band_limit_fx;
   j.lim_y = r.band_limit_fy;
+}
+
+// ------------------------------------------------------------ inverse loops
+
+// The element chain in front of each propagation of a design (elements of
+// the steps since the previous propagation), and the trailing chain after
+// the last one.  flat[q] is the element's index in step order (the order
+// of osgpu_frame.d_grad).
+struct Chain {
+  int prop_step = -1;  // step whose z_after follows the chain (-1: trailing chain)
+  ElementList list;
+  int flat[kMaxElements];
+};
+
+int make_chains(const osgpu_step* steps, int n_steps, const std::vector<Elements>& E, int f32,
+                std::vector<Chain>& out) {
+  out.clear();
+  Chain cur;
+  std::memset(&cur.list, 0, sizeof(cur.list));
+  bool fast = true;
+  int flat = 0;
+  for (int s = 0; s < n_steps; ++s) {
+    for (int q = 0; q < E[s].list.count; ++q) {
+      if (cur.list.count == kMaxElements) {
+        set_err("more than %d elements between two propagations", kMaxElements);
+        return OSGPU_E_UNSUPPORTED;
+      }
+      cur.flat[cur.list.count] = flat++;
+      cur.list.el[cur.list.count++] = E[s].list.el[q];
+      fast = fast && E[s].list.fast;
+    }
+    if (steps[s].z_after != 0.0) {
+      cur.prop_step = s;
+      cur.list.fast = f32 && fast;
+      out.push_back(cur);
+      std::memset(&cur.list, 0, sizeof(cur.list));
+      fast = true;
+    }
+  }
+  cur.prop_step = -1;
+  cur.list.fast = f32 && fast;
+  out.push_back(cur);
+  return OSGPU_OK;
+}
+
+int check_frames(const osgpu_frame* frames, int n, int dtype) {
+  if ((n > 0 && !frames) || n < 0 || (dtype != OSGPU_C128 && dtype != OSGPU_C64)) {
+    set_err("bad frame list or dtype");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  for (int f = 0; f < n; ++f) {
+    const osgpu_frame& fr = frames[f];
+    if (!fr.d_source || fr.n_steps < 0 || (fr.n_steps > 0 && !fr.steps)) {
+      set_err("frame %d: bad source or steps", f);
+      return OSGPU_E_BAD_ARGUMENT;
+    }
+    if (fr.grid.nx == 0 || fr.grid.ny == 0) {
+      set_err("frame %d: empty grid", f);
+      return OSGPU_E_EMPTY_GRID;
+    }
+  }
+  return OSGPU_OK;
+}
+
+int count_props(const osgpu_frame& fr) {
+  int k = 0;
+  for (int s = 0; s < fr.n_steps; ++s)
+    if (fr.steps[s].z_after != 0.0) ++k;
+  return k;
+}
+
+}  // namespace
+
+// Forward planes recorded by osgpu_render_batch_device: for every frame,
+// the output field of each propagation, in one device allocation that is
+// kept and grown across calls.
+struct osgpu_tape {
+  uint64_t budget = 0;  // 0: unlimited
+  void* buf = nullptr;
+  size_t cap = 0;
+  int valid = 0;
+  int dtype = -1;
+  std::vector<size_t> off;     // per frame: byte offset of its first plane
+  std::vector<int> planes;     // per frame: number of planes
+  std::vector<uint64_t> nfld;  // per frame: samples per plane
+};
+
+namespace {
+
+// Forward trace of one frame: propagations write into `plane(k)` (k-th
+// propagation); the detector intensity goes to fr.d_intensity.
+template <typename PlaneFn>
+int forward_frame(Context& c, const osgpu_frame& fr, const std::vector<Elements>& E,
+                  const std::vector<osgpu_asm_report>& R, const std::vector<Chain>& ch,
+                  const osgpu_asm_config& cfg, int f32, int c128, PlaneFn plane,
+                  bool want_last_field, cudaStream_t st) {
+  (void)E;
+  const osgpu_grid& g = fr.grid;
+  const void* src = fr.d_source;
+  const int K = (int)ch.size() - 1;  // propagations
+  const Chain& tail = ch[K];
+  int rc;
+  for (int k = 0; k < K; ++k) {
+    const int s = ch[k].prop_step;
+    osgpu_asm_config sc = cfg;
+    sc.medium = fr.steps[s].medium;
+    PropJob j;
+    fill_asm_job(j, g, fr.steps[s].z_after, R[s], sc);
+    j.els = ch[k].list;
+    j.d_in = src;
+    j.in_c128 = c128;
+    const bool last = (k == K - 1);
+    void* out = plane(k);
+    j.d_out = (last && tail.list.count == 0 && !want_last_field) ? nullptr : out;
+    j.out_c128 = c128;
+    if (last && tail.list.count == 0 && fr.d_intensity) {
+      if (c128) j.d_int64 = reinterpret_cast<double*>(fr.d_intensity);
+      else j.d_int = reinterpret_cast<float*>(fr.d_intensity);
+    }
+    if ((rc = run_prop_dispatch(c, j, f32, st))) return rc;
+    src = out;
+  }
+  if ((K == 0 || tail.list.count > 0) && fr.d_intensity) {
+    ProfScope ps(c, st, PC_APPLY, (double)g.nx * g.ny * ((c128 ? 16 : 8) + (c128 ? 8 : 4)));
+    CK(launch_apply_intensity(src, c128, nullptr, c128, tail.list, (int)g.nx, (int)g.ny, g.dx,
+                              g.dy, fr.d_intensity, c128, f32, st));
+  }
+  return OSGPU_OK;
 }
 
 }  // namespace
@@ -898,6 +1061,12 @@ int prepare_trace(Context& c, const double* host_in, size_t n, const osgpu_grid&
       if (first_prop >= 0 && first_prop < s) rc = scan_then(host_in, n, rc);
       return rc;
     }
+    if (!f32)
+      for (int q = 0; q < E[s].list.count; ++q)
+        if (E[s].list.el[q].kind == EL_PHASE && !E[s].list.el[q].lat) {
+          set_err("step %d: an f32 device lattice needs the f32 engine", s);
+          return OSGPU_E_BAD_ARGUMENT;
+        }
     if (f32 && (rc = build_fast_tables(c, E[s].list, g, E[s].tables, st))) return rc;
     std::memset(&R[s], 0, sizeof(R[s]));
     if (steps[s].z_after != 0.0) {
@@ -1050,6 +1219,368 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
                         *cfg, f32, st)))
       return rc;
   }
+  return OSGPU_OK;
+}
+
+// ------------------------------------------------------------ inverse loops
+
+int osgpu_tape_create(uint64_t budget_bytes, osgpu_tape** out) {
+  if (!out) return OSGPU_E_BAD_ARGUMENT;
+  *out = new osgpu_tape();
+  (*out)->budget = budget_bytes;
+  return OSGPU_OK;
+}
+
+int osgpu_tape_destroy(osgpu_tape* t) {
+  if (!t) return OSGPU_OK;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if (t->buf) cudaFree(t->buf);
+  delete t;
+  return OSGPU_OK;
+}
+
+uint64_t osgpu_tape_bytes(const osgpu_tape* t) { return t ? (uint64_t)t->cap : 0; }
+
+int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
+                              const osgpu_asm_config* cfg, int32_t dtype, void* stream,
+                              osgpu_tape* tape, osgpu_asm_report* reports,
+                              int32_t reports_stride) {
+  int rc;
+  if (!cfg) return OSGPU_E_BAD_ARGUMENT;
+  if ((rc = check_frames(frames, n_frames, dtype))) return rc;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f32 = dtype == OSGPU_C64, c128 = dtype == OSGPU_C128;
+  const size_t es = c128 ? 16 : 8;
+  bool record = false;
+  if (tape) {
+    tape->valid = 0;
+    size_t need = 0;
+    tape->off.assign(n_frames, 0);
+    tape->planes.assign(n_frames, 0);
+    tape->nfld.assign(n_frames, 0);
+    for (int f = 0; f < n_frames; ++f) {
+      tape->off[f] = need;
+      tape->planes[f] = count_props(frames[f]);
+      tape->nfld[f] = frames[f].grid.nx * frames[f].grid.ny;
+      need += (size_t)tape->planes[f] * ((tape->nfld[f] * es + 255) & ~(size_t)255);
+    }
+    if (tape->budget == 0 || need <= tape->budget) {
+      if (need > tape->cap) {
+        CK(cudaStreamSynchronize(st));
+        if (tape->buf) CK(cudaFree(tape->buf));
+        tape->buf = nullptr;
+        tape->cap = 0;
+        CK(cudaMalloc(&tape->buf, need ? need : 256));
+        tape->cap = need;
+      }
+      record = true;
+    }
+  }
+  for (int f = 0; f < n_frames; ++f) {
+    const osgpu_frame& fr = frames[f];
+    std::vector<Elements> E;
+    std::vector<osgpu_asm_report> R;
+    std::vector<Chain> ch;
+    rc = prepare_trace(c, nullptr, 0, fr.grid, fr.steps, fr.n_steps, *cfg, f32, E, R, st);
+    if (reports && reports_stride > 0)
+      for (int s = 0; s < fr.n_steps && s < reports_stride && s < (int)R.size(); ++s)
+        reports[(size_t)f * reports_stride + s] = R[s];
+    if (rc) {
+      set_err("frame %d: %s", f, t_err);
+      return rc;
+    }
+    if ((rc = make_chains(fr.steps, fr.n_steps, E, f32, ch))) return rc;
+    const size_t pl = (fr.grid.nx * fr.grid.ny * es + 255) & ~(size_t)255;
+    DBuf work;
+    if (!record) CK(work.alloc(pl, st));
+    char* base = record ? reinterpret_cast<char*>(tape->buf) + tape->off[f] : nullptr;
+    auto plane = [&](int k) -> void* {
+      return record ? static_cast<void*>(base + (size_t)k * pl) : work.p;
+    };
+    if ((rc = forward_frame(c, fr, E, R, ch, *cfg, f32, c128, plane, record, st))) return rc;
+  }
+  if (record) {
+    tape->valid = 1;
+    tape->dtype = dtype;
+  }
+  return OSGPU_OK;
+}
+
+int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
+                                 const osgpu_asm_config* cfg, int32_t dtype, void* stream,
+                                 const osgpu_tape* tape) {
+  int rc;
+  if (!cfg) return OSGPU_E_BAD_ARGUMENT;
+  if ((rc = check_frames(frames, n_frames, dtype))) return rc;
+  const bool use_tape = tape && tape->valid;
+  if (use_tape) {
+    if (tape->dtype != dtype || (int)tape->planes.size() != n_frames) {
+      set_err("tape was recorded for another frame list or dtype");
+      return OSGPU_E_BAD_ARGUMENT;
+    }
+    for (int f = 0; f < n_frames; ++f)
+      if (tape->planes[f] != count_props(frames[f]) ||
+          tape->nfld[f] != frames[f].grid.nx * frames[f].grid.ny) {
+        set_err("frame %d does not match the tape", f);
+        return OSGPU_E_BAD_ARGUMENT;
+      }
+  }
+  for (int f = 0; f < n_frames; ++f)
+    if (!frames[f].d_dmdi) {
+      set_err("frame %d: no seed dM/dI", f);
+      return OSGPU_E_BAD_ARGUMENT;
+    }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f32 = dtype == OSGPU_C64, c128 = dtype == OSGPU_C128;
+  const size_t es = c128 ? 16 : 8;
+  for (int f = 0; f < n_frames; ++f) {
+    const osgpu_frame& fr = frames[f];
+    const osgpu_grid& g = fr.grid;
+    std::vector<Elements> E;
+    std::vector<osgpu_asm_report> R;
+    std::vector<Chain> ch;
+    if ((rc = prepare_trace(c, nullptr, 0, g, fr.steps, fr.n_steps, *cfg, f32, E, R, st))) {
+      set_err("frame %d: %s", f, t_err);
+      return rc;
+    }
+    if ((rc = make_chains(fr.steps, fr.n_steps, E, f32, ch))) return rc;
+    const int K = (int)ch.size() - 1;
+    const size_t pl = (g.nx * g.ny * es + 255) & ~(size_t)255;
+    // forward planes: from the tape, or recomputed (reference push_back)
+    DBuf planes;
+    char* base;
+    if (use_tape) {
+      base = reinterpret_cast<char*>(tape->buf) + tape->off[f];
+    } else {
+      CK(planes.alloc(pl * (K > 0 ? K : 1), st));
+      base = reinterpret_cast<char*>(planes.p);
+      osgpu_frame fw = fr;
+      fw.d_intensity = nullptr;
+      auto plane = [&](int k) -> void* { return base + (size_t)k * pl; };
+      if ((rc = forward_frame(c, fw, E, R, ch, *cfg, f32, c128, plane, true, st))) return rc;
+    }
+    auto uin = [&](int k) -> const void* {
+      return k == 0 ? fr.d_source : static_cast<const void*>(base + (size_t)(k - 1) * pl);
+    };
+    auto grads = [&](const Chain& cn, void** out) {
+      for (int q = 0; q < kMaxElements; ++q)
+        out[q] = (q < cn.list.count && fr.d_grad) ? fr.d_grad[cn.flat[q]] : nullptr;
+    };
+    const int seed_f64 = c128;
+    DBuf mu;
+    CK(mu.alloc(pl, st));
+    const Chain& tail = ch[K];
+    bool seeded = false;
+    if (K == 0 || tail.list.count > 0) {
+      AdjGrads ag;
+      grads(tail, ag.p);
+      ProfScope ps(c, st, PC_APPLY, (double)g.nx * g.ny * (2.0 * es + (c128 ? 8 : 4)));
+      CK(launch_adjoint_seed_plane(uin(K), c128, tail.list, ag, fr.d_dmdi, seed_f64,
+                                   fr.dmdi_scale, (int)g.nx, (int)g.ny, g.dx, g.dy,
+                                   K > 0 ? mu.p : nullptr, c128, f32, st));
+      seeded = true;
+    }
+    for (int k = K - 1; k >= 0; --k) {
+      const Chain& cn = ch[k];
+      if (k == 0 && cn.list.count == 0) break;  // nothing left to differentiate
+      const int s = cn.prop_step;
+      osgpu_asm_config sc = *cfg;
+      sc.medium = fr.steps[s].medium;
+      osgpu_asm_report ra;
+      const double z = -fr.steps[s].z_after;  // asm_adjoint: A(z)^dagger = A(-z)
+      if ((rc = asm_resolve(g, z, sc, ra)) > 0) {
+        set_err("frame %d step %d: adjoint propagation failed (status %d)", f, s, rc);
+        return rc;
+      }
+      PropJob j;
+      fill_asm_job(j, g, z, ra, sc);
+      if (!seeded) {
+        j.d_in = uin(K);
+        j.seed = fr.d_dmdi;
+        j.seed_f64 = seed_f64;
+        j.seed_scale = fr.dmdi_scale;
+        seeded = true;
+      } else {
+        j.d_in = mu.p;
+      }
+      j.in_c128 = c128;
+      j.els = cn.list;
+      j.adj = cn.list.count > 0;
+      j.adj_uin = uin(k);
+      j.adj_uin_c128 = c128;
+      grads(cn, j.adj_grad);
+      j.d_out = k > 0 ? mu.p : nullptr;
+      j.out_c128 = c128;
+      if ((rc = run_prop_dispatch(c, j, f32, st))) return rc;
+    }
+  }
+  return OSGPU_OK;
+}
+
+namespace {
+int merit_sync(cudaStream_t st, const DBuf& buf, double* host, int n) {
+  CK(cudaMemcpyAsync(host, buf.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return OSGPU_OK;
+}
+}  // namespace
+
+int osgpu_field_power_device(const void* d_field, int32_t dtype, uint64_t n, void* stream,
+                             double* out) {
+  if (!d_field || !out || (dtype != OSGPU_C128 && dtype != OSGPU_C64))
+    return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  DBuf scr;
+  CK(scr.alloc(reduce_scratch_bytes(1), st));
+  double* part = reinterpret_cast<double*>(scr.p);
+  double* res = part + (reduce_scratch_bytes(1) / sizeof(double) - 3);
+  CK(launch_power(d_field, dtype == OSGPU_C128, n, part, res, st));
+  CK(cudaMemcpyAsync(out, res, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return OSGPU_OK;
+}
+
+int osgpu_merit_spot_efficiency_device(const void* d_obs, int32_t real_dtype, int32_t n_frames,
+                                       uint64_t frame_len, const uint8_t* d_windows,
+                                       const double* p_in, void* d_seed, void* stream,
+                                       double* value) {
+  if (!d_obs || !d_windows || !p_in || n_frames <= 0 || frame_len == 0 ||
+      (real_dtype != OSGPU_F64 && real_dtype != OSGPU_F32))
+    return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f64 = real_dtype == OSGPU_F64;
+  const size_t sb = reduce_scratch_bytes(n_frames);
+  DBuf scr, res;
+  CK(scr.alloc(sb, st));
+  CK(res.alloc(sizeof(double) * 2 * n_frames, st));
+  double* sums = reinterpret_cast<double*>(res.p);
+  CK(launch_window_sums(d_obs, f64, n_frames, frame_len, d_windows,
+                        reinterpret_cast<double*>(scr.p), sums, st));
+  if (d_seed) {
+    std::vector<double> coef(n_frames);
+    for (int f = 0; f < n_frames; ++f) coef[f] = -1.0 / p_in[f];
+    CK(cudaMemcpyAsync(sums + n_frames, coef.data(), sizeof(double) * n_frames,
+                       cudaMemcpyHostToDevice, st));
+    CK(launch_window_seed(d_seed, f64, n_frames, frame_len, d_windows, sums + n_frames, st));
+  }
+  std::vector<double> h(n_frames);
+  if ((rc = merit_sync(st, res, h.data(), n_frames))) return rc;
+  if (value) {
+    double tot = 0.0;
+    for (int f = 0; f < n_frames; ++f) tot += h[f] / p_in[f];
+    *value = -tot;
+  }
+  return OSGPU_OK;
+}
+
+int osgpu_merit_mse_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                           int32_t n_scenes, uint64_t frame_len, const double* d_target,
+                           int32_t band, int32_t scene, void* d_seed, void* stream,
+                           double* value) {
+  if (!d_obs || !d_target || n_bands <= 0 || n_scenes <= 0 || frame_len == 0 ||
+      band >= n_bands || scene >= n_scenes ||
+      (real_dtype != OSGPU_F64 && real_dtype != OSGPU_F32))
+    return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  DBuf scr, res;
+  CK(scr.alloc(reduce_scratch_bytes(1), st));
+  CK(res.alloc(sizeof(double), st));
+  CK(launch_mse(d_obs, real_dtype == OSGPU_F64, frame_len, n_bands, n_scenes, band, scene,
+                d_target, d_seed, reinterpret_cast<double*>(scr.p),
+                reinterpret_cast<double*>(res.p), st));
+  double h = 0.0;
+  if ((rc = merit_sync(st, res, &h, 1))) return rc;
+  if (value) *value = h / (double)frame_len;
+  return OSGPU_OK;
+}
+
+int osgpu_merit_encircled_energy_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                                        int32_t n_scenes, uint64_t nx, uint64_t ny, double dx,
+                                        double dy, double radius, int32_t band, int32_t scene,
+                                        void* d_seed, void* stream, double* value) {
+  if (!d_obs || n_bands <= 0 || n_scenes <= 0 || nx == 0 || ny == 0 || band >= n_bands ||
+      scene >= n_scenes || (real_dtype != OSGPU_F64 && real_dtype != OSGPU_F32))
+    return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  DBuf scr, res;
+  CK(scr.alloc(reduce_scratch_bytes(2), st));
+  CK(res.alloc(2 * sizeof(double), st));
+  double* sums = reinterpret_cast<double*>(res.p);
+  CK(launch_ee(d_obs, real_dtype == OSGPU_F64, (int)nx, (int)ny, dx, dy, radius, n_bands,
+               n_scenes, band, scene, nullptr, reinterpret_cast<double*>(scr.p), sums, st));
+  double h[2];
+  if ((rc = merit_sync(st, res, h, 2))) return rc;
+  if (value) *value = (h[0] <= 0.0) ? 0.0 : -h[1] / h[0];
+  if (d_seed) {
+    if (h[0] <= 0.0) {  // obs_gradient is None (merit.rs:222-224)
+      set_err("encircled energy: total intensity is not positive, no obs gradient");
+      return OSGPU_E_ADJOINT;
+    }
+    CK(launch_ee(d_obs, real_dtype == OSGPU_F64, (int)nx, (int)ny, dx, dy, radius, n_bands,
+                 n_scenes, band, scene, d_seed, reinterpret_cast<double*>(scr.p), sums, st));
+  }
+  return OSGPU_OK;
+}
+
+int osgpu_adam_step_device(double* d_x, float* d_x32, const void* d_g, int32_t g_real_dtype,
+                           double* d_m, double* d_v, uint64_t n, const osgpu_adam_config* cfg,
+                           int32_t t, double lo, double hi, void* stream) {
+  if (!d_x || !d_g || !d_m || !d_v || !cfg || t < 1 ||
+      (g_real_dtype != OSGPU_F64 && g_real_dtype != OSGPU_F32))
+    return OSGPU_E_BAD_ARGUMENT;
+  // AdamConfig::validate (fd.rs:95-121)
+  if (!std::isfinite(cfg->lr_frac) || !(cfg->lr_frac > 0.0) ||
+      !std::isfinite(cfg->beta1) || !(cfg->beta1 >= 0.0 && cfg->beta1 < 1.0) ||
+      !std::isfinite(cfg->beta2) || !(cfg->beta2 >= 0.0 && cfg->beta2 < 1.0) ||
+      !std::isfinite(cfg->eps) || cfg->eps < 0.0 ||
+      (cfg->clip && (!std::isfinite(cfg->clip_norm) || !(cfg->clip_norm > 0.0)))) {
+    set_err("invalid Adam config");
+    return OSGPU_E_RENDER;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  AdamArgs p;
+  p.beta1 = cfg->beta1;
+  p.beta2 = cfg->beta2;
+  p.eps = cfg->eps;
+  p.bc1 = 1.0 - std::pow(cfg->beta1, (double)t);
+  p.bc2 = 1.0 - std::pow(cfg->beta2, (double)t);
+  p.step = cfg->lr_frac * (hi - lo);
+  p.lo = lo;
+  p.hi = hi;
+  p.clip = cfg->clip;
+  p.clip_norm = cfg->clip_norm;
+  DBuf scr;
+  CK(scr.alloc(reduce_scratch_bytes(1), st));
+  double* part = reinterpret_cast<double*>(scr.p);
+  double* norm2 = part + (reduce_scratch_bytes(1) / sizeof(double) - 3);
+  CK(launch_adam(d_x, d_x32, d_g, g_real_dtype == OSGPU_F64, d_m, d_v, n, p, part, norm2, st));
   return OSGPU_OK;
 }
 

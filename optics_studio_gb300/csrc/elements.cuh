@@ -67,100 +67,169 @@ static __device__ __forceinline__ void cmul_phase(double& re, double& im, double
   im = i2;
 }
 
-// Per-sample FP64 evaluation of every element at sample (ix, iy), in the
-// reference's operation order (element.rs:754-790, 900-929, 1115-1154,
-// 1443-1484, 1668-1703).  Elements apply in list order.
+// FP64 evaluation of one element at the origin-centred coordinate (x, y),
+// in the reference's operation order (element.rs:754-790, 900-929,
+// 1115-1154, 1443-1484, 1668-1703): (re, im) <- t(x, y) (re, im).
+static __device__ __forceinline__ void apply_one_exact(const DevElement& e, double x, double y,
+                                                       double& re, double& im) {
+  const double xr = __dsub_rn(x, e.cx), yr = __dsub_rn(y, e.cy);
+  double fx, fy;
+  to_frame(xr, yr, e.cpsi, e.spsi, fx, fy);
+  switch (e.kind) {
+    case EL_ELLIPSE: {
+      double a2 = __dmul_rn(e.a, e.a), b2 = __dmul_rn(e.b, e.b);
+      double lhs = __dadd_rn(__dmul_rn(__dmul_rn(b2, fx), fx), __dmul_rn(__dmul_rn(a2, fy), fy));
+      if (lhs > __dmul_rn(a2, b2)) { re = 0.0; im = 0.0; }
+      break;
+    }
+    case EL_RECT:
+      if (fabs(fx) > e.a || fabs(fy) > e.b) { re = 0.0; im = 0.0; }
+      break;
+    case EL_LENS: {
+      if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+      double r2 = __dadd_rn(__dmul_rn(xr, xr), __dmul_rn(yr, yr));
+      double phase = __ddiv_rn(__dmul_rn(-e.k, r2), __dmul_rn(2.0, e.f));
+      cmul_phase(re, im, phase);
+      break;
+    }
+    case EL_PHASE: {
+      if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+      cmul_phase(re, im, lattice_at(e, fx, fy));
+      break;
+    }
+    case EL_GRATING: {
+      if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+      double u = __dmul_rn(fx, e.inv_period);
+      double phi = __dmul_rn(e.depth, __dsub_rn(u, floor(u)));
+      cmul_phase(re, im, phi);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Per-sample FP64 evaluation of every element of L at sample (ix, iy), in
+// list order.
 static __device__ void apply_elements_exact(const ElementList& L, int ix, int iy, int nx, int ny,
                                      double dx, double dy, double& re, double& im) {
   const double x = coord_d(ix, nx, dx);
   const double y = coord_d(iy, ny, dy);
-  for (int q = 0; q < L.count; ++q) {
-    const DevElement& e = L.el[q];
-    const double xr = __dsub_rn(x, e.cx), yr = __dsub_rn(y, e.cy);
-    double fx, fy;
-    to_frame(xr, yr, e.cpsi, e.spsi, fx, fy);
-    switch (e.kind) {
-      case EL_ELLIPSE: {
-        double a2 = __dmul_rn(e.a, e.a), b2 = __dmul_rn(e.b, e.b);
-        double lhs = __dadd_rn(__dmul_rn(__dmul_rn(b2, fx), fx), __dmul_rn(__dmul_rn(a2, fy), fy));
-        if (lhs > __dmul_rn(a2, b2)) { re = 0.0; im = 0.0; }
-        break;
-      }
-      case EL_RECT:
-        if (fabs(fx) > e.a || fabs(fy) > e.b) { re = 0.0; im = 0.0; }
-        break;
-      case EL_LENS: {
-        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
-        double r2 = __dadd_rn(__dmul_rn(xr, xr), __dmul_rn(yr, yr));
-        double phase = __ddiv_rn(__dmul_rn(-e.k, r2), __dmul_rn(2.0, e.f));
-        cmul_phase(re, im, phase);
-        break;
-      }
-      case EL_PHASE: {
-        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
-        cmul_phase(re, im, lattice_at(e, fx, fy));
-        break;
-      }
-      case EL_GRATING: {
-        if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
-        double u = __dmul_rn(fx, e.inv_period);
-        double phi = __dmul_rn(e.depth, __dsub_rn(u, floor(u)));
-        cmul_phase(re, im, phi);
-        break;
-      }
-      default:
-        break;
-    }
-  }
+  for (int q = 0; q < L.count; ++q) apply_one_exact(L.el[q], x, y, re, im);
 }
 
-// f32 fast path: every element has psi == 0 and tables built in FP64 by
-// k_element_tables, so the per-sample work is table lookups plus one
-// sincosf for a phase lattice.  Decisions (stops, lattice span) are the
-// reference's exact FP64 decisions, precomputed per row / column.
-static __device__ __forceinline__ float2 apply_elements_fast(const ElementList& L, int ix, int iy,
-                                                      float2 v) {
-  for (int q = 0; q < L.count; ++q) {
-    const DevElement& e = L.el[q];
-    if (e.span) {
-      const int2 sp = e.span[iy];
-      if (ix < sp.x || ix > sp.y) return make_float2(0.f, 0.f);
-    }
-    switch (e.kind) {
-      case EL_LENS: {
-        const float2 a = e.tabx[ix], b = e.taby[iy];
-        const float2 t = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-        v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
-        break;
-      }
-      case EL_GRATING: {
-        const float2 t = e.tabx[ix];
-        v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
-        break;
-      }
-      case EL_PHASE: {
-        const int4 bx = e.bilx[ix], by = e.bily[iy];
-        float phi = 0.f;
-        if (bx.w && by.w) {
-          const float tx = __int_as_float(bx.z), ty = __int_as_float(by.z);
-          const float* r0 = e.latf + (size_t)by.x * e.lnx;
-          const float* r1 = e.latf + (size_t)by.y * e.lnx;
-          const float v00 = r0[bx.x], v10 = r0[bx.y], v01 = r1[bx.x], v11 = r1[bx.y];
-          const float A = v00 + (v10 - v00) * tx;
-          const float B = v01 + (v11 - v01) * tx;
-          phi = A + (B - A) * ty;
-        }
-        float sn, cs;
-        sincosf(phi, &sn, &cs);
-        v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
-        break;
-      }
-      default:
-        break;
+// f32 fast path for one element (psi == 0, tables built in FP64 by
+// k_element_tables): table lookups plus one sincosf for a phase lattice.
+// The decisions (stops, lattice span) are the reference's exact FP64
+// decisions, precomputed per row / column.  Returns false when the sample
+// is outside the element's transmitting set (the result is then zero).
+static __device__ __forceinline__ bool apply_one_fast(const DevElement& e, int ix, int iy,
+                                                      float2& v) {
+  if (e.span) {
+    const int2 sp = e.span[iy];
+    if (ix < sp.x || ix > sp.y) {
+      v = make_float2(0.f, 0.f);
+      return false;
     }
   }
+  switch (e.kind) {
+    case EL_LENS: {
+      const float2 a = e.tabx[ix], b = e.taby[iy];
+      const float2 t = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+      v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
+      break;
+    }
+    case EL_GRATING: {
+      const float2 t = e.tabx[ix];
+      v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
+      break;
+    }
+    case EL_PHASE: {
+      const int4 bx = e.bilx[ix], by = e.bily[iy];
+      float phi = 0.f;
+      if (bx.w && by.w) {
+        const float tx = __int_as_float(bx.z), ty = __int_as_float(by.z);
+        const float* r0 = e.latf + (size_t)by.x * e.lnx;
+        const float* r1 = e.latf + (size_t)by.y * e.lnx;
+        const float v00 = r0[bx.x], v10 = r0[bx.y], v01 = r1[bx.x], v11 = r1[bx.y];
+        const float A = v00 + (v10 - v00) * tx;
+        const float B = v01 + (v11 - v01) * tx;
+        phi = A + (B - A) * ty;
+      }
+      float sn, cs;
+      sincosf(phi, &sn, &cs);
+      v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
+      break;
+    }
+    default:
+      break;
+  }
+  return true;
+}
+
+static __device__ __forceinline__ float2 apply_elements_fast(const ElementList& L, int ix, int iy,
+                                                             float2 v) {
+  for (int q = 0; q < L.count; ++q)
+    if (!apply_one_fast(L.el[q], ix, iy, v)) return make_float2(0.f, 0.f);
   return v;
 }
 
+// Adjoint element plane at sample (ix, iy) (reference adjoint.rs:205-227,
+// element by element in reverse): the chain L acted on the forward field
+// u (the field entering the plane); mu is the adjoint field arriving from
+// the detector side.  For the last element first: grad[q] += -2 Im(conj(mu)
+// v_q) with v_q the forward field right after element q, then mu <-
+// conj(t_q) mu with t_q = element q applied to 1.  grad[q] is a double* for
+// the FP64 engine and a float* for the f32 engine (arithmetic in T); null
+// entries are skipped.  Elements are evaluated in FP64 (exact) unless the
+// list carries f32 tables (`fast`).
+template <typename T>
+static __device__ __forceinline__ void adjoint_plane(const ElementList& L, void* const* grad,
+                                                     int ix, int iy, int nx, int ny, double dx,
+                                                     double dy, size_t o, T ur, T ui, T& mr,
+                                                     T& mi) {
+  T vr[kMaxElements], vi[kMaxElements], tr[kMaxElements], ti[kMaxElements];
+  if (sizeof(T) == 4 && L.fast) {
+    float2 w = make_float2((float)ur, (float)ui);
+#pragma unroll
+    for (int q = 0; q < kMaxElements; ++q) {
+      if (q < L.count) {
+        float2 t = make_float2(1.f, 0.f);
+        apply_one_fast(L.el[q], ix, iy, t);
+        apply_one_fast(L.el[q], ix, iy, w);
+        tr[q] = (T)t.x; ti[q] = (T)t.y;
+        vr[q] = (T)w.x; vi[q] = (T)w.y;
+      }
+    }
+  } else {
+    const double x = coord_d(ix, nx, dx), y = coord_d(iy, ny, dy);
+    double wr = (double)ur, wi = (double)ui;
+#pragma unroll
+    for (int q = 0; q < kMaxElements; ++q) {
+      if (q < L.count) {
+        double a = 1.0, b = 0.0;
+        apply_one_exact(L.el[q], x, y, a, b);
+        apply_one_exact(L.el[q], x, y, wr, wi);
+        tr[q] = (T)a; ti[q] = (T)b;
+        vr[q] = (T)wr; vi[q] = (T)wi;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = kMaxElements - 1; q >= 0; --q) {
+    if (q < L.count) {
+      if (grad[q]) {
+        // Im(conj(mu) v) = mu.re v.im + (-mu.im) v.re
+        const T im = mr * vi[q] + (-mi) * vr[q];
+        reinterpret_cast<T*>(grad[q])[o] += (T)-2 * im;
+      }
+      // mu * conj(t)
+      const T nr = mr * tr[q] - mi * (-ti[q]);
+      const T ni = mr * (-ti[q]) + mi * tr[q];
+      mr = nr;
+      mi = ni;
+    }
+  }
+}
 
 }  // namespace osgpu

@@ -1,0 +1,465 @@
+// Device kernels of the inverse loops (optics-inverse observe.rs, merit.rs,
+// adjoint.rs, fd.rs): element planes outside a propagation, intensity
+// frames, FP64-compensated merit and power reductions, the merit seeds
+// dM/dI, and the Adam parameter update.
+//
+// Reductions are deterministic: each block folds a grid-stride slice into a
+// Neumaier-compensated FP64 pair, the pairs of all blocks land in a partial
+// buffer, and one block folds the partials in a fixed order.
+#include <cuda_runtime.h>
+
+#include "elements.cuh"
+#include "inverse_kernels.cuh"
+#include "prop_kernels.cuh"
+
+namespace osgpu {
+
+extern unsigned long long& launch_counter();
+
+namespace {
+
+constexpr int kRedThreads = 256;
+
+// Compensated FP64 accumulator (Neumaier).
+struct Acc {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ void add(const Acc& o) {
+    add(o.s);
+    c += o.c;
+  }
+  __device__ __forceinline__ double value() const { return s + c; }
+};
+
+__device__ __forceinline__ Acc shfl_down(const Acc& a, int d) {
+  Acc b;
+  b.s = __shfl_down_sync(0xffffffffu, a.s, d);
+  b.c = __shfl_down_sync(0xffffffffu, a.c, d);
+  return b;
+}
+
+// Block fold of one Acc per thread; the result is valid in thread 0.
+__device__ Acc block_fold(Acc a) {
+  __shared__ double ss[kRedThreads / 32], sc[kRedThreads / 32];
+  for (int d = 16; d > 0; d >>= 1) a.add(shfl_down(a, d));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    ss[w] = a.s;
+    sc[w] = a.c;
+  }
+  __syncthreads();
+  Acc r;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kRedThreads / 32; ++i) {
+      Acc o;
+      o.s = ss[i];
+      o.c = sc[i];
+      r.add(o);
+    }
+  }
+  __syncthreads();
+  return r;
+}
+
+template <typename R>
+__device__ __forceinline__ double ldr(const void* p, size_t i) {
+  return (double)reinterpret_cast<const R*>(p)[i];
+}
+
+__device__ __forceinline__ double ld_real(const void* p, int f64, size_t i) {
+  return f64 ? ldr<double>(p, i) : ldr<float>(p, i);
+}
+
+__device__ __forceinline__ void st_real(void* p, int f64, size_t i, double v) {
+  if (f64) reinterpret_cast<double*>(p)[i] = v;
+  else reinterpret_cast<float*>(p)[i] = (float)v;
+}
+
+template <typename T>
+__device__ __forceinline__ void ld_cx(const void* p, int c128, size_t i, T& re, T& im) {
+  if (c128) {
+    const double2 v = reinterpret_cast<const double2*>(p)[i];
+    re = (T)v.x;
+    im = (T)v.y;
+  } else {
+    const float2 v = reinterpret_cast<const float2*>(p)[i];
+    re = (T)v.x;
+    im = (T)v.y;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void st_cx(void* p, int c128, size_t i, T re, T im) {
+  if (c128) reinterpret_cast<double2*>(p)[i] = make_double2((double)re, (double)im);
+  else reinterpret_cast<float2*>(p)[i] = make_float2((float)re, (float)im);
+}
+
+template <typename T>
+__device__ __forceinline__ void apply_chain(const ElementList& L, int ix, int iy, int nx, int ny,
+                                            double dx, double dy, T& re, T& im) {
+  if (L.count == 0) return;
+  if (sizeof(T) == 4 && L.fast) {
+    float2 v = make_float2((float)re, (float)im);
+    v = apply_elements_fast(L, ix, iy, v);
+    re = (T)v.x;
+    im = (T)v.y;
+    return;
+  }
+  double r = (double)re, i = (double)im;
+  apply_elements_exact(L, ix, iy, nx, ny, dx, dy, r, i);
+  re = (T)r;
+  im = (T)i;
+}
+
+// Elements then |u|^2 (render of a design whose last steps are elements).
+template <typename T>
+__global__ void k_apply_intensity(const void* in, int in_c128, void* out, int out_c128,
+                                  ElementList els, int nx, int ny, double dx, double dy,
+                                  void* inten, int inten_f64) {
+  const size_t n = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(k % nx), iy = (int)(k / nx);
+    T re, im;
+    ld_cx<T>(in, in_c128, k, re, im);
+    apply_chain<T>(els, ix, iy, nx, ny, dx, dy, re, im);
+    if (out) st_cx<T>(out, out_c128, k, re, im);
+    if (inten) {
+      if (inten_f64) reinterpret_cast<double*>(inten)[k] = (double)re * re + (double)im * im;
+      else reinterpret_cast<float*>(inten)[k] = re * re + im * im;
+    }
+  }
+}
+
+// Detector seed plus the element plane in front of it, outside any
+// propagation: u_det = chain(u_in), mu = w u_det (w = seed * scale), then
+// the adjoint plane of the chain (reference adjoint.rs:198-227).
+template <typename T>
+__global__ void k_adjoint_seed_plane(const void* uin, int uin_c128, ElementList els,
+                                     AdjGrads grads, const void* seed, int seed_f64,
+                                     double scale, int nx, int ny, double dx, double dy,
+                                     void* mu_out, int mu_c128) {
+  const size_t n = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(k % nx), iy = (int)(k / nx);
+    T ur, ui;
+    ld_cx<T>(uin, uin_c128, k, ur, ui);
+    T dr = ur, di = ui;
+    apply_chain<T>(els, ix, iy, nx, ny, dx, dy, dr, di);
+    const T w = (T)(ld_real(seed, seed_f64, k) * scale);
+    T mr = w * dr, mi = w * di;
+    adjoint_plane<T>(els, grads.p, ix, iy, nx, ny, dx, dy, k, ur, ui, mr, mi);
+    if (mu_out) st_cx<T>(mu_out, mu_c128, k, mr, mi);
+  }
+}
+
+// Per-frame partial sums: part[(f * nb + b) * 2 + {0,1}] = (s, c).
+__device__ __forceinline__ void write_part(double* part, int f, const Acc& a) {
+  if (threadIdx.x == 0) {
+    const size_t o = ((size_t)f * gridDim.x + blockIdx.x) * 2;
+    part[o] = a.s;
+    part[o + 1] = a.c;
+  }
+}
+
+// sum over the window mask of each frame's intensity.
+__global__ void k_window_sums(const void* obs, int f64, uint64_t len, const unsigned char* win,
+                              double* part) {
+  const int f = blockIdx.y;
+  const size_t base = (size_t)f * len;
+  Acc a;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x)
+    if (win[k]) a.add(ld_real(obs, f64, base + k));
+  write_part(part, f, block_fold(a));
+}
+
+// seed_f[k] = win[k] ? coef[f] : 0
+__global__ void k_window_seed(void* seed, int f64, uint64_t len, const unsigned char* win,
+                              const double* coef) {
+  const int f = blockIdx.y;
+  const double c = coef[f];
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x)
+    st_real(seed, f64, (size_t)f * len + k, win[k] ? c : 0.0);
+}
+
+// Sum of the selected frames at sample k (reference merit.rs:44-81: bands
+// outer, scenes inner, from 0).
+__device__ __forceinline__ double selected_sum(const void* obs, int f64, uint64_t len, int nb,
+                                               int ns, int band, int scene, size_t k) {
+  double acc = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    if (band >= 0 && b != band) continue;
+    for (int s = 0; s < ns; ++s) {
+      if (scene >= 0 && s != scene) continue;
+      acc += ld_real(obs, f64, ((size_t)b * ns + s) * len + k);
+    }
+  }
+  return acc;
+}
+
+// MSE: sum_k (frame[k] - target[k])^2.
+__global__ void k_mse_sum(const void* obs, int f64, uint64_t len, int nb, int ns, int band,
+                          int scene, const double* target, double* part) {
+  Acc a;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const double d = selected_sum(obs, f64, len, nb, ns, band, scene, k) - target[k];
+    a.add(d * d);
+  }
+  write_part(part, 0, block_fold(a));
+}
+
+// MSE seed (merit.rs:141-163): 2 (I_f[k] - target[k]) / len on selected frames.
+__global__ void k_mse_seed(const void* obs, int f64, void* seed, uint64_t len, int nb, int ns,
+                           int band, int scene, const double* target) {
+  const int f = blockIdx.y;
+  const int b = f / ns, s = f - b * ns;
+  const bool sel = (band < 0 || b == band) && (scene < 0 || s == scene);
+  const double n = (double)len;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = (size_t)f * len + k;
+    st_real(seed, f64, i, sel ? 2.0 * (ld_real(obs, f64, i) - target[k]) / n : 0.0);
+  }
+}
+
+// Encircled-energy mask (merit.rs:175-189): centred coordinates in FP64.
+__device__ __forceinline__ bool ee_inside(size_t k, int nx, int ny, double dx, double dy,
+                                          double radius) {
+  const int ix = (int)(k % nx), iy = (int)(k / nx);
+  const double y = ((double)iy - ((double)ny - 1.0) / 2.0) * dy;
+  const double x = ((double)ix - ((double)nx - 1.0) / 2.0) * dx;
+  return x * x + y * y <= radius * radius;
+}
+
+// EE: part frame 0 = total, frame 1 = inside.
+__global__ void k_ee_sums(const void* obs, int f64, int nx, int ny, double dx, double dy,
+                          double radius, int nb, int ns, int band, int scene, double* part) {
+  const uint64_t len = (uint64_t)nx * ny;
+  Acc tot, ins;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const double v = selected_sum(obs, f64, len, nb, ns, band, scene, k);
+    tot.add(v);
+    if (ee_inside(k, nx, ny, dx, dy, radius)) ins.add(v);
+  }
+  write_part(part, 0, block_fold(tot));
+  write_part(part, 1, block_fold(ins));
+}
+
+// EE seed (merit.rs:214-244): -((m_k total - inside) / total^2) on selected frames.
+__global__ void k_ee_seed(void* seed, int f64, int nx, int ny, double dx, double dy,
+                          double radius, int ns, int band, int scene, const double* sums) {
+  const uint64_t len = (uint64_t)nx * ny;
+  const int f = blockIdx.y;
+  const int b = f / ns, s = f - b * ns;
+  const bool sel = (band < 0 || b == band) && (scene < 0 || s == scene);
+  const double total = sums[0], inside = sums[1];
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x) {
+    double g = 0.0;
+    if (sel) g = -(((ee_inside(k, nx, ny, dx, dy, radius) ? total : 0.0) - inside) /
+                   (total * total));
+    st_real(seed, f64, (size_t)f * len + k, g);
+  }
+}
+
+// Field power sum |u|^2.
+__global__ void k_power(const void* u, int c128, uint64_t n, double* part) {
+  Acc a;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    double re, im;
+    ld_cx<double>(u, c128, k, re, im);
+    a.add(re * re + im * im);
+  }
+  write_part(part, 0, block_fold(a));
+}
+
+// Sum of squares of a real vector.
+__global__ void k_sumsq(const void* g, int f64, uint64_t n, double* part) {
+  Acc a;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const double v = ld_real(g, f64, k);
+    a.add(v * v);
+  }
+  write_part(part, 0, block_fold(a));
+}
+
+// Final fold of nb partial pairs per frame: out[f] = compensated sum.
+__global__ void k_fold_parts(const double* part, int nb, int nf, double* out) {
+  for (int f = 0; f < nf; ++f) {
+    Acc a;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      Acc o;
+      o.s = part[((size_t)f * nb + b) * 2];
+      o.c = part[((size_t)f * nb + b) * 2 + 1];
+      a.add(o);
+    }
+    a = block_fold(a);
+    if (threadIdx.x == 0) out[f] = a.value();
+  }
+}
+
+// Adam update (reference fd.rs:217-235): optional global-norm clip scale from
+// norm2 = sum g^2 (device), bias-corrected moments, x -= step m^/(sqrt(v^)+eps)
+// when the denominator is positive, then clamp into [lo, hi].
+__global__ void k_adam(double* x, float* x32, const void* g, int g_f64, double* m, double* v,
+                       uint64_t n, AdamArgs p, const double* norm2) {
+  double scale = 1.0;
+  if (p.clip) {
+    const double norm = sqrt(*norm2);
+    if (norm > p.clip_norm && norm > 0.0) scale = p.clip_norm / norm;
+  }
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    // reference operation order, no contraction
+    const double gi = __dmul_rn(ld_real(g, g_f64, i), scale);
+    const double mi = __dadd_rn(__dmul_rn(p.beta1, m[i]), __dmul_rn(1.0 - p.beta1, gi));
+    const double vi =
+        __dadd_rn(__dmul_rn(p.beta2, v[i]), __dmul_rn(__dmul_rn(1.0 - p.beta2, gi), gi));
+    m[i] = mi;
+    v[i] = vi;
+    const double mh = __ddiv_rn(mi, p.bc1);
+    const double vh = __ddiv_rn(vi, p.bc2);
+    const double denom = __dadd_rn(__dsqrt_rn(vh), p.eps);
+    double xi = x[i];
+    if (denom > 0.0) xi = __dsub_rn(xi, __ddiv_rn(__dmul_rn(p.step, mh), denom));
+    if (xi < p.lo) xi = p.lo;  // f64::clamp (NaN stays NaN)
+    if (xi > p.hi) xi = p.hi;
+    x[i] = xi;
+    if (x32) x32[i] = (float)xi;
+  }
+}
+
+int red_blocks(uint64_t n) {
+  const uint64_t b = (n + kRedThreads - 1) / kRedThreads;
+  return (int)(b < 1216 ? (b ? b : 1) : 1216);  // <= 8 per SM on 152 SMs
+}
+
+}  // namespace
+
+#define OSGPU_LAUNCH ++launch_counter()
+
+cudaError_t launch_apply_intensity(const void* in, int in_c128, void* out, int out_c128,
+                                   const ElementList& els, int nx, int ny, double dx, double dy,
+                                   void* inten, int inten_f64, int f32, cudaStream_t st) {
+  const uint64_t n = (uint64_t)nx * ny;
+  OSGPU_LAUNCH;
+  if (f32)
+    k_apply_intensity<float><<<red_blocks(n), kRedThreads, 0, st>>>(in, in_c128, out, out_c128,
+                                                                   els, nx, ny, dx, dy, inten,
+                                                                   inten_f64);
+  else
+    k_apply_intensity<double><<<red_blocks(n), kRedThreads, 0, st>>>(in, in_c128, out, out_c128,
+                                                                    els, nx, ny, dx, dy, inten,
+                                                                    inten_f64);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_seed_plane(const void* uin, int uin_c128, const ElementList& els,
+                                      const AdjGrads& grads, const void* seed, int seed_f64,
+                                      double scale, int nx, int ny, double dx, double dy,
+                                      void* mu_out, int mu_c128, int f32, cudaStream_t st) {
+  const uint64_t n = (uint64_t)nx * ny;
+  OSGPU_LAUNCH;
+  if (f32)
+    k_adjoint_seed_plane<float><<<red_blocks(n), kRedThreads, 0, st>>>(
+        uin, uin_c128, els, grads, seed, seed_f64, scale, nx, ny, dx, dy, mu_out, mu_c128);
+  else
+    k_adjoint_seed_plane<double><<<red_blocks(n), kRedThreads, 0, st>>>(
+        uin, uin_c128, els, grads, seed, seed_f64, scale, nx, ny, dx, dy, mu_out, mu_c128);
+  return cudaGetLastError();
+}
+
+size_t reduce_scratch_bytes(int n_frames) {
+  return (size_t)n_frames * 1216 * 2 * sizeof(double) + (size_t)(n_frames + 2) * sizeof(double);
+}
+
+cudaError_t launch_window_sums(const void* obs, int f64, int nf, uint64_t len,
+                               const unsigned char* win, double* scratch, double* out,
+                               cudaStream_t st) {
+  const int nb = red_blocks(len);
+  OSGPU_LAUNCH;
+  k_window_sums<<<dim3(nb, nf), kRedThreads, 0, st>>>(obs, f64, len, win, scratch);
+  OSGPU_LAUNCH;
+  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, nb, nf, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_window_seed(void* seed, int f64, int nf, uint64_t len,
+                               const unsigned char* win, const double* coef, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_window_seed<<<dim3(red_blocks(len), nf), kRedThreads, 0, st>>>(seed, f64, len, win, coef);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mse(const void* obs, int f64, uint64_t len, int nb, int ns, int band,
+                       int scene, const double* target, void* seed, double* scratch,
+                       double* out, cudaStream_t st) {
+  const int blocks = red_blocks(len);
+  OSGPU_LAUNCH;
+  k_mse_sum<<<blocks, kRedThreads, 0, st>>>(obs, f64, len, nb, ns, band, scene, target, scratch);
+  OSGPU_LAUNCH;
+  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 1, out);
+  if (seed) {
+    OSGPU_LAUNCH;
+    k_mse_seed<<<dim3(blocks, nb * ns), kRedThreads, 0, st>>>(obs, f64, seed, len, nb, ns, band,
+                                                              scene, target);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, double dy,
+                      double radius, int nb, int ns, int band, int scene, void* seed,
+                      double* scratch, double* out, cudaStream_t st) {
+  const uint64_t len = (uint64_t)nx * ny;
+  const int blocks = red_blocks(len);
+  OSGPU_LAUNCH;
+  k_ee_sums<<<blocks, kRedThreads, 0, st>>>(obs, f64, nx, ny, dx, dy, radius, nb, ns, band,
+                                            scene, scratch);
+  OSGPU_LAUNCH;
+  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 2, out);
+  if (seed) {
+    OSGPU_LAUNCH;
+    k_ee_seed<<<dim3(blocks, nb * ns), kRedThreads, 0, st>>>(seed, f64, nx, ny, dx, dy, radius,
+                                                             ns, band, scene, out);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_power(const void* u, int c128, uint64_t n, double* scratch, double* out,
+                         cudaStream_t st) {
+  const int blocks = red_blocks(n);
+  OSGPU_LAUNCH;
+  k_power<<<blocks, kRedThreads, 0, st>>>(u, c128, n, scratch);
+  OSGPU_LAUNCH;
+  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 1, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(double* x, float* x32, const void* g, int g_f64, double* m, double* v,
+                        uint64_t n, const AdamArgs& p, double* scratch, double* norm2,
+                        cudaStream_t st) {
+  const int blocks = red_blocks(n);
+  if (p.clip) {
+    OSGPU_LAUNCH;
+    k_sumsq<<<blocks, kRedThreads, 0, st>>>(g, g_f64, n, scratch);
+    OSGPU_LAUNCH;
+    k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 1, norm2);
+  }
+  OSGPU_LAUNCH;
+  k_adam<<<blocks, kRedThreads, 0, st>>>(x, x32, g, g_f64, m, v, n, p, norm2);
+  return cudaGetLastError();
+}
+
+}  // namespace osgpu

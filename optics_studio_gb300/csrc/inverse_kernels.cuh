@@ -1,0 +1,51 @@
+// Launchers of the inverse-loop kernels (inverse_kernels.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "osgpu_types.h"
+
+namespace osgpu {
+
+// Per-element dM/dphi accumulators of one element plane (null: skipped).
+struct AdjGrads {
+  void* p[kMaxElements];
+};
+
+// Adam step constants, computed on the host in the reference's order:
+// step = lr_frac * (hi - lo), bc1 = 1 - beta1^t, bc2 = 1 - beta2^t.
+struct AdamArgs {
+  double beta1, beta2, eps, bc1, bc2, step, lo, hi, clip_norm;
+  int clip;
+};
+
+cudaError_t launch_apply_intensity(const void* in, int in_c128, void* out, int out_c128,
+                                   const ElementList& els, int nx, int ny, double dx, double dy,
+                                   void* inten, int inten_f64, int f32, cudaStream_t st);
+cudaError_t launch_adjoint_seed_plane(const void* uin, int uin_c128, const ElementList& els,
+                                      const AdjGrads& grads, const void* seed, int seed_f64,
+                                      double scale, int nx, int ny, double dx, double dy,
+                                      void* mu_out, int mu_c128, int f32, cudaStream_t st);
+// Scratch (device) needed by the reductions below for n_frames frames.
+size_t reduce_scratch_bytes(int n_frames);
+// out[f] = sum over win of frame f (f = 0..nf-1)
+cudaError_t launch_window_sums(const void* obs, int f64, int nf, uint64_t len,
+                               const unsigned char* win, double* scratch, double* out,
+                               cudaStream_t st);
+cudaError_t launch_window_seed(void* seed, int f64, int nf, uint64_t len,
+                               const unsigned char* win, const double* coef, cudaStream_t st);
+// out[0] = sum (selected frame - target)^2; seed (optional) per frame
+cudaError_t launch_mse(const void* obs, int f64, uint64_t len, int nb, int ns, int band,
+                       int scene, const double* target, void* seed, double* scratch,
+                       double* out, cudaStream_t st);
+// out[0] = total, out[1] = inside; seed (optional) per frame
+cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, double dy,
+                      double radius, int nb, int ns, int band, int scene, void* seed,
+                      double* scratch, double* out, cudaStream_t st);
+cudaError_t launch_power(const void* u, int c128, uint64_t n, double* scratch, double* out,
+                         cudaStream_t st);
+cudaError_t launch_adam(double* x, float* x32, const void* g, int g_f64, double* m, double* v,
+                        uint64_t n, const AdamArgs& p, double* scratch, double* norm2,
+                        cudaStream_t st);
+
+}  // namespace osgpu

@@ -293,7 +293,13 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
     if (j < nx) {
       x = ld_in(a.in, a.in_c128, (size_t)iy * nx + j);
       if (a.status && (!isfinite(x.x) || !isfinite(x.y))) atomicOr(a.status, 1);
-      if (a.els.count) {
+      if (a.seed) {
+        const size_t k = (size_t)iy * nx + j;
+        const double w = a.seed_f64 ? reinterpret_cast<const double*>(a.seed)[k]
+                                    : (double)reinterpret_cast<const float*>(a.seed)[k];
+        const float ws = (float)(w * a.seed_scale);
+        x = make_float2(ws * x.x, ws * x.y);
+      } else if (a.els.count && !a.adj) {
         if (a.els.fast) {
           x = apply_elements_fast(a.els, j, iy, x);
         } else {
@@ -388,6 +394,10 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
 #pragma unroll
     for (int gg = 1; gg < G; ++gg) v = cadd(v, bufs[gg * SB + j]);
     const size_t o = (size_t)iy * nx + j;
+    if (a.adj) {
+      const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
+      adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x, v.y);
+    }
     if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
     if (a.out) {
       if (a.out_c128) reinterpret_cast<double2*>(a.out)[o] = make_double2(v.x, v.y);

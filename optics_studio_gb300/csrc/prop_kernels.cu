@@ -63,6 +63,31 @@ __device__ __forceinline__ cx<T> apply_elements(const ElementList& L, int ix, in
   return mkc<cx<T>>((T)re, (T)im);
 }
 
+// Per-sample input stage of pass A: adjoint seed weight, else the fused
+// forward elements.
+template <typename T>
+__device__ __forceinline__ cx<T> pass_a_input(const PropArgs& a, int ix, int iy, size_t k,
+                                              cx<T> v) {
+  if (a.seed) {
+    const double w = a.seed_f64 ? reinterpret_cast<const double*>(a.seed)[k]
+                                : (double)reinterpret_cast<const float*>(a.seed)[k];
+    const T ws = (T)(w * a.seed_scale);
+    return mkc<cx<T>>(ws * v.x, ws * v.y);
+  }
+  if (a.els.count && !a.adj) return apply_elements<T>(a.els, ix, iy, a.nx, a.ny, a.dx, a.dy, v);
+  return v;
+}
+
+// Per-sample output stage of pass C for an adjoint element plane.
+template <typename T>
+__device__ __forceinline__ cx<T> pass_c_adjoint(const PropArgs& a, int ix, int iy, size_t o,
+                                                cx<T> v) {
+  const cx<T> u = load_in<T>(a.adj_uin, a.adj_uin_c128, o);
+  T mr = v.x, mi = v.y;
+  adjoint_plane<T>(a.els, a.adj_grad, ix, iy, a.nx, a.ny, a.dx, a.dy, o, (T)u.x, (T)u.y, mr, mi);
+  return mkc<cx<T>>(mr, mi);
+}
+
 // Transmitting-set predicate of one element with psi == 0 (frame
 // coordinates are then exactly (xr, yr)); same FP64 expressions as
 // apply_elements_exact.
@@ -397,7 +422,7 @@ __global__ void __launch_bounds__(kThreads) k_passA(PropArgs a, int rows) {
       if (iy < ny) {
         v = load_in<T>(a.in, a.in_c128, (size_t)iy * nx + j);
         if (a.status && nonfinite2((double)v.x, (double)v.y)) atomicOr(a.status, 1);
-        if (a.els.count) v = apply_elements<T>(a.els, j, iy, nx, ny, a.dx, a.dy, v);
+        v = pass_a_input<T>(a, j, iy, (size_t)iy * nx + j, v);
       }
       xin[(size_t)i * nx + j] = v;
     }
@@ -414,7 +439,7 @@ __global__ void __launch_bounds__(kThreads) k_passA(PropArgs a, int rows) {
         } else {
           v = load_in<T>(a.in, a.in_c128, (size_t)iy * nx + j);
           if (a.status && nonfinite2((double)v.x, (double)v.y)) atomicOr(a.status, 1);
-          if (a.els.count) v = apply_elements<T>(a.els, j, iy, nx, ny, a.dx, a.dy, v);
+          v = pass_a_input<T>(a, j, iy, (size_t)iy * nx + j, v);
         }
       }
       bufA[(size_t)i * ld + j] = v;
@@ -645,8 +670,9 @@ __global__ void __launch_bounds__(kThreads) k_passC(PropArgs a, int rows) {
   for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
     const int i = e / nx, j = e - i * nx, iy = row0 + i;
     if (iy >= ny) continue;
-    const V v = acc[(size_t)i * nx + j];
+    V v = acc[(size_t)i * nx + j];
     const size_t o = (size_t)iy * nx + j;
+    if (a.adj) v = pass_c_adjoint<T>(a, j, iy, o, v);
     if (a.status && nonfinite2((double)v.x, (double)v.y)) atomicOr(a.status, 2);
     if (a.out) store_out<T>(a.out, a.out_c128, o, v);
     if (a.out_intensity) a.out_intensity[o] = (float)((double)v.x * v.x + (double)v.y * v.y);

@@ -52,6 +52,19 @@ struct PropArgs {
   const void* hx;      // ENG_KSEP: per-column spectrum factor (includes prefactor, scale)
   const void* hy;      // ENG_KSEP: per-row spectrum factor
   int* status;         // bit 0: non-finite input sample, bit 1: non-finite output
+  // adjoint seed (pass A): each input sample is multiplied by the real weight
+  // seed[k] * seed_scale (seed is float, or double when seed_f64)
+  const void* seed;
+  int seed_f64;
+  double seed_scale;
+  // adjoint element plane (pass C epilogue, see adjoint_plane in
+  // elements.cuh): els is the element chain the plane crosses (pass A then
+  // applies no elements), adj_uin the forward field that entered the chain,
+  // adj_grad the per-element dM/dphi accumulators (null: skipped)
+  int adj;
+  const void* adj_uin;
+  int adj_uin_c128;
+  void* adj_grad[kMaxElements];
 };
 
 // Fraunhofer arguments (no padding; two passes).

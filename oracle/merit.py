@@ -64,3 +64,44 @@ class SpotArrayEfficiency:
             for s in range(len(obs.scenes)):
                 g[0, b, s] = np.where(self.windows, -1.0 / self.p_in[b], 0.0)
         return g
+
+
+class EncircledEnergyMerit:
+    """merit.rs:167-245: M = -S_in / S_tot over a centred circle of ``radius``."""
+
+    def __init__(self, radius, band=None, scene=None):
+        self.radius = radius
+        self.band, self.scene = band, scene
+
+    def _mask(self, obs):
+        nx, ny = obs.dims
+        dx, dy = obs.pitch
+        y = (np.arange(ny, dtype=np.float64) - (ny - 1.0) / 2.0) * dy
+        x = (np.arange(nx, dtype=np.float64) - (nx - 1.0) / 2.0) * dx
+        return x[None, :] * x[None, :] + y[:, None] * y[:, None] <= self.radius * self.radius
+
+    def _frame(self, obs):
+        B, S = len(obs.bands), len(obs.scenes)
+        bs = range(B) if self.band is None else [self.band]
+        ss = range(S) if self.scene is None else [self.scene]
+        return sum(obs.data[0, b, s] for b in bs for s in ss), bs, ss
+
+    def evaluate(self, obs):
+        frame, _, _ = self._frame(obs)
+        total = float(np.sum(frame))
+        if total <= 0.0:
+            return 0.0
+        return -float(np.sum(frame[self._mask(obs)])) / total
+
+    def obs_gradient(self, obs):
+        frame, bs, ss = self._frame(obs)
+        total = float(np.sum(frame))
+        if total <= 0.0:
+            return None
+        m = self._mask(obs)
+        inside = float(np.sum(frame[m]))
+        g = np.zeros_like(obs.data)
+        for b in bs:
+            for s in ss:
+                g[0, b, s] = -((np.where(m, total, 0.0) - inside) / (total * total))
+        return g

@@ -35,11 +35,37 @@ def test_library_exports_every_declared_symbol():
     assert set(syms) == bound
 
 
-def test_struct_layouts_match_header_sizes():
-    # sizes implied by the header's field lists (natural alignment, x86-64/aarch64)
-    assert ctypes.sizeof(_ffi.Grid) == 40
-    assert ctypes.sizeof(_ffi.AsmConfigC) == 32
-    assert ctypes.sizeof(_ffi.ElementC) == 120
+# ctypes mirror of each struct typedef of the header
+STRUCTS = {
+    "osgpu_grid": "Grid", "osgpu_asm_config": "AsmConfigC", "osgpu_asm_report": "AsmReportC",
+    "osgpu_fresnel_config": "FresnelConfigC", "osgpu_fresnel_report": "FresnelReportC",
+    "osgpu_fraunhofer_config": "FraunhoferConfigC",
+    "osgpu_fraunhofer_report": "FraunhoferReportC", "osgpu_rs_config": "RsConfigC",
+    "osgpu_rs_report": "RsReportC", "osgpu_element": "ElementC", "osgpu_step": "StepC",
+    "osgpu_trace_item": "TraceItemC", "osgpu_kernel_stat": "KernelStatC",
+    "osgpu_frame": "FrameC", "osgpu_adam_config": "AdamConfigC",
+}
+
+
+def test_struct_layouts_match_header_sizes(tmp_path):
+    """Every struct typedef of the header has a ctypes mirror of the same size,
+    with sizes taken from the header compiled by the host C compiler."""
+    import shutil
+    import subprocess
+    typedefs = set(re.findall(r"\}\s*(osgpu_[a-z0-9_]+)\s*;", HEADER.read_text()))
+    assert typedefs == set(STRUCTS), typedefs ^ set(STRUCTS)
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    src = tmp_path / "sizes.c"
+    body = "".join(f'  printf("{t} %zu\\n", sizeof({t}));\n' for t in sorted(STRUCTS))
+    src.write_text(f'#include <stdio.h>\n#include "{HEADER}"\nint main(void) {{\n{body}  return 0;\n}}\n')
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-std=c99", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    sizes = {k: int(v) for k, v in (ln.split() for ln in out.splitlines())}
+    for t, name in STRUCTS.items():
+        assert ctypes.sizeof(getattr(_ffi, name)) == sizes[t], (t, sizes[t])
 
 
 GEOMS = [

@@ -7,7 +7,7 @@ import pathlib
 import numpy as np
 import pytest
 
-from oracle import asm, fresnel, fraunhofer, rs, element, field, gs, adjoint, carrier, observe, merit
+from oracle import asm, fresnel, fraunhofer, rs, element, field, gs, adjoint, carrier, observe, merit, adam
 from oracle.fft import fft2, ifft2, fftfreq, padded_len
 
 GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
@@ -316,3 +316,35 @@ def test_hypercam_golden_forward_render():
     assert obs.data.shape == ref.shape
     rel = np.max(np.abs(obs.data - ref)) / np.max(np.abs(ref))
     assert rel < 1e-6, rel
+
+
+# ---- merit.rs / fd.rs restatements -------------------------------------------
+
+def test_encircled_energy_gradient_is_derivative_of_merit():
+    """merit.rs:214-244: obs_gradient is dM/dI of evaluate (central differences)."""
+    rng = np.random.default_rng(4)
+    data = rng.uniform(0.1, 1.0, (1, 2, 1, 8, 8))
+    obs = observe.Observation(["intensity"], [5e-7, 6e-7], [(0, 0)], (8, 8), (1e-6, 1e-6), data)
+    m = merit.EncircledEnergyMerit(2.5e-6)
+    g = m.obs_gradient(obs)
+    for idx in [(0, 0, 0, 3, 4), (0, 1, 0, 0, 0), (0, 1, 0, 7, 2)]:
+        h = 1e-6
+        dp = data.copy(); dp[idx] += h
+        dm = data.copy(); dm[idx] -= h
+        fd = (m.evaluate(observe.Observation(obs.channels, obs.bands, obs.scenes, obs.dims,
+                                             obs.pitch, dp))
+              - m.evaluate(observe.Observation(obs.channels, obs.bands, obs.scenes, obs.dims,
+                                               obs.pitch, dm))) / (2 * h)
+        assert g[idx] == pytest.approx(fd, rel=1e-6, abs=1e-12)
+
+
+def test_adam_first_step_by_hand():
+    """fd.rs:217-235 at t = 1: m^ = g, v^ = g^2, so x -= lr_frac span g / (|g| + eps)."""
+    x = np.array([1.0, 2.0, 3.0])
+    g = np.array([0.3, -0.4, 0.0])  # |g| = 0.5 < clip 1.0
+    xo, m, v = adam.adam_step(x, g, np.zeros(3), np.zeros(3), 1, 0.0, 4.0, lr_frac=0.1)
+    step = 0.1 * 4.0 * g / (np.abs(g) + 1e-8)
+    np.testing.assert_allclose(xo, x - step, rtol=1e-12)
+    # |10 g| = 5 > clip 1: g is rescaled to 2 g before the moments
+    xc, _, _ = adam.adam_step(x, g * 10, np.zeros(3), np.zeros(3), 1, 0.0, 4.0, lr_frac=0.1)
+    np.testing.assert_allclose(xc, x - 0.1 * 4.0 * (2 * g) / (np.abs(2 * g) + 1e-8), rtol=1e-12)
