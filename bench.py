@@ -8,7 +8,10 @@ gives a 8192 x 8192 padded grid for every band).  One step = the whole
 32-band batch, device resident, through osgpu_beamline_trace_batch_device.
 Metric: propagations (band-planes) per second.
 
-Also reported: the same batch on the plain FP64 path, end-to-end throughput
+Also reported: adjoint gradients/s of the 2048^2 inverse-design workload
+(ADJ_WORKLOAD below; f32 batched, with an FP64-plain sample and the f32
+gradient's relative L2 error against the FP64 engine), the same batch on
+the plain FP64 path, end-to-end throughput
 through the reference-facing host-buffer C ABI (osgpu_beamline_trace with
 pinned complex128 buffers, copies inside the timed region), the roofline of
 the dominant kernel (CUDA events recorded by the library on the launching
@@ -162,6 +165,97 @@ def cpu_baseline_band0():
     return out.samples, dt
 
 
+# Adjoint inverse-design workload: 2048^2 phase parameters (uniform [0, 2pi),
+# seeded), design [DOE, ASM 20 mm] [circular aperture 6 mm, ASM 80 mm], 8
+# wavelengths 500-600 nm, unit plane wave, merit = -summed efficiency into a
+# 9 x 9 array of 7 x 7-sample spot windows (pitch 96 samples, centred).
+# One gradient = render of the 8 bands (tape recorded), merit + seed,
+# adjoint sweep of the 8 bands, Adam step (lr 0.05 rad).
+ADJ_LAMS = np.linspace(500e-9, 600e-9, 8)
+ADJ_Z1, ADJ_Z2, ADJ_R = 20e-3, 80e-3, 3e-3
+ADJ_SEED = 2025
+ADJ_WORKLOAD = ("2048^2 phase DOE -> ASM 20 mm -> aperture 6 mm -> ASM 80 mm, 8 bands 500-600 nm, "
+                "9x9 spot-window efficiency merit, Adam lr 0.05 rad")
+
+
+def adjoint_setup(precision, bands):
+    import torch
+    from optics_studio_gb300 import inverse as inv, element as el
+    from optics_studio_gb300.propagation.asm import AsmConfig
+    cdt = torch.complex128 if precision == "f64" else torch.complex64
+    phi = torch.from_numpy(np.random.default_rng(ADJ_SEED).uniform(0.0, 2 * math.pi, (N, N)))
+    phi = phi.cuda()
+    phi32 = phi.float() if precision == "f32" else None
+    src = torch.ones((N, N), dtype=cdt, device="cuda")
+
+    def carrier(values, lam):
+        d = inv.Design()
+        d.push(inv.DevicePhaseMask(phi32 if phi32 is not None else values, (N, N), (DX, DX)),
+               ADJ_Z1)
+        d.push(el.EllipticalAperture.circle(ADJ_R), ADJ_Z2)
+        return d
+
+    rend = inv.Renderer(carrier, lambda x0, y0, lam: src, (DX, DX), bands=list(bands),
+                        asm_cfg=AsmConfig(), precision=precision)
+    win = torch.zeros((N, N), dtype=torch.uint8, device="cuda")
+    for i in range(9):
+        for j in range(9):
+            cy, cx = N // 2 + 96 * (i - 4), N // 2 + 96 * (j - 4)
+            win[cy - 3:cy + 4, cx - 3:cx + 4] = 1
+    merit = inv.SpotArrayEfficiency(win, [float(N * N)] * len(bands))
+    opt = inv.Adam(phi, 0.0, 2 * math.pi, inv.AdamConfig(lr_frac=0.05 / (2 * math.pi)), x32=phi32)
+    tape = inv.Tape()
+    return rend, merit, opt, tape, phi
+
+
+def adjoint_leg(args, stream):
+    """Adjoint gradients/s (f32 batched) and the FP64 plain path on a sample."""
+    import torch
+    from optics_studio_gb300 import inverse as inv
+    rend, merit, opt, tape, phi = adjoint_setup("f32", ADJ_LAMS)
+
+    def step():
+        g, val, _ = inv.grid_gradient(rend, phi, merit, tape)
+        opt.step(g[0])
+        return g, val
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(1, args.warmup)):
+            step()
+        torch.cuda.synchronize()
+        nsteps = max(3, args.steps // 3)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(nsteps):
+            g, val = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / nsteps
+        out = {"value": 1e3 / ms, "unit": "gradients/s", "ms_per_gradient": ms,
+               "gradients": nsteps, "merit_last": val, "tape_bytes": tape.nbytes(),
+               "workload": ADJ_WORKLOAD, "dtype": "f32"}
+        tape.close()
+        if not args.no_f64:
+            # same gradient (first 2 bands) on both engines from the same phases
+            rend32, merit32, _, tape32, phi0 = adjoint_setup("f32", ADJ_LAMS[:2])
+            g32, _, _ = inv.grid_gradient(rend32, phi0, merit32, tape32)
+            rend64, merit64, _, tape64, _ = adjoint_setup("f64", ADJ_LAMS[:2])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g64, _, _ = inv.grid_gradient(rend64, phi0, merit64, tape64)
+            torch.cuda.synchronize()
+            dt64 = (time.perf_counter() - t0) * 4  # 2 of the 8 bands
+            a, b = g32[0].double(), g64[0]
+            out["f64_plain"] = {"value": 1.0 / dt64, "unit": "gradients/s",
+                                "sample": "bands 1-2 of 8 (complex128), scaled to 8 bands"}
+            out["rel_l2_f32_vs_f64"] = float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+            out["speedup_vs_f64"] = out["value"] / out["f64_plain"]["value"]
+            tape32.close()
+            tape64.close()
+    return out
+
+
 def reference_arm(args):
     """--impl reference: the f64 oracle port on all usable host cores, one
     band per worker process per step (spawned processes, no GPU)."""
@@ -216,6 +310,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--bands", type=int, default=NBANDS,
                     help="bands per step (profiling runs use a smaller batch)")
     args = ap.parse_args()
@@ -384,6 +479,10 @@ def main():
                        "h2d_bytes_per_step": NBANDS * N * N * 16,
                        "d2h_bytes_per_step": NBANDS * N * N * 16,
                        "api": "osgpu_beamline_trace (host complex128, pinned), f32 engine"}
+
+    # adjoint gradients of the inverse-design workload
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_leg(args, stream)
 
     # accuracy of band 0 against the f64 oracle + bounded CPU baseline
     if rank == 0 and not args.no_cpu_baseline:
