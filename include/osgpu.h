@@ -389,6 +389,70 @@ int osgpu_adam_step_device(double* d_x, float* d_x32, const void* d_g, int32_t g
                            double* d_m, double* d_v, uint64_t n, const osgpu_adam_config* cfg,
                            int32_t t, double lo, double hi, void* stream);
 
+/* ------------------------------------------------------ Gerchberg-Saxton */
+/* gs::run (optics-inverse gs.rs:347-597) on the device, batched over items.
+ * Engines: OSGPU_GS_ASM_RELAY is the reference's relay (input -> ASM z/2 ->
+ * DOE -> ASM z/2 -> target, back-propagation ASM -z/2, illumination
+ * |ASM(input, z/2)|); OSGPU_GS_FRAUNHOFER puts the DOE at the input plane
+ * (illumination |input|), propagates with fraunhofer::propagate (source_pos
+ * None) and back with its exact adjoint (no reference counterpart).  The
+ * merit of the stopping test is MseToTarget over the target-plane intensity
+ * (merit.rs:112-146); the loop state, best-so-far phase and history stay on
+ * the device.  Synchronous: results and history are on the host when the
+ * call returns. */
+enum { OSGPU_GS_CLASSIC = 0, OSGPU_GS_DVR = 1, OSGPU_GS_FPR = 2 }; /* GsVariant (gs.rs:125-179) */
+enum { OSGPU_GS_ASM_RELAY = 0, OSGPU_GS_FRAUNHOFER = 1 };
+
+/* GsConfig (gs.rs:197-221) plus the carrier slot bounds and the engine. */
+typedef struct {
+  int32_t max_iterations;
+  int32_t patience;
+  double merit_tolerance;
+  int32_t variant;  /* OSGPU_GS_* */
+  double beta;      /* Dvr / Fpr beta */
+  double lo, hi;    /* carrier slot bounds (encode_bounds, gs.rs:115-121) */
+  int32_t engine;   /* OSGPU_GS_ASM_RELAY / OSGPU_GS_FRAUNHOFER */
+} osgpu_gs_config;
+
+/* GsRecord (gs.rs:252-266). */
+typedef struct {
+  uint64_t iteration;
+  double merit, best_merit, amplitude_mse, target_error_rms, phase_update_rms;
+} osgpu_gs_record;
+
+/* Scalars of GsSolution (gs.rs:268-306). */
+typedef struct {
+  double merit;
+  uint64_t best_iteration;
+  double amplitude_mse;
+  int32_t converged;
+  uint64_t iterations;
+} osgpu_gs_result;
+
+/* One GS problem.  Real arrays are double (OSGPU_C128) or float (OSGPU_C64). */
+typedef struct {
+  osgpu_grid grid;                 /* input / DOE grid and wavelength */
+  double z;                        /* ASM relay: z_total; Fraunhofer: DOE -> target */
+  int32_t aperture;                /* carrier aperture (OSGPU_STOP_*), centred at center_x/y */
+  double aperture_a, aperture_b, center_x, center_y;
+  const void* d_input;             /* complex input field */
+  const void* d_target_amplitude;  /* T (target-plane layout) */
+  const void* d_target_intensity;  /* MseToTarget target; NULL: T^2 */
+  void* d_phase;                   /* in: initial phase (GsInit::Given); out: best phase */
+  void* d_last_phase;              /* optional: phase after the last update */
+  void* d_best_intensity;          /* optional: target intensity of the best iteration */
+  void* d_target_error;            /* optional: |U_t| - T of the last iteration */
+  void* d_phase_error;             /* optional: wrapped phase update of the last iteration */
+  void* d_illumination;            /* optional: illumination amplitude at the DOE */
+  osgpu_gs_record* history;        /* optional host array of max_iterations records */
+  osgpu_gs_result result;          /* out */
+} osgpu_gs_item;
+
+int osgpu_gs_run_batch_device(osgpu_gs_item* items, int32_t n_items, const osgpu_gs_config* cfg,
+                              const osgpu_asm_config* asm_cfg,
+                              const osgpu_fraunhofer_config* fraunhofer_cfg, int32_t dtype,
+                              void* stream);
+
 /* ------------------------------------------------------- allocation-free */
 /* ASM propagation that allocates no device memory, on any call.  No
  * counterpart in the reference: it exists for callers that must not have a

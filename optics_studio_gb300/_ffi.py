@@ -116,6 +116,36 @@ class AdamConfigC(C.Structure):
                 ("eps", C.c_double), ("clip_norm", C.c_double), ("clip", C.c_int32)]
 
 
+class GsConfigC(C.Structure):
+    _fields_ = [("max_iterations", C.c_int32), ("patience", C.c_int32),
+                ("merit_tolerance", C.c_double), ("variant", C.c_int32), ("beta", C.c_double),
+                ("lo", C.c_double), ("hi", C.c_double), ("engine", C.c_int32)]
+
+
+class GsRecordC(C.Structure):
+    _fields_ = [("iteration", C.c_uint64), ("merit", C.c_double), ("best_merit", C.c_double),
+                ("amplitude_mse", C.c_double), ("target_error_rms", C.c_double),
+                ("phase_update_rms", C.c_double)]
+
+
+class GsResultC(C.Structure):
+    _fields_ = [("merit", C.c_double), ("best_iteration", C.c_uint64),
+                ("amplitude_mse", C.c_double), ("converged", C.c_int32),
+                ("iterations", C.c_uint64)]
+
+
+class GsItemC(C.Structure):
+    _fields_ = [("grid", Grid), ("z", C.c_double), ("aperture", C.c_int32),
+                ("aperture_a", C.c_double), ("aperture_b", C.c_double),
+                ("center_x", C.c_double), ("center_y", C.c_double),
+                ("d_input", C.c_void_p), ("d_target_amplitude", C.c_void_p),
+                ("d_target_intensity", C.c_void_p), ("d_phase", C.c_void_p),
+                ("d_last_phase", C.c_void_p), ("d_best_intensity", C.c_void_p),
+                ("d_target_error", C.c_void_p), ("d_phase_error", C.c_void_p),
+                ("d_illumination", C.c_void_p), ("history", C.POINTER(GsRecordC)),
+                ("result", GsResultC)]
+
+
 class KernelStatC(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double),
                 ("bytes", C.c_double)]
@@ -188,6 +218,9 @@ SIGNATURES = [
     ("osgpu_adam_step_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64,
       C.POINTER(AdamConfigC), C.c_int32, C.c_double, C.c_double, C.c_void_p]),
+    ("osgpu_gs_run_batch_device", C.c_int,
+     [C.POINTER(GsItemC), C.c_int32, C.POINTER(GsConfigC), C.POINTER(AsmConfigC),
+      C.POINTER(FraunhoferConfigC), C.c_int32, C.c_void_p]),
     ("osgpu_asm_propagate_noalloc", C.c_int,
      [C.c_void_p, C.c_void_p, C.POINTER(Grid), C.c_double, C.POINTER(AsmConfigC), C.c_void_p,
       C.POINTER(AsmReportC)]),

@@ -46,10 +46,10 @@ struct ProfRec {
   double bytes;
 };
 enum { PC_PREP = 0, PC_ELEMENTS, PC_APPLY, PC_PASS_A, PC_PASS_B, PC_PASS_C, PC_KSPEC, PC_FRAUN,
-       PC_N };
+       PC_GS, PC_N };
 const char* kProfNames[PC_N] = {"prep_tables", "element_tables", "element_apply",
                                 "pass_a_rows", "pass_b_columns", "pass_c_rows",
-                                "kernel_spectrum", "fraunhofer"};
+                                "kernel_spectrum", "fraunhofer", "gs_planes"};
 
 struct Context {
   std::recursive_mutex mu;
@@ -1581,6 +1581,180 @@ int osgpu_adam_step_device(double* d_x, float* d_x32, const void* d_g, int32_t g
   double* part = reinterpret_cast<double*>(scr.p);
   double* norm2 = part + (reduce_scratch_bytes(1) / sizeof(double) - 3);
   CK(launch_adam(d_x, d_x32, d_g, g_real_dtype == OSGPU_F64, d_m, d_v, n, p, part, norm2, st));
+  return OSGPU_OK;
+}
+
+// ------------------------------------------------------------ Gerchberg-Saxton
+
+int osgpu_gs_run_batch_device(osgpu_gs_item* items, int32_t n_items, const osgpu_gs_config* cfg,
+                              const osgpu_asm_config* asm_cfg,
+                              const osgpu_fraunhofer_config* fraunhofer_cfg, int32_t dtype,
+                              void* stream) {
+  if (!items || n_items < 0 || !cfg || (dtype != OSGPU_C128 && dtype != OSGPU_C64) ||
+      (cfg->engine != OSGPU_GS_ASM_RELAY && cfg->engine != OSGPU_GS_FRAUNHOFER) ||
+      (cfg->engine == OSGPU_GS_ASM_RELAY && !asm_cfg) ||
+      (cfg->engine == OSGPU_GS_FRAUNHOFER && !fraunhofer_cfg)) {
+    set_err("bad GS arguments");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  // GsVariant::validate (gs.rs:165-178)
+  double beta_f = 1.0, beta_p = 1.0;
+  if (cfg->variant == OSGPU_GS_DVR) {
+    if (!(std::isfinite(cfg->beta) && cfg->beta > 0.0 && cfg->beta < 2.0)) {
+      set_err("Dvr beta must be in (0, 2), got %g", cfg->beta);
+      return OSGPU_E_RENDER;
+    }
+    beta_p = cfg->beta;
+  } else if (cfg->variant == OSGPU_GS_FPR) {
+    if (!(std::isfinite(cfg->beta) && cfg->beta > 0.0 && cfg->beta <= 1.0)) {
+      set_err("Fpr beta must be in (0, 1], got %g", cfg->beta);
+      return OSGPU_E_RENDER;
+    }
+    beta_f = cfg->beta;
+  } else if (cfg->variant != OSGPU_GS_CLASSIC) {
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  if (cfg->max_iterations <= 0) {
+    set_err("gs max_iterations must be > 0");
+    return OSGPU_E_RENDER;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f32 = dtype == OSGPU_C64, c128 = dtype == OSGPU_C128, rf64 = c128;
+  const size_t es = c128 ? 16 : 8, rs = c128 ? 8 : 4;
+  const int max_it = cfg->max_iterations;
+  for (int i = 0; i < n_items; ++i) {
+    osgpu_gs_item& it = items[i];
+    const osgpu_grid& g = it.grid;
+    const uint64_t n = g.nx * g.ny;
+    if (!it.d_input || !it.d_target_amplitude || !it.d_phase || n == 0) {
+      set_err("GS item %d: missing buffers or empty grid", i);
+      return OSGPU_E_BAD_ARGUMENT;
+    }
+    if (!(std::isfinite(it.z) && it.z > 0.0)) {
+      set_err("z must be positive and finite, got %g", it.z);
+      return OSGPU_E_RENDER;
+    }
+    // engine set-up (host analysis once per item)
+    osgpu_asm_report rf, rb;
+    osgpu_fraunhofer_report fr;
+    const double half = it.z / 2.0;
+    if (cfg->engine == OSGPU_GS_ASM_RELAY) {
+      if ((rc = asm_resolve(g, half, *asm_cfg, rf)) > 0 ||
+          (rc = asm_resolve(g, -half, *asm_cfg, rb)) > 0) {
+        set_err("GS item %d: ASM half-transform failed (status %d)", i, rc);
+        return rc;
+      }
+    } else if ((rc = fraunhofer_resolve(g, it.z, *fraunhofer_cfg, fr)) > 0) {
+      set_err("GS item %d: Fraunhofer regime check failed (status %d)", i, rc);
+      return rc;
+    }
+    ElementList none;
+    std::memset(&none, 0, sizeof(none));
+    auto prop = [&](const void* in, void* out, int back) -> int {
+      if (cfg->engine == OSGPU_GS_FRAUNHOFER) {
+        return f32 ? run_fraun<float>(c, g, it.z, fr, none, in, c128, out, c128, nullptr, back, st)
+                   : run_fraun<double>(c, g, it.z, fr, none, in, c128, out, c128, nullptr, back,
+                                       st);
+      }
+      PropJob j;
+      fill_asm_job(j, g, back ? -half : half, back ? rb : rf, *asm_cfg);
+      j.d_in = in;
+      j.in_c128 = c128;
+      j.d_out = out;
+      j.out_c128 = c128;
+      return run_prop_dispatch(c, j, f32, st);
+    };
+    DBuf cur, open, illum, mask, ubuf, vbuf, part, dstate, hist;
+    CK(cur.alloc(n * rs, st));
+    CK(open.alloc(n, st));
+    CK(illum.alloc(n * rs, st));
+    CK(mask.alloc(n * es, st));
+    CK(ubuf.alloc(n * es, st));
+    CK(vbuf.alloc(n * es, st));
+    CK(part.alloc(reduce_scratch_bytes(2), st));
+    CK(dstate.alloc(sizeof(GsState), st));
+    CK(hist.alloc(sizeof(GsRecordDev) * max_it, st));
+    GsState h0;
+    std::memset(&h0, 0, sizeof(h0));
+    h0.best_it = -1;
+    CK(cudaMemcpyAsync(dstate.p, &h0, sizeof(h0), cudaMemcpyHostToDevice, st));
+    GsState* S = reinterpret_cast<GsState*>(dstate.p);
+    GsRecordDev* H = reinterpret_cast<GsRecordDev*>(hist.p);
+    double* P = reinterpret_cast<double*>(part.p);
+    unsigned char* O = reinterpret_cast<unsigned char*>(open.p);
+    CK(launch_gs_init(it.d_phase, cur.p, rf64, cfg->lo, cfg->hi, O, it.aperture, it.aperture_a,
+                      it.aperture_b, it.center_x, it.center_y, (int)g.nx, (int)g.ny, g.dx, g.dy,
+                      st));
+    if (cfg->engine == OSGPU_GS_ASM_RELAY) {  // gs.rs:436-444
+      if ((rc = prop(it.d_input, ubuf.p, 0))) return rc;
+      CK(launch_abs(ubuf.p, c128, illum.p, rf64, 0, n, st));
+    } else {
+      CK(launch_abs(it.d_input, c128, illum.p, rf64, 0, n, st));
+    }
+    constexpr int kChunk = 8;  // iterations queued between looks at the stop flag
+    for (int k = 0; k < max_it; ++k) {
+      if (k > 0 && k % kChunk == 0) {
+        int stop = 0;
+        CK(cudaMemcpyAsync(&stop, &S->stop, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (stop) break;
+      }
+      {
+        ProfScope ps(c, st, PC_GS, (double)n * (rs + 1 + rs + es));
+        CK(launch_gs_mask(cur.p, rf64, illum.p, O, mask.p, c128, n, S, st));
+      }
+      if ((rc = prop(mask.p, ubuf.p, 0))) return rc;
+      {
+        ProfScope ps(c, st, PC_GS, (double)n * (es + rs * (it.d_target_intensity ? 2 : 1) + es));
+        CK(launch_gs_project(ubuf.p, c128, it.d_target_amplitude, it.d_target_intensity, rf64,
+                             beta_f, vbuf.p, n, P, it.d_target_error, S, H, k, st));
+      }
+      if ((rc = prop(vbuf.p, ubuf.p, 1))) return rc;
+      {
+        ProfScope ps(c, st, PC_GS, (double)n * (es + 2 * rs));
+        CK(launch_gs_update(ubuf.p, c128, cur.p, it.d_phase, rf64, beta_p, cfg->lo, cfg->hi, n,
+                            P, it.d_phase_error, S, H, k, cfg->patience, cfg->merit_tolerance,
+                            max_it, st));
+      }
+    }
+    GsState hs;
+    CK(cudaMemcpyAsync(&hs, S, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    std::vector<GsRecordDev> hh(max_it);
+    CK(cudaMemcpyAsync(hh.data(), H, sizeof(GsRecordDev) * max_it, cudaMemcpyDeviceToHost, st));
+    if (it.d_best_intensity) {  // the best iteration's forward pass, recomputed
+      CK(launch_gs_mask(it.d_phase, rf64, illum.p, O, mask.p, c128, n, nullptr, st));
+      if ((rc = prop(mask.p, ubuf.p, 0))) return rc;
+      CK(launch_abs(ubuf.p, c128, it.d_best_intensity, rf64, 1, n, st));
+    }
+    if (it.d_last_phase)
+      CK(cudaMemcpyAsync(it.d_last_phase, cur.p, n * rs, cudaMemcpyDeviceToDevice, st));
+    if (it.d_illumination)
+      CK(cudaMemcpyAsync(it.d_illumination, illum.p, n * rs, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    if (hs.best_it < 0) {
+      set_err("gs loop ran zero iterations");
+      return OSGPU_E_RENDER;
+    }
+    it.result.merit = hs.best_merit;
+    it.result.best_iteration = (uint64_t)hs.best_it;
+    it.result.amplitude_mse = hh[hs.best_it].amplitude_mse;
+    it.result.converged = hs.converged;
+    it.result.iterations = (uint64_t)hs.iterations;
+    if (it.history)
+      for (int k = 0; k < hs.iterations; ++k) {
+        osgpu_gs_record& r = it.history[k];
+        r.iteration = (uint64_t)k;
+        r.merit = hh[k].merit;
+        r.best_merit = hh[k].best_merit;
+        r.amplitude_mse = hh[k].amplitude_mse;
+        r.target_error_rms = hh[k].target_error_rms;
+        r.phase_update_rms = hh[k].phase_update_rms;
+      }
+  }
   return OSGPU_OK;
 }
 

@@ -341,6 +341,197 @@ __global__ void k_adam(double* x, float* x32, const void* g, int g_f64, double* 
   }
 }
 
+// ------------------------------------------------------------ GS loop
+// (reference gs.rs:425-597).  Per iteration: k_gs_mask -> forward half ->
+// k_gs_project -> k_gs_fold_merit -> back half -> k_gs_update ->
+// k_gs_fold_update.  The loop state lives on the device (GsState); every
+// kernel returns at once when state->stop is set, so the host can queue
+// iterations ahead of the convergence decision.
+
+constexpr double kTau = 6.283185307179586;  // 2 pi as f64 (gs.rs:105)
+constexpr double kPi = 3.141592653589793;
+
+__device__ __forceinline__ double rem_euclid(double a, double m) {
+  const double r = fmod(a, m);
+  return r < 0.0 ? r + fabs(m) : r;
+}
+
+// gs.rs:108-110
+__device__ __forceinline__ double wrap_pi(double v) {
+  return __dsub_rn(rem_euclid(__dadd_rn(v, kPi), kTau), kPi);
+}
+
+// gs.rs:115-121
+__device__ __forceinline__ double encode_bounds(double phi, double lo, double hi) {
+  if (__dsub_rn(hi, lo) >= kTau) return __dadd_rn(lo, rem_euclid(__dsub_rn(phi, lo), kTau));
+  return phi < lo ? lo : (phi > hi ? hi : phi);
+}
+
+// mask = open ? illum e^{i phase} : 0   (gs.rs:482-491, Complex::from_polar)
+__global__ void k_gs_mask(const void* phase, int f64, const void* illum,
+                          const unsigned char* open, void* mask, int c128, uint64_t n,
+                          const GsState* state) {
+  if (state && state->stop) return;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    if (open[k]) {
+      const double r = ld_real(illum, f64, k), th = ld_real(phase, f64, k);
+      double s, c;
+      sincos(th, &s, &c);
+      re = r * c;
+      im = r * s;
+    }
+    st_cx<double>(mask, c128, k, re, im);
+  }
+}
+
+// Target-plane error, merit terms and projection (gs.rs:494-545):
+// part frame 0 = sum (|u| - T)^2, frame 1 = sum (|u|^2 - Tint)^2.
+__global__ void k_gs_project(const void* u, int c128, const void* tamp, const void* tint,
+                             int f64, double beta_f, void* proj, uint64_t n, double* part,
+                             void* err_out, const GsState* state) {
+  if (state && state->stop) return;
+  Acc e2, m2;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    double re, im;
+    ld_cx<double>(u, c128, k, re, im);
+    const double amp = hypot(re, im);
+    const double t = ld_real(tamp, f64, k);
+    const double inten = __dmul_rn(amp, amp);
+    const double err = amp - t;
+    const double ti = tint ? ld_real(tint, f64, k) : __dmul_rn(t, t);
+    const double dm = inten - ti;
+    e2.add(__dmul_rn(err, err));
+    m2.add(__dmul_rn(dm, dm));
+    if (err_out) st_real(err_out, f64, k, err);
+    const double a = __dadd_rn(__dmul_rn(1.0 - beta_f, amp), __dmul_rn(beta_f, t));
+    double pr, pi;
+    if (amp > 0.0) {
+      const double sc = a / amp;
+      pr = re * sc;
+      pi = im * sc;
+    } else {
+      pr = a;
+      pi = 0.0;
+    }
+    st_cx<double>(proj, c128, k, pr, pi);
+  }
+  write_part(part, 0, block_fold(e2));
+  write_part(part, 1, block_fold(m2));
+}
+
+// Merit, best-so-far and the history record of iteration `it` (gs.rs:496-531).
+__global__ void k_gs_fold_merit(const double* part, int nb, uint64_t n, int it, GsState* state,
+                                GsRecordDev* hist) {
+  if (state->stop) return;
+  double sums[2];
+  for (int f = 0; f < 2; ++f) {
+    Acc a;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      Acc o;
+      o.s = part[((size_t)f * nb + b) * 2];
+      o.c = part[((size_t)f * nb + b) * 2 + 1];
+      a.add(o);
+    }
+    a = block_fold(a);
+    sums[f] = a.value();
+  }
+  if (threadIdx.x == 0) {
+    const double amp_mse = sums[0] / (double)n;
+    const double merit = sums[1] / (double)n;  // MseToTarget::evaluate (merit.rs:128-146)
+    const bool improved = state->best_it < 0 || merit < state->best_merit;
+    if (improved) {
+      state->best_merit = merit;
+      state->best_it = it;
+    }
+    state->improved = improved ? 1 : 0;
+    GsRecordDev& h = hist[it];
+    h.iteration = (double)it;
+    h.merit = merit;
+    h.best_merit = state->best_merit;
+    h.amplitude_mse = amp_mse;
+    h.target_error_rms = sqrt(amp_mse);
+    h.phase_update_rms = 0.0;
+  }
+}
+
+// DOE-plane update (gs.rs:557-566); the phase of an improving iteration is
+// kept as the best phase first.  part frame 0 = sum dphi^2.
+__global__ void k_gs_update(const void* v, int c128, void* phase, void* best, int f64,
+                            double beta_p, double lo, double hi, uint64_t n, double* part,
+                            void* dphi_out, const GsState* state) {
+  if (state->stop) return;
+  const bool keep = state->improved != 0;
+  Acc d2;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    double re, im;
+    ld_cx<double>(v, c128, k, re, im);
+    const double p = ld_real(phase, f64, k);
+    if (keep) st_real(best, f64, k, p);
+    const double dphi = wrap_pi(__dsub_rn(atan2(im, re), p));
+    st_real(phase, f64, k, encode_bounds(__dadd_rn(p, __dmul_rn(beta_p, dphi)), lo, hi));
+    if (dphi_out) st_real(dphi_out, f64, k, dphi);
+    d2.add(dphi * dphi);
+  }
+  write_part(part, 0, block_fold(d2));
+}
+
+// Phase-update RMS and the patience stop (gs.rs:567-578).
+__global__ void k_gs_fold_update(const double* part, int nb, uint64_t n, int it, int patience,
+                                 double tol, int max_it, GsState* state, GsRecordDev* hist) {
+  if (state->stop) return;
+  Acc a;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    Acc o;
+    o.s = part[(size_t)b * 2];
+    o.c = part[(size_t)b * 2 + 1];
+    a.add(o);
+  }
+  a = block_fold(a);
+  if (threadIdx.x == 0) {
+    hist[it].phase_update_rms = sqrt(a.value()) / sqrt((double)n);
+    state->iterations = it + 1;
+    if (it + 1 > patience) {
+      const double earlier = hist[it - patience].best_merit;
+      const double scale = fmax(fabs(earlier), 1e-30);
+      if ((earlier - state->best_merit) / scale < tol) {
+        state->converged = 1;
+        state->stop = 1;
+      }
+    }
+    if (it + 1 >= max_it) state->stop = 1;
+  }
+}
+
+// |u| (illumination amplitude) and |u|^2 (best intensity).
+__global__ void k_abs(const void* u, int c128, void* out, int f64, int square, uint64_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    double re, im;
+    ld_cx<double>(u, c128, k, re, im);
+    const double a = hypot(re, im);
+    st_real(out, f64, k, square ? a * a : a);
+  }
+}
+
+// Initial phase encoded into the bounds, and the carrier aperture mask
+// (gs.rs:429-435, 446-475).
+__global__ void k_gs_init(const void* init, void* phase, int f64, double lo, double hi,
+                          unsigned char* open, int stop, double a, double b, double cx,
+                          double cy, int nx, int ny, double dx, double dy) {
+  const uint64_t n = (uint64_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    st_real(phase, f64, k, encode_bounds(ld_real(init, f64, k), lo, hi));
+    const int ix = (int)(k % nx), iy = (int)(k / nx);
+    const double x = coord_d(ix, nx, dx), y = coord_d(iy, ny, dy);
+    open[k] = stop_contains(stop, a, b, __dsub_rn(x, cx), __dsub_rn(y, cy)) ? 1 : 0;
+  }
+}
+
 int red_blocks(uint64_t n) {
   const uint64_t b = (n + kRedThreads - 1) / kRedThreads;
   return (int)(b < 1216 ? (b ? b : 1) : 1216);  // <= 8 per SM on 152 SMs
@@ -459,6 +650,58 @@ cudaError_t launch_adam(double* x, float* x32, const void* g, int g_f64, double*
   }
   OSGPU_LAUNCH;
   k_adam<<<blocks, kRedThreads, 0, st>>>(x, x32, g, g_f64, m, v, n, p, norm2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_init(const void* init, void* phase, int f64, double lo, double hi,
+                           unsigned char* open, int stop, double a, double b, double cx,
+                           double cy, int nx, int ny, double dx, double dy, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_gs_init<<<red_blocks((uint64_t)nx * ny), kRedThreads, 0, st>>>(init, phase, f64, lo, hi, open,
+                                                                   stop, a, b, cx, cy, nx, ny, dx,
+                                                                   dy);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_abs(const void* u, int c128, void* out, int f64, int square, uint64_t n,
+                       cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_abs<<<red_blocks(n), kRedThreads, 0, st>>>(u, c128, out, f64, square, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_mask(const void* phase, int f64, const void* illum,
+                           const unsigned char* open, void* mask, int c128, uint64_t n,
+                           const GsState* state, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_gs_mask<<<red_blocks(n), kRedThreads, 0, st>>>(phase, f64, illum, open, mask, c128, n, state);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_project(const void* u, int c128, const void* tamp, const void* tint,
+                              int f64, double beta_f, void* proj, uint64_t n, double* part,
+                              void* err_out, GsState* state, GsRecordDev* hist, int it,
+                              cudaStream_t st) {
+  const int nb = red_blocks(n);
+  OSGPU_LAUNCH;
+  k_gs_project<<<nb, kRedThreads, 0, st>>>(u, c128, tamp, tint, f64, beta_f, proj, n, part,
+                                           err_out, state);
+  OSGPU_LAUNCH;
+  k_gs_fold_merit<<<1, kRedThreads, 0, st>>>(part, nb, n, it, state, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_update(const void* v, int c128, void* phase, void* best, int f64,
+                             double beta_p, double lo, double hi, uint64_t n, double* part,
+                             void* dphi_out, GsState* state, GsRecordDev* hist, int it,
+                             int patience, double tol, int max_it, cudaStream_t st) {
+  const int nb = red_blocks(n);
+  OSGPU_LAUNCH;
+  k_gs_update<<<nb, kRedThreads, 0, st>>>(v, c128, phase, best, f64, beta_p, lo, hi, n, part,
+                                          dphi_out, state);
+  OSGPU_LAUNCH;
+  k_gs_fold_update<<<1, kRedThreads, 0, st>>>(part, nb, n, it, patience, tol, max_it, state,
+                                              hist);
   return cudaGetLastError();
 }
 

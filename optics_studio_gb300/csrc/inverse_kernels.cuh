@@ -19,6 +19,38 @@ struct AdamArgs {
   int clip;
 };
 
+// Device-resident state of one Gerchberg-Saxton run.
+struct GsState {
+  double best_merit;
+  int best_it;   // -1 before the first iteration
+  int improved;  // the current iteration improved on the best merit
+  int stop;      // converged or iteration cap reached: later kernels return
+  int converged;
+  int iterations;
+};
+// One history record (layout of osgpu_gs_record).
+struct GsRecordDev {
+  double iteration, merit, best_merit, amplitude_mse, target_error_rms, phase_update_rms;
+};
+
+cudaError_t launch_gs_init(const void* init, void* phase, int f64, double lo, double hi,
+                           unsigned char* open, int stop, double a, double b, double cx,
+                           double cy, int nx, int ny, double dx, double dy, cudaStream_t st);
+cudaError_t launch_abs(const void* u, int c128, void* out, int f64, int square, uint64_t n,
+                       cudaStream_t st);
+cudaError_t launch_gs_mask(const void* phase, int f64, const void* illum,
+                           const unsigned char* open, void* mask, int c128, uint64_t n,
+                           const GsState* state, cudaStream_t st);
+// part: reduce_scratch_bytes(2)
+cudaError_t launch_gs_project(const void* u, int c128, const void* tamp, const void* tint,
+                              int f64, double beta_f, void* proj, uint64_t n, double* part,
+                              void* err_out, GsState* state, GsRecordDev* hist, int it,
+                              cudaStream_t st);
+cudaError_t launch_gs_update(const void* v, int c128, void* phase, void* best, int f64,
+                             double beta_p, double lo, double hi, uint64_t n, double* part,
+                             void* dphi_out, GsState* state, GsRecordDev* hist, int it,
+                             int patience, double tol, int max_it, cudaStream_t st);
+
 cudaError_t launch_apply_intensity(const void* in, int in_c128, void* out, int out_c128,
                                    const ElementList& els, int nx, int ny, double dx, double dy,
                                    void* inten, int inten_f64, int f32, cudaStream_t st);

@@ -44,6 +44,8 @@ STRUCTS = {
     "osgpu_rs_report": "RsReportC", "osgpu_element": "ElementC", "osgpu_step": "StepC",
     "osgpu_trace_item": "TraceItemC", "osgpu_kernel_stat": "KernelStatC",
     "osgpu_frame": "FrameC", "osgpu_adam_config": "AdamConfigC",
+    "osgpu_gs_config": "GsConfigC", "osgpu_gs_record": "GsRecordC",
+    "osgpu_gs_result": "GsResultC", "osgpu_gs_item": "GsItemC",
 }
 
 
