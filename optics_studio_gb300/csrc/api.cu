@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -20,6 +21,7 @@
 
 #include "../../include/osgpu.h"
 #include "host_analysis.h"
+#include "gs_fast.cuh"
 #include "inverse_kernels.cuh"
 #include "prop_kernels.cuh"
 
@@ -46,10 +48,11 @@ struct ProfRec {
   double bytes;
 };
 enum { PC_PREP = 0, PC_ELEMENTS, PC_APPLY, PC_PASS_A, PC_PASS_B, PC_PASS_C, PC_KSPEC, PC_FRAUN,
-       PC_GS, PC_N };
+       PC_GS, PC_GS_COLS, PC_GS_ROWS, PC_N };
 const char* kProfNames[PC_N] = {"prep_tables", "element_tables", "element_apply",
                                 "pass_a_rows", "pass_b_columns", "pass_c_rows",
-                                "kernel_spectrum", "fraunhofer", "gs_planes"};
+                                "kernel_spectrum", "fraunhofer", "gs_planes", "gs_columns",
+                                "gs_rows"};
 
 struct Context {
   std::recursive_mutex mu;
@@ -708,6 +711,199 @@ int forward_frame(Context& c, const osgpu_frame& fr, const std::vector<Elements>
     ProfScope ps(c, st, PC_APPLY, (double)g.nx * g.ny * ((c128 ? 16 : 8) + (c128 ? 8 : 4)));
     CK(launch_apply_intensity(src, c128, nullptr, c128, tail.list, (int)g.nx, (int)g.ny, g.dx,
                               g.dy, fr.d_intensity, c128, f32, st));
+  }
+  return OSGPU_OK;
+}
+
+// Fused f32 Fraunhofer GS (gs_fast.cu) over all items of a batch: every
+// item is M x M, z > 0, no source offset.
+int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_config& cfg,
+             const osgpu_fraunhofer_config& fcfg, double beta_f, double beta_p, int M,
+             cudaStream_t st) {
+  const size_t n = (size_t)M * M;
+  const int nb = gs_fast_blocks(M);
+  const int max_it = cfg.max_iterations;
+  int rc;
+  const void* tw = nullptr;
+  if ((rc = get_tw(c, M, 0, &tw))) return rc;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  // per-item layout in one allocation
+  const size_t o_W = 0, o_ph = o_W + al(n * 8), o_il = o_ph + al(n * 4), o_op = o_il + al(n * 4),
+               o_ta = o_op + al(n), o_ti = o_ta + al(n * 4), o_tab = o_ti + al(n * 4),
+               o_pc = o_tab + al((size_t)4 * M * 8), o_pr = o_pc + al((size_t)4 * nb * 8),
+               o_hi = o_pr + al((size_t)2 * nb * 8), per = o_hi + al(sizeof(GsRecordDev) * max_it);
+  DBuf mem, dstates, ditems, dfolds;
+  CK(mem.alloc(per * n_items, st));
+  CK(dstates.alloc(sizeof(GsState) * n_items, st));
+  CK(ditems.alloc(sizeof(GsFastItem) * n_items, st));
+  CK(dfolds.alloc(sizeof(GsFoldItem) * n_items, st));
+  char* base = reinterpret_cast<char*>(mem.p);
+  GsState* S = reinterpret_cast<GsState*>(dstates.p);
+  std::vector<GsState> hs(n_items);
+  for (auto& h : hs) {
+    std::memset(&h, 0, sizeof(h));
+    h.best_it = -1;
+  }
+  CK(cudaMemcpyAsync(S, hs.data(), sizeof(GsState) * n_items, cudaMemcpyHostToDevice, st));
+  std::vector<GsFastItem> fi(n_items);
+  std::vector<GsFoldItem> fo(n_items);
+  std::vector<float2> tabs((size_t)4 * M * n_items);
+  for (int i = 0; i < n_items; ++i) {
+    osgpu_gs_item& it = items[i];
+    const osgpu_grid& g = it.grid;
+    char* b = base + per * i;
+    osgpu_fraunhofer_report fr;
+    if ((rc = fraunhofer_resolve(g, it.z, fcfg, fr)) > 0) {
+      set_err("GS item %d: Fraunhofer regime check failed (status %d)", i, rc);
+      return rc;
+    }
+    // separable pre / post factors in FP64 (fraunhofer.rs:396-438, no source offset)
+    const double cxc = ((double)M - 1.0) / 2.0, lz = g.lambda * it.z;
+    const double kz = (2.0 * PI / g.lambda) * it.z;
+    const double qre = std::sin(kz) / lz, qim = -std::cos(kz) / lz;  // e^{ikz} / (i lam z)
+    const double w = g.dx * g.dy;
+    float2* T4 = tabs.data() + (size_t)4 * M * i;
+    for (int j = 0; j < M; ++j) {
+      const double pre = 2.0 * PI * cxc * (double)j / (double)M;
+      T4[j] = make_float2((float)std::cos(pre), (float)std::sin(pre));          // prx
+      T4[M + j] = T4[j];                                                          // pry
+      const double dxp = ((double)j - cxc) * fr.dx_out, dyp = ((double)j - cxc) * fr.dy_out;
+      const double post = 2.0 * PI * cxc * ((double)j - cxc) / (double)M;
+      const double ax = PI * dxp * dxp / lz + post, ay = PI * dyp * dyp / lz + post;
+      const double cx_ = std::cos(ax), sx_ = std::sin(ax);
+      T4[2 * M + j] = make_float2((float)((qre * cx_ - qim * sx_) * w),
+                                  (float)((qre * sx_ + qim * cx_) * w));          // qx
+      T4[3 * M + j] = make_float2((float)std::cos(ay), (float)std::sin(ay));      // qy
+    }
+    GsFastItem& f = fi[i];
+    std::memset(&f, 0, sizeof(f));
+    f.W = reinterpret_cast<float2*>(b + o_W);
+    f.phase = reinterpret_cast<float*>(b + o_ph);
+    f.best = reinterpret_cast<float*>(it.d_phase);
+    f.illum = reinterpret_cast<const float*>(b + o_il);
+    f.open = reinterpret_cast<const unsigned char*>(b + o_op);
+    f.tamp_t = reinterpret_cast<const float*>(b + o_ta);
+    f.tint_t = it.d_target_intensity ? reinterpret_cast<const float*>(b + o_ti) : nullptr;
+    f.prx = reinterpret_cast<const float2*>(b + o_tab);
+    f.pry = f.prx + M;
+    f.qx = f.prx + 2 * M;
+    f.qy = f.prx + 3 * M;
+    f.c = (float)(w / lz);
+    f.terr = reinterpret_cast<float*>(it.d_target_error);
+    f.perr = reinterpret_cast<float*>(it.d_phase_error);
+    f.state = S + i;
+    f.part_col = reinterpret_cast<double*>(b + o_pc);
+    f.part_row = reinterpret_cast<double*>(b + o_pr);
+    fo[i].part_merit = f.part_col;
+    fo[i].part_update = f.part_row;
+    fo[i].state = S + i;
+    fo[i].hist = reinterpret_cast<GsRecordDev*>(b + o_hi);
+    CK(cudaMemcpyAsync(b + o_tab, T4, sizeof(float2) * 4 * M, cudaMemcpyHostToDevice, st));
+    CK(launch_gs_init(it.d_phase, f.phase, 0, cfg.lo, cfg.hi,
+                      reinterpret_cast<unsigned char*>(b + o_op), it.aperture,
+                      it.aperture_a, it.aperture_b, it.center_x, it.center_y, M, M, g.dx, g.dy,
+                      st));
+    CK(launch_abs(it.d_input, 0, b + o_il, 0, 0, n, st));
+    CK(launch_transpose_real(reinterpret_cast<const float*>(it.d_target_amplitude),
+                             reinterpret_cast<float*>(b + o_ta), M, st));
+    if (it.d_target_intensity)
+      CK(launch_transpose_real(reinterpret_cast<const float*>(it.d_target_intensity),
+                               reinterpret_cast<float*>(b + o_ti), M, st));
+  }
+  CK(cudaMemcpyAsync(ditems.p, fi.data(), sizeof(GsFastItem) * n_items, cudaMemcpyHostToDevice,
+                     st));
+  CK(cudaMemcpyAsync(dfolds.p, fo.data(), sizeof(GsFoldItem) * n_items, cudaMemcpyHostToDevice,
+                     st));
+  CK(cudaStreamSynchronize(st));  // host tables and descriptors are copied
+  const GsFastItem* DI = reinterpret_cast<const GsFastItem*>(ditems.p);
+  const GsFoldItem* DF = reinterpret_cast<const GsFoldItem*>(dfolds.p);
+  GsFastArgs a;
+  a.M = M;
+  a.tw = tw;
+  a.beta_f = (float)beta_f;
+  a.beta_p = (float)beta_p;
+  a.lo = (float)cfg.lo;
+  a.hi = (float)cfg.hi;
+  a.wrap = (cfg.hi - cfg.lo >= 2.0 * PI) ? 1 : 0;
+  const double bytes_cols = (double)n * (2 * 8 + 4) * n_items;
+  const double bytes_rows = (double)n * (2 * 8 + 4 + 4 + 4 + 1) * n_items;
+  {
+    ProfScope ps(c, st, PC_GS_ROWS, bytes_rows);
+    CK(launch_gs_rows(DI, n_items, a, 0, st));
+  }
+  constexpr int kChunk = 8;
+  for (int k = 0; k < max_it; ++k) {
+    if (k > 0 && k % kChunk == 0) {
+      CK(cudaMemcpyAsync(hs.data(), S, sizeof(GsState) * n_items, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      bool all = true;
+      for (auto& h : hs) all = all && h.stop;
+      if (all) break;
+    }
+    {
+      ProfScope ps(c, st, PC_GS_COLS, bytes_cols);
+      CK(launch_gs_cols(DI, n_items, a, st));
+    }
+    CK(launch_gs_fold_merit_batch(DF, n_items, nb, n, k, st));
+    {
+      ProfScope ps(c, st, PC_GS_ROWS, bytes_rows);
+      CK(launch_gs_rows(DI, n_items, a, 1, st));
+    }
+    CK(launch_gs_fold_update_batch(DF, n_items, nb, n, k, cfg.patience, cfg.merit_tolerance,
+                                   max_it, st));
+  }
+  CK(cudaMemcpyAsync(hs.data(), S, sizeof(GsState) * n_items, cudaMemcpyDeviceToHost, st));
+  std::vector<GsRecordDev> hh((size_t)max_it * n_items);
+  for (int i = 0; i < n_items; ++i)
+    CK(cudaMemcpyAsync(hh.data() + (size_t)max_it * i, fo[i].hist, sizeof(GsRecordDev) * max_it,
+                       cudaMemcpyDeviceToHost, st));
+  ElementList none;
+  std::memset(&none, 0, sizeof(none));
+  DBuf mask, ubuf;
+  CK(mask.alloc(n * 8, st));
+  CK(ubuf.alloc(n * 8, st));
+  for (int i = 0; i < n_items; ++i) {
+    osgpu_gs_item& it = items[i];
+    char* b = base + per * i;
+    if (it.d_best_intensity) {  // the best iteration's forward pass, recomputed
+      osgpu_fraunhofer_report fr;
+      fraunhofer_resolve(it.grid, it.z, fcfg, fr);
+      CK(launch_gs_mask(it.d_phase, 0, b + o_il, reinterpret_cast<unsigned char*>(b + o_op),
+                        mask.p, 0, n, nullptr, st));
+      if ((rc = run_fraun<float>(c, it.grid, it.z, fr, none, mask.p, 0, ubuf.p, 0, nullptr, 0,
+                                 st)))
+        return rc;
+      CK(launch_abs(ubuf.p, 0, it.d_best_intensity, 0, 1, n, st));
+    }
+    if (it.d_last_phase)
+      CK(cudaMemcpyAsync(it.d_last_phase, b + o_ph, n * 4, cudaMemcpyDeviceToDevice, st));
+    if (it.d_illumination)
+      CK(cudaMemcpyAsync(it.d_illumination, b + o_il, n * 4, cudaMemcpyDeviceToDevice, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  for (int i = 0; i < n_items; ++i) {
+    osgpu_gs_item& it = items[i];
+    const GsState& h = hs[i];
+    const GsRecordDev* H = hh.data() + (size_t)max_it * i;
+    if (h.best_it < 0) {
+      set_err("gs loop ran zero iterations");
+      return OSGPU_E_RENDER;
+    }
+    it.result.merit = h.best_merit;
+    it.result.best_iteration = (uint64_t)h.best_it;
+    it.result.amplitude_mse = H[h.best_it].amplitude_mse;
+    it.result.converged = h.converged;
+    it.result.iterations = (uint64_t)h.iterations;
+    if (it.history)
+      for (int k = 0; k < h.iterations; ++k) {
+        osgpu_gs_record& r = it.history[k];
+        r.iteration = (uint64_t)k;
+        r.merit = H[k].merit;
+        r.best_merit = H[k].best_merit;
+        r.amplitude_mse = H[k].amplitude_mse;
+        r.target_error_rms = H[k].target_error_rms;
+        r.phase_update_rms = H[k].phase_update_rms;
+      }
   }
   return OSGPU_OK;
 }
@@ -1626,6 +1822,18 @@ int osgpu_gs_run_batch_device(osgpu_gs_item* items, int32_t n_items, const osgpu
   const int f32 = dtype == OSGPU_C64, c128 = dtype == OSGPU_C128, rf64 = c128;
   const size_t es = c128 ? 16 : 8, rs = c128 ? 8 : 4;
   const int max_it = cfg->max_iterations;
+  // fused f32 Fraunhofer path: every item M x M (power of two), z > 0, no source offset
+  if (f32 && cfg->engine == OSGPU_GS_FRAUNHOFER && !fraunhofer_cfg->has_source_pos &&
+      n_items > 0 && !std::getenv("OSGPU_GS_GENERIC")) {
+    const int M = (int)items[0].grid.nx;
+    bool ok = gs_fast_size(M);
+    for (int i = 0; i < n_items && ok; ++i) {
+      const osgpu_gs_item& it = items[i];
+      ok = it.grid.nx == (uint64_t)M && it.grid.ny == (uint64_t)M && it.d_input &&
+           it.d_target_amplitude && it.d_phase && std::isfinite(it.z) && it.z > 0.0;
+    }
+    if (ok) return gs_fused(c, items, n_items, *cfg, *fraunhofer_cfg, beta_f, beta_p, M, st);
+  }
   for (int i = 0; i < n_items; ++i) {
     osgpu_gs_item& it = items[i];
     const osgpu_grid& g = it.grid;

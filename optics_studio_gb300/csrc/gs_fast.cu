@@ -1,0 +1,257 @@
+// Fused f32 Gerchberg-Saxton iteration for the Fraunhofer engine (square
+// power-of-two grids, M in [256, 4096]), batched over items.
+//
+// Forward operator (reference fraunhofer.rs:364-443, z > 0, no source
+// offset): U = D o FFT2(pre o u), pre(ix, iy) = prx[ix] pry[iy] and
+// D(ix, iy) = qx[ix] qy[iy] with |D| = c = dx dy / (lam z) everywhere.  Its
+// adjoint is conj(pre) o FFT2^H(conj(D) o U).  The target-plane projection
+// U' = U a / |U| (gs.rs:533-545) followed by conj(D) is therefore
+// c a F / |F| in the raw transform domain F = FFT2(pre o u), so one column
+// pass does the forward column FFT, the projection and its reductions, and
+// the inverse column FFT; one row pass does the inverse row FFT, conj(pre),
+// the DOE-plane update (gs.rs:557-566) and, for the next iteration, the
+// mask, pre and the forward row FFT.  The spectrum W is column-major
+// (W[kx * M + ky]).  Every kernel returns at once for an item whose state
+// says stop.
+#include <cuda_runtime.h>
+
+#include "fft_reg.cuh"
+#include "gs_fast.cuh"
+#include "inverse_kernels.cuh"
+
+namespace osgpu {
+
+extern unsigned long long& launch_counter();
+
+namespace {
+
+using namespace regfft;
+
+constexpr float kPiF = 3.14159265358979f;
+constexpr float kTauF = 6.28318530717959f;
+
+__device__ __forceinline__ float wrap_pi_f(float v) {
+  float r = fmodf(v + kPiF, kTauF);
+  if (r < 0.f) r += kTauF;
+  return r - kPiF;
+}
+
+__device__ __forceinline__ float encode_f(float p, const GsFastArgs& a) {
+  if (a.wrap) {
+    float r = fmodf(p - a.lo, kTauF);
+    if (r < 0.f) r += kTauF;
+    return a.lo + r;
+  }
+  return p < a.lo ? a.lo : (p > a.hi ? a.hi : p);
+}
+
+// Sum of one float per thread over the CTA into part[(f * gridDim.x + blockIdx.x) * 2]
+// (compensation slot 0), the layout of the GS fold kernels.
+__device__ __forceinline__ void cta_sum(float x, double* part, int f, double* red) {
+  double v = (double)x;
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < nw; ++i) s += red[i];
+    const size_t o = ((size_t)f * gridDim.x + blockIdx.x) * 2;
+    part[o] = s;
+    part[o + 1] = 0.0;
+  }
+}
+
+template <int M, int G>
+struct GsLay {
+  static constexpr int T = M / 16;
+  static constexpr int THREADS = G * T;
+  static constexpr size_t SMEM =
+      ((size_t)TwLay<M>::SIZE + (size_t)G * Plan<M>::SMEM) * sizeof(float2) + 32 * sizeof(double);
+};
+
+template <int M, int G>
+__global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
+    k_gs_cols(const GsFastItem* __restrict__ items, GsFastArgs a) {
+  constexpr int T = M / 16;
+  const GsFastItem& it = items[blockIdx.y];
+  if (it.state->stop) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  double* red = reinterpret_cast<double*>(bufs + G * Plan<M>::SMEM);
+  const int g = threadIdx.x / T, tid = threadIdx.x - g * T;
+  const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
+  const int BAR_N = (T % 32 == 0) ? T : GsLay<M, G>::THREADS;
+  float2* buf = bufs + g * Plan<M>::SMEM;
+  load_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw), threadIdx.x, blockDim.x);
+  const int kx = blockIdx.x * G + g;
+  float2* col = it.W + (size_t)kx * M;
+  float2 v[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = col[tid + T * q];
+  __syncthreads();
+  fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
+  float e2 = 0.f, m2 = 0.f;
+  const float c = it.c, bf = a.beta_f;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int ky = tid + T * q;
+    const size_t kt = (size_t)kx * M + ky;  // column-major target index
+    const float2 f = v[q];
+    const float m = sqrtf(f.x * f.x + f.y * f.y);
+    const float amp = c * m;
+    const float t = __ldg(it.tamp_t + kt);
+    const float ti = it.tint_t ? __ldg(it.tint_t + kt) : t * t;
+    const float err = amp - t;
+    const float inten = amp * amp;
+    e2 = fmaf(err, err, e2);
+    m2 = fmaf(inten - ti, inten - ti, m2);
+    if (it.terr) it.terr[(size_t)ky * M + kx] = err;
+    const float aa = (1.f - bf) * amp + bf * t;
+    float2 gq;
+    if (m > 0.f) {
+      const float s = c * aa / m;
+      gq = make_float2(f.x * s, f.y * s);
+    } else {  // projection (a, 0) through conj(D)
+      const float2 d = cmul(__ldg(it.qx + kx), __ldg(it.qy + ky));
+      gq = make_float2(d.x * aa, -d.y * aa);
+    }
+    v[q] = gq;
+  }
+  fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) col[tid + T * q] = v[q];
+  cta_sum(e2, it.part_col, 0, red);
+  cta_sum(m2, it.part_col, 1, red);
+}
+
+template <int M, int G>
+__global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
+    k_gs_rows(const GsFastItem* __restrict__ items, GsFastArgs a, int iterate) {
+  constexpr int T = M / 16;
+  const GsFastItem& it = items[blockIdx.y];
+  if (iterate && it.state->stop) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  double* red = reinterpret_cast<double*>(bufs + G * Plan<M>::SMEM);
+  const int g = threadIdx.x / T, tid = threadIdx.x - g * T;
+  const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
+  const int BAR_N = (T % 32 == 0) ? T : GsLay<M, G>::THREADS;
+  float2* buf = bufs + g * Plan<M>::SMEM;
+  load_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw), threadIdx.x, blockDim.x);
+  const int iy = blockIdx.x * G + g;
+  const float2 py = __ldg(it.pry + iy);
+  float2 v[16];
+  float d2 = 0.f;
+  if (iterate) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = it.W[(size_t)(tid + T * q) * M + iy];
+  }
+  __syncthreads();
+  if (iterate) {
+    fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
+  }
+  const bool keep = iterate && it.state->improved;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int ix = tid + T * q;
+    const size_t k = (size_t)iy * M + ix;
+    const float2 pre = cmul(__ldg(it.prx + ix), py);
+    float p = it.phase[k];
+    if (iterate) {
+      const float2 w = cmulc(v[q], pre);  // conj(pre) v
+      const float dphi = wrap_pi_f(atan2f(w.y, w.x) - p);
+      if (keep) it.best[k] = p;
+      p = encode_f(p + a.beta_p * dphi, a);
+      it.phase[k] = p;
+      d2 = fmaf(dphi, dphi, d2);
+      if (it.perr) it.perr[k] = dphi;
+    }
+    float2 x = make_float2(0.f, 0.f);
+    if (it.open[k]) {
+      float s, cs;
+      sincosf(p, &s, &cs);
+      const float r = __ldg(it.illum + k);
+      x = cmul(make_float2(r * cs, r * s), pre);
+    }
+    v[q] = x;
+  }
+  fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) it.W[(size_t)(tid + T * q) * M + iy] = v[q];
+  if (iterate) cta_sum(d2, it.part_row, 0, red);
+}
+
+// Column-major copy of a real M x M array (32 x 32 tiles through shared memory).
+__global__ void k_transpose_real(const float* __restrict__ in, float* __restrict__ out, int M) {
+  __shared__ float tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y)
+    tile[j][threadIdx.x] = in[(size_t)(by + j) * M + bx + threadIdx.x];
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y)
+    out[(size_t)(bx + j) * M + by + threadIdx.x] = tile[threadIdx.x][j];
+}
+
+constexpr int kG = 2;
+
+template <int M>
+cudaError_t launch_cols(const GsFastItem* items, int n_items, const GsFastArgs& a,
+                        cudaStream_t st) {
+  using L = GsLay<M, kG>;
+  cudaError_t e = cudaFuncSetAttribute(k_gs_cols<M, kG>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  k_gs_cols<M, kG><<<dim3(M / kG, n_items), L::THREADS, L::SMEM, st>>>(items, a);
+  return cudaGetLastError();
+}
+
+template <int M>
+cudaError_t launch_rows(const GsFastItem* items, int n_items, const GsFastArgs& a, int iterate,
+                        cudaStream_t st) {
+  using L = GsLay<M, kG>;
+  cudaError_t e = cudaFuncSetAttribute(k_gs_rows<M, kG>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  k_gs_rows<M, kG><<<dim3(M / kG, n_items), L::THREADS, L::SMEM, st>>>(items, a, iterate);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool gs_fast_size(int m) { return m == 256 || m == 512 || m == 1024 || m == 2048 || m == 4096; }
+
+int gs_fast_blocks(int m) { return m / kG; }
+
+#define OSGPU_GS_DISPATCH(m, fn, ...)          \
+  switch (m) {                                 \
+    case 256: return fn<256>(__VA_ARGS__);     \
+    case 512: return fn<512>(__VA_ARGS__);     \
+    case 1024: return fn<1024>(__VA_ARGS__);   \
+    case 2048: return fn<2048>(__VA_ARGS__);   \
+    case 4096: return fn<4096>(__VA_ARGS__);   \
+    default: return cudaErrorInvalidValue;     \
+  }
+
+cudaError_t launch_gs_cols(const GsFastItem* items, int n_items, const GsFastArgs& a,
+                           cudaStream_t st) {
+  OSGPU_GS_DISPATCH(a.M, launch_cols, items, n_items, a, st)
+}
+
+cudaError_t launch_gs_rows(const GsFastItem* items, int n_items, const GsFastArgs& a,
+                           int iterate, cudaStream_t st) {
+  OSGPU_GS_DISPATCH(a.M, launch_rows, items, n_items, a, iterate, st)
+}
+
+cudaError_t launch_transpose_real(const float* in, float* out, int M, cudaStream_t st) {
+  ++launch_counter();
+  k_transpose_real<<<dim3(M / 32, M / 32), dim3(32, 8), 0, st>>>(in, out, M);
+  return cudaGetLastError();
+}
+
+}  // namespace osgpu

@@ -1,0 +1,46 @@
+// Fused f32 Gerchberg-Saxton kernels of the Fraunhofer engine (gs_fast.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "inverse_kernels.cuh"
+
+namespace osgpu {
+
+// Device-side view of one GS item on an M x M grid.
+struct GsFastItem {
+  float2* W;                  // spectrum scratch, column-major M x M
+  float* phase;               // current phase
+  float* best;                // best phase (the caller's phase buffer)
+  const float* illum;         // illumination amplitude
+  const unsigned char* open;  // carrier aperture
+  const float* tamp_t;        // target amplitude, column-major
+  const float* tint_t;        // merit target intensity, column-major (null: T^2)
+  const float2* prx;          // pre = prx[ix] pry[iy]
+  const float2* pry;
+  const float2* qx;           // D = qx[ix] qy[iy]
+  const float2* qy;
+  float c;                    // |D|
+  float* terr;                // optional: |U| - T of the last iteration (row-major)
+  float* perr;                // optional: phase update of the last iteration
+  GsState* state;
+  double* part_col;           // 2 frames x gs_fast_blocks(M) pairs
+  double* part_row;           // 1 frame x gs_fast_blocks(M) pairs
+};
+
+struct GsFastArgs {
+  int M;
+  const void* tw;  // M-point f32 twiddle table
+  float beta_f, beta_p, lo, hi;
+  int wrap;        // hi - lo >= 2 pi (encode_bounds wraps instead of clamping)
+};
+
+bool gs_fast_size(int m);
+int gs_fast_blocks(int m);  // CTAs per item of the row and column kernels
+cudaError_t launch_gs_cols(const GsFastItem* items, int n_items, const GsFastArgs& a,
+                           cudaStream_t st);
+// iterate = 0: first forward rows from the initial phase only
+cudaError_t launch_gs_rows(const GsFastItem* items, int n_items, const GsFastArgs& a,
+                           int iterate, cudaStream_t st);
+cudaError_t launch_transpose_real(const float* in, float* out, int M, cudaStream_t st);
+
+}  // namespace osgpu

@@ -423,8 +423,8 @@ __global__ void k_gs_project(const void* u, int c128, const void* tamp, const vo
 }
 
 // Merit, best-so-far and the history record of iteration `it` (gs.rs:496-531).
-__global__ void k_gs_fold_merit(const double* part, int nb, uint64_t n, int it, GsState* state,
-                                GsRecordDev* hist) {
+__device__ void gs_fold_merit(const double* part, int nb, uint64_t n, int it, GsState* state,
+                              GsRecordDev* hist) {
   if (state->stop) return;
   double sums[2];
   for (int f = 0; f < 2; ++f) {
@@ -457,6 +457,17 @@ __global__ void k_gs_fold_merit(const double* part, int nb, uint64_t n, int it, 
   }
 }
 
+__global__ void k_gs_fold_merit(const double* part, int nb, uint64_t n, int it, GsState* state,
+                                GsRecordDev* hist) {
+  gs_fold_merit(part, nb, n, it, state, hist);
+}
+
+// One block per item of a batch.
+__global__ void k_gs_fold_merit_batch(const GsFoldItem* items, int nb, uint64_t n, int it) {
+  const GsFoldItem& f = items[blockIdx.x];
+  gs_fold_merit(f.part_merit, nb, n, it, f.state, f.hist);
+}
+
 // DOE-plane update (gs.rs:557-566); the phase of an improving iteration is
 // kept as the best phase first.  part frame 0 = sum dphi^2.
 __global__ void k_gs_update(const void* v, int c128, void* phase, void* best, int f64,
@@ -480,8 +491,8 @@ __global__ void k_gs_update(const void* v, int c128, void* phase, void* best, in
 }
 
 // Phase-update RMS and the patience stop (gs.rs:567-578).
-__global__ void k_gs_fold_update(const double* part, int nb, uint64_t n, int it, int patience,
-                                 double tol, int max_it, GsState* state, GsRecordDev* hist) {
+__device__ void gs_fold_update(const double* part, int nb, uint64_t n, int it, int patience,
+                               double tol, int max_it, GsState* state, GsRecordDev* hist) {
   if (state->stop) return;
   Acc a;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -504,6 +515,17 @@ __global__ void k_gs_fold_update(const double* part, int nb, uint64_t n, int it,
     }
     if (it + 1 >= max_it) state->stop = 1;
   }
+}
+
+__global__ void k_gs_fold_update(const double* part, int nb, uint64_t n, int it, int patience,
+                                 double tol, int max_it, GsState* state, GsRecordDev* hist) {
+  gs_fold_update(part, nb, n, it, patience, tol, max_it, state, hist);
+}
+
+__global__ void k_gs_fold_update_batch(const GsFoldItem* items, int nb, uint64_t n, int it,
+                                       int patience, double tol, int max_it) {
+  const GsFoldItem& f = items[blockIdx.x];
+  gs_fold_update(f.part_update, nb, n, it, patience, tol, max_it, f.state, f.hist);
 }
 
 // |u| (illumination amplitude) and |u|^2 (best intensity).
@@ -702,6 +724,22 @@ cudaError_t launch_gs_update(const void* v, int c128, void* phase, void* best, i
   OSGPU_LAUNCH;
   k_gs_fold_update<<<1, kRedThreads, 0, st>>>(part, nb, n, it, patience, tol, max_it, state,
                                               hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_fold_merit_batch(const GsFoldItem* items, int n_items, int nb, uint64_t n,
+                                       int it, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_gs_fold_merit_batch<<<n_items, kRedThreads, 0, st>>>(items, nb, n, it);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_fold_update_batch(const GsFoldItem* items, int n_items, int nb, uint64_t n,
+                                        int it, int patience, double tol, int max_it,
+                                        cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_gs_fold_update_batch<<<n_items, kRedThreads, 0, st>>>(items, nb, n, it, patience, tol,
+                                                          max_it);
   return cudaGetLastError();
 }
 

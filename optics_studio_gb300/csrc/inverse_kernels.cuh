@@ -33,6 +33,19 @@ struct GsRecordDev {
   double iteration, merit, best_merit, amplitude_mse, target_error_rms, phase_update_rms;
 };
 
+// Per-item pointers of a batched fold (fused GS path).
+struct GsFoldItem {
+  const double* part_merit;   // 2 frames x nb compensated pairs
+  const double* part_update;  // 1 frame x nb pairs
+  GsState* state;
+  GsRecordDev* hist;
+};
+cudaError_t launch_gs_fold_merit_batch(const GsFoldItem* items, int n_items, int nb, uint64_t n,
+                                       int it, cudaStream_t st);
+cudaError_t launch_gs_fold_update_batch(const GsFoldItem* items, int n_items, int nb, uint64_t n,
+                                        int it, int patience, double tol, int max_it,
+                                        cudaStream_t st);
+
 cudaError_t launch_gs_init(const void* init, void* phase, int f64, double lo, double hi,
                            unsigned char* open, int stop, double a, double b, double cx,
                            double cy, int nx, int ny, double dx, double dy, cudaStream_t st);

@@ -149,3 +149,63 @@ def test_gs_aperture_and_batch():
         assert g.merit == pytest.approx(w.merit, rel=1e-10)
         ph = g.phase.cpu().numpy()
         assert np.linalg.norm(ph - w.phase) / np.linalg.norm(w.phase) <= 1e-9
+
+
+def inputs_fraunhofer(n, seed=3):
+    rng = np.random.default_rng(seed)
+    u = np.ones((n, n), dtype=np.complex128)
+    z = 50e-3
+    init = rng.uniform(-math.pi, math.pi, (n, n))
+    tamp = spot_target(n, seed)
+    scale = (D * D / (LAM * z)) * math.sqrt(np.sum(np.abs(u) ** 2))
+    return u, tamp / math.sqrt(np.sum(tamp ** 2)) * scale, init, z
+
+
+def oracle_fraunhofer(n, u, tamp, init, z, iters, patience=1000):
+    cfg = o_fr.FraunhoferConfig(strict=False)
+    fwd = lambda s: o_fr.propagate(o_field.BandField(s, D, D, LAM), z, cfg).samples
+    back = lambda s: o_gs.fraunhofer_adjoint(s, n, n, D, D, LAM, z)
+    tint = tamp * tamp
+    merit = lambda inten: float(np.sum((inten - tint) ** 2) / inten.size)
+    return o_gs.run(u, np.ones((n, n), bool), tamp, -math.pi, math.pi, init, fwd, back, merit,
+                    max_iterations=iters, patience=patience, illum=np.abs(u))
+
+
+def fraunhofer_problem(n, u, tamp, init, z, iters, patience=1000):
+    cfg = ggs.GsConfig(max_iterations=iters, patience=patience)
+    return ggs.GsProblem(torch.from_numpy(u).to("cuda", torch.complex64), (D, D), LAM, z,
+                         torch.from_numpy(tamp).to("cuda", torch.float32),
+                         torch.from_numpy(init).to("cuda", torch.float32), config=cfg,
+                         engine="fraunhofer", fraunhofer=FraunhoferConfig(strict=False))
+
+
+def test_gs_fused_f32_follows_oracle_at_256():
+    """The fused f32 Fraunhofer kernels (square power-of-two grids) against the
+    oracle loop: merit history to 1e-4, same best iteration, best intensity
+    to 1e-4 relative L2."""
+    n = 256
+    u, tamp, init, z = inputs_fraunhofer(n)
+    want = oracle_fraunhofer(n, u, tamp, init, z, 10)
+    got = ggs.run(fraunhofer_problem(n, u, tamp, init, z, 10))
+    assert got.iterations == 10
+    for hg, hw in zip(got.history, want.history):
+        assert hg["merit"] == pytest.approx(hw.merit, rel=1e-4)
+        assert hg["amplitude_mse"] == pytest.approx(hw.amplitude_mse, rel=1e-4)
+    assert got.best_iteration == want.best_iteration
+    bi = got.target_intensity.cpu().numpy()
+    assert np.linalg.norm(bi - want.target_intensity) / np.linalg.norm(want.target_intensity) <= 1e-4
+
+
+def test_gs_fused_matches_generic_path_and_patience(monkeypatch):
+    n = 256
+    u, tamp, init, z = inputs_fraunhofer(n, seed=8)
+    probs = lambda: [fraunhofer_problem(n, u, tamp, init, z, 40, patience=4),
+                     fraunhofer_problem(n, u, tamp * 0.9, init, z, 40, patience=4)]
+    fused = ggs.run_batch(probs())
+    monkeypatch.setenv("OSGPU_GS_GENERIC", "1")
+    generic = ggs.run_batch(probs())
+    for f, g in zip(fused, generic):
+        assert f.iterations == g.iterations
+        assert f.converged == g.converged
+        for hf, hg in zip(f.history, g.history):
+            assert hf["merit"] == pytest.approx(hg["merit"], rel=1e-4)
