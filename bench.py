@@ -8,7 +8,10 @@ gives a 8192 x 8192 padded grid for every band).  One step = the whole
 32-band batch, device resident, through osgpu_beamline_trace_batch_device.
 Metric: propagations (band-planes) per second.
 
-Also reported: adjoint gradients/s of the 2048^2 inverse-design workload
+Also reported: Gerchberg-Saxton target-iterations/s of the 16 x 2048^2
+spot-array batch (GS_WORKLOAD below, with the spot efficiency / uniformity
+of target 0 on the f32 and FP64 engines), adjoint gradients/s of the 2048^2
+inverse-design workload
 (ADJ_WORKLOAD below; f32 batched, with an FP64-plain sample and the f32
 gradient's relative L2 error against the FP64 engine), the same batch on
 the plain FP64 path, end-to-end throughput
@@ -256,6 +259,113 @@ def adjoint_leg(args, stream):
     return out
 
 
+# Gerchberg-Saxton batch: 16 targets at 2048^2, each an N x N array (N uniform
+# in 4-16) of Gaussian spots (sigma 2 samples, amplitudes uniform 0.5-1) on a
+# centred pitch of 3/4 of the frame / N; uniform input amplitude, seeded
+# random initial phase, Fraunhofer far field (z = 0.2 m, dx = 3 um, 532 nm,
+# strict off), 200 iterations with no early stop.  Work unit: one GS
+# iteration of one target.
+GS_TARGETS, GS_ITERS, GS_SEED = 16, 200, 77
+GS_LAM, GS_Z = 532e-9, 0.2
+GS_WORKLOAD = ("16 spot-array targets x 2048^2, Fraunhofer GS (z 0.2 m, 532 nm), 200 iterations, "
+               "uniform input amplitude, seeded random initial phase")
+
+
+def gs_targets(n_targets, rng):
+    """Target amplitudes (unit total power) and spot centres of each target."""
+    yy, xx = np.mgrid[0:N, 0:N]
+    out = []
+    for _ in range(n_targets):
+        k = int(rng.integers(4, 17))
+        pitch = 0.75 * N / k
+        c0 = N / 2 - pitch * (k - 1) / 2
+        cs = [(c0 + pitch * i, c0 + pitch * j) for i in range(k) for j in range(k)]
+        t = np.zeros((N, N))
+        for (cy, cx) in cs:
+            a = rng.uniform(0.5, 1.0)
+            y0, y1 = int(cy) - 8, int(cy) + 9
+            x0, x1 = int(cx) - 8, int(cx) + 9
+            t[y0:y1, x0:x1] += a * np.exp(-((yy[y0:y1, x0:x1] - cy) ** 2
+                                            + (xx[y0:y1, x0:x1] - cx) ** 2) / (2 * 2.0 ** 2))
+        amp = np.sqrt(t)
+        out.append((amp / math.sqrt(np.sum(t)), cs))
+    return out
+
+
+def spot_metrics(inten, centres):
+    """Efficiency = power in 5 x 5 windows at the spot centres / total power;
+    uniformity = 1 - (max - min) / (max + min) of the window powers."""
+    p = []
+    for (cy, cx) in centres:
+        iy, ix = int(round(cy)), int(round(cx))
+        p.append(float(inten[iy - 2:iy + 3, ix - 2:ix + 3].sum()))
+    p = np.array(p)
+    return float(p.sum() / inten.sum()), float(1.0 - (p.max() - p.min()) / (p.max() + p.min()))
+
+
+def gs_leg(args, stream):
+    import torch
+    from optics_studio_gb300 import gs as ggs
+    from optics_studio_gb300.propagation.fraunhofer import FraunhoferConfig
+    rng = np.random.default_rng(GS_SEED)
+    targets = gs_targets(GS_TARGETS, rng)
+    init = rng.uniform(-math.pi, math.pi, (GS_TARGETS, N, N))
+    c = DX * DX / (GS_LAM * GS_Z)
+    scale = c * N * N  # sum |U|^2 = c^2 N^2 sum |u|^2 for a unit input
+    u = torch.ones((N, N), dtype=torch.complex64, device="cuda")
+
+    def problems(dtype, idx, iters):
+        cdt, rdt = (torch.complex64, torch.float32) if dtype == "f32" else (torch.complex128,
+                                                                             torch.float64)
+        cfg = ggs.GsConfig(max_iterations=iters, patience=iters + 1)
+        return [ggs.GsProblem(u.to(cdt), (DX, DX), GS_LAM, GS_Z,
+                              torch.from_numpy(targets[i][0] * scale).to("cuda", rdt),
+                              torch.from_numpy(init[i]).to("cuda", rdt), config=cfg,
+                              engine="fraunhofer", fraunhofer=FraunhoferConfig(strict=False))
+                for i in idx]
+
+    with torch.cuda.stream(stream):
+        ggs.run_batch(problems("f32", range(GS_TARGETS), 3), stream)  # warm-up
+        probs = problems("f32", range(GS_TARGETS), GS_ITERS)
+        torch.cuda.synchronize()
+        import ctypes as C
+        import optics_studio_gb300 as og
+        from optics_studio_gb300 import _ffi as ffi
+        L = og.lib()
+        ffi.check(L.osgpu_profile_begin())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sols = ggs.run_batch(probs, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        stats = (ffi.KernelStatC * 16)()
+        nst = C.c_int32()
+        ffi.check(L.osgpu_profile_end(stats, 16, C.byref(nst)))
+        ms = e0.elapsed_time(e1)
+        its = sum(s.iterations for s in sols)
+        kst = {stats[i].name.decode(): {"launches": int(stats[i].launches),
+                                        "total_ms": stats[i].total_ms, "bytes": stats[i].bytes}
+               for i in range(nst.value)}
+        eff32, uni32 = spot_metrics(sols[0].target_intensity.double().cpu().numpy(),
+                                    targets[0][1])
+        out = {"value": its / (ms / 1e3), "unit": "target-iterations/s", "ms_total": ms,
+               "targets": GS_TARGETS, "iterations_per_target": GS_ITERS,
+               "workload": GS_WORKLOAD, "dtype": "f32", "kernels": kst,
+               "target0": {"efficiency": eff32, "uniformity": uni32}}
+        if not args.no_f64:
+            t0 = time.perf_counter()
+            s64 = ggs.run_batch(problems("f64", [0], GS_ITERS), stream)[0]
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            eff64, uni64 = spot_metrics(s64.target_intensity.cpu().numpy(), targets[0][1])
+            out["f64_plain"] = {"value": s64.iterations / dt, "unit": "target-iterations/s",
+                                "sample": "target 0, complex128, generic GS path",
+                                "efficiency": eff64, "uniformity": uni64}
+            out["speedup_vs_f64"] = out["value"] / out["f64_plain"]["value"]
+    return out
+
+
 def reference_arm(args):
     """--impl reference: the f64 oracle port on all usable host cores, one
     band per worker process per step (spawned processes, no GPU)."""
@@ -311,6 +421,7 @@ def main():
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-gs", action="store_true")
     ap.add_argument("--bands", type=int, default=NBANDS,
                     help="bands per step (profiling runs use a smaller batch)")
     args = ap.parse_args()
@@ -483,6 +594,10 @@ def main():
     # adjoint gradients of the inverse-design workload
     if not args.no_adjoint:
         line["adjoint"] = adjoint_leg(args, stream)
+
+    # Gerchberg-Saxton batch
+    if not args.no_gs:
+        line["gs"] = gs_leg(args, stream)
 
     # accuracy of band 0 against the f64 oracle + bounded CPU baseline
     if rank == 0 and not args.no_cpu_baseline:

@@ -721,7 +721,7 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
              const osgpu_fraunhofer_config& fcfg, double beta_f, double beta_p, int M,
              cudaStream_t st) {
   const size_t n = (size_t)M * M;
-  const int nb = gs_fast_blocks(M);
+  const int nb = gs_fast_blocks(M), nbr = gs_fast_row_blocks(M);
   const int max_it = cfg.max_iterations;
   int rc;
   const void* tw = nullptr;
@@ -730,7 +730,8 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
   // per-item layout in one allocation
   const size_t o_W = 0, o_ph = o_W + al(n * 8), o_il = o_ph + al(n * 4), o_op = o_il + al(n * 4),
                o_ta = o_op + al(n), o_ti = o_ta + al(n * 4), o_tab = o_ti + al(n * 4),
-               o_pc = o_tab + al((size_t)4 * M * 8), o_pr = o_pc + al((size_t)4 * nb * 8),
+               o_am = o_tab + al((size_t)4 * M * 8), o_pc = o_am + al(n * 4),
+               o_pr = o_pc + al((size_t)4 * nb * 8),
                o_hi = o_pr + al((size_t)2 * nb * 8), per = o_hi + al(sizeof(GsRecordDev) * max_it);
   DBuf mem, dstates, ditems, dfolds;
   CK(mem.alloc(per * n_items, st));
@@ -780,8 +781,7 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
     f.W = reinterpret_cast<float2*>(b + o_W);
     f.phase = reinterpret_cast<float*>(b + o_ph);
     f.best = reinterpret_cast<float*>(it.d_phase);
-    f.illum = reinterpret_cast<const float*>(b + o_il);
-    f.open = reinterpret_cast<const unsigned char*>(b + o_op);
+    f.amask = reinterpret_cast<const float*>(b + o_am);
     f.tamp_t = reinterpret_cast<const float*>(b + o_ta);
     f.tint_t = it.d_target_intensity ? reinterpret_cast<const float*>(b + o_ti) : nullptr;
     f.prx = reinterpret_cast<const float2*>(b + o_tab);
@@ -804,6 +804,8 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
                       it.aperture_a, it.aperture_b, it.center_x, it.center_y, M, M, g.dx, g.dy,
                       st));
     CK(launch_abs(it.d_input, 0, b + o_il, 0, 0, n, st));
+    CK(launch_mask_amplitude(b + o_il, reinterpret_cast<const unsigned char*>(b + o_op),
+                             b + o_am, 0, n, st));
     CK(launch_transpose_real(reinterpret_cast<const float*>(it.d_target_amplitude),
                              reinterpret_cast<float*>(b + o_ta), M, st));
     if (it.d_target_intensity)
@@ -825,6 +827,7 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
   a.lo = (float)cfg.lo;
   a.hi = (float)cfg.hi;
   a.wrap = (cfg.hi - cfg.lo >= 2.0 * PI) ? 1 : 0;
+  a.intensity_only = 0;
   const double bytes_cols = (double)n * (2 * 8 + 4) * n_items;
   const double bytes_rows = (double)n * (2 * 8 + 4 + 4 + 4 + 1) * n_items;
   {
@@ -849,7 +852,7 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
       ProfScope ps(c, st, PC_GS_ROWS, bytes_rows);
       CK(launch_gs_rows(DI, n_items, a, 1, st));
     }
-    CK(launch_gs_fold_update_batch(DF, n_items, nb, n, k, cfg.patience, cfg.merit_tolerance,
+    CK(launch_gs_fold_update_batch(DF, n_items, nbr, n, k, cfg.patience, cfg.merit_tolerance,
                                    max_it, st));
   }
   CK(cudaMemcpyAsync(hs.data(), S, sizeof(GsState) * n_items, cudaMemcpyDeviceToHost, st));
@@ -857,28 +860,33 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
   for (int i = 0; i < n_items; ++i)
     CK(cudaMemcpyAsync(hh.data() + (size_t)max_it * i, fo[i].hist, sizeof(GsRecordDev) * max_it,
                        cudaMemcpyDeviceToHost, st));
-  ElementList none;
-  std::memset(&none, 0, sizeof(none));
-  DBuf mask, ubuf;
-  CK(mask.alloc(n * 8, st));
-  CK(ubuf.alloc(n * 8, st));
+  bool want_int = false;
   for (int i = 0; i < n_items; ++i) {
     osgpu_gs_item& it = items[i];
     char* b = base + per * i;
-    if (it.d_best_intensity) {  // the best iteration's forward pass, recomputed
-      osgpu_fraunhofer_report fr;
-      fraunhofer_resolve(it.grid, it.z, fcfg, fr);
-      CK(launch_gs_mask(it.d_phase, 0, b + o_il, reinterpret_cast<unsigned char*>(b + o_op),
-                        mask.p, 0, n, nullptr, st));
-      if ((rc = run_fraun<float>(c, it.grid, it.z, fr, none, mask.p, 0, ubuf.p, 0, nullptr, 0,
-                                 st)))
-        return rc;
-      CK(launch_abs(ubuf.p, 0, it.d_best_intensity, 0, 1, n, st));
-    }
     if (it.d_last_phase)
       CK(cudaMemcpyAsync(it.d_last_phase, b + o_ph, n * 4, cudaMemcpyDeviceToDevice, st));
     if (it.d_illumination)
       CK(cudaMemcpyAsync(it.d_illumination, b + o_il, n * 4, cudaMemcpyDeviceToDevice, st));
+    want_int = want_int || it.d_best_intensity;
+  }
+  if (want_int) {  // the best iteration's forward pass, recomputed by the fused kernels
+    for (int i = 0; i < n_items; ++i) {
+      CK(cudaMemcpyAsync(fi[i].phase, items[i].d_phase, n * 4, cudaMemcpyDeviceToDevice, st));
+      fi[i].out_intensity = reinterpret_cast<float*>(items[i].d_best_intensity);
+    }
+    CK(cudaMemcpyAsync(ditems.p, fi.data(), sizeof(GsFastItem) * n_items,
+                       cudaMemcpyHostToDevice, st));
+    GsFastArgs af = a;
+    af.intensity_only = 1;
+    {
+      ProfScope ps(c, st, PC_GS_ROWS, bytes_rows);
+      CK(launch_gs_rows(DI, n_items, af, 0, st));
+    }
+    {
+      ProfScope ps(c, st, PC_GS_COLS, bytes_cols);
+      CK(launch_gs_cols(DI, n_items, af, st));
+    }
   }
   CK(cudaStreamSynchronize(st));
   for (int i = 0; i < n_items; ++i) {

@@ -30,18 +30,22 @@ using namespace regfft;
 constexpr float kPiF = 3.14159265358979f;
 constexpr float kTauF = 6.28318530717959f;
 
-__device__ __forceinline__ float wrap_pi_f(float v) {
-  float r = fmodf(v + kPiF, kTauF);
+// r mod 2 pi in [0, 2 pi): one conditional step covers the common range
+// (|r| < 4 pi), fmodf the rest.
+__device__ __forceinline__ float rem_tau(float r) {
   if (r < 0.f) r += kTauF;
-  return r - kPiF;
+  else if (r >= kTauF) r -= kTauF;
+  if (r < 0.f || r >= kTauF) {
+    r = fmodf(r, kTauF);
+    if (r < 0.f) r += kTauF;
+  }
+  return r;
 }
 
+__device__ __forceinline__ float wrap_pi_f(float v) { return rem_tau(v + kPiF) - kPiF; }
+
 __device__ __forceinline__ float encode_f(float p, const GsFastArgs& a) {
-  if (a.wrap) {
-    float r = fmodf(p - a.lo, kTauF);
-    if (r < 0.f) r += kTauF;
-    return a.lo + r;
-  }
+  if (a.wrap) return a.lo + rem_tau(p - a.lo);
   return p < a.lo ? a.lo : (p > a.hi ? a.hi : p);
 }
 
@@ -67,16 +71,17 @@ template <int M, int G>
 struct GsLay {
   static constexpr int T = M / 16;
   static constexpr int THREADS = G * T;
+  static constexpr int MINB = THREADS >= 512 ? 1 : 2;  // 128 registers per thread
   static constexpr size_t SMEM =
       ((size_t)TwLay<M>::SIZE + (size_t)G * Plan<M>::SMEM) * sizeof(float2) + 32 * sizeof(double);
 };
 
 template <int M, int G>
-__global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
+__global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     k_gs_cols(const GsFastItem* __restrict__ items, GsFastArgs a) {
   constexpr int T = M / 16;
   const GsFastItem& it = items[blockIdx.y];
-  if (it.state->stop) return;
+  if (a.intensity_only ? !it.out_intensity : it.state->stop) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tws = reinterpret_cast<float2*>(smem_raw);
   float2* bufs = tws + TwLay<M>::SIZE;
@@ -89,12 +94,25 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
   const int kx = blockIdx.x * G + g;
   float2* col = it.W + (size_t)kx * M;
   float2 v[16];
+  float tq[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) v[q] = col[tid + T * q];
+  if (!a.intensity_only) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) tq[q] = __ldg(it.tamp_t + (size_t)kx * M + tid + T * q);
+  }
   __syncthreads();
   fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
-  float e2 = 0.f, m2 = 0.f;
   const float c = it.c, bf = a.beta_f;
+  if (a.intensity_only) {  // |U|^2 = c^2 |F|^2 of the forward pass, row-major
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const float m2q = v[q].x * v[q].x + v[q].y * v[q].y;
+      it.out_intensity[(size_t)(tid + T * q) * M + kx] = c * c * m2q;
+    }
+    return;
+  }
+  float e2 = 0.f, m2 = 0.f;
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int ky = tid + T * q;
@@ -102,7 +120,7 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
     const float2 f = v[q];
     const float m = sqrtf(f.x * f.x + f.y * f.y);
     const float amp = c * m;
-    const float t = __ldg(it.tamp_t + kt);
+    const float t = tq[q];
     const float ti = it.tint_t ? __ldg(it.tint_t + kt) : t * t;
     const float err = amp - t;
     const float inten = amp * amp;
@@ -128,7 +146,7 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
 }
 
 template <int M, int G>
-__global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
+__global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     k_gs_rows(const GsFastItem* __restrict__ items, GsFastArgs a, int iterate) {
   constexpr int T = M / 16;
   const GsFastItem& it = items[blockIdx.y];
@@ -144,11 +162,19 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
   load_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw), threadIdx.x, blockDim.x);
   const int iy = blockIdx.x * G + g;
   const float2 py = __ldg(it.pry + iy);
+  float* __restrict__ prow = it.phase + (size_t)iy * M;
   float2 v[16];
+  float ph[16], am[16];
   float d2 = 0.f;
   if (iterate) {
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = it.W[(size_t)(tid + T * q) * M + iy];
+  }
+  // per-sample inputs issued before the transform (no store precedes them)
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    ph[q] = prow[tid + T * q];
+    am[q] = __ldg(it.amask + (size_t)iy * M + tid + T * q);
   }
   __syncthreads();
   if (iterate) {
@@ -160,24 +186,20 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, 2)
     const int ix = tid + T * q;
     const size_t k = (size_t)iy * M + ix;
     const float2 pre = cmul(__ldg(it.prx + ix), py);
-    float p = it.phase[k];
+    float p = ph[q];
     if (iterate) {
       const float2 w = cmulc(v[q], pre);  // conj(pre) v
       const float dphi = wrap_pi_f(atan2f(w.y, w.x) - p);
       if (keep) it.best[k] = p;
       p = encode_f(p + a.beta_p * dphi, a);
-      it.phase[k] = p;
+      prow[ix] = p;
       d2 = fmaf(dphi, dphi, d2);
       if (it.perr) it.perr[k] = dphi;
     }
-    float2 x = make_float2(0.f, 0.f);
-    if (it.open[k]) {
-      float s, cs;
-      sincosf(p, &s, &cs);
-      const float r = __ldg(it.illum + k);
-      x = cmul(make_float2(r * cs, r * s), pre);
-    }
-    v[q] = x;
+    // open ? illum e^{i p} : 0, with the aperture folded into the amplitude
+    float s, cs;
+    __sincosf(wrap_pi_f(p), &s, &cs);  // argument in [-pi, pi)
+    v[q] = cmul(make_float2(am[q] * cs, am[q] * s), pre);
   }
   fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
 #pragma unroll
@@ -196,7 +218,9 @@ __global__ void k_transpose_real(const float* __restrict__ in, float* __restrict
     out[(size_t)(bx + j) * M + by + threadIdx.x] = tile[threadIdx.x][j];
 }
 
-constexpr int kG = 2;
+constexpr int kG = 2;   // columns per CTA
+constexpr int kGR = 4;  // rows per CTA: 4 adjacent rows share the 32-byte sectors
+                        // of the column-major spectrum they gather and scatter
 
 template <int M>
 cudaError_t launch_cols(const GsFastItem* items, int n_items, const GsFastArgs& a,
@@ -213,12 +237,13 @@ cudaError_t launch_cols(const GsFastItem* items, int n_items, const GsFastArgs& 
 template <int M>
 cudaError_t launch_rows(const GsFastItem* items, int n_items, const GsFastArgs& a, int iterate,
                         cudaStream_t st) {
-  using L = GsLay<M, kG>;
-  cudaError_t e = cudaFuncSetAttribute(k_gs_rows<M, kG>,
+  constexpr int G = (M / 16 * kGR <= 512) ? kGR : 512 / (M / 16);
+  using L = GsLay<M, G>;
+  cudaError_t e = cudaFuncSetAttribute(k_gs_rows<M, G>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM);
   if (e != cudaSuccess) return e;
   ++launch_counter();
-  k_gs_rows<M, kG><<<dim3(M / kG, n_items), L::THREADS, L::SMEM, st>>>(items, a, iterate);
+  k_gs_rows<M, G><<<dim3(M / G, n_items), L::THREADS, L::SMEM, st>>>(items, a, iterate);
   return cudaGetLastError();
 }
 
@@ -227,6 +252,11 @@ cudaError_t launch_rows(const GsFastItem* items, int n_items, const GsFastArgs& 
 bool gs_fast_size(int m) { return m == 256 || m == 512 || m == 1024 || m == 2048 || m == 4096; }
 
 int gs_fast_blocks(int m) { return m / kG; }
+
+int gs_fast_row_blocks(int m) {
+  const int g = (m / 16 * kGR <= 512) ? kGR : 512 / (m / 16);
+  return m / g;
+}
 
 #define OSGPU_GS_DISPATCH(m, fn, ...)          \
   switch (m) {                                 \

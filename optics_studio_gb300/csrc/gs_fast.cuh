@@ -11,8 +11,7 @@ struct GsFastItem {
   float2* W;                  // spectrum scratch, column-major M x M
   float* phase;               // current phase
   float* best;                // best phase (the caller's phase buffer)
-  const float* illum;         // illumination amplitude
-  const unsigned char* open;  // carrier aperture
+  const float* amask;         // illumination amplitude, zero outside the carrier aperture
   const float* tamp_t;        // target amplitude, column-major
   const float* tint_t;        // merit target intensity, column-major (null: T^2)
   const float2* prx;          // pre = prx[ix] pry[iy]
@@ -24,7 +23,8 @@ struct GsFastItem {
   float* perr;                // optional: phase update of the last iteration
   GsState* state;
   double* part_col;           // 2 frames x gs_fast_blocks(M) pairs
-  double* part_row;           // 1 frame x gs_fast_blocks(M) pairs
+  double* part_row;           // 1 frame x gs_fast_row_blocks(M) pairs
+  float* out_intensity;       // intensity_only pass: |U|^2 (row-major)
 };
 
 struct GsFastArgs {
@@ -32,10 +32,12 @@ struct GsFastArgs {
   const void* tw;  // M-point f32 twiddle table
   float beta_f, beta_p, lo, hi;
   int wrap;        // hi - lo >= 2 pi (encode_bounds wraps instead of clamping)
+  int intensity_only;  // column pass: forward transform and |U|^2 only
 };
 
 bool gs_fast_size(int m);
-int gs_fast_blocks(int m);  // CTAs per item of the row and column kernels
+int gs_fast_blocks(int m);      // CTAs per item of the column kernel
+int gs_fast_row_blocks(int m);  // CTAs per item of the row kernel
 cudaError_t launch_gs_cols(const GsFastItem* items, int n_items, const GsFastArgs& a,
                            cudaStream_t st);
 // iterate = 0: first forward rows from the initial phase only

@@ -539,6 +539,14 @@ __global__ void k_abs(const void* u, int c128, void* out, int f64, int square, u
   }
 }
 
+// Illumination amplitude with the carrier aperture folded in (zero outside).
+__global__ void k_mask_amplitude(const void* illum, const unsigned char* open, void* out, int f64,
+                                 uint64_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    st_real(out, f64, k, open[k] ? ld_real(illum, f64, k) : 0.0);
+}
+
 // Initial phase encoded into the bounds, and the carrier aperture mask
 // (gs.rs:429-435, 446-475).
 __global__ void k_gs_init(const void* init, void* phase, int f64, double lo, double hi,
@@ -682,6 +690,13 @@ cudaError_t launch_gs_init(const void* init, void* phase, int f64, double lo, do
   k_gs_init<<<red_blocks((uint64_t)nx * ny), kRedThreads, 0, st>>>(init, phase, f64, lo, hi, open,
                                                                    stop, a, b, cx, cy, nx, ny, dx,
                                                                    dy);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask_amplitude(const void* illum, const unsigned char* open, void* out,
+                                  int f64, uint64_t n, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_mask_amplitude<<<red_blocks(n), kRedThreads, 0, st>>>(illum, open, out, f64, n);
   return cudaGetLastError();
 }
 

@@ -49,6 +49,8 @@ cudaError_t launch_gs_fold_update_batch(const GsFoldItem* items, int n_items, in
 cudaError_t launch_gs_init(const void* init, void* phase, int f64, double lo, double hi,
                            unsigned char* open, int stop, double a, double b, double cx,
                            double cy, int nx, int ny, double dx, double dy, cudaStream_t st);
+cudaError_t launch_mask_amplitude(const void* illum, const unsigned char* open, void* out,
+                                  int f64, uint64_t n, cudaStream_t st);
 cudaError_t launch_abs(const void* u, int c128, void* out, int f64, int square, uint64_t n,
                        cudaStream_t st);
 cudaError_t launch_gs_mask(const void* phase, int f64, const void* illum,
