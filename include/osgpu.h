@@ -295,6 +295,21 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
                                       const osgpu_asm_config* cfg, int32_t dtype, void* stream,
                                       osgpu_asm_report* reports, int32_t reports_stride);
 
+/* A batched trace captured once into a CUDA graph and replayed: creation
+ * runs the batch once on the library stream (so every twiddle table and
+ * kernel attribute exists), then captures it; each launch replays the same
+ * kernels and stream-ordered workspace on `stream` (NULL: the library
+ * stream).  The items' device buffers are baked into the graph and must
+ * stay valid; host-memory phase lattices are not capturable (use
+ * lattice_on_device).  Batched frames of a renderer are the use: the same
+ * wavelengths, designs and buffers every frame. */
+typedef struct osgpu_graph osgpu_graph;
+int osgpu_beamline_trace_batch_graph(const osgpu_trace_item* items, int32_t n_items,
+                                     const osgpu_asm_config* cfg, int32_t dtype,
+                                     osgpu_graph** out);
+int osgpu_graph_launch(osgpu_graph* graph, void* stream);
+int osgpu_graph_destroy(osgpu_graph* graph);
+
 /* ---------------------------------------------------------- inverse loops */
 /* One frame (band x scene) of a render or adjoint batch: the design traced on
  * the frame's source field with the ASM engine (optics-inverse observe.rs:

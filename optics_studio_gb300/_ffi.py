@@ -195,6 +195,11 @@ SIGNATURES = [
     ("osgpu_lattice_create", C.c_int,
      [c_double_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]),
     ("osgpu_lattice_destroy", C.c_int, [C.c_void_p]),
+    ("osgpu_beamline_trace_batch_graph", C.c_int,
+     [C.POINTER(TraceItemC), C.c_int32, C.POINTER(AsmConfigC), C.c_int32,
+      C.POINTER(C.c_void_p)]),
+    ("osgpu_graph_launch", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("osgpu_graph_destroy", C.c_int, [C.c_void_p]),
     ("osgpu_tape_create", C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
     ("osgpu_tape_destroy", C.c_int, [C.c_void_p]),
     ("osgpu_tape_bytes", C.c_uint64, [C.c_void_p]),

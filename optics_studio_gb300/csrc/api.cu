@@ -658,6 +658,12 @@ int count_props(const osgpu_frame& fr) {
 
 }  // namespace
 
+// An instantiated capture of a batched trace (osgpu_beamline_trace_batch_graph).
+struct osgpu_graph {
+  cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;
+};
+
 // Forward planes recorded by osgpu_render_batch_device: for every frame,
 // the output field of each propagation, in one device allocation that is
 // kept and grown across calls.
@@ -1423,6 +1429,76 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
                         *cfg, f32, st)))
       return rc;
   }
+  return OSGPU_OK;
+}
+
+// ------------------------------------------------------------ graphs
+
+int osgpu_beamline_trace_batch_graph(const osgpu_trace_item* items, int32_t n_items,
+                                     const osgpu_asm_config* cfg, int32_t dtype,
+                                     osgpu_graph** out) {
+  if (!out) return OSGPU_E_BAD_ARGUMENT;
+  *out = nullptr;
+  for (int i = 0; i < n_items && items; ++i)
+    for (int s = 0; s < items[i].n_steps; ++s)
+      for (int q = 0; q < items[i].steps[s].n_elements; ++q) {
+        const osgpu_element& e = items[i].steps[s].elements[q];
+        if (e.kind == OSGPU_EL_PHASE_MASK_SAMPLED && !e.lattice_on_device) {
+          set_err("item %d: a host-memory lattice cannot be captured", i);
+          return OSGPU_E_BAD_ARGUMENT;
+        }
+      }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  // warm-up run: twiddle tables and kernel attributes are created outside capture
+  if ((rc = osgpu_beamline_trace_batch_device(items, n_items, cfg, dtype, c.stream, nullptr, 0)))
+    return rc;
+  CK(cudaStreamSynchronize(c.stream));
+  cudaStream_t cs = nullptr;
+  CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  const bool prof = c.profiling;
+  c.profiling = false;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess)
+    rc = osgpu_beamline_trace_batch_device(items, n_items, cfg, dtype, cs, nullptr, 0);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+  c.profiling = prof;
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  osgpu_graph* g = new osgpu_graph();
+  g->exec = exec;
+  g->kernels = 0;
+  *out = g;
+  return OSGPU_OK;
+}
+
+int osgpu_graph_launch(osgpu_graph* graph, void* stream) {
+  if (!graph || !graph->exec) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  CK(cudaGraphLaunch(graph->exec, st));
+  return OSGPU_OK;
+}
+
+int osgpu_graph_destroy(osgpu_graph* graph) {
+  if (!graph) return OSGPU_OK;
+  if (graph->exec) cudaGraphExecDestroy(graph->exec);
+  delete graph;
   return OSGPU_OK;
 }
 

@@ -89,3 +89,63 @@ def test_profile_reports_kernel_classes():
     assert {"pass_a_rows", "pass_b_columns", "pass_c_rows"} <= names
     for i in range(k.value):
         assert stats[i].total_ms >= 0 and stats[i].launches >= 1
+
+
+def ragged_items(rng, sides, n_items):
+    """Gaussian-source ASM items of the ragged batch form: side from `sides`,
+    z log-uniform 1-50 mm, waist 50-500 um (scaled to the grid), dx 3 um,
+    lam 450-650 nm."""
+    out = []
+    for _ in range(n_items):
+        n = int(rng.choice(sides))
+        z = float(np.exp(rng.uniform(np.log(1e-3), np.log(50e-3))))
+        lam = float(rng.uniform(450e-9, 650e-9))
+        w0 = float(rng.uniform(50e-6, 500e-6)) * n / 2048
+        out.append((n, 3e-6, lam, z, max(w0, 6e-6)))
+    return out
+
+
+@pytest.mark.parametrize("dtype,tol", [(ffi.C64, 1e-5), (ffi.C128, 1e-12)])
+def test_ragged_batch_graph_replays_the_batch(dtype, tol):
+    """osgpu_beamline_trace_batch_graph: a captured ragged batch replays
+    bit-identically to the direct batched call and matches the oracle."""
+    L = og.lib()
+    tdt = torch.complex64 if dtype == ffi.C64 else torch.complex128
+    rng = np.random.default_rng(11)
+    spec = ragged_items(rng, [64, 96, 128, 256], 12)
+    arr = (ffi.TraceItemC * len(spec))()
+    keep, ins, outs, refs = [], [], [], []
+    for i, (n, dx, lam, z, w0) in enumerate(spec):
+        b = ofield.gaussian(w0, 1.0, (0.0, 0.0), 0.0, lam, n, n, dx, dx)
+        if i < 4:
+            refs.append(oasm.propagate(b, z, oasm.AsmConfig()).samples)
+        tin = torch.from_numpy(b.samples).to("cuda", tdt)
+        tout = torch.zeros_like(tin)
+        steps = (ffi.StepC * 1)(ffi.StepC(None, 0, z, 1.0))
+        keep += [tin, steps]
+        ins.append(tin)
+        outs.append(tout)
+        arr[i] = ffi.TraceItemC(tin.data_ptr(), tout.data_ptr(), ffi.Grid(n, n, dx, dx, lam),
+                                steps, 1)
+    cfg = ffi.AsmConfigC(2, 1, 1, 8, 1)
+    ffi.check(L.osgpu_beamline_trace_batch_device(arr, len(spec), cfg, dtype, None, None, 0))
+    torch.cuda.synchronize()
+    direct = [o.clone() for o in outs]
+    for o in outs:
+        o.zero_()
+    g = C.c_void_p()
+    ffi.check(L.osgpu_beamline_trace_batch_graph(arr, len(spec), cfg, dtype, C.byref(g)))
+    for o in outs:
+        o.zero_()
+    torch.cuda.synchronize()
+    launches0 = L.osgpu_launch_count()
+    for _ in range(2):
+        ffi.check(L.osgpu_graph_launch(g, None))
+    torch.cuda.synchronize()
+    assert L.osgpu_launch_count() == launches0  # replays launch no host-side kernels
+    ffi.check(L.osgpu_sync_status())
+    for d, o in zip(direct, outs):
+        assert torch.equal(d, o)
+    for i, ref in enumerate(refs):
+        assert rel_l2(outs[i].cpu().numpy().astype(np.complex128), ref) <= tol
+    ffi.check(L.osgpu_graph_destroy(g))
