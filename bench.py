@@ -8,7 +8,8 @@ gives a 8192 x 8192 padded grid for every band).  One step = the whole
 32-band batch, device resident, through osgpu_beamline_trace_batch_device.
 Metric: propagations (band-planes) per second.
 
-Also reported: Gerchberg-Saxton target-iterations/s of the 16 x 2048^2
+Also reported: the ragged 64-item ASM batch replayed from one captured CUDA
+graph (sides 256-2048, z 1 mm - 1 m), Gerchberg-Saxton target-iterations/s of the 16 x 2048^2
 spot-array batch (GS_WORKLOAD below, with the spot efficiency / uniformity
 of target 0 on the f32 and FP64 engines), adjoint gradients/s of the 2048^2
 inverse-design workload
@@ -259,6 +260,74 @@ def adjoint_leg(args, stream):
     return out
 
 
+# Ragged batch: 64 independent ASM propagations, side uniform in {256, 512,
+# 1024, 2048}, z log-uniform 1 mm - 1 m, Gaussian waist uniform 50-500 um,
+# dx 3 um, lam uniform 450-650 nm, default AsmConfig (strict densification),
+# complex64, replayed from one captured CUDA graph.
+RAGGED_ITEMS, RAGGED_SEED = 64, 4242
+
+
+def ragged_leg(args, stream):
+    import ctypes as C
+    import torch
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import _ffi as ffi
+    L = og.lib()
+    rng = np.random.default_rng(RAGGED_SEED)
+    arr = (ffi.TraceItemC * RAGGED_ITEMS)()
+    keep, samples, pads = [], 0, []
+    cfg = ffi.AsmConfigC(2.0, 1, 1, 8.0, 1.0)
+    for i in range(RAGGED_ITEMS):
+        n = int(rng.choice([256, 512, 1024, 2048]))
+        z = float(np.exp(rng.uniform(np.log(1e-3), np.log(1.0))))
+        w0 = float(rng.uniform(50e-6, 500e-6))
+        lam = float(rng.uniform(450e-9, 650e-9))
+        x = (np.arange(n) - (n - 1) / 2.0) * DX
+        u = np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / (w0 * w0)).astype(np.complex64)
+        tin = torch.from_numpy(u).cuda()
+        tout = torch.empty_like(tin)
+        steps = (ffi.StepC * 1)(ffi.StepC(None, 0, z, 1.0))
+        keep += [tin, tout, steps]
+        arr[i] = ffi.TraceItemC(tin.data_ptr(), tout.data_ptr(), ffi.Grid(n, n, DX, DX, lam),
+                                steps, 1)
+        rep = ffi.AsmReportC()
+        ffi.check(L.osgpu_asm_sampling_report(C.byref(ffi.Grid(n, n, DX, DX, lam)), z,
+                                              C.byref(cfg), C.byref(rep)))
+        pads.append(int(rep.nx_pad))
+        samples += n * n
+    sptr = C.c_void_p(stream.cuda_stream)
+    g = C.c_void_p()
+    ffi.check(L.osgpu_beamline_trace_batch_graph(arr, RAGGED_ITEMS, cfg, ffi.C64, C.byref(g)))
+    reps = max(3, args.steps // 3)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_graph = timed(lambda: ffi.check(L.osgpu_graph_launch(g, sptr)))
+    ms_direct = timed(lambda: ffi.check(L.osgpu_beamline_trace_batch_device(
+        arr, RAGGED_ITEMS, cfg, ffi.C64, sptr, None, 0)))
+    ffi.check(L.osgpu_graph_destroy(g))
+    ffi.check(L.osgpu_sync_status())
+    sides = {}
+    for i in range(RAGGED_ITEMS):
+        sides[int(arr[i].grid.nx)] = sides.get(int(arr[i].grid.nx), 0) + 1
+    return {"value": RAGGED_ITEMS / (ms_graph / 1e3), "unit": "propagations/s",
+            "ms_per_batch_graph": ms_graph, "ms_per_batch_direct": ms_direct,
+            "items": RAGGED_ITEMS, "sides": sides, "padded_sides": sorted(set(pads)),
+            "workload": "64 ASM items, side {256..2048}, z log-uniform 1 mm-1 m, Gaussian waist "
+                        "50-500 um, dx 3 um, 450-650 nm, complex64, one captured CUDA graph"}
+
+
 # Gerchberg-Saxton batch: 16 targets at 2048^2, each an N x N array (N uniform
 # in 4-16) of Gaussian spots (sigma 2 samples, amplitudes uniform 0.5-1) on a
 # centred pitch of 3/4 of the frame / N; uniform input amplitude, seeded
@@ -422,6 +491,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-gs", action="store_true")
+    ap.add_argument("--no-ragged", action="store_true")
     ap.add_argument("--bands", type=int, default=NBANDS,
                     help="bands per step (profiling runs use a smaller batch)")
     args = ap.parse_args()
@@ -569,14 +639,15 @@ def main():
         host_out = torch.empty((NBANDS, N, N), dtype=torch.complex128).pin_memory()
         cfg = ffi.AsmConfigC(2.0, 1, 1, 8.0, 1.0)
 
+        hitems = (ffi.HostTraceItemC * NBANDS)()
+        for b in range(NBANDS):
+            hitems[b] = ffi.HostTraceItemC(
+                C.cast(C.c_void_p(host_in[b].data_ptr()), ffi.c_double_p),
+                C.cast(C.c_void_p(host_out[b].data_ptr()), ffi.c_double_p), items[b].grid,
+                items[b].steps, 3)
+
         def e2e_step():
-            for b in range(NBANDS):
-                it = items[b]
-                code = L.osgpu_beamline_trace(
-                    C.cast(C.c_void_p(host_in[b].data_ptr()), ffi.c_double_p),
-                    C.cast(C.c_void_p(host_out[b].data_ptr()), ffi.c_double_p),
-                    C.byref(it.grid), it.steps, 3, cfg, ffi.F32, None)
-                ffi.check(code)
+            ffi.check(L.osgpu_beamline_trace_batch(hitems, NBANDS, cfg, ffi.F32, None, 0))
 
         e2e_step()
         barrier()
@@ -589,11 +660,16 @@ def main():
         line["e2e"] = {"value": NBANDS * world / dt, "unit": "propagations/s",
                        "h2d_bytes_per_step": NBANDS * N * N * 16,
                        "d2h_bytes_per_step": NBANDS * N * N * 16,
-                       "api": "osgpu_beamline_trace (host complex128, pinned), f32 engine"}
+                       "api": "osgpu_beamline_trace_batch (host complex128, pinned; copies "
+                              "pipelined against the traces), f32 engine"}
 
     # adjoint gradients of the inverse-design workload
     if not args.no_adjoint:
         line["adjoint"] = adjoint_leg(args, stream)
+
+    # ragged batch from a captured graph
+    if not args.no_ragged:
+        line["ragged"] = ragged_leg(args, stream)
 
     # Gerchberg-Saxton batch
     if not args.no_gs:

@@ -295,6 +295,25 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
                                       const osgpu_asm_config* cfg, int32_t dtype, void* stream,
                                       osgpu_asm_report* reports, int32_t reports_stride);
 
+/* Beamline::trace of many bands from HOST buffers (complex128, the Rust
+ * layout), e.g. every band of Renderer::render_frame (observe.rs:195-210):
+ * the host->device copy of band i+1 and the device->host copy of band i-1
+ * run on their own streams while band i is traced (two device slots each
+ * way).  Page-locked host buffers overlap fully; pageable ones are copied
+ * by the driver.  Synchronous: outputs are on the host when it returns; a
+ * non-finite input sample anywhere returns OSGPU_E_NON_FINITE_SAMPLE. */
+typedef struct {
+  const double* in;
+  double* out;
+  osgpu_grid grid;
+  const osgpu_step* steps;
+  int32_t n_steps;
+} osgpu_host_trace_item;
+
+int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_items,
+                               const osgpu_asm_config* cfg, int32_t precision,
+                               osgpu_asm_report* reports, int32_t reports_stride);
+
 /* A batched trace captured once into a CUDA graph and replayed: creation
  * runs the batch once on the library stream (so every twiddle table and
  * kernel attribute exists), then captures it; each launch replays the same

@@ -146,6 +146,11 @@ class GsItemC(C.Structure):
                 ("result", GsResultC)]
 
 
+class HostTraceItemC(C.Structure):
+    _fields_ = [("in_", c_double_p), ("out", c_double_p), ("grid", Grid),
+                ("steps", C.POINTER(StepC)), ("n_steps", C.c_int32)]
+
+
 class KernelStatC(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double),
                 ("bytes", C.c_double)]
@@ -195,6 +200,9 @@ SIGNATURES = [
     ("osgpu_lattice_create", C.c_int,
      [c_double_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]),
     ("osgpu_lattice_destroy", C.c_int, [C.c_void_p]),
+    ("osgpu_beamline_trace_batch", C.c_int,
+     [C.POINTER(HostTraceItemC), C.c_int32, C.POINTER(AsmConfigC), C.c_int32,
+      C.POINTER(AsmReportC), C.c_int32]),
     ("osgpu_beamline_trace_batch_graph", C.c_int,
      [C.POINTER(TraceItemC), C.c_int32, C.POINTER(AsmConfigC), C.c_int32,
       C.POINTER(C.c_void_p)]),

@@ -9,6 +9,7 @@
 // host scan the input itself.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstdarg>
@@ -58,6 +59,7 @@ struct Context {
   std::recursive_mutex mu;
   int device = -1;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;  // host-buffer batch pipeline
   int* d_status = nullptr;
   std::map<std::pair<int, int>, void*> tw;  // (n, is_double) -> twiddle table
   bool profiling = false;
@@ -1396,6 +1398,104 @@ int osgpu_beamline_trace(const double* in, double* out, const osgpu_grid* g,
   return host_call(c, in, out, n, [&](const void* din, void* dout) {
     return run_trace(c, din, 1, dout, 1, *g, steps, n_steps, E, R, *cfg, f32, c.stream);
   });
+}
+
+int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_items,
+                               const osgpu_asm_config* cfg, int32_t precision,
+                               osgpu_asm_report* reports, int32_t reports_stride) {
+  int rc;
+  if ((rc = check_precision(precision))) return rc;
+  if (!cfg || n_items < 0 || (n_items > 0 && !items)) return OSGPU_E_BAD_ARGUMENT;
+  size_t max_n = 0;
+  for (int i = 0; i < n_items; ++i) {
+    const osgpu_host_trace_item& it = items[i];
+    if (!it.in || !it.out || it.n_steps < 0 || (it.n_steps > 0 && !it.steps))
+      return OSGPU_E_BAD_ARGUMENT;
+    if (it.grid.nx == 0 || it.grid.ny == 0) return OSGPU_E_EMPTY_GRID;
+    max_n = std::max(max_n, (size_t)(it.grid.nx * it.grid.ny));
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  if (!c.copy_in) {
+    CK(cudaStreamCreateWithFlags(&c.copy_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c.copy_out, cudaStreamNonBlocking));
+  }
+  const int f32 = precision == OSGPU_F32;
+  const cudaStream_t cs = c.stream, si = c.copy_in, so = c.copy_out;
+  // two device slots each way; the copy streams run ahead of the compute stream
+  DBuf din[2], dout[2];
+  for (int k = 0; k < 2; ++k) {
+    CK(din[k].alloc(max_n * 16, cs));
+    CK(dout[k].alloc(max_n * 16, cs));
+  }
+  CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), cs));
+  CK(cudaStreamSynchronize(cs));  // slots allocated before the copy streams use them
+  cudaEvent_t ev_in[2], ev_comp[2], ev_out[2];
+  for (int k = 0; k < 2; ++k) {
+    CK(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_comp[k], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_out[k], cudaEventDisableTiming));
+  }
+  auto release = [&]() {
+    cudaStreamSynchronize(si);
+    cudaStreamSynchronize(cs);
+    cudaStreamSynchronize(so);
+    for (int k = 0; k < 2; ++k) {
+      cudaEventDestroy(ev_in[k]);
+      cudaEventDestroy(ev_comp[k]);
+      cudaEventDestroy(ev_out[k]);
+    }
+  };
+  for (int i = 0; i < n_items; ++i) {
+    const osgpu_host_trace_item& it = items[i];
+    const int k = i & 1;
+    const size_t bytes = (size_t)(it.grid.nx * it.grid.ny) * 16;
+    std::vector<Elements> E;
+    std::vector<osgpu_asm_report> R;
+    rc = prepare_trace(c, it.in, bytes / 16, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, cs);
+    if (reports && reports_stride > 0)
+      for (int s = 0; s < it.n_steps && s < reports_stride && s < (int)R.size(); ++s)
+        reports[(size_t)i * reports_stride + s] = R[s];
+    if (rc) {
+      set_err("item %d: %s", i, t_err);
+      release();
+      return rc;
+    }
+    cudaError_t e = cudaSuccess;
+    if (i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
+    if (e == cudaSuccess) e = cudaMemcpyAsync(din[k].p, it.in, bytes, cudaMemcpyHostToDevice, si);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], si);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_in[k], 0);
+    if (e == cudaSuccess && i >= 2) e = cudaStreamWaitEvent(cs, ev_out[k], 0);  // out slot drained
+    if (e != cudaSuccess) {
+      release();
+      return cuda_fail(e, "batch copy in");
+    }
+    if ((rc = run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, E, R, *cfg,
+                        f32, cs))) {
+      release();
+      return rc;
+    }
+    e = cudaEventRecord(ev_comp[k], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(so, ev_comp[k], 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(it.out, dout[k].p, bytes, cudaMemcpyDeviceToHost, so);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], so);
+    if (e != cudaSuccess) {
+      release();
+      return cuda_fail(e, "batch copy out");
+    }
+  }
+  int status = 0;
+  cudaError_t e = cudaStreamSynchronize(so);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, cs);
+  release();
+  if (e != cudaSuccess) return cuda_fail(e, "batch sync");
+  if (status & 1) {
+    set_err("a field of the batch contains non-finite samples");
+    return OSGPU_E_NON_FINITE_SAMPLE;
+  }
+  return OSGPU_OK;
 }
 
 int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_items,

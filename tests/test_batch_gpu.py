@@ -149,3 +149,48 @@ def test_ragged_batch_graph_replays_the_batch(dtype, tol):
     for i, ref in enumerate(refs):
         assert rel_l2(outs[i].cpu().numpy().astype(np.complex128), ref) <= tol
     ffi.check(L.osgpu_graph_destroy(g))
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_batch_pipeline_equals_single_calls(pinned):
+    """osgpu_beamline_trace_batch (host complex128 buffers, copies pipelined
+    against the traces) returns exactly what one osgpu_beamline_trace call
+    per band returns."""
+    L = og.lib()
+    rng = np.random.default_rng(5)
+    spec = [(64, 4e-6, 480e-9, 2e-3), (128, 3e-6, 520e-9, 5e-3), (96, 3e-6, 600e-9, -3e-3),
+            (128, 3e-6, 640e-9, 8e-3), (64, 4e-6, 455e-9, 1e-3)]
+    items = (ffi.HostTraceItemC * len(spec))()
+    keep, outs, want = [], [], []
+    for i, (n, dx, lam, z) in enumerate(spec):
+        u = (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))).astype(np.complex128)
+        if pinned:
+            hin = torch.from_numpy(u).pin_memory()
+            hout = torch.zeros((n, n), dtype=torch.complex128).pin_memory()
+            pin, pout = hin.data_ptr(), hout.data_ptr()
+        else:
+            hin, hout = u, np.zeros((n, n), dtype=np.complex128)
+            pin, pout = hin.ctypes.data, hout.ctypes.data
+        lens = (ffi.ElementC * 1)(ffi.ElementC(3, 1, 100e-6, 100e-6, 0, 0, 0, 0.04, 0, 0, None,
+                                               0, 0, 0, 0, 0))
+        steps = (ffi.StepC * 2)(ffi.StepC(lens, 1, z, 1.0), ffi.StepC(None, 0, z / 2, 1.0))
+        keep += [hin, hout, lens, steps, u]
+        outs.append(hout)
+        items[i] = ffi.HostTraceItemC(C.cast(C.c_void_p(pin), ffi.c_double_p),
+                                      C.cast(C.c_void_p(pout), ffi.c_double_p),
+                                      ffi.Grid(n, n, dx, dx, lam), steps, 2)
+        ref = np.empty_like(u)
+        ffi.check(L.osgpu_beamline_trace(u.ctypes.data_as(ffi.c_double_p),
+                                         ref.ctypes.data_as(ffi.c_double_p),
+                                         C.byref(ffi.Grid(n, n, dx, dx, lam)), steps, 2,
+                                         C.byref(ffi.AsmConfigC(2, 1, 1, 8, 1)), ffi.F32, None))
+        want.append(ref)
+    ffi.check(L.osgpu_beamline_trace_batch(items, len(spec), ffi.AsmConfigC(2, 1, 1, 8, 1),
+                                           ffi.F32, None, 0))
+    for o, w in zip(outs, want):
+        got = o.numpy() if pinned else o
+        assert np.array_equal(got, w)
+    bad = np.full((64, 64), np.nan, dtype=np.complex128)
+    items[0].in_ = bad.ctypes.data_as(ffi.c_double_p)
+    code = L.osgpu_beamline_trace_batch(items, 1, ffi.AsmConfigC(2, 1, 1, 8, 1), ffi.F32, None, 0)
+    assert ffi.STATUS_NAMES[code] == "NonFiniteSample"
