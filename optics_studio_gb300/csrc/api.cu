@@ -166,8 +166,10 @@ int get_tw(Context& c, int n, int is_d, const void** out) {
     return OSGPU_OK;
   }
   void* p = nullptr;
-  CK(cudaMalloc(&p, (size_t)(n > 0 ? n : 1) * (is_d ? 16 : 8)));
+  const bool staged = !is_d && reg_fft_size(n);  // + stage-ordered copy behind it
+  CK(cudaMalloc(&p, (size_t)(n > 0 ? n : 1) * (is_d ? 16 : 8) * (staged ? 2 : 1)));
   CK(launch_twiddles(p, n, is_d, c.stream));
+  if (staged) CK(launch_stage_twiddles(p, n, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   c.tw[key] = p;
   *out = p;

@@ -125,8 +125,9 @@ static __device__ void apply_elements_exact(const ElementList& L, int ix, int iy
 // is outside the element's transmitting set (the result is then zero).
 static __device__ __forceinline__ bool apply_one_fast(const DevElement& e, int ix, int iy,
                                                       float2& v) {
+  // the tables are read-only for the kernel's lifetime: non-coherent loads
   if (e.span) {
-    const int2 sp = e.span[iy];
+    const int2 sp = __ldg(e.span + iy);
     if (ix < sp.x || ix > sp.y) {
       v = make_float2(0.f, 0.f);
       return false;
@@ -134,24 +135,25 @@ static __device__ __forceinline__ bool apply_one_fast(const DevElement& e, int i
   }
   switch (e.kind) {
     case EL_LENS: {
-      const float2 a = e.tabx[ix], b = e.taby[iy];
+      const float2 a = __ldg(e.tabx + ix), b = __ldg(e.taby + iy);
       const float2 t = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
       v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
       break;
     }
     case EL_GRATING: {
-      const float2 t = e.tabx[ix];
+      const float2 t = __ldg(e.tabx + ix);
       v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
       break;
     }
     case EL_PHASE: {
-      const int4 bx = e.bilx[ix], by = e.bily[iy];
+      const int4 bx = __ldg(e.bilx + ix), by = __ldg(e.bily + iy);
       float phi = 0.f;
       if (bx.w && by.w) {
         const float tx = __int_as_float(bx.z), ty = __int_as_float(by.z);
         const float* r0 = e.latf + (size_t)by.x * e.lnx;
         const float* r1 = e.latf + (size_t)by.y * e.lnx;
-        const float v00 = r0[bx.x], v10 = r0[bx.y], v01 = r1[bx.x], v11 = r1[bx.y];
+        const float v00 = __ldg(r0 + bx.x), v10 = __ldg(r0 + bx.y), v01 = __ldg(r1 + bx.x),
+                    v11 = __ldg(r1 + bx.y);
         const float A = v00 + (v10 - v00) * tx;
         const float B = v01 + (v11 - v01) * tx;
         phi = A + (B - A) * ty;

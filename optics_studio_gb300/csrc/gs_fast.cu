@@ -90,7 +90,10 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
   const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
   const int BAR_N = (T % 32 == 0) ? T : GsLay<M, G>::THREADS;
   float2* buf = bufs + g * Plan<M>::SMEM;
-  load_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw), threadIdx.x, blockDim.x);
+  {  // stage-ordered table stored behind the M-point table
+    const float2* twm = reinterpret_cast<const float2*>(a.tw);
+    for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
+  }
   const int kx = blockIdx.x * G + g;
   float2* col = it.W + (size_t)kx * M;
   float2 v[16];
@@ -159,7 +162,10 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
   const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
   const int BAR_N = (T % 32 == 0) ? T : GsLay<M, G>::THREADS;
   float2* buf = bufs + g * Plan<M>::SMEM;
-  load_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw), threadIdx.x, blockDim.x);
+  {  // stage-ordered table stored behind the M-point table
+    const float2* twm = reinterpret_cast<const float2*>(a.tw);
+    for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
+  }
   const int iy = blockIdx.x * G + g;
   const float2 py = __ldg(it.pry + iy);
   float* __restrict__ prow = it.phase + (size_t)iy * M;

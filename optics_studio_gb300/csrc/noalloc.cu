@@ -109,8 +109,9 @@ extern "C" int osgpu_asm_propagate_noalloc(const void* d_in, void* d_out, const 
     off += al(bytes);
     return o;
   };
-  const size_t o_twmx = carve((size_t)a.ax.m * 8), o_twPx = carve(Px * 8);
-  const size_t o_twmy = carve((size_t)a.ay.m * 8), o_twPy = carve(Py * 8);
+  // m-point tables carry their stage-ordered copy behind them (2 m entries)
+  const size_t o_twmx = carve((size_t)a.ax.m * 16), o_twPx = carve(Px * 8);
+  const size_t o_twmy = carve((size_t)a.ay.m * 16), o_twPy = carve(Py * 8);
   const size_t o_work = carve(Px * (size_t)ny * 8);
   const size_t o_fxv = carve(Px * 8), o_fyv = carve(Py * 8);
   const size_t o_Ex = carve(Px * 8), o_Ey = carve(Py * 8);
@@ -133,7 +134,9 @@ extern "C" int osgpu_asm_propagate_noalloc(const void* d_in, void* d_out, const 
   if ((e = launch_twiddles(base + o_twmx, a.ax.m, 0, st)) != cudaSuccess ||
       (e = launch_twiddles(base + o_twPx, (int)Px, 0, st)) != cudaSuccess ||
       (e = launch_twiddles(base + o_twmy, a.ay.m, 0, st)) != cudaSuccess ||
-      (e = launch_twiddles(base + o_twPy, (int)Py, 0, st)) != cudaSuccess) {
+      (e = launch_twiddles(base + o_twPy, (int)Py, 0, st)) != cudaSuccess ||
+      (reg_fft_size(a.ax.m) && (e = launch_stage_twiddles(base + o_twmx, a.ax.m, st)) != cudaSuccess) ||
+      (reg_fft_size(a.ay.m) && (e = launch_stage_twiddles(base + o_twmy, a.ay.m, st)) != cudaSuccess)) {
     return OSGPU_E_CUDA;
   }
   a.in = d_in;

@@ -5,9 +5,9 @@
 //   pass B: column kx: for t < r: c W_P^{t j} -> FFT_m -> x H -> IFFT_m
 //           -> x W_P^{-t j}, summed; rewritten in place
 //   pass C: rows   sum_s W_P^{-s j} IFFT_m(W[(r q + s) ny + iy])
-// Pass B runs one CTA per column pair (kx, Px - kx): the transfer functions
-// of the engines it serves are even in fx and fy, so one shared table of
-// H(kx, |k_y|) for |k_y| <= Py/2 serves all 4 quadrant bins of both columns.
+// Pass B runs one CTA per spectral column kx: the transfer functions of the
+// engines it serves are even in fy, so one shared-memory table of
+// H(kx, |k_y|) for |k_y| <= Py/2 serves both halves of the column.
 #include <cstdlib>
 
 #include "fft_reg.cuh"
@@ -73,6 +73,20 @@ struct Lay {
   static constexpr int MINB = THREADS >= 512 ? 1 : 512 / THREADS;
 };
 
+// The f32 twiddle tables of register-FFT lengths carry the stage-ordered
+// copy (TwLay<M>) right behind the M-point table (launch_stage_twiddles).
+template <int M>
+__device__ __forceinline__ void copy_stage_twiddles(float2* tws, const float2* __restrict__ twm,
+                                                    int t0, int nt) {
+  for (int i = t0; i < TwLay<M>::SIZE; i += nt) tws[i] = __ldg(twm + M + i);
+}
+
+template <int M>
+__global__ void k_stage_twiddles(float2* tw) {
+  load_stage_twiddles<M>(tw + M, tw, blockIdx.x * blockDim.x + threadIdx.x,
+                         gridDim.x * blockDim.x);
+}
+
 __device__ __forceinline__ void load_ptw(float2* tb, float2* tq, const float2* __restrict__ twP, int r,
                                          int T) {
   for (int i = threadIdx.x; i < r * T; i += blockDim.x) {
@@ -108,6 +122,54 @@ __device__ __forceinline__ float2 h_asm_split_row(const PropArgs& a, float2 exc,
   return make_float2(hr * cs - hi * sn, hr * sn + hi * cs);
 }
 
+// H(kx, |k_y|) for |k_y| <= Py/2 of an even transfer function (ASM split
+// phase or Fresnel TF) into the shared table htab[rr * U + u], |k_y| = ry u + rr
+// (row rr = residue class of |k_y| mod ry, so the pass-B reads are unit
+// stride), by threads t0, t0 + nt, ...
+template <int M>
+__device__ __forceinline__ void build_htab(const PropArgs& a, int kx, float2* htab, int t0,
+                                           int nt) {
+  constexpr int U = M / 2 + 1;
+  const int Py = a.ay.P, ry = a.ay.r;
+  const bool asm_split = (a.engine == ENG_ASM);
+  const float2 exc = a.Ex[kx];
+  float cah = 0.f, cal = 0.f, sac = 0.f;
+  int kmc = -1;
+  if (asm_split) {
+    cah = a.ca_hi[kx];
+    cal = a.ca_lo[kx];
+    sac = a.sa[kx];
+    kmc = a.kmax[kx];
+  }
+  const int hh = Py / 2;
+  const float4* rt = reinterpret_cast<const float4*>(a.rowtab);
+  constexpr int UNR = 4;
+  for (int base = t0; base < ry * U; base += UNR * nt) {
+    float4 rv[UNR];
+    int ak[UNR];
+#pragma unroll
+    for (int k = 0; k < UNR; ++k) {  // issue the loads first
+      const int idx = base + k * nt;
+      const int rr = idx / U, u = idx - rr * U;
+      ak[k] = ry * u + rr;
+      rv[k] = (idx < ry * U && ak[k] <= hh) ? __ldg(rt + ak[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int k = 0; k < UNR; ++k) {
+      const int idx = base + k * nt;
+      if (idx >= ry * U || ak[k] > hh) continue;
+      const float2 ey = make_float2(rv[k].x, rv[k].y);
+      float2 h;
+      if (asm_split) {
+        h = h_asm_split_row(a, exc, cah, cal, sac, kmc, ak[k], ey, rv[k].z, rv[k].w);
+      } else {
+        h = make_float2(exc.x * ey.x - exc.y * ey.y, exc.x * ey.y + exc.y * ey.x);
+      }
+      htab[idx] = h;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- pass B
 
 template <int M, int G>
@@ -141,48 +203,9 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
     const int i = threadIdx.x + k * NT;
     col[i] = (i < ny) ? W[i] : make_float2(0.f, 0.f);
   }
-  load_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
+  copy_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, ry, T);
-  if (use_table) {
-    // H(kx, |k_y|) for |k_y| <= Py/2 (H even in fy), row rr = |k_y| mod ry
-    const bool asm_split = (a.engine == ENG_ASM);
-    const float2 exc = a.Ex[kx];
-    float cah = 0.f, cal = 0.f, sac = 0.f;
-    int kmc = -1;
-    if (asm_split) {
-      cah = a.ca_hi[kx];
-      cal = a.ca_lo[kx];
-      sac = a.sa[kx];
-      kmc = a.kmax[kx];
-    }
-    const int hh = Py / 2;
-    const float4* rt = reinterpret_cast<const float4*>(a.rowtab);
-    constexpr int UNR = 4;
-    for (int base = threadIdx.x; base < ry * U; base += UNR * NT) {
-      float4 rv[UNR];
-      int ak[UNR];
-#pragma unroll
-      for (int k = 0; k < UNR; ++k) {  // issue the loads first
-        const int idx = base + k * NT;
-        const int rr = idx / U, u = idx - rr * U;
-        ak[k] = ry * u + rr;
-        rv[k] = (idx < ry * U && ak[k] <= hh) ? __ldg(rt + ak[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-#pragma unroll
-      for (int k = 0; k < UNR; ++k) {
-        const int idx = base + k * NT;
-        if (idx >= ry * U || ak[k] > hh) continue;
-        const float2 ey = make_float2(rv[k].x, rv[k].y);
-        float2 h;
-        if (asm_split) {
-          h = h_asm_split_row(a, exc, cah, cal, sac, kmc, ak[k], ey, rv[k].z, rv[k].w);
-        } else {
-          h = make_float2(exc.x * ey.x - exc.y * ey.y, exc.x * ey.y + exc.y * ey.x);
-        }
-        htab[idx] = h;
-      }
-    }
-  }
+  if (use_table) build_htab<M>(a, kx, htab, threadIdx.x, NT);
   __syncthreads();
 
   float2 acc[16];
@@ -202,24 +225,18 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
       v[q] = x;
     }
     fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
+    // Table index of bin ky = ry (tid + T q) + tt: with Py = ry M, ky is in the
+    // non-negative half (ky <= (Py - 1) / 2) exactly when q < 8; otherwise
+    // |k_y| = Py - ky lies in residue class (ry - tt) mod ry (0 when tt = 0).
+    const int hb_lo = tt * U + tid;
+    const int hb_hi = (tt == 0) ? M - tid : (ry - tt) * U + M - 1 - tid;
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const int pp = tid + T * q;
       const int ky = ry * pp + tt;
       float2 h;
       if (use_table) {
-        int rr, u;
-        if (ky <= (Py - 1) / 2) {
-          rr = tt;
-          u = pp;
-        } else if (tt == 0) {
-          rr = 0;
-          u = M - pp;
-        } else {
-          rr = ry - tt;
-          u = M - pp - 1;
-        }
-        h = htab[rr * U + u];
+        h = (q < 8) ? htab[hb_lo + T * q] : htab[hb_hi - T * q];
       } else if (a.engine == ENG_KSPEC) {
         h = __ldg(reinterpret_cast<const float2*>(a.kspec) + (size_t)kx * Py + ky);
         if (a.conj_h) h.y = -h.y;
@@ -262,6 +279,82 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
   }
 }
 
+// Pass B for an even transfer function with a shared-memory table, one CTA
+// per mirror pair of columns (kx, Px - kx): H depends on fx only through
+// fx^2 and fftfreq(Px - kx) = -fftfreq(kx) exactly, so the two columns have
+// bit-identical tables and per-column factors.  The CTA builds the table
+// once; group 0 then runs all ry sub-transforms of column kx and group 1
+// those of column Px - kx (the self-mirrored columns 0 and Px/2 leave group 1
+// idle), reading its column from global memory for each sub-transform and
+// accumulating in registers.
+template <int M>
+__global__ void __launch_bounds__(Lay<M, 2>::THREADS, Lay<M, 2>::MINB)
+    k_passB_pair(PropArgs a) {
+  constexpr int T = M / 16;
+  constexpr int U = M / 2 + 1;
+  constexpr int SB = Plan<M>::SMEM;
+  constexpr int NT = Lay<M, 2>::THREADS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Px = a.ax.P, ry = a.ay.r, ny = a.ny;
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  float2* tb = bufs + 2 * SB;
+  float2* tq = tb + ry * T;
+  float2* htab = tq + ry * 16;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
+  const int BAR_N = (T % 32 == 0) ? T : NT;
+  const int c = blockIdx.x;                        // 0 .. Px/2
+  const bool mirrored = (c == 0 || 2 * c == Px);   // column equals its mirror
+  const bool active = (g == 0) || !mirrored;
+  const int kx = (g == 0) ? c : (mirrored ? c : Px - c);
+  float2* buf = bufs + g * SB;
+  const float2* twm = reinterpret_cast<const float2*>(a.tw_my);
+  const float2* twP = reinterpret_cast<const float2*>(a.tw_Py);
+  copy_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
+  load_ptw(tb, tq, twP, ry, T);
+  build_htab<M>(a, c, htab, threadIdx.x, NT);
+  __syncthreads();
+  if (!active && T % 32 == 0) return;  // per-group barriers only from here on
+  float2* col = reinterpret_cast<float2*>(a.work) + (size_t)kx * ny;
+  float2 acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
+  for (int t = 0; t < ry; ++t) {
+    const float2 wb = tb[t * T + tid];
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int j = tid + T * q;
+      float2 x = (active && j < ny) ? col[j] : make_float2(0.f, 0.f);
+      if (t > 0) x = cmul(x, cmul(wb, tq[t * 16 + q]));
+      v[q] = x;
+    }
+    fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
+    const int hb_lo = t * U + tid;
+    const int hb_hi = (t == 0) ? M - tid : (ry - t) * U + M - 1 - tid;
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      v[q] = cmul(v[q], (q < 8) ? htab[hb_lo + T * q] : htab[hb_hi - T * q]);
+    fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      float2 y = v[q];
+      if (t > 0) y = cmulc(y, cmul(wb, tq[t * 16 + q]));
+      acc[q] = cadd(acc[q], y);
+    }
+  }
+  // every read of the column precedes this group's last barrier
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int j = tid + T * q;
+      if (j < ny) col[j] = acc[q];
+    }
+  }
+}
+
 // ---------------------------------------------------------------- pass A
 
 template <int M, int G>
@@ -286,17 +379,28 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   float2* W = reinterpret_cast<float2*>(a.work);
   constexpr int NT = Lay<M, G>::THREADS;
+  constexpr int KS = M / NT;  // input samples per thread
+  // all input loads first (no store or atomic between them), then one status
+  // check, then the per-sample stage
+  float2 xs[KS];
+  bool bad = false;
 #pragma unroll
-  for (int k = 0; k < M / NT; ++k) {
+  for (int k = 0; k < KS; ++k) {
     const int j = threadIdx.x + k * NT;
-    float2 x = make_float2(0.f, 0.f);
+    xs[k] = (j < nx) ? ld_in(a.in, a.in_c128, (size_t)iy * nx + j) : make_float2(0.f, 0.f);
+  }
+#pragma unroll
+  for (int k = 0; k < KS; ++k) bad = bad || !isfinite(xs[k].x) || !isfinite(xs[k].y);
+  if (a.status && bad) atomicOr(a.status, 1);
+#pragma unroll
+  for (int k = 0; k < KS; ++k) {
+    const int j = threadIdx.x + k * NT;
+    float2 x = xs[k];
     if (j < nx) {
-      x = ld_in(a.in, a.in_c128, (size_t)iy * nx + j);
-      if (a.status && (!isfinite(x.x) || !isfinite(x.y))) atomicOr(a.status, 1);
       if (a.seed) {
-        const size_t k = (size_t)iy * nx + j;
-        const double w = a.seed_f64 ? reinterpret_cast<const double*>(a.seed)[k]
-                                    : (double)reinterpret_cast<const float*>(a.seed)[k];
+        const size_t kk = (size_t)iy * nx + j;
+        const double w = a.seed_f64 ? reinterpret_cast<const double*>(a.seed)[kk]
+                                    : (double)reinterpret_cast<const float*>(a.seed)[kk];
         const float ws = (float)(w * a.seed_scale);
         x = make_float2(ws * x.x, ws * x.y);
       } else if (a.els.count && !a.adj) {
@@ -311,7 +415,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
     }
     xin[j] = x;
   }
-  load_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
+  copy_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, rx, T);
   __syncthreads();
   const int iters = (rx + G - 1) / G;
@@ -358,7 +462,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   const float2* W = reinterpret_cast<const float2*>(a.work);
   constexpr int NT = Lay<M, G>::THREADS;
-  load_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
+  copy_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, rx, T);
   // first gathers before the barrier: they overlap the table loads
   const int iters = (rx + G - 1) / G;
@@ -479,8 +583,24 @@ int pick_groups(int kind, int r, int table, int want) {
 }
 
 template <int M>
+size_t smem_pair(int r) {
+  constexpr int T = M / 16;
+  return ((size_t)TwLay<M>::SIZE + 2 * (size_t)Plan<M>::SMEM + (size_t)r * (T + 16) +
+          (size_t)r * (M / 2 + 1)) * sizeof(float2);
+}
+
+template <int M>
 cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
   const bool even = (a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF) && a.h_mode == 1;
+  if (even && (a.ax.P % 2) == 0 && smem_pair<M>(a.ay.r) <= kMaxSmemB && !getenv("OSGPU_NO_PAIR")) {
+    const size_t smem = smem_pair<M>(a.ay.r);
+    cudaError_t e = cudaFuncSetAttribute(k_passB_pair<M>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    ++launch_counter();
+    k_passB_pair<M><<<a.ax.P / 2 + 1, Lay<M, 2>::THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+  }
   int table = even ? 1 : 0;
   if (table && smem_v3<M, 1>(1, a.ay.r, 1) > kMaxSmemB) table = 0;
   const int g = pick_groups<M>(1, a.ay.r, table, env_groups("OSGPU_GROUPS_B", 2));
@@ -507,6 +627,13 @@ cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
 
 }  // namespace
 
+template <int M>
+cudaError_t launch_stage(void* tw, cudaStream_t st) {
+  ++launch_counter();
+  k_stage_twiddles<M><<<(TwLay<M>::SIZE + 255) / 256, 256, 0, st>>>(reinterpret_cast<float2*>(tw));
+  return cudaGetLastError();
+}
+
 bool reg_fft_size(int m) {
   return m == 256 || m == 512 || m == 1024 || m == 2048 || m == 4096;
 }
@@ -520,6 +647,10 @@ bool reg_fft_size(int m) {
     case 4096: return fn<4096>(__VA_ARGS__);          \
     default: return cudaErrorInvalidValue;            \
   }
+
+cudaError_t launch_stage_twiddles(void* tw, int m, cudaStream_t st) {
+  OSGPU_DISPATCH(m, launch_stage, tw, st)
+}
 
 cudaError_t launch_passA_reg(const PropArgs& a, cudaStream_t st) { OSGPU_DISPATCH(a.ax.m, launch_A, a, st) }
 cudaError_t launch_passB_reg(const PropArgs& a, cudaStream_t st) { OSGPU_DISPATCH(a.ay.m, launch_B, a, st) }

@@ -97,6 +97,9 @@ template <typename T> cudaError_t launch_passC(const PropArgs& a, cudaStream_t s
 template <typename T> cudaError_t launch_fraunhofer(const FraunArgs& a, cudaStream_t st);
 
 cudaError_t launch_twiddles(void* dst, int n, int is_double, cudaStream_t st);
+// f32 tables of register-FFT lengths (reg_fft_size): fills the stage-ordered
+// copy at tw + m from the m-point table at tw (the allocation holds 2 m float2).
+cudaError_t launch_stage_twiddles(void* tw, int m, cudaStream_t st);
 // Separable Fresnel-convolution kernel spectrum: fills hx (Px) and hy (Py).
 template <typename T>
 cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp, cudaStream_t st);
