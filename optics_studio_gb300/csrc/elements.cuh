@@ -151,15 +151,24 @@ static __device__ __forceinline__ bool apply_one_fast(const DevElement& e, int i
       if (bx.w && by.w) {
         const float tx = __int_as_float(bx.z), ty = __int_as_float(by.z);
         const float* r0 = e.latf + (size_t)by.x * e.lnx;
-        const float* r1 = e.latf + (size_t)by.y * e.lnx;
-        const float v00 = __ldg(r0 + bx.x), v10 = __ldg(r0 + bx.y), v01 = __ldg(r1 + bx.x),
-                    v11 = __ldg(r1 + bx.y);
-        const float A = v00 + (v10 - v00) * tx;
-        const float B = v01 + (v11 - v01) * tx;
-        phi = A + (B - A) * ty;
+        const float v00 = __ldg(r0 + bx.x);
+        if (bx.z == 0 && by.z == 0) {
+          phi = v00;  // sample on a lattice node: the bilinear form reduces to v00
+        } else {
+          const float* r1 = e.latf + (size_t)by.y * e.lnx;
+          const float v10 = __ldg(r0 + bx.y), v01 = __ldg(r1 + bx.x), v11 = __ldg(r1 + bx.y);
+          const float A = v00 + (v10 - v00) * tx;
+          const float B = v01 + (v11 - v01) * tx;
+          phi = A + (B - A) * ty;
+        }
       }
+      // reduce by 2 pi (two-part Cody-Waite constant) into [-pi, pi], then the
+      // hardware sine / cosine, accurate to ~5e-7 absolute on that range
+      const float nq = rintf(phi * 0.159154943091895336f);
+      float rr = fmaf(-nq, 6.28125f, phi);
+      rr = fmaf(-nq, 1.93530717958647692e-3f, rr);
       float sn, cs;
-      sincosf(phi, &sn, &cs);
+      __sincosf(rr, &sn, &cs);
       v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
       break;
     }

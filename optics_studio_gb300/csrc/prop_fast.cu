@@ -560,19 +560,20 @@ __global__ void __launch_bounds__(4 * (M / 16), 1) k_passA_r4(PropArgs a) {
   load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
   // inputs of the 4 rows: loads batched 8 at a time, then one status check
   constexpr int KS = 4 * M / NT;  // 16 samples per thread
+  constexpr int KB = 16;          // loads in flight per batch
   bool bad = false;
 #pragma unroll
-  for (int h = 0; h < KS; h += 8) {
-    float2 xs[8];
+  for (int h = 0; h < KS; h += KB) {
+    float2 xs[KB];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < KB; ++k) {
       const int e = threadIdx.x + (h + k) * NT;
       const int r = e / M, j = e - r * M;
       xs[k] = (j < nx) ? ld_in(a.in, a.in_c128, (size_t)(iy0 + r) * nx + j)
                        : make_float2(0.f, 0.f);
     }
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < KB; ++k) {
       const int e = threadIdx.x + (h + k) * NT;
       const int r = e / M, j = e - r * M;
       bad = bad || !isfinite(xs[k].x) || !isfinite(xs[k].y);
