@@ -657,11 +657,25 @@ def main():
             e2e_step()
         dt = (time.perf_counter() - t0) / nrep
         barrier()
+        # the host link's own pinned copy rates on this machine (one 2 GiB copy each way)
+        dev = torch.empty((NBANDS, N, N), dtype=torch.complex128, device="cuda")
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        dev.copy_(host_in, non_blocking=True)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        host_out.copy_(dev, non_blocking=True)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        nb = float(NBANDS * N * N * 16)
+        link = {"h2d_gbs": nb / (t2 - t1) / 1e9, "d2h_gbs": nb / (t3 - t2) / 1e9}
+        del dev
         line["e2e"] = {"value": NBANDS * world / dt, "unit": "propagations/s",
                        "h2d_bytes_per_step": NBANDS * N * N * 16,
                        "d2h_bytes_per_step": NBANDS * N * N * 16,
                        "api": "osgpu_beamline_trace_batch (host complex128, pinned; copies "
-                              "pipelined against the traces), f32 engine"}
+                              "pipelined against the traces), f32 engine",
+                       "host_link": link}
 
     # adjoint gradients of the inverse-design workload
     if not args.no_adjoint:

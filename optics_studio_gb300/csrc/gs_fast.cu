@@ -166,15 +166,29 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     const float2* twm = reinterpret_cast<const float2*>(a.tw);
     for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
   }
-  const int iy = blockIdx.x * G + g;
+  const int iy0 = blockIdx.x * G, iy = iy0 + g;
   const float2 py = __ldg(it.pry + iy);
   float* __restrict__ prow = it.phase + (size_t)iy * M;
+  // 4-row tiles: the spectrum moves through the groups' exchange buffers in
+  // 32-byte runs W[kx * M + iy0 .. iy0 + 3] (one sector per request)
+  constexpr bool kTile = (G == 4) && (T % 32 == 0);
   float2 v[16];
   float ph[16], am[16];
   float d2 = 0.f;
   if (iterate) {
+    if (kTile) {
+      for (int p = threadIdx.x; p < M; p += blockDim.x) {
+        const float4* src = reinterpret_cast<const float4*>(it.W + (size_t)p * M + iy0);
+        const float4 a0 = src[0], a1 = src[1];
+        bufs[p] = make_float2(a0.x, a0.y);
+        bufs[Plan<M>::SMEM + p] = make_float2(a0.z, a0.w);
+        bufs[2 * Plan<M>::SMEM + p] = make_float2(a1.x, a1.y);
+        bufs[3 * Plan<M>::SMEM + p] = make_float2(a1.z, a1.w);
+      }
+    } else {
 #pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = it.W[(size_t)(tid + T * q) * M + iy];
+      for (int q = 0; q < 16; ++q) v[q] = it.W[(size_t)(tid + T * q) * M + iy];
+    }
   }
   // per-sample inputs issued before the transform (no store precedes them)
 #pragma unroll
@@ -183,6 +197,10 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     am[q] = __ldg(it.amask + (size_t)iy * M + tid + T * q);
   }
   __syncthreads();
+  if (iterate && kTile) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = buf[tid + T * q];
+  }
   if (iterate) {
     fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
   }
@@ -208,8 +226,22 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     v[q] = cmul(make_float2(am[q] * cs, am[q] * s), pre);
   }
   fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
+  if (kTile) {
+    group_sync(BAR_ID, BAR_N);  // the transform's last reads of buf are done
 #pragma unroll
-  for (int q = 0; q < 16; ++q) it.W[(size_t)(tid + T * q) * M + iy] = v[q];
+    for (int q = 0; q < 16; ++q) buf[tid + T * q] = v[q];
+    __syncthreads();
+    for (int p = threadIdx.x; p < M; p += blockDim.x) {
+      float4* dst = reinterpret_cast<float4*>(it.W + (size_t)p * M + iy0);
+      const float2 r0 = bufs[p], r1 = bufs[Plan<M>::SMEM + p], r2 = bufs[2 * Plan<M>::SMEM + p],
+                   r3 = bufs[3 * Plan<M>::SMEM + p];
+      dst[0] = make_float4(r0.x, r0.y, r1.x, r1.y);
+      dst[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) it.W[(size_t)(tid + T * q) * M + iy] = v[q];
+  }
   if (iterate) cta_sum(d2, it.part_row, 0, red);
 }
 
