@@ -46,6 +46,7 @@ enum {
   OSGPU_E_INVALID_GRID = 26,
   OSGPU_E_INVALID_GRID_PITCH = 27,
   OSGPU_E_INVALID_GRATING = 28,
+  OSGPU_E_INVALID_SAG = 29, /* raised by bindings that evaluate a sag (RefractiveSurface) */
   /* InverseError (crates/optics-inverse/src/error.rs:11-85) */
   OSGPU_E_WRONG_DIMENSION = 40,
   OSGPU_E_NOT_FINITE = 41,
@@ -219,7 +220,17 @@ enum {
   OSGPU_EL_RECTANGULAR_APERTURE = 2, /* element.rs:817-929 */
   OSGPU_EL_THIN_LENS = 3,            /* element.rs:965-1154 */
   OSGPU_EL_PHASE_MASK_SAMPLED = 4,   /* element.rs:1321-1484 */
-  OSGPU_EL_BLAZED_GRATING = 5        /* element.rs:1519-1703 */
+  OSGPU_EL_BLAZED_GRATING = 5,       /* element.rs:1519-1703 */
+  /* Phase screen sampled on the field grid: transmission stop(x', y') *
+   * exp(i * depth * v[iy][ix]) with v the lattice (lnx = nx, lny = ny, one
+   * value per field sample, finite everywhere; ldx/ldy unused) and the stop
+   * evaluated in the element frame (orientation, center).  The binding of the
+   * elements whose phase the caller evaluates per sample at the exact
+   * element-frame coordinates: analytic PhaseMask::new (v = profile, depth =
+   * 1), RefractiveSurface (v = surface_z, depth = k (n1 - n2), element.rs:
+   * 2043-2123), ThickLens (v = thickness, element.rs:2272-2330) and Wedge
+   * (v = thickness, depth = k (n - 1), element.rs:2470-2540). */
+  OSGPU_EL_GRID_SCREEN = 6
 };
 /* ClearAperture (element.rs:384-408) */
 enum { OSGPU_STOP_FIELD = 0, OSGPU_STOP_CIRCLE = 1, OSGPU_STOP_ELLIPSE = 2, OSGPU_STOP_RECT = 3 };

@@ -203,12 +203,14 @@ int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid
       set_err("element %d: %s (status %d)", i, msg, est);
       return est;
     }
-    if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED && els[i].lattice_on_device == 2) {
+    const bool lat_el = els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED ||
+                        els[i].kind == OSGPU_EL_GRID_SCREEN;
+    if (lat_el && els[i].lattice_on_device == 2) {
       d.lat = nullptr;  // f32 engine only (checked in prepare_trace)
       d.latf = reinterpret_cast<const float*>(els[i].lattice);
-    } else if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED && els[i].lattice_on_device) {
+    } else if (lat_el && els[i].lattice_on_device) {
       d.lat = reinterpret_cast<const double*>(els[i].lattice);
-    } else if (els[i].kind == OSGPU_EL_PHASE_MASK_SAMPLED) {
+    } else if (lat_el) {
       const size_t bytes = (size_t)els[i].lnx * els[i].lny * sizeof(double);
       DBuf b;
       CK(b.alloc(bytes, st));
@@ -230,7 +232,7 @@ int build_fast_tables(Context& c, ElementList& L, const osgpu_grid& g, DBuf& kee
   size_t bytes = 0;
   for (int q = 0; q < L.count; ++q) {
     if (L.el[q].psi != 0.0) {
-      if (L.el[q].kind == EL_PHASE && !L.el[q].lat) {
+      if ((L.el[q].kind == EL_PHASE || L.el[q].kind == EL_SCREEN) && !L.el[q].lat) {
         set_err("an f32 device lattice needs orientation 0");
         return OSGPU_E_UNSUPPORTED;
       }
@@ -243,9 +245,10 @@ int build_fast_tables(Context& c, ElementList& L, const osgpu_grid& g, DBuf& kee
   char* p = reinterpret_cast<char*>(keep.p);
   for (int q = 0; q < L.count; ++q) {
     DevElement& e = L.el[q];
-    if (!(e.kind == EL_PHASE && e.latf && !e.lat)) {  // not a caller-owned f32 lattice
+    const bool lat_el = (e.kind == EL_PHASE || e.kind == EL_SCREEN);
+    if (!(lat_el && e.latf && !e.lat)) {  // not a caller-owned f32 lattice
       auto hit = c.lattices.find(e.lat);
-      e.latf = (e.kind == EL_PHASE && hit != c.lattices.end()) ? hit->second : nullptr;
+      e.latf = (lat_el && hit != c.lattices.end()) ? hit->second : nullptr;
     }
     CK(launch_element_tables(e, (int)g.nx, (int)g.ny, g.dx, g.dy, p, st));
     p += element_tables_bytes(e, (int)g.nx, (int)g.ny);
@@ -258,7 +261,8 @@ int build_fast_tables(Context& c, ElementList& L, const osgpu_grid& g, DBuf& kee
 double element_bytes(const ElementList& L, int f32) {
   double b = 0;
   for (int q = 0; q < L.count; ++q)
-    if (L.el[q].kind == EL_PHASE) b += (double)L.el[q].lnx * L.el[q].lny * (f32 ? 4 : 8);
+    if (L.el[q].kind == EL_PHASE || L.el[q].kind == EL_SCREEN)
+      b += (double)L.el[q].lnx * L.el[q].lny * (f32 ? 4 : 8);
   return b;
 }
 
@@ -1277,7 +1281,8 @@ int prepare_trace(Context& c, const double* host_in, size_t n, const osgpu_grid&
     }
     if (!f32)
       for (int q = 0; q < E[s].list.count; ++q)
-        if (E[s].list.el[q].kind == EL_PHASE && !E[s].list.el[q].lat) {
+        if ((E[s].list.el[q].kind == EL_PHASE || E[s].list.el[q].kind == EL_SCREEN) &&
+            !E[s].list.el[q].lat) {
           set_err("step %d: an f32 device lattice needs the f32 engine", s);
           return OSGPU_E_BAD_ARGUMENT;
         }
@@ -1545,7 +1550,8 @@ int osgpu_beamline_trace_batch_graph(const osgpu_trace_item* items, int32_t n_it
     for (int s = 0; s < items[i].n_steps; ++s)
       for (int q = 0; q < items[i].steps[s].n_elements; ++q) {
         const osgpu_element& e = items[i].steps[s].elements[q];
-        if (e.kind == OSGPU_EL_PHASE_MASK_SAMPLED && !e.lattice_on_device) {
+        if ((e.kind == OSGPU_EL_PHASE_MASK_SAMPLED || e.kind == OSGPU_EL_GRID_SCREEN) &&
+            !e.lattice_on_device) {
           set_err("item %d: a host-memory lattice cannot be captured", i);
           return OSGPU_E_BAD_ARGUMENT;
         }

@@ -70,8 +70,9 @@ static __device__ __forceinline__ void cmul_phase(double& re, double& im, double
 // FP64 evaluation of one element at the origin-centred coordinate (x, y),
 // in the reference's operation order (element.rs:754-790, 900-929,
 // 1115-1154, 1443-1484, 1668-1703): (re, im) <- t(x, y) (re, im).
-static __device__ __forceinline__ void apply_one_exact(const DevElement& e, double x, double y,
-                                                       double& re, double& im) {
+static __device__ __forceinline__ void apply_one_exact(const DevElement& e, int ix, int iy,
+                                                       double x, double y, double& re,
+                                                       double& im) {
   const double xr = __dsub_rn(x, e.cx), yr = __dsub_rn(y, e.cy);
   double fx, fy;
   to_frame(xr, yr, e.cpsi, e.spsi, fx, fy);
@@ -97,6 +98,11 @@ static __device__ __forceinline__ void apply_one_exact(const DevElement& e, doub
       cmul_phase(re, im, lattice_at(e, fx, fy));
       break;
     }
+    case EL_SCREEN: {  // exp(i (depth * v)), the reference's (k * dn * z) order
+      if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
+      cmul_phase(re, im, __dmul_rn(e.depth, e.lat[(size_t)iy * e.lnx + ix]));
+      break;
+    }
     case EL_GRATING: {
       if (!stop_contains(e.stop, e.a, e.b, fx, fy)) { re = 0.0; im = 0.0; break; }
       double u = __dmul_rn(fx, e.inv_period);
@@ -115,7 +121,7 @@ static __device__ void apply_elements_exact(const ElementList& L, int ix, int iy
                                      double dx, double dy, double& re, double& im) {
   const double x = coord_d(ix, nx, dx);
   const double y = coord_d(iy, ny, dy);
-  for (int q = 0; q < L.count; ++q) apply_one_exact(L.el[q], x, y, re, im);
+  for (int q = 0; q < L.count; ++q) apply_one_exact(L.el[q], ix, iy, x, y, re, im);
 }
 
 // f32 fast path for one element (psi == 0, tables built in FP64 by
@@ -172,6 +178,11 @@ static __device__ __forceinline__ bool apply_one_fast(const DevElement& e, int i
       v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
       break;
     }
+    case EL_SCREEN: {  // transmission table built with the phase in FP64
+      const float2 t = __ldg(e.scr + (size_t)iy * e.lnx + ix);
+      v = make_float2(v.x * t.x - v.y * t.y, v.x * t.y + v.y * t.x);
+      break;
+    }
     default:
       break;
   }
@@ -219,8 +230,8 @@ static __device__ __forceinline__ void adjoint_plane(const ElementList& L, void*
     for (int q = 0; q < kMaxElements; ++q) {
       if (q < L.count) {
         double a = 1.0, b = 0.0;
-        apply_one_exact(L.el[q], x, y, a, b);
-        apply_one_exact(L.el[q], x, y, wr, wi);
+        apply_one_exact(L.el[q], ix, iy, x, y, a, b);
+        apply_one_exact(L.el[q], ix, iy, x, y, wr, wi);
         tr[q] = (T)a; ti[q] = (T)b;
         vr[q] = (T)wr; vi[q] = (T)wi;
       }

@@ -413,6 +413,23 @@ int element_check(const osgpu_element& e, const osgpu_grid& g, double lambda, De
       d.ldy = e.ldy;
       return OSGPU_OK;
     }
+    case OSGPU_EL_GRID_SCREEN: {
+      d.kind = EL_SCREEN;
+      if (e.lattice == nullptr || e.lnx != g.nx || e.lny != g.ny) return OSGPU_E_INVALID_GRID;
+      if (!std::isfinite(e.depth)) return OSGPU_E_INVALID_PHASE;
+      if (!e.lattice_on_device) {  // host values: all finite (0 outside the stop)
+        const double* v = reinterpret_cast<const double*>(e.lattice);
+        const uint64_t n = e.lnx * e.lny;
+        for (uint64_t k = 0; k < n; ++k)
+          if (!std::isfinite(v[k])) return OSGPU_E_INVALID_PHASE;
+      }
+      int st = stop_check();
+      if (st) return st;
+      d.lnx = (int)e.lnx;
+      d.lny = (int)e.lny;
+      d.depth = e.depth;
+      return OSGPU_OK;
+    }
     case OSGPU_EL_BLAZED_GRATING: {
       d.kind = EL_GRATING;
       if (!std::isfinite(e.period) || e.period <= 0.0 || !std::isfinite(e.depth))

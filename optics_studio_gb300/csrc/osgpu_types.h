@@ -40,6 +40,7 @@ enum ElementKind : int {
   EL_LENS = 3,      // ThinLens with a clear-aperture stop
   EL_PHASE = 4,     // PhaseMask::sampled (bilinear lattice) with a stop
   EL_GRATING = 5,   // BlazedGrating with a stop
+  EL_SCREEN = 6,    // phase screen sampled on the field grid, with a stop
 };
 
 enum StopKind : int { STOP_FIELD = 0, STOP_CIRCLE = 1, STOP_ELLIPSE = 2, STOP_RECT = 3 };
@@ -61,7 +62,8 @@ struct DevElement {
   const int2* span;          // per row inclusive [lo, hi] of the transmitting set (lo > hi: none)
   const float2* tabx;        // per column factor (lens x part, grating)
   const float2* taby;        // per row factor (lens y part)
-  const float* latf;         // f32 copy of the phase lattice
+  const float* latf;         // f32 copy of the phase lattice (caller-owned f32 screen values)
+  const float2* scr;         // screen: per-sample transmission e^{i depth v} (f32 engine)
   const int4* bilx;          // per column bilinear lookup (i0, i1, bits of tx, inside)
   const int4* bily;          // per row bilinear lookup (j0, j1, bits of ty, inside)
 };

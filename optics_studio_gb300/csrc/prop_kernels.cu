@@ -202,6 +202,20 @@ __global__ void k_cast_f64_f32(const double* src, float* dst, size_t n) {
   if (i < n) dst[i] = (float)src[i];
 }
 
+// Grid-screen transmission e^{i depth v}: the phase formed and reduced mod
+// 2 pi in FP64 (a thick element's phase reaches hundreds of radians), the
+// reduced angle's sine and cosine in f32.
+__global__ void k_screen_table(const double* v64, const float* v32, double depth, float2* out,
+                               size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double phi = __dmul_rn(depth, v64 ? v64[i] : (double)v32[i]);
+  const double r = phi - 6.283185307179586 * rint(phi * 0.15915494309189535);
+  float s, c;
+  sincosf((float)r, &s, &c);
+  out[i] = make_float2(c, s);
+}
+
 size_t element_tables_bytes(const DevElement& e, int nx, int ny) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t b = al((size_t)ny * sizeof(int2));
@@ -210,6 +224,7 @@ size_t element_tables_bytes(const DevElement& e, int nx, int ny) {
   if (e.kind == EL_PHASE)
     b += al((size_t)nx * sizeof(int4)) + al((size_t)ny * sizeof(int4)) +
          al((size_t)e.lnx * e.lny * sizeof(float));
+  if (e.kind == EL_SCREEN) b += al((size_t)e.lnx * e.lny * sizeof(float2));
   return b;
 }
 
@@ -236,6 +251,16 @@ cudaError_t launch_element_tables(DevElement& e, int nx, int ny, double dx, doub
     p += al((size_t)nx * sizeof(int4));
     by = reinterpret_cast<int4*>(p);
     p += al((size_t)ny * sizeof(int4));
+  }
+  if (e.kind == EL_SCREEN) {
+    float2* t = reinterpret_cast<float2*>(p);
+    p += al((size_t)e.lnx * e.lny * sizeof(float2));
+    const size_t n = (size_t)e.lnx * e.lny;
+    COUNT_LAUNCH();
+    k_screen_table<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(e.lat, e.latf, e.depth, t, n);
+    e.scr = t;
+  }
+  if (e.kind == EL_PHASE) {
     if (e.latf) {
       lf = const_cast<float*>(e.latf);  // f32 copy kept with the lattice handle
     } else {

@@ -15,7 +15,7 @@ import numpy as np
 from . import _ffi
 from .field import ptr, precision_code
 
-EL_ELLIPSE, EL_RECT, EL_LENS, EL_PHASE, EL_GRATING = 1, 2, 3, 4, 5
+EL_ELLIPSE, EL_RECT, EL_LENS, EL_PHASE, EL_GRATING, EL_SCREEN = 1, 2, 3, 4, 5, 6
 STOP_FIELD, STOP_CIRCLE, STOP_ELLIPSE, STOP_RECT = 0, 1, 2, 3
 
 
@@ -157,10 +157,13 @@ class PhaseMask(Element):
             lat = self.lattice
             dx, dy = self.pitch
         else:
-            # analytic closure: evaluate in the element frame on the field grid
-            # and pass it as a lattice with identical geometry (element frame
-            # coordinates of the field samples, sampled on the host).
-            raise NotImplementedError("analytic PhaseMask: sample it with PhaseMask.sampled")
+            # analytic closure: evaluated on the host at each field sample's
+            # element-frame coordinates, passed as a grid screen (depth 1)
+            _, _, fx, fy = frame_coords(band, self.center, self.psi)
+            vals = np.ascontiguousarray(np.broadcast_to(self.profile(fx, fy), fx.shape),
+                                        dtype=np.float64)
+            vals = np.where(ap_contains(ap, fx, fy), vals, 0.0)
+            return _screen_desc(vals, 1.0, ap, self.psi, self.center), vals
         return _desc(EL_PHASE, ap.kind, ap.a, ap.b, self.psi, self.center, lattice=lat,
                      lnx=nx, lny=ny, ldx=dx, ldy=dy), lat
 
@@ -184,3 +187,115 @@ class BlazedGrating(Element):
         ap = self.aperture
         return _desc(EL_GRATING, ap.kind, ap.a, ap.b, self.psi, self.center, period=self.period,
                      depth=self.depth), None
+
+
+TAU = 2.0 * math.pi
+
+
+def wrap_angle(radians):
+    """``Angle::new``: rem_euclid into [0, 2 pi) (common.rs:36-40)."""
+    r = math.fmod(radians, TAU)
+    return r + TAU if r < 0.0 else r
+
+
+def frame_coords(band, center, orientation):
+    """Element-frame coordinates of every field sample: origin-centred grid
+    coordinates (field.rs:216-221), shifted by the centre and rotated by the
+    wrapped orientation (element.rs:557-560), in the reference's order."""
+    psi = wrap_angle(orientation or 0.0)
+    x = (np.arange(band.nx, dtype=np.float64) - (band.nx - 1.0) / 2.0) * band.dx
+    y = (np.arange(band.ny, dtype=np.float64) - (band.ny - 1.0) / 2.0) * band.dy
+    xr = x[None, :] - center[0]
+    yr = y[:, None] - center[1]
+    c, s = math.cos(psi), math.sin(psi)
+    return xr, yr, c * xr + s * yr, -s * xr + c * yr
+
+
+def ap_contains(ap, fx, fy):
+    """ClearAperture::contains (element.rs:476-488), inclusive boundary."""
+    if ap.kind == STOP_FIELD:
+        return np.ones(fx.shape, dtype=bool)
+    if ap.kind == STOP_CIRCLE:
+        return fx * fx + fy * fy <= ap.a * ap.a
+    if ap.kind == STOP_ELLIPSE:
+        a2, b2 = ap.a * ap.a, ap.b * ap.b
+        return b2 * fx * fx + a2 * fy * fy <= a2 * b2
+    return (np.abs(fx) <= ap.a) & (np.abs(fy) <= ap.b)
+
+
+def _screen_desc(values, depth, ap, psi, center):
+    ny, nx = values.shape
+    return _ffi.ElementC(EL_SCREEN, ap.kind, ap.a, ap.b, psi, center[0], center[1], 0.0, 0.0,
+                         depth, ptr(values), nx, ny, 0.0, 0.0, 0)
+
+
+def conic_sag(r, radius, conic, coeffs=()):
+    """Conic + even-asphere sag z(r) (element.rs:1850-1862)."""
+    c = 1.0 / radius
+    r2 = r * r
+    root = np.sqrt(np.maximum(1.0 - (1.0 + conic) * c * c * r2, 0.0))
+    z = c * r2 / (1.0 + root)
+    poly = 0.0
+    for a in reversed(list(coeffs)):
+        poly = poly * r2 + a
+    return z + poly * r2 * r2
+
+
+def _index(n, lam):
+    return float(n(lam)) if callable(n) else float(n)
+
+
+class RefractiveSurface(Element):
+    """element.rs:1910-2123: exp(i k (n1 - n2) z) inside the stop, z = conic /
+    even-asphere sag plus a linear tilt.  The sag is evaluated on the host at
+    the element-frame coordinate of every field sample and bound as a grid
+    screen with depth k (n1 - n2); indices are constants or callables n(lam)."""
+
+    def __init__(self, radius, conic=0.0, coeffs=(), n_front=1.0, n_back=1.5, tilt=(0.0, 0.0),
+                 orientation=None, aperture=ClearAperture.field(), center=(0.0, 0.0)):
+        if not (math.isfinite(radius) and radius != 0.0):
+            raise _ffi.OsgpuError(23)
+        self.radius, self.conic, self.coeffs = radius, conic, tuple(coeffs)
+        self.n_front, self.n_back, self.tilt = n_front, n_back, tilt
+        self.psi = 0.0 if orientation is None else orientation
+        self.aperture, self.center = aperture, center
+
+    def values(self, band):
+        _, _, fx, fy = frame_coords(band, self.center, self.psi)
+        z = (conic_sag(np.sqrt(fx * fx + fy * fy), self.radius, self.conic, self.coeffs)
+             + self.tilt[0] * fx + self.tilt[1] * fy)
+        inside = ap_contains(self.aperture, fx, fy)
+        if not np.all(np.isfinite(z[inside])):
+            raise _ffi.OsgpuError(29)
+        return np.ascontiguousarray(np.where(inside, z, 0.0))
+
+    def descriptor(self, band):
+        k = 2.0 * math.pi / band.lam
+        dn = _index(self.n_front, band.lam) - _index(self.n_back, band.lam)
+        v = self.values(band)
+        return _screen_desc(v, k * dn, self.aperture, self.psi, self.center), v
+
+
+class Wedge(Element):
+    """element.rs:2383-2540: exp(i k (n - 1) t) inside the stop with the
+    thickness t = t0 - tan(angle) (x' cos o + y' sin o) evaluated on the host
+    per field sample and bound as a grid screen with depth k (n - 1)."""
+
+    def __init__(self, angle, n, base_thickness, orientation, aperture=ClearAperture.field(),
+                 center=(0.0, 0.0)):
+        self.angle, self.n, self.t0 = angle, n, base_thickness
+        self.psi = orientation
+        self.aperture, self.center = aperture, center
+
+    def values(self, band):
+        _, _, fx, fy = frame_coords(band, self.center, self.psi)
+        o = wrap_angle(self.psi)
+        g = fx * math.cos(o) + fy * math.sin(o)
+        t = self.t0 - math.tan(self.angle) * g
+        return np.ascontiguousarray(np.where(ap_contains(self.aperture, fx, fy), t, 0.0))
+
+    def descriptor(self, band):
+        k = 2.0 * math.pi / band.lam
+        v = self.values(band)
+        return _screen_desc(v, k * (_index(self.n, band.lam) - 1.0), self.aperture, self.psi,
+                            self.center), v

@@ -312,3 +312,65 @@ class BlazedGrating(Element):
 def transmission(element, band):
     """``adjoint::transmission``: t = apply(1) on ``band``'s grid (adjoint.rs:102-108)."""
     return element.transmission(band)
+
+
+def conic_sag(r, radius, conic, coeffs=()):
+    """Conic + even-asphere sag (element.rs:1850-1862)."""
+    c = 1.0 / radius
+    r2 = r * r
+    root = np.sqrt(np.maximum(1.0 - (1.0 + conic) * c * c * r2, 0.0))
+    z = c * r2 / (1.0 + root)
+    poly = 0.0
+    for a in reversed(list(coeffs)):
+        poly = poly * r2 + a
+    return z + poly * r2 * r2
+
+
+class RefractiveSurface(Element):
+    """element.rs:1910-2123 with constant indices: t = stop * exp(i (k (n1 - n2)) z),
+    z(x', y') = sag(sqrt(x'^2 + y'^2)) + tau_x x' + tau_y y'."""
+
+    def __init__(self, radius, conic=0.0, coeffs=(), n_front=1.0, n_back=1.5, tilt=(0.0, 0.0),
+                 orientation=None, aperture=ClearAperture.field(), center=(0.0, 0.0)):
+        self.radius, self.conic, self.coeffs = radius, conic, tuple(coeffs)
+        self.n1, self.n2, self.tilt = n_front, n_back, tilt
+        self.psi = resolve_orientation(orientation)
+        aperture.validate(center)
+        self.aperture, self.center = aperture, center
+
+    def surface_z(self, fx, fy):
+        return (conic_sag(np.sqrt(fx * fx + fy * fy), self.radius, self.conic, self.coeffs)
+                + self.tilt[0] * fx + self.tilt[1] * fy)
+
+    def transmission(self, band):
+        _check_footprint(self.aperture.footprint_at(self.psi), self.center, band)
+        _, _, fx, fy = _frame_coords(band, self.center, self.psi)
+        inside = self.aperture.contains(fx, fy)
+        k = 2.0 * math.pi / band.lam
+        dn = self.n1 - self.n2
+        z = self.surface_z(fx, fy)
+        return np.where(inside, np.exp(1j * ((k * dn) * z)), 0.0)
+
+
+class Wedge(Element):
+    """element.rs:2383-2540 with a constant index: t = stop * exp(i (k (n - 1)) t(x', y')),
+    t = t0 - tan(angle) (x' cos(o) + y' sin(o))."""
+
+    def __init__(self, angle, n, base_thickness, orientation, aperture=ClearAperture.field(),
+                 center=(0.0, 0.0)):
+        self.angle, self.n, self.t0 = angle, n, base_thickness
+        self.psi = resolve_orientation(orientation)
+        aperture.validate(center)
+        self.aperture, self.center = aperture, center
+
+    def thickness_at(self, fx, fy):
+        g = fx * math.cos(self.psi) + fy * math.sin(self.psi)
+        return self.t0 - math.tan(self.angle) * g
+
+    def transmission(self, band):
+        _check_footprint(self.aperture.footprint_at(self.psi), self.center, band)
+        _, _, fx, fy = _frame_coords(band, self.center, self.psi)
+        inside = self.aperture.contains(fx, fy)
+        k = 2.0 * math.pi / band.lam
+        dn = self.n - 1.0
+        return np.where(inside, np.exp(1j * ((k * dn) * self.thickness_at(fx, fy))), 0.0)

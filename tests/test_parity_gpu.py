@@ -268,3 +268,51 @@ def test_fresnel_f32_register_fft(z):
                   ofr.propagate(ob, z, cfg).samples) <= TOL32
     assert rel_l2(gfr.propagate_convolution(g, z, gcfg, "f32").samples,
                   ofr.propagate_convolution(ob, z, cfg).samples) <= TOL32
+
+
+def screen_pairs():
+    """Elements bound as grid screens (host-evaluated values): refractive
+    surfaces (conic + asphere + tilt), wedges and an analytic phase mask,
+    rotated and unrotated (unrotated ones take the f32 table path)."""
+    prof = lambda x, y: 3e8 * x * y + 2e4 * x - 1e9 * y * y
+    return [
+        (gel.RefractiveSurface(2e-3, -0.5, (1e3, -2e6), 1.0, 1.52, (1e-3, -2e-3), 0.3,
+                               gel.ClearAperture.circle(80e-6), (10e-6, -5e-6)),
+         oel.RefractiveSurface(2e-3, -0.5, (1e3, -2e6), 1.0, 1.52, (1e-3, -2e-3), 0.3,
+                               oel.ClearAperture.circle(80e-6), (10e-6, -5e-6))),
+        (gel.RefractiveSurface(-3e-3, 0.0, (), 1.33, 1.0, (0.0, 0.0), None,
+                               gel.ClearAperture.rectangle(70e-6, 60e-6)),
+         oel.RefractiveSurface(-3e-3, 0.0, (), 1.33, 1.0, (0.0, 0.0), None,
+                               oel.ClearAperture.rectangle(70e-6, 60e-6))),
+        (gel.Wedge(0.01, 1.45, 1e-4, 0.7, gel.ClearAperture.ellipse(70e-6, 50e-6), (0.0, 8e-6)),
+         oel.Wedge(0.01, 1.45, 1e-4, 0.7, oel.ClearAperture.ellipse(70e-6, 50e-6), (0.0, 8e-6))),
+        (gel.Wedge(-0.02, 1.6, 5e-5, 0.0), oel.Wedge(-0.02, 1.6, 5e-5, 0.0)),
+        (gel.PhaseMask.new(prof, 0.2, gel.ClearAperture.circle(85e-6)),
+         oel.PhaseMask(prof, 0.2, oel.ClearAperture.circle(85e-6))),
+    ]
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-14), ("f32", 2e-6)])
+def test_grid_screens_match_oracle(prec, tol):
+    n = 48
+    ob = ofield.BandField(rng_field(n, n, 12), 4e-6, 4e-6, 600e-9)
+    for ge, oe in screen_pairs():
+        ref = oe.apply(ob).samples
+        out = ge.apply(to_gpu_band(ob), prec).samples
+        assert np.array_equal(out == 0, ref == 0), type(ge).__name__
+        assert np.max(np.abs(out - ref)) <= tol * np.max(np.abs(ref)), type(ge).__name__
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", TOL64), ("f32", TOL32)])
+def test_refractive_surface_fused_in_beamline(prec, tol):
+    n, d, lam = 96, 4e-6, 532e-9
+    ob = ofield.plane_wave(0.0, 0.0, 1.0, n, n, d, d, lam)
+    obl_ = obl.Beamline()
+    obl_.push(oel.RefractiveSurface(5e-3, -1.0, (), 1.0, 1.5, (0.0, 0.0), None,
+                                    oel.ClearAperture.circle(150e-6)), 3e-3)
+    ref = obl_.trace(ob, obl.asm_engine(oasm.AsmConfig()))
+    gbl = Beamline()
+    gbl.push(gel.RefractiveSurface(5e-3, -1.0, (), 1.0, 1.5, (0.0, 0.0), None,
+                                   gel.ClearAperture.circle(150e-6)), 3e-3)
+    out = gbl.trace(to_gpu_band(ob), AsmEngine(gasm.AsmConfig(), prec))
+    assert rel_l2(out.samples, ref.samples) <= tol
