@@ -129,6 +129,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(ms, world):
+    """Slowest rank's time (the job finishes with it); the all-reduce runs on
+    the device of the process group's backend (NCCL: cuda, gloo: cpu)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, ms_per_step):
+    """Whole-job throughput: the units all ranks processed per second."""
+    return units_per_rank * world / (ms_per_step / 1e3)
+
+
 def make_items(og, ffi, d_in, d_out, lattice_handle, keep):
     """One osgpu_trace_item per band: DOE -> aperture -> lens -> ASM z."""
     items = (ffi.TraceItemC * NBANDS)()
@@ -563,13 +581,9 @@ def main():
     clk = clocks.stop()
     ffi.check(L.osgpu_sync_status())
 
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(ms_total, world)
     ms_step = ms_total / args.steps
-    value = NBANDS * world / (ms_step / 1e3)
+    value = job_rate(NBANDS, world, ms_step)
 
     kstats = {}
     for i in range(nst.value):
@@ -655,7 +669,7 @@ def main():
         nrep = max(1, min(args.steps, 3))
         for _ in range(nrep):
             e2e_step()
-        dt = (time.perf_counter() - t0) / nrep
+        dt = max_over_ranks((time.perf_counter() - t0) / nrep * 1e3, world) / 1e3
         barrier()
         # the host link's own pinned copy rates on this machine (one 2 GiB copy each way)
         dev = torch.empty((NBANDS, N, N), dtype=torch.complex128, device="cuda")
