@@ -246,6 +246,11 @@ def adjoint_leg(args, stream):
             step()
         torch.cuda.synchronize()
         nsteps = max(3, args.steps // 3)
+        import ctypes as C
+        import optics_studio_gb300 as og
+        from optics_studio_gb300 import _ffi as ffi
+        L = og.lib()
+        ffi.check(L.osgpu_profile_begin())
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -253,10 +258,17 @@ def adjoint_leg(args, stream):
             g, val = step()
         e1.record(stream)
         torch.cuda.synchronize()
+        stats = (ffi.KernelStatC * 16)()
+        nst = C.c_int32()
+        ffi.check(L.osgpu_profile_end(stats, 16, C.byref(nst)))
         ms = e0.elapsed_time(e1) / nsteps
+        kst = {stats[i].name.decode(): round(stats[i].total_ms / nsteps, 4)
+               for i in range(nst.value)}
         out = {"value": 1e3 / ms, "unit": "gradients/s", "ms_per_gradient": ms,
                "gradients": nsteps, "merit_last": val, "tape_bytes": tape.nbytes(),
-               "workload": ADJ_WORKLOAD, "dtype": "f32"}
+               "workload": ADJ_WORKLOAD, "dtype": "f32",
+               "kernel_ms_per_gradient": kst,
+               "library_kernels_ms": round(sum(kst.values()), 4)}
         tape.close()
         if not args.no_f64:
             # same gradient (first 2 bands) on both engines from the same phases

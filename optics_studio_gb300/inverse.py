@@ -209,13 +209,15 @@ class Renderer:
         keep.append(arr)
         return arr
 
-    def render_frames(self, values, jobs, tape=None):
-        """Intensity of each (lam, x0, y0) job: tensor (len(jobs), ny, nx)."""
+    def render_frames(self, values, jobs, tape=None, out=None):
+        """Intensity of each (lam, x0, y0) job: tensor (len(jobs), ny, nx)
+        (written into `out` when given)."""
         torch = _torch()
         dtype, _, rdt, _ = _dtypes(self.precision)
-        b0 = self.source(jobs[0][1], jobs[0][2], jobs[0][0])
-        ny, nx = b0.shape
-        out = torch.empty((len(jobs), ny, nx), dtype=rdt, device=b0.device)
+        if out is None:
+            b0 = self.source(jobs[0][1], jobs[0][2], jobs[0][0])
+            ny, nx = b0.shape
+            out = torch.empty((len(jobs), ny, nx), dtype=rdt, device=b0.device)
         keep = []
         arr = self._frames(values, jobs, out, keep)
         _ffi.check(_ffi.lib().osgpu_render_batch_device(
@@ -235,12 +237,13 @@ class Renderer:
         if self.deriv_lambda:
             chans.append(DLAMBDA)
         jobs = [(lam, x0, y0) for lam in self.bands for (x0, y0) in self.scenes]
-        inten = self.render_frames(values, jobs, tape)
         B, S = len(self.bands), len(self.scenes)
-        ny, nx = inten.shape[-2:]
         torch = _torch()
-        data = torch.zeros((len(chans), B, S, ny, nx), dtype=inten.dtype, device=inten.device)
-        data[0] = inten.reshape(B, S, ny, nx)
+        _, _, rdt, _ = _dtypes(self.precision)
+        b0 = self.source(jobs[0][1], jobs[0][2], jobs[0][0])
+        ny, nx = b0.shape
+        data = torch.empty((len(chans), B, S, ny, nx), dtype=rdt, device=b0.device)
+        self.render_frames(values, jobs, tape, out=data[0].view(B * S, ny, nx))
         h, hl = self.scene_step, self.lambda_step
 
         def fd(ci, hi_jobs, lo_jobs, step):
@@ -260,14 +263,23 @@ class Renderer:
         return Observation(chans, list(self.bands), list(self.scenes), (nx, ny), self.pitch, data,
                            (h, hl))
 
-    def push_back_frames(self, values, jobs, seeds, grads, tape=None):
-        """adjoint.rs:140-246 per job, accumulated into grads {element index: tensor}."""
-        dtype, _, _, _ = _dtypes(self.precision)
+    def prepare_push_back(self, values, jobs, seeds, grads):
+        """Frame array of a push_back batch (host work only; the seeds and
+        gradient buffers may still be in flight)."""
         keep = []
         arr = self._frames(values, jobs, None, keep, seeds=seeds, grads=grads)
+        return arr, len(jobs), keep
+
+    def launch_push_back(self, prepared, tape=None):
+        dtype, _, _, _ = _dtypes(self.precision)
+        arr, n, _keep = prepared
         _ffi.check(_ffi.lib().osgpu_push_back_batch_device(
-            arr, len(jobs), self.asm_cfg.c(), dtype, self._stream_ptr(),
+            arr, n, self.asm_cfg.c(), dtype, self._stream_ptr(),
             tape.handle if tape is not None else None))
+
+    def push_back_frames(self, values, jobs, seeds, grads, tape=None):
+        """adjoint.rs:140-246 per job, accumulated into grads {element index: tensor}."""
+        self.launch_push_back(self.prepare_push_back(values, jobs, seeds, grads), tape)
 
 
 def push_back(renderer, values, lam, x0, y0, dmdi):
@@ -294,30 +306,47 @@ def grid_gradient(renderer, values, merit, tape=None):
         tape = Tape()
     try:
         obs = renderer.render(values, tape)
-        value = merit.evaluate(obs)
-        seed = merit.obs_gradient(obs)
-        if seed is None:
-            raise _ffi.OsgpuError(44)
+        # everything the adjoint sweep needs is prepared while the render runs;
+        # the merit is the one host synchronisation of the step
+        seed = torch.zeros_like(obs.data)
         jobs = [(lam, x0, y0) for lam in renderer.bands for (x0, y0) in renderer.scenes]
         B, S = len(renderer.bands), len(renderer.scenes)
-        seeds = [seed[0, b, s].contiguous() for b in range(B) for s in range(S)]
-        if len(obs.channels) > 1 and bool(torch.any(seed[1:] != 0)):
-            raise _ffi.OsgpuError(44)
-        if not bool(torch.any(seed[0] != 0)):
-            return {}, value, obs
+        seeds = [seed[0, b, s] for b in range(B) for s in range(S)]
         design = renderer.carrier(values, renderer.bands[0])
         grads = {}
         for ei, _z, _m in design.steps:
             if ei is not None and ei not in grads:
                 grads[ei] = torch.zeros(obs.data.shape[-2:], dtype=obs.data.dtype,
                                         device=obs.data.device)
+        prepared = renderer.prepare_push_back(values, jobs, seeds, grads)
+        value, ok = merit_value_and_seed(merit, obs, seed)
+        if not ok:
+            raise _ffi.OsgpuError(44)
+        if len(obs.channels) > 1 and bool(torch.any(seed[1:] != 0)):
+            raise _ffi.OsgpuError(44)
+        if not bool(torch.any(seed[0] != 0)):
+            return {}, value, obs
         # the tape holds the intensity frames' planes (the finite-difference
         # renders of the other channels record nothing)
-        renderer.push_back_frames(values, jobs, seeds, grads, tape)
+        renderer.launch_push_back(prepared, tape)
         return dict(sorted(grads.items())), value, obs
     finally:
         if own:
             tape.close()
+
+
+def merit_value_and_seed(merit, obs, seed):
+    """(M, ok): the merit value, with dM/dI written into `seed` (shape of
+    obs.data); ok is False when the merit has no obs_gradient.  The device
+    merits produce both in one call."""
+    if hasattr(merit, "value_and_seed"):
+        return merit.value_and_seed(obs, seed)
+    value = merit.evaluate(obs)
+    g = merit.obs_gradient(obs)
+    if g is None:
+        return value, False
+    seed.copy_(g)
+    return value, True
 
 
 def _real_code(t):
@@ -364,6 +393,9 @@ class MseToTarget:
         self._call(obs, g[0])
         return g
 
+    def value_and_seed(self, obs, seed):
+        return self._call(obs, seed[0]), True
+
 
 class EncircledEnergyMerit:
     """merit.rs:167-245."""
@@ -396,6 +428,13 @@ class EncircledEnergyMerit:
         _ffi.check(code)
         return g
 
+    def value_and_seed(self, obs, seed):
+        code, v = self._call(obs, seed[0])
+        if code == 44:
+            return v, False
+        _ffi.check(code)
+        return v, True
+
 
 class SpotArrayEfficiency:
     """Negative summed efficiency into a set of spot windows (the merit of the
@@ -424,6 +463,9 @@ class SpotArrayEfficiency:
         g = _torch().zeros_like(obs.data)
         self._call(obs, g[0])
         return g
+
+    def value_and_seed(self, obs, seed):
+        return self._call(obs, seed[0]), True
 
 
 def field_power(u):
