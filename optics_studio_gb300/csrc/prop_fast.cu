@@ -87,6 +87,36 @@ __global__ void k_stage_twiddles(float2* tw) {
                          gridDim.x * blockDim.x);
 }
 
+// Programmatic dependent launch (sm_90+).  The three f32 passes of a
+// propagation are launched with programmatic stream serialization: each
+// block signals at its start that the next pass may be scheduled (so the
+// next pass's blocks fill the SMs its last wave leaves idle), and each pass
+// runs its prologue that needs nothing from the pass before it (twiddle and
+// pruning tables; in pass B the H table, built from the per-axis tables of
+// the prep kernel, which every pass-A block has waited for) before
+// griddepcontrol.wait, which returns once the previous pass has completed
+// and its memory is visible.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename K, typename... Args>
+cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = getenv("OSGPU_NO_PDL") ? 0 : 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 __device__ __forceinline__ void load_ptw(float2* tb, float2* tq, const float2* __restrict__ twP, int r,
                                          int T) {
   for (int i = threadIdx.x; i < r * T; i += blockDim.x) {
@@ -312,9 +342,11 @@ __global__ void __launch_bounds__(Lay<M, 2>::THREADS, Lay<M, 2>::MINB)
   float2* buf = bufs + g * SB;
   const float2* twm = reinterpret_cast<const float2*>(a.tw_my);
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Py);
+  pdl_trigger();
   copy_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, ry, T);
   build_htab<M>(a, c, htab, threadIdx.x, NT);
+  pdl_wait();  // pass A's spectrum is complete
   __syncthreads();
   if (!active && T % 32 == 0) return;  // per-group barriers only from here on
   float2* col = reinterpret_cast<float2*>(a.work) + (size_t)kx * ny;
@@ -441,7 +473,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passA_v
 
 // ---------------------------------------------------------------- pass C
 
-template <int M, int G>
+template <int M, int G, bool ADJ>
 __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v3(PropArgs a) {
   constexpr int T = M / 16;
   constexpr int SB = Plan<M>::SMEM;
@@ -462,9 +494,10 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
   const float2* twP = reinterpret_cast<const float2*>(a.tw_Px);
   const float2* W = reinterpret_cast<const float2*>(a.work);
   constexpr int NT = Lay<M, G>::THREADS;
+  pdl_trigger();
   copy_stage_twiddles<M>(tws, twm, threadIdx.x, NT);
   load_ptw(tb, tq, twP, rx, T);
-  // first gathers before the barrier: they overlap the table loads
+  pdl_wait();  // pass B's spectrum is complete
   const int iters = (rx + G - 1) / G;
   float2 acc[16];
 #pragma unroll
@@ -498,7 +531,7 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
 #pragma unroll
     for (int gg = 1; gg < G; ++gg) v = cadd(v, bufs[gg * SB + j]);
     const size_t o = (size_t)iy * nx + j;
-    if (a.adj) {
+    if (ADJ) {  // adjoint element plane (a.adj)
       const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
       adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x, v.y);
     }
@@ -556,9 +589,10 @@ __global__ void __launch_bounds__(4 * (M / 16), 1) k_passA_r4(PropArgs a) {
   const int iy0 = blockIdx.x * 4;
   float2* buf = bufs + g * SB;
   float2* W = reinterpret_cast<float2*>(a.work);
+  pdl_trigger();
   copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
   load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
-  // inputs of the 4 rows: loads batched 8 at a time, then one status check
+  // inputs of the 4 rows: loads batched, then one status check
   constexpr int KS = 4 * M / NT;  // 16 samples per thread
   constexpr int KB = 16;          // loads in flight per batch
   bool bad = false;
@@ -581,6 +615,7 @@ __global__ void __launch_bounds__(4 * (M / 16), 1) k_passA_r4(PropArgs a) {
     }
   }
   if (a.status && bad) atomicOr(a.status, 1);
+  pdl_wait();  // the kernel before this one has completed (its workspace is ours to write)
   __syncthreads();
   const float2* xr = xin + g * M;
   for (int s = 0; s < rx; ++s) {
@@ -659,15 +694,19 @@ cudaError_t launchA_mg(const PropArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int M, int G>
-cudaError_t launchC_mg(const PropArgs& a, cudaStream_t st) {
+template <int M, int G, bool ADJ>
+cudaError_t launchC_mga(const PropArgs& a, cudaStream_t st) {
   const size_t smem = smem_v3<M, G>(2, a.ax.r, 0);
-  cudaError_t e = cudaFuncSetAttribute(k_passC_v3<M, G>,
+  cudaError_t e = cudaFuncSetAttribute(k_passC_v3<M, G, ADJ>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   ++launch_counter();
-  k_passC_v3<M, G><<<a.ny, Lay<M, G>::THREADS, smem, st>>>(a);
-  return cudaGetLastError();
+  return launch_pdl(k_passC_v3<M, G, ADJ>, dim3(a.ny), dim3(Lay<M, G>::THREADS), smem, st, a);
+}
+
+template <int M, int G>
+cudaError_t launchC_mg(const PropArgs& a, cudaStream_t st) {
+  return a.adj ? launchC_mga<M, G, true>(a, st) : launchC_mga<M, G, false>(a, st);
 }
 
 // Largest group count <= want (and <= r) whose shared memory fits, with
@@ -705,8 +744,8 @@ cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     ++launch_counter();
-    k_passB_pair<M><<<a.ax.P / 2 + 1, Lay<M, 2>::THREADS, smem, st>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(k_passB_pair<M>, dim3(a.ax.P / 2 + 1), dim3(Lay<M, 2>::THREADS), smem, st,
+                      a);
   }
   int table = even ? 1 : 0;
   if (table && smem_v3<M, 1>(1, a.ay.r, 1) > kMaxSmemB) table = 0;
@@ -725,8 +764,7 @@ cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       ++launch_counter();
-      k_passA_r4<M><<<a.ny / 4, 4 * (M / 16), smem, st>>>(a);
-      return cudaGetLastError();
+      return launch_pdl(k_passA_r4<M>, dim3(a.ny / 4), dim3(4 * (M / 16)), smem, st, a);
     }
   }
   const int g = pick_groups<M>(0, a.ax.r, 0, env_groups("OSGPU_GROUPS_A", 2));
