@@ -545,14 +545,14 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB) k_passC_v
   }
 }
 
-// ------------------------------------------------- 4-row tiles (pass A)
+// ---------------------------------------------------- row tiles (pass A)
 //
 // The spectrum is column-major (W[kx * ny + iy]), so one row of it is a
 // strided scatter with 8 bytes per 32-byte sector.  This variant gives a CTA
-// 4 adjacent rows (one group of T threads per row, every sub-transform of
-// its row in turn) and stores each sub-transform's 4-row tile through shared
-// memory in 32-byte runs W[kx * ny + iy0 .. iy0 + 3], one full sector per
-// request.  Needs ny % 4 == 0 and 4 T <= 512 threads.
+// R adjacent rows (one group of T threads per row, every sub-transform of
+// its row in turn) and stores each sub-transform's R-row tile through shared
+// memory in runs W[kx * ny + iy0 .. iy0 + R - 1] of 8 R bytes (R = 4: one
+// full sector per request).  Needs ny % R == 0 and R T <= 512 threads.
 
 // Per-sample input stage shared by the pass-A kernels.
 __device__ __forceinline__ float2 pass_a_sample(const PropArgs& a, int j, int iy, float2 x) {
@@ -572,43 +572,41 @@ __device__ __forceinline__ float2 pass_a_sample(const PropArgs& a, int j, int iy
   return x;
 }
 
-template <int M>
-__global__ void __launch_bounds__(4 * (M / 16), 1) k_passA_r4(PropArgs a) {
+template <int M, int R>
+__global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(PropArgs a) {
   constexpr int T = M / 16;
   constexpr int SB = Plan<M>::SMEM;
-  constexpr int NT = 4 * T;
+  constexpr int NT = R * T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nx = a.nx, ny = a.ny, rx = a.ax.r;
   float2* tws = reinterpret_cast<float2*>(smem_raw);
-  float2* xin = tws + TwLay<M>::SIZE;  // 4 rows of M
-  float2* bufs = xin + 4 * M;
-  float2* tb = bufs + 4 * SB;
+  float2* xin = tws + TwLay<M>::SIZE;  // R rows of M
+  float2* bufs = xin + R * M;
+  float2* tb = bufs + R * SB;
   float2* tq = tb + rx * T;
   const int g = threadIdx.x / T;
   const int tid = threadIdx.x - g * T;
-  const int iy0 = blockIdx.x * 4;
+  const int iy0 = blockIdx.x * R;
   float2* buf = bufs + g * SB;
   float2* W = reinterpret_cast<float2*>(a.work);
   pdl_trigger();
   copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
   load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
-  // inputs of the 4 rows: loads batched, then one status check
-  constexpr int KS = 4 * M / NT;  // 16 samples per thread
-  constexpr int KB = 16;          // loads in flight per batch
+  // inputs of the R rows: loads batched, then one status check
+  constexpr int KS = R * M / NT;  // 16 samples per thread
   bool bad = false;
+  {
+    float2 xs[KS];
 #pragma unroll
-  for (int h = 0; h < KS; h += KB) {
-    float2 xs[KB];
-#pragma unroll
-    for (int k = 0; k < KB; ++k) {
-      const int e = threadIdx.x + (h + k) * NT;
+    for (int k = 0; k < KS; ++k) {
+      const int e = threadIdx.x + k * NT;
       const int r = e / M, j = e - r * M;
       xs[k] = (j < nx) ? ld_in(a.in, a.in_c128, (size_t)(iy0 + r) * nx + j)
                        : make_float2(0.f, 0.f);
     }
 #pragma unroll
-    for (int k = 0; k < KB; ++k) {
-      const int e = threadIdx.x + (h + k) * NT;
+    for (int k = 0; k < KS; ++k) {
+      const int e = threadIdx.x + k * NT;
       const int r = e / M, j = e - r * M;
       bad = bad || !isfinite(xs[k].x) || !isfinite(xs[k].y);
       xin[e] = (j < nx) ? pass_a_sample(a, j, iy0 + r, xs[k]) : xs[k];
@@ -634,9 +632,12 @@ __global__ void __launch_bounds__(4 * (M / 16), 1) k_passA_r4(PropArgs a) {
     __syncthreads();
     for (int p = threadIdx.x; p < M; p += NT) {
       float4* dst = reinterpret_cast<float4*>(W + (size_t)(rx * p + s) * ny + iy0);
-      const float2 r0 = bufs[p], r1 = bufs[SB + p], r2 = bufs[2 * SB + p], r3 = bufs[3 * SB + p];
+      const float2 r0 = bufs[p], r1 = bufs[SB + p];
       dst[0] = make_float4(r0.x, r0.y, r1.x, r1.y);
-      dst[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
+      if (R == 4) {
+        const float2 r2 = bufs[2 * SB + p], r3 = bufs[3 * SB + p];
+        dst[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
+      }
     }
     __syncthreads();
   }
@@ -647,11 +648,21 @@ constexpr bool r4_ok() {
   return M >= 512 && M <= 2048;
 }
 
-template <int M>
-size_t smem_r4(int r) {
+template <int M, int R>
+size_t smem_tile(int r) {
   constexpr int T = M / 16;
-  return ((size_t)TwLay<M>::SIZE + 4 * (size_t)Plan<M>::SMEM + (size_t)r * (T + 16) +
-          4 * (size_t)M) * sizeof(float2);
+  return ((size_t)TwLay<M>::SIZE + R * (size_t)Plan<M>::SMEM + (size_t)r * (T + 16) +
+          R * (size_t)M) * sizeof(float2);
+}
+
+template <int M, int R>
+cudaError_t launch_A_tile(const PropArgs& a, cudaStream_t st) {
+  const size_t smem = smem_tile<M, R>(a.ax.r);
+  cudaError_t e = cudaFuncSetAttribute(k_passA_tile<M, R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  return launch_pdl(k_passA_tile<M, R>, dim3(a.ny / R), dim3(R * (M / 16)), smem, st, a);
 }
 
 constexpr size_t kMaxSmemB = 232448;
@@ -758,14 +769,8 @@ cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
 template <int M>
 cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
   if constexpr (r4_ok<M>()) {
-    if (a.ny % 4 == 0 && smem_r4<M>(a.ax.r) <= kMaxSmemB && !getenv("OSGPU_NO_R4")) {
-      const size_t smem = smem_r4<M>(a.ax.r);
-      cudaError_t e = cudaFuncSetAttribute(k_passA_r4<M>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      ++launch_counter();
-      return launch_pdl(k_passA_r4<M>, dim3(a.ny / 4), dim3(4 * (M / 16)), smem, st, a);
-    }
+    // 4-row tiles (2-row tiles measured the same on the 2048^2 workload)
+    if (a.ny % 4 == 0 && smem_tile<M, 4>(a.ax.r) <= kMaxSmemB) return launch_A_tile<M, 4>(a, st);
   }
   const int g = pick_groups<M>(0, a.ax.r, 0, env_groups("OSGPU_GROUPS_A", 2));
   if (g == 4) return launchA_mg<M, 4>(a, st);
