@@ -406,9 +406,10 @@ def gs_leg(args, stream):
     import torch
     from optics_studio_gb300 import gs as ggs
     from optics_studio_gb300.propagation.fraunhofer import FraunhoferConfig
+    n_t, n_it = args.gs_targets, args.gs_iters
     rng = np.random.default_rng(GS_SEED)
-    targets = gs_targets(GS_TARGETS, rng)
-    init = rng.uniform(-math.pi, math.pi, (GS_TARGETS, N, N))
+    targets = gs_targets(n_t, rng)
+    init = rng.uniform(-math.pi, math.pi, (n_t, N, N))
     c = DX * DX / (GS_LAM * GS_Z)
     scale = c * N * N  # sum |U|^2 = c^2 N^2 sum |u|^2 for a unit input
     u = torch.ones((N, N), dtype=torch.complex64, device="cuda")
@@ -424,8 +425,8 @@ def gs_leg(args, stream):
                 for i in idx]
 
     with torch.cuda.stream(stream):
-        ggs.run_batch(problems("f32", range(GS_TARGETS), 3), stream)  # warm-up
-        probs = problems("f32", range(GS_TARGETS), GS_ITERS)
+        ggs.run_batch(problems("f32", range(n_t), 3), stream)  # warm-up
+        probs = problems("f32", range(n_t), n_it)
         torch.cuda.synchronize()
         import ctypes as C
         import optics_studio_gb300 as og
@@ -449,12 +450,12 @@ def gs_leg(args, stream):
         eff32, uni32 = spot_metrics(sols[0].target_intensity.double().cpu().numpy(),
                                     targets[0][1])
         out = {"value": its / (ms / 1e3), "unit": "target-iterations/s", "ms_total": ms,
-               "targets": GS_TARGETS, "iterations_per_target": GS_ITERS,
+               "targets": n_t, "iterations_per_target": n_it,
                "workload": GS_WORKLOAD, "dtype": "f32", "kernels": kst,
                "target0": {"efficiency": eff32, "uniformity": uni32}}
         if not args.no_f64:
             t0 = time.perf_counter()
-            s64 = ggs.run_batch(problems("f64", [0], GS_ITERS), stream)[0]
+            s64 = ggs.run_batch(problems("f64", [0], n_it), stream)[0]
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
             eff64, uni64 = spot_metrics(s64.target_intensity.cpu().numpy(), targets[0][1])
@@ -522,6 +523,9 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-gs", action="store_true")
     ap.add_argument("--no-ragged", action="store_true")
+    ap.add_argument("--gs-targets", type=int, default=GS_TARGETS,
+                    help="GS leg targets (profiling runs use a smaller batch)")
+    ap.add_argument("--gs-iters", type=int, default=GS_ITERS)
     ap.add_argument("--bands", type=int, default=NBANDS,
                     help="bands per step (profiling runs use a smaller batch)")
     args = ap.parse_args()
@@ -687,12 +691,15 @@ def main():
         barrier()
         nrep = max(1, min(args.steps, 5))
         calls = []
+        eclk = ClockSampler(local)
+        eclk.start()
         t0 = time.perf_counter()
         for _ in range(nrep):
             tc = time.perf_counter()
             e2e_step()
             calls.append(NBANDS / (time.perf_counter() - tc))
         dt = max_over_ranks((time.perf_counter() - t0) / nrep * 1e3, world) / 1e3
+        e2e_clocks = eclk.stop()
         barrier()
         # the host link's own pinned copy rates on this machine (one 2 GiB copy each way)
         dev = torch.empty((NBANDS, N, N), dtype=torch.complex128, device="cuda")
@@ -712,7 +719,7 @@ def main():
                        "d2h_bytes_per_step": NBANDS * N * N * 16,
                        "api": "osgpu_beamline_trace_batch (host complex128, pinned; copies "
                               "pipelined against the traces), f32 engine",
-                       "host_link": link, "calls": nrep,
+                       "host_link": link, "calls": nrep, "clocks": e2e_clocks,
                        "per_call_rates": [round(r, 1) for r in calls]}
 
     # adjoint gradients of the inverse-design workload
