@@ -214,6 +214,34 @@ int osgpu_rs_sampling_report(const osgpu_grid* g, double z, const osgpu_rs_confi
 int osgpu_rs_propagate(const double* in, double* out, const osgpu_grid* g, double z,
                        const osgpu_rs_config* cfg, int32_t precision, osgpu_rs_report* report);
 
+/* --------------------------------------------------------------- fft */
+/* fft::fft2 / fft::ifft2 (propagation/fft.rs:40-108): 2D DFT of a row-major
+ * ny x nx complex grid in the NumPy convention (forward unnormalised with
+ * kernel e^{-2 pi i k n / N}, inverse scaled by 1/(nx ny), unshifted bins),
+ * any sizes the shared-memory plan holds.  Host complex128 buffers (may
+ * alias); precision OSGPU_F64, or OSGPU_F32 (computed in f32). */
+int osgpu_fft2(const double* in, double* out, uint64_t nx, uint64_t ny, int32_t inverse,
+               int32_t precision);
+/* Device variant: complex128 (f64 engine) or complex64 (f32 engine) buffers
+ * (may not alias), asynchronous on `stream` (NULL: the library stream). */
+int osgpu_fft2_device(const void* d_in, void* d_out, int32_t dtype, uint64_t nx, uint64_t ny,
+                      int32_t inverse, void* stream);
+
+/* --------------------------------------------------------------- sources */
+/* Source fields written on the device (complex128 or complex64 per dtype),
+ * per sample in FP64: sources::gaussian, the q-form beam at distance z from
+ * its waist (sources.rs:259-296; invalid beam or plane: OSGPU_E_BAD_ARGUMENT),
+ * BandField::plane_wave (field.rs:360-386) and BandField::uniform
+ * (field.rs:315-330).  Asynchronous on `stream` (NULL: the library stream). */
+int osgpu_source_gaussian_device(void* d_out, int32_t dtype, const osgpu_grid* g, double w0,
+                                 double amplitude, double center_x, double center_y, double z,
+                                 void* stream);
+int osgpu_source_plane_wave_device(void* d_out, int32_t dtype, const osgpu_grid* g,
+                                   double theta_x, double theta_y, double amplitude,
+                                   void* stream);
+int osgpu_source_uniform_device(void* d_out, int32_t dtype, const osgpu_grid* g,
+                                double amplitude, double phase, void* stream);
+
 /* --------------------------------------------------------------- elements */
 enum {
   OSGPU_EL_ELLIPTICAL_APERTURE = 1, /* element.rs:635-790 */

@@ -208,6 +208,17 @@ SIGNATURES = [
       C.POINTER(C.c_void_p)]),
     ("osgpu_graph_launch", C.c_int, [C.c_void_p, C.c_void_p]),
     ("osgpu_graph_destroy", C.c_int, [C.c_void_p]),
+    ("osgpu_source_gaussian_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.POINTER(Grid), C.c_double, C.c_double, C.c_double, C.c_double,
+      C.c_double, C.c_void_p]),
+    ("osgpu_source_plane_wave_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.POINTER(Grid), C.c_double, C.c_double, C.c_double, C.c_void_p]),
+    ("osgpu_source_uniform_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.POINTER(Grid), C.c_double, C.c_double, C.c_void_p]),
+    ("osgpu_fft2", C.c_int, [c_double_p, c_double_p, C.c_uint64, C.c_uint64, C.c_int32,
+                             C.c_int32]),
+    ("osgpu_fft2_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_uint64, C.c_uint64,
+                                    C.c_int32, C.c_void_p]),
     ("osgpu_tape_create", C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
     ("osgpu_tape_destroy", C.c_int, [C.c_void_p]),
     ("osgpu_tape_bytes", C.c_uint64, [C.c_void_p]),

@@ -49,11 +49,11 @@ struct ProfRec {
   double bytes;
 };
 enum { PC_PREP = 0, PC_ELEMENTS, PC_APPLY, PC_PASS_A, PC_PASS_B, PC_PASS_C, PC_KSPEC, PC_FRAUN,
-       PC_GS, PC_GS_COLS, PC_GS_ROWS, PC_N };
+       PC_GS, PC_GS_COLS, PC_GS_ROWS, PC_FFT2, PC_N };
 const char* kProfNames[PC_N] = {"prep_tables", "element_tables", "element_apply",
                                 "pass_a_rows", "pass_b_columns", "pass_c_rows",
                                 "kernel_spectrum", "fraunhofer", "gs_planes", "gs_columns",
-                                "gs_rows"};
+                                "gs_rows", "fft2"};
 
 struct Context {
   std::recursive_mutex mu;
@@ -458,6 +458,51 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
     ProfScope ps(c, st, PC_PASS_C, nsp * es + nin * ob + adj_bytes);
     CK(launch_passC<T>(a, st));
   }
+  return OSGPU_OK;
+}
+
+// fft::transform2 of an nx x ny grid: forward (unnormalised) or inverse
+// (1/(nx ny)) through conj(fft2(conj x)) / N.
+template <typename T>
+int run_fft2(Context& c, const void* d_in, int in_c128, void* d_out, int out_c128, int nx, int ny,
+             int inverse, cudaStream_t st) {
+  const int is_d = sizeof(T) == 8;
+  const size_t es = is_d ? 16 : 8;
+  PropArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nx = nx;
+  a.ny = ny;
+  a.ax = make_axis(nx, nx);
+  a.ay = make_axis(ny, ny);
+  if (a.ax.nst < 0 || a.ay.nst < 0 || smem_passA_bytes(a.ax, is_d, 1) > kMaxSmem ||
+      smem_passB_bytes(a.ay, is_d) > kMaxSmem) {
+    set_err("fft2 of %dx%d exceeds the shared-memory plan of this build", nx, ny);
+    return OSGPU_E_UNSUPPORTED;
+  }
+  int rc;
+  if ((rc = get_tw(c, nx, is_d, &a.tw_mx))) return rc;
+  if ((rc = get_tw(c, ny, is_d, &a.tw_my))) return rc;
+  a.tw_Px = a.tw_mx;
+  a.tw_Py = a.tw_my;
+  const size_t n = (size_t)nx * ny;
+  DBuf ws;
+  CK(ws.alloc(align256(n * es) * (inverse ? 3 : 2), st));
+  char* base = reinterpret_cast<char*>(ws.p);
+  a.work = base;
+  void* spec = base + align256(n * es);
+  a.in = d_in;
+  a.in_c128 = in_c128;
+  if (inverse) {  // conj(x) in the engine's type
+    void* tmp = base + 2 * align256(n * es);
+    CK(launch_conj_copy<T>(d_in, in_c128, tmp, n, st));
+    a.in = tmp;
+    a.in_c128 = is_d;
+  }
+  a.engine = ENG_IDENTITY;
+  a.scale = inverse ? 1.0 / ((double)nx * (double)ny) : 1.0;
+  a.status = nullptr;  // transform2 does not validate samples
+  ProfScope ps(c, st, PC_FFT2, (double)n * (2 * es + 4 * es));
+  CK(launch_fft2<T>(a, spec, d_out, out_c128, inverse, st));
   return OSGPU_OK;
 }
 
@@ -1013,6 +1058,46 @@ int osgpu_asm_propagate(const double* in, double* out, const osgpu_grid* g, doub
     j.out_c128 = 1;
     return run_prop_dispatch(c, j, precision == OSGPU_F32, c.stream);
   });
+}
+
+int osgpu_fft2(const double* in, double* out, uint64_t nx, uint64_t ny, int32_t inverse,
+               int32_t precision) {
+  int rc;
+  if ((rc = check_precision(precision))) return rc;
+  if (!in || !out) return OSGPU_E_BAD_ARGUMENT;
+  if (nx == 0 || ny == 0) return OSGPU_OK;  // nothing to transform (fft.rs:41-44)
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  const size_t n = nx * ny;
+  DBuf din, dout;
+  CK(din.alloc(n * 16, c.stream));
+  CK(dout.alloc(n * 16, c.stream));
+  CK(cudaMemcpyAsync(din.p, in, n * 16, cudaMemcpyHostToDevice, c.stream));
+  rc = precision == OSGPU_F32
+           ? run_fft2<float>(c, din.p, 1, dout.p, 1, (int)nx, (int)ny, inverse, c.stream)
+           : run_fft2<double>(c, din.p, 1, dout.p, 1, (int)nx, (int)ny, inverse, c.stream);
+  if (rc) {
+    cudaStreamSynchronize(c.stream);
+    return rc;
+  }
+  CK(cudaMemcpyAsync(out, dout.p, n * 16, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return OSGPU_OK;
+}
+
+int osgpu_fft2_device(const void* d_in, void* d_out, int32_t dtype, uint64_t nx, uint64_t ny,
+                      int32_t inverse, void* stream) {
+  if (!d_in || !d_out || (dtype != OSGPU_C128 && dtype != OSGPU_C64)) return OSGPU_E_BAD_ARGUMENT;
+  if (nx == 0 || ny == 0) return OSGPU_OK;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int c128 = dtype == OSGPU_C128;
+  return c128 ? run_fft2<double>(c, d_in, 1, d_out, 1, (int)nx, (int)ny, inverse, st)
+              : run_fft2<float>(c, d_in, 0, d_out, 0, (int)nx, (int)ny, inverse, st);
 }
 
 int osgpu_asm_propagate_device(const void* d_in, void* d_out, int32_t dtype,
@@ -1969,6 +2054,81 @@ int osgpu_adam_step_device(double* d_x, float* d_x32, const void* d_g, int32_t g
   double* part = reinterpret_cast<double*>(scr.p);
   double* norm2 = part + (reduce_scratch_bytes(1) / sizeof(double) - 3);
   CK(launch_adam(d_x, d_x32, d_g, g_real_dtype == OSGPU_F64, d_m, d_v, n, p, part, norm2, st));
+  return OSGPU_OK;
+}
+
+// ------------------------------------------------------------ sources
+
+namespace {
+int source_prologue(void* d_out, int32_t dtype, const osgpu_grid* g, Context*& cp,
+                    cudaStream_t& st, void* stream) {
+  if (!d_out || !g || (dtype != OSGPU_C128 && dtype != OSGPU_C64)) return OSGPU_E_BAD_ARGUMENT;
+  if (g->nx == 0 || g->ny == 0) return OSGPU_E_EMPTY_GRID;
+  if (!(std::isfinite(g->lambda) && g->lambda > 0.0)) return OSGPU_E_INVALID_WAVELENGTH;
+  Context& c = ctx();
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cp = &c;
+  st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  return OSGPU_OK;
+}
+}  // namespace
+
+int osgpu_source_gaussian_device(void* d_out, int32_t dtype, const osgpu_grid* g, double w0,
+                                 double amplitude, double center_x, double center_y, double z,
+                                 void* stream) {
+  Context* c = nullptr;
+  cudaStream_t st;
+  int rc;
+  if ((rc = source_prologue(d_out, dtype, g, c, st, stream))) return rc;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  if (!(std::isfinite(w0) && w0 > 0.0 && std::isfinite(amplitude) && std::isfinite(center_x) &&
+        std::isfinite(center_y))) {
+    set_err("invalid beam");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  if (!std::isfinite(z)) {
+    set_err("invalid plane z");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  // q-form beam at distance z from the waist (sources.rs:259-296)
+  const double lam = g->lambda;
+  const double z_r = PI * w0 * w0 / lam;
+  const double w_z = w0 * std::sqrt(1.0 + (z / z_r) * (z / z_r));
+  const double k = 2.0 * PI / lam;
+  const double inv_r = z / (z * z + z_r * z_r);
+  const double carrier = k * z - std::atan(z / z_r);
+  const double amp = amplitude * w0 / w_z;
+  CK(launch_gaussian(d_out, dtype == OSGPU_C128, (int)g->nx, (int)g->ny, g->dx, g->dy, center_x,
+                     center_y, amp, w_z * w_z, 0.5 * k, inv_r, carrier, st));
+  return OSGPU_OK;
+}
+
+int osgpu_source_plane_wave_device(void* d_out, int32_t dtype, const osgpu_grid* g,
+                                   double theta_x, double theta_y, double amplitude,
+                                   void* stream) {
+  Context* c = nullptr;
+  cudaStream_t st;
+  int rc;
+  if ((rc = source_prologue(d_out, dtype, g, c, st, stream))) return rc;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  // BandField::plane_wave (field.rs:360-386)
+  const double k = 2.0 * PI / g->lambda;
+  CK(launch_plane_wave(d_out, dtype == OSGPU_C128, (int)g->nx, (int)g->ny, g->dx, g->dy,
+                       amplitude, k, std::sin(theta_x), std::sin(theta_y), st));
+  return OSGPU_OK;
+}
+
+int osgpu_source_uniform_device(void* d_out, int32_t dtype, const osgpu_grid* g,
+                                double amplitude, double phase, void* stream) {
+  Context* c = nullptr;
+  cudaStream_t st;
+  int rc;
+  if ((rc = source_prologue(d_out, dtype, g, c, st, stream))) return rc;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  // BandField::uniform (field.rs:315-330): A e^{i phase}
+  CK(launch_fill(d_out, dtype == OSGPU_C128, (size_t)(g->nx * g->ny),
+                 amplitude * std::cos(phase), amplitude * std::sin(phase), st));
   return OSGPU_OK;
 }
 

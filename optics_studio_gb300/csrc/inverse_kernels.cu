@@ -562,6 +562,47 @@ __global__ void k_gs_init(const void* init, void* phase, int f64, double lo, dou
   }
 }
 
+// ------------------------------------------------------------ sources
+// (reference sources.rs:259-296, field.rs:315-386): per sample in FP64,
+// scalars of the beam formed on the host in the reference's order.
+__global__ void k_gaussian(void* out, int c128, int nx, int ny, double dx, double dy, double cx,
+                           double cy, double amp, double w2, double half_k, double inv_r,
+                           double carrier) {
+  const size_t n = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(k % nx), iy = (int)(k / nx);
+    const double x = __dsub_rn(coord_d(ix, nx, dx), cx);
+    const double y = __dsub_rn(coord_d(iy, ny, dy), cy);
+    const double rho2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+    const double env = __dmul_rn(amp, exp(__ddiv_rn(-rho2, w2)));
+    const double ph = __dadd_rn(carrier, __dmul_rn(__dmul_rn(half_k, rho2), inv_r));
+    double s, c;
+    sincos(ph, &s, &c);
+    st_cx<double>(out, c128, k, __dmul_rn(env, c), __dmul_rn(env, s));
+  }
+}
+
+__global__ void k_plane_wave(void* out, int c128, int nx, int ny, double dx, double dy,
+                             double amp, double k_, double alpha, double beta) {
+  const size_t n = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(k % nx), iy = (int)(k / nx);
+    const double x = coord_d(ix, nx, dx), y = coord_d(iy, ny, dy);
+    const double ph = __dmul_rn(k_, __dadd_rn(__dmul_rn(alpha, x), __dmul_rn(beta, y)));
+    double s, c;
+    sincos(ph, &s, &c);
+    st_cx<double>(out, c128, k, __dmul_rn(amp, c), __dmul_rn(amp, s));
+  }
+}
+
+__global__ void k_fill(void* out, int c128, size_t n, double re, double im) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    st_cx<double>(out, c128, k, re, im);
+}
+
 int red_blocks(uint64_t n) {
   const uint64_t b = (n + kRedThreads - 1) / kRedThreads;
   return (int)(b < 1216 ? (b ? b : 1) : 1216);  // <= 8 per SM on 152 SMs
@@ -755,6 +796,30 @@ cudaError_t launch_gs_fold_update_batch(const GsFoldItem* items, int n_items, in
   OSGPU_LAUNCH;
   k_gs_fold_update_batch<<<n_items, kRedThreads, 0, st>>>(items, nb, n, it, patience, tol,
                                                           max_it);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gaussian(void* out, int c128, int nx, int ny, double dx, double dy, double cx,
+                            double cy, double amp, double w2, double half_k, double inv_r,
+                            double carrier, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_gaussian<<<red_blocks((uint64_t)nx * ny), kRedThreads, 0, st>>>(out, c128, nx, ny, dx, dy, cx,
+                                                                    cy, amp, w2, half_k, inv_r,
+                                                                    carrier);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plane_wave(void* out, int c128, int nx, int ny, double dx, double dy,
+                              double amp, double k, double alpha, double beta, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_plane_wave<<<red_blocks((uint64_t)nx * ny), kRedThreads, 0, st>>>(out, c128, nx, ny, dx, dy,
+                                                                      amp, k, alpha, beta);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill(void* out, int c128, size_t n, double re, double im, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_fill<<<red_blocks(n), kRedThreads, 0, st>>>(out, c128, n, re, im);
   return cudaGetLastError();
 }
 

@@ -66,6 +66,14 @@ cudaError_t launch_gs_update(const void* v, int c128, void* phase, void* best, i
                              void* dphi_out, GsState* state, GsRecordDev* hist, int it,
                              int patience, double tol, int max_it, cudaStream_t st);
 
+// Sources (see inverse_kernels.cu).
+cudaError_t launch_gaussian(void* out, int c128, int nx, int ny, double dx, double dy, double cx,
+                            double cy, double amp, double w2, double half_k, double inv_r,
+                            double carrier, cudaStream_t st);
+cudaError_t launch_plane_wave(void* out, int c128, int nx, int ny, double dx, double dy,
+                              double amp, double k, double alpha, double beta, cudaStream_t st);
+cudaError_t launch_fill(void* out, int c128, size_t n, double re, double im, cudaStream_t st);
+
 cudaError_t launch_apply_intensity(const void* in, int in_c128, void* out, int out_c128,
                                    const ElementList& els, int nx, int ny, double dx, double dy,
                                    void* inten, int inten_f64, int f32, cudaStream_t st);

@@ -852,6 +852,70 @@ cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStr
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ plain 2D DFT
+
+// Input stage of an inverse transform: dst = conj(src) in the engine's type.
+template <typename T>
+__global__ void k_conj_copy(const void* src, int c128, cx<T>* dst, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  cx<T> v = load_in<T>(src, c128, i);
+  v.y = -v.y;
+  dst[i] = v;
+}
+
+// Column-major spectrum S[kx * ny + ky] -> row-major out[ky * nx + kx]
+// (conjugated for an inverse), 32 x 32 tiles through shared memory.
+template <typename T>
+__global__ void k_fft2_finish(const cx<T>* S, int nx, int ny, void* out, int out_c128, int conj) {
+  __shared__ cx<T> tile[32][33];
+  const int kx0 = blockIdx.x * 32, ky0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int kx = kx0 + j, ky = ky0 + threadIdx.x;
+    if (kx < nx && ky < ny) tile[j][threadIdx.x] = S[(size_t)kx * ny + ky];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int ky = ky0 + j, kx = kx0 + threadIdx.x;
+    if (kx < nx && ky < ny) {
+      cx<T> v = tile[threadIdx.x][j];
+      if (conj) v.y = -v.y;
+      store_out<T>(out, out_c128, (size_t)ky * nx + kx, v);
+    }
+  }
+}
+
+// fft::transform2 (reference propagation/fft.rs:40-108) on the device: row
+// transforms (pass A with P = n), forward-only column transforms (pass B,
+// scaled by a.scale), then the transpose to row-major.  `a` carries the
+// full-support axis plans, twiddles, engine ENG_IDENTITY and the input;
+// `spec` is an nx * ny scratch of the engine's type.
+template <typename T>
+cudaError_t launch_fft2(const PropArgs& a, void* spec, void* out, int out_c128, int conj,
+                        cudaStream_t st) {
+  cudaError_t e = launch_passA<T>(a, st);
+  if (e != cudaSuccess) return e;
+  e = launch_passB_impl<T>(a, 1, spec, st);
+  if (e != cudaSuccess) return e;
+  COUNT_LAUNCH();
+  k_fft2_finish<T><<<dim3((a.nx + 31) / 32, (a.ny + 31) / 32), dim3(32, 8), 0, st>>>(
+      reinterpret_cast<const cx<T>*>(spec), a.nx, a.ny, out, out_c128, conj);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_conj_copy(const void* src, int c128, void* dst, size_t n, cudaStream_t st) {
+  COUNT_LAUNCH();
+  k_conj_copy<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, c128,
+                                                                reinterpret_cast<cx<T>*>(dst), n);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_fft2<float>(const PropArgs&, void*, void*, int, int, cudaStream_t);
+template cudaError_t launch_fft2<double>(const PropArgs&, void*, void*, int, int, cudaStream_t);
+template cudaError_t launch_conj_copy<float>(const void*, int, void*, size_t, cudaStream_t);
+template cudaError_t launch_conj_copy<double>(const void*, int, void*, size_t, cudaStream_t);
+
 // ------------------------------------------------------------ Fraunhofer
 
 // Pass FA: offset-DFT pre-phase and off-axis ramp (reference

@@ -95,6 +95,12 @@ template <typename T> cudaError_t launch_passA(const PropArgs& a, cudaStream_t s
 template <typename T> cudaError_t launch_passB(const PropArgs& a, cudaStream_t st);
 template <typename T> cudaError_t launch_passC(const PropArgs& a, cudaStream_t st);
 template <typename T> cudaError_t launch_fraunhofer(const FraunArgs& a, cudaStream_t st);
+// Plain 2D DFT (see prop_kernels.cu) and the conjugating copy of an inverse.
+template <typename T>
+cudaError_t launch_fft2(const PropArgs& a, void* spec, void* out, int out_c128, int conj,
+                        cudaStream_t st);
+template <typename T>
+cudaError_t launch_conj_copy(const void* src, int c128, void* dst, size_t n, cudaStream_t st);
 
 cudaError_t launch_twiddles(void* dst, int n, int is_double, cudaStream_t st);
 // f32 tables of register-FFT lengths (reg_fft_size): fills the stage-ordered
