@@ -196,6 +196,97 @@ static __device__ __forceinline__ float2 apply_elements_fast(const ElementList& 
   return v;
 }
 
+// The same transmissions for K samples of one thread at (ix[k], iy[k]),
+// element by element, so that the table and lattice loads of all K samples
+// are in flight together (the per-sample form above chains them sample after
+// sample).  Samples whose bit in `live` is clear are left untouched and read
+// no table (zero padding); a sample outside an element's transmitting set
+// becomes zero, as in apply_one_fast.  K <= 32.
+template <int K>
+static __device__ __forceinline__ void apply_elements_fast_k(const ElementList& L,
+                                                             const int (&ix)[K],
+                                                             const int (&iy)[K], unsigned live,
+                                                             float2 (&v)[K]) {
+  const unsigned inb = live;
+  for (int q = 0; q < L.count; ++q) {
+    const DevElement& e = L.el[q];
+    unsigned pass = inb;
+    if (e.span) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int2 sp = (inb >> k & 1u) ? __ldg(e.span + iy[k]) : make_int2(0, -1);
+        if (ix[k] < sp.x || ix[k] > sp.y) pass &= ~(1u << k);
+      }
+    }
+    switch (e.kind) {
+      case EL_LENS:
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if (!(inb >> k & 1u)) continue;
+          const float2 a = __ldg(e.tabx + ix[k]), b = __ldg(e.taby + iy[k]);
+          const float2 t = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+          v[k] = make_float2(v[k].x * t.x - v[k].y * t.y, v[k].x * t.y + v[k].y * t.x);
+        }
+        break;
+      case EL_GRATING:
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if (!(inb >> k & 1u)) continue;
+          const float2 t = __ldg(e.tabx + ix[k]);
+          v[k] = make_float2(v[k].x * t.x - v[k].y * t.y, v[k].x * t.y + v[k].y * t.x);
+        }
+        break;
+      case EL_PHASE: {
+        float phi[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          phi[k] = 0.f;
+          if (!(inb >> k & 1u)) continue;
+          const int4 bx = __ldg(e.bilx + ix[k]), by = __ldg(e.bily + iy[k]);
+          if (!(bx.w && by.w)) continue;
+          const float* r0 = e.latf + (size_t)by.x * e.lnx;
+          const float v00 = __ldg(r0 + bx.x);
+          if (bx.z == 0 && by.z == 0) {
+            phi[k] = v00;
+          } else {
+            const float tx = __int_as_float(bx.z), ty = __int_as_float(by.z);
+            const float* r1 = e.latf + (size_t)by.y * e.lnx;
+            const float v10 = __ldg(r0 + bx.y), v01 = __ldg(r1 + bx.x), v11 = __ldg(r1 + bx.y);
+            const float A = v00 + (v10 - v00) * tx;
+            const float B = v01 + (v11 - v01) * tx;
+            phi[k] = A + (B - A) * ty;
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if (!(inb >> k & 1u)) continue;
+          const float nq = rintf(phi[k] * 0.159154943091895336f);
+          float rr = fmaf(-nq, 6.28125f, phi[k]);
+          rr = fmaf(-nq, 1.93530717958647692e-3f, rr);
+          float sn, cs;
+          __sincosf(rr, &sn, &cs);
+          v[k] = make_float2(v[k].x * cs - v[k].y * sn, v[k].x * sn + v[k].y * cs);
+        }
+        break;
+      }
+      case EL_SCREEN:
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if (!(inb >> k & 1u)) continue;
+          const float2 t = __ldg(e.scr + (size_t)iy[k] * e.lnx + ix[k]);
+          v[k] = make_float2(v[k].x * t.x - v[k].y * t.y, v[k].x * t.y + v[k].y * t.x);
+        }
+        break;
+      default:
+        break;
+    }
+    live &= pass;
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if ((inb >> k & 1u) && !(live >> k & 1u)) v[k] = make_float2(0.f, 0.f);
+}
+
 // Adjoint element plane at sample (ix, iy) (reference adjoint.rs:205-227,
 // element by element in reverse): the chain L acted on the forward field
 // u (the field entering the plane); mu is the adjoint field arriving from

@@ -572,45 +572,85 @@ __device__ __forceinline__ float2 pass_a_sample(const PropArgs& a, int j, int iy
   return x;
 }
 
+// Exchange-buffer stride of the row-tile kernel: the FFT's padded size plus
+// 4 entries, so that buffers 0..3 start 0, 8, 16 and 24 banks apart and the
+// paired-lane spectrum stores read them without bank conflicts.
+template <int M>
+__host__ __device__ constexpr int tile_stride() {
+  return Plan<M>::SMEM + 4;
+}
+
 template <int M, int R>
 __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(PropArgs a) {
   constexpr int T = M / 16;
-  constexpr int SB = Plan<M>::SMEM;
+  constexpr int SBT = tile_stride<M>();
   constexpr int NT = R * T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nx = a.nx, ny = a.ny, rx = a.ax.r;
   float2* tws = reinterpret_cast<float2*>(smem_raw);
   float2* xin = tws + TwLay<M>::SIZE;  // R rows of M
   float2* bufs = xin + R * M;
-  float2* tb = bufs + R * SB;
+  float2* tb = bufs + R * SBT;
   float2* tq = tb + rx * T;
   const int g = threadIdx.x / T;
   const int tid = threadIdx.x - g * T;
   const int iy0 = blockIdx.x * R;
-  float2* buf = bufs + g * SB;
+  float2* buf = bufs + g * SBT;
   float2* W = reinterpret_cast<float2*>(a.work);
   pdl_trigger();
   copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
   load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
   // inputs of the R rows: loads batched, then one status check
   constexpr int KS = R * M / NT;  // 16 samples per thread
+  static_assert(KS <= 32, "sample mask is 32 bits");
   bool bad = false;
   {
     float2 xs[KS];
+    int jx[KS], jy[KS];
+    unsigned inb = 0;
 #pragma unroll
     for (int k = 0; k < KS; ++k) {
       const int e = threadIdx.x + k * NT;
       const int r = e / M, j = e - r * M;
+      jx[k] = j;
+      jy[k] = iy0 + r;
+      if (j < nx) inb |= 1u << k;
       xs[k] = (j < nx) ? ld_in(a.in, a.in_c128, (size_t)(iy0 + r) * nx + j)
                        : make_float2(0.f, 0.f);
     }
 #pragma unroll
-    for (int k = 0; k < KS; ++k) {
-      const int e = threadIdx.x + k * NT;
-      const int r = e / M, j = e - r * M;
-      bad = bad || !isfinite(xs[k].x) || !isfinite(xs[k].y);
-      xin[e] = (j < nx) ? pass_a_sample(a, j, iy0 + r, xs[k]) : xs[k];
+    for (int k = 0; k < KS; ++k) bad = bad || !isfinite(xs[k].x) || !isfinite(xs[k].y);
+    // per-sample stage, each kind for all KS samples at once (loads in flight together)
+    if (a.seed) {
+#pragma unroll
+      for (int k = 0; k < KS; ++k)
+        if (inb >> k & 1u) xs[k] = pass_a_sample(a, jx[k], jy[k], xs[k]);
+    } else if (a.els.count && !a.adj) {
+      if (a.els.fast) {
+        // two halves of KS / 2 samples (bounded register pressure)
+        constexpr int KH = KS / 2;
+        float2 xh[KH];
+        int hx[KH], hy[KH];
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+#pragma unroll
+          for (int k = 0; k < KH; ++k) {
+            xh[k] = xs[hh * KH + k];
+            hx[k] = jx[hh * KH + k];
+            hy[k] = jy[hh * KH + k];
+          }
+          apply_elements_fast_k<KH>(a.els, hx, hy, (inb >> (hh * KH)) & ((1u << KH) - 1u), xh);
+#pragma unroll
+          for (int k = 0; k < KH; ++k) xs[hh * KH + k] = xh[k];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < KS; ++k)
+          if (inb >> k & 1u) xs[k] = pass_a_sample(a, jx[k], jy[k], xs[k]);
+      }
     }
+#pragma unroll
+    for (int k = 0; k < KS; ++k) xin[threadIdx.x + k * NT] = xs[k];
   }
   if (a.status && bad) atomicOr(a.status, 1);
   pdl_wait();  // the kernel before this one has completed (its workspace is ours to write)
@@ -630,14 +670,14 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(Pro
 #pragma unroll
     for (int q = 0; q < 16; ++q) buf[tid + T * q] = v[q];
     __syncthreads();
-    for (int p = threadIdx.x; p < M; p += NT) {
-      float4* dst = reinterpret_cast<float4*>(W + (size_t)(rx * p + s) * ny + iy0);
-      const float2 r0 = bufs[p], r1 = bufs[SB + p];
-      dst[0] = make_float4(r0.x, r0.y, r1.x, r1.y);
-      if (R == 4) {
-        const float2 r2 = bufs[2 * SB + p], r3 = bufs[3 * SB + p];
-        dst[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
-      }
+    // 16 bytes (two rows) per lane; with R = 4 the two lanes of a pair write
+    // the two halves of one 32-byte run, so a warp store covers whole sectors
+    constexpr int HV = R / 2;
+    for (int h = threadIdx.x; h < HV * M; h += NT) {
+      const int p = h / HV, hf = h - p * HV;
+      float4* dst = reinterpret_cast<float4*>(W + (size_t)(rx * p + s) * ny + iy0) + hf;
+      const float2 r0 = bufs[2 * hf * SBT + p], r1 = bufs[(2 * hf + 1) * SBT + p];
+      *dst = make_float4(r0.x, r0.y, r1.x, r1.y);
     }
     __syncthreads();
   }
@@ -651,7 +691,7 @@ constexpr bool r4_ok() {
 template <int M, int R>
 size_t smem_tile(int r) {
   constexpr int T = M / 16;
-  return ((size_t)TwLay<M>::SIZE + R * (size_t)Plan<M>::SMEM + (size_t)r * (T + 16) +
+  return ((size_t)TwLay<M>::SIZE + R * (size_t)tile_stride<M>() + (size_t)r * (T + 16) +
           R * (size_t)M) * sizeof(float2);
 }
 
