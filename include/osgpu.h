@@ -562,6 +562,31 @@ typedef struct {
 int osgpu_profile_begin(void);
 int osgpu_profile_end(osgpu_kernel_stat* out, int32_t max_out, int32_t* n_out);
 
+/* ------------------------------------------------- kernel-spectrum plans */
+/* No counterpart in the reference (its ASM recomputes H on every call,
+ * src/propagation/asm.rs:505-522).  An f32 ASM propagation whose padded grid
+ * exceeds twice the field only reaches kernel offsets |d| < n, so it equals a
+ * circular convolution of period 2n with the kernel h = IFFT_P(H) restricted
+ * to those offsets.  With plans enabled, the first f32 ASM propagation of a
+ * given (grid, pitch, wavelength, medium, |z|, padding, band limits) builds
+ * that kernel's spectrum once (an FP64 propagation of a unit sample, then a
+ * 2n x 2n FP64 transform, rounded to an f32 quarter table of (nx+1)(ny+1)
+ * entries) and every later one, forward (+z) or adjoint (-z, the conjugate
+ * table), runs at 2n instead of the padded size.  Applies to power-of-two
+ * sides 256..4096 on streams that are not being captured; other calls take
+ * the padded path.  Tables are evicted least recently used beyond max_bytes
+ * (eviction synchronises the device).  Off by default. */
+typedef struct {
+  uint64_t plans;   /* tables held */
+  uint64_t bytes;   /* device bytes held */
+  uint64_t hits;    /* propagations that used a held table */
+  uint64_t builds;  /* tables built */
+} osgpu_plan_stats;
+
+int osgpu_plan_cache_config(int32_t enable, uint64_t max_bytes);
+int osgpu_plan_cache_clear(void);
+int osgpu_plan_cache_stats(osgpu_plan_stats* out);
+
 /* ---------------------------------------------------------------- runtime */
 int osgpu_init(int32_t device);
 /* Copies the last error message (NUL-terminated, truncated to len). */

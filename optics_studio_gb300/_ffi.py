@@ -156,6 +156,11 @@ class KernelStatC(C.Structure):
                 ("bytes", C.c_double)]
 
 
+class PlanStatsC(C.Structure):
+    _fields_ = [("plans", C.c_uint64), ("bytes", C.c_uint64), ("hits", C.c_uint64),
+                ("builds", C.c_uint64)]
+
+
 # (name, restype, argtypes) for every symbol of include/osgpu.h
 SIGNATURES = [
     ("osgpu_init", C.c_int, [C.c_int32]),
@@ -248,6 +253,9 @@ SIGNATURES = [
     ("osgpu_asm_propagate_noalloc", C.c_int,
      [C.c_void_p, C.c_void_p, C.POINTER(Grid), C.c_double, C.POINTER(AsmConfigC), C.c_void_p,
       C.POINTER(AsmReportC)]),
+    ("osgpu_plan_cache_config", C.c_int, [C.c_int32, C.c_uint64]),
+    ("osgpu_plan_cache_clear", C.c_int, []),
+    ("osgpu_plan_cache_stats", C.c_int, [C.POINTER(PlanStatsC)]),
     ("osgpu_profile_begin", C.c_int, []),
     ("osgpu_profile_end", C.c_int, [C.POINTER(KernelStatC), C.c_int32, C.POINTER(C.c_int32)]),
 ]

@@ -49,11 +49,23 @@ struct ProfRec {
   double bytes;
 };
 enum { PC_PREP = 0, PC_ELEMENTS, PC_APPLY, PC_PASS_A, PC_PASS_B, PC_PASS_C, PC_KSPEC, PC_FRAUN,
-       PC_GS, PC_GS_COLS, PC_GS_ROWS, PC_FFT2, PC_N };
+       PC_GS, PC_GS_COLS, PC_GS_ROWS, PC_FFT2, PC_PLAN, PC_N };
 const char* kProfNames[PC_N] = {"prep_tables", "element_tables", "element_apply",
                                 "pass_a_rows", "pass_b_columns", "pass_c_rows",
                                 "kernel_spectrum", "fraunhofer", "gs_planes", "gs_columns",
-                                "gs_rows", "fft2"};
+                                "gs_rows", "fft2", "plan_build"};
+
+// Kernel-spectrum plan of an f32 ASM propagation whose padded grid exceeds
+// twice the field (prop_kernels.cu, launch_even_kspec): keyed by everything
+// that determines H and the padding; |z| (the plan of -z is the conjugate).
+struct KPlan {
+  uint64_t nx, ny, Px, Py;
+  double dx, dy, lam, medium, zabs, lim_x, lim_y;
+  int band_limited;
+  void* kq = nullptr;  // f32 quarter table, (nx + 1) x (ny + 1)
+  size_t bytes = 0;
+  uint64_t last_use = 0;
+};
 
 struct Context {
   std::recursive_mutex mu;
@@ -66,6 +78,11 @@ struct Context {
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> event_pool;
   std::map<const void*, float*> lattices;  // osgpu_lattice_create handle -> f32 copy
+  // kernel-spectrum plans (osgpu_plan_cache_config); off by default
+  bool plans_on = false;
+  size_t plan_cap = 0, plan_bytes = 0;
+  uint64_t plan_tick = 0, plan_hits = 0, plan_builds = 0;
+  std::vector<KPlan> plans;
 };
 
 Context& ctx() {
@@ -296,14 +313,161 @@ struct PropJob {
   const void* adj_uin;
   int adj_uin_c128;
   void* adj_grad[kMaxElements];
+  const void* kspec_ext;  // ENG_KEVEN: the plan's quarter table
 };
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 template <typename T>
-int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
+int run_prop(Context& c, const PropJob& j, cudaStream_t st);
+
+__global__ void k_unit_sample(double2* p) { *p = make_double2(1.0, 0.0); }
+
+}  // namespace
+namespace osgpu {
+unsigned long long& launch_counter();
+}
+namespace {
+
+// Quarter table of the kernel-spectrum plan for the f32 ASM job j, built on
+// first use: the FP64 propagation of a unit sample at the origin gives the
+// kernel quadrant h(y, x) on the field grid, whose even 2n-periodic extension
+// is transformed (launch_even_kspec).  *kq stays null when no plan applies:
+// plans off, padding at most 2n, a grid outside the register-FFT lengths,
+// a stream being captured, or a table larger than the cache.
+int plan_lookup(Context& c, const PropJob& j, cudaStream_t st, const void** kq) {
+  *kq = nullptr;
+  if (!c.plans_on || j.engine != ENG_ASM) return OSGPU_OK;
+  const uint64_t nx = j.g.nx, ny = j.g.ny;
+  if (j.Px <= 2 * nx && j.Py <= 2 * ny) return OSGPU_OK;
+  if (!reg_fft_size((int)nx) || !reg_fft_size((int)ny)) return OSGPU_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+    return OSGPU_OK;
+  const double zabs = std::fabs(j.z);
+  for (KPlan& p : c.plans) {
+    if (p.nx == nx && p.ny == ny && p.Px == j.Px && p.Py == j.Py && p.dx == j.g.dx &&
+        p.dy == j.g.dy && p.lam == j.g.lambda && p.medium == j.medium && p.zabs == zabs &&
+        p.band_limited == j.band_limited && p.lim_x == j.lim_x && p.lim_y == j.lim_y) {
+      p.last_use = ++c.plan_tick;
+      ++c.plan_hits;
+      *kq = p.kq;
+      return OSGPU_OK;
+    }
+  }
+  const size_t qbytes = (size_t)(nx + 1) * (ny + 1) * sizeof(float2);
+  if (qbytes > c.plan_cap) return OSGPU_OK;
+  if (c.plan_bytes + qbytes > c.plan_cap) {
+    CK(cudaDeviceSynchronize());  // evicted tables may still be read by queued work
+    while (c.plan_bytes + qbytes > c.plan_cap && !c.plans.empty()) {
+      auto lru = std::min_element(c.plans.begin(), c.plans.end(),
+                                  [](const KPlan& a, const KPlan& b) { return a.last_use < b.last_use; });
+      cudaFree(lru->kq);
+      c.plan_bytes -= lru->bytes;
+      c.plans.erase(lru);
+    }
+  }
+  KPlan p;
+  p.nx = nx; p.ny = ny; p.Px = j.Px; p.Py = j.Py;
+  p.dx = j.g.dx; p.dy = j.g.dy; p.lam = j.g.lambda; p.medium = j.medium; p.zabs = zabs;
+  p.lim_x = j.lim_x; p.lim_y = j.lim_y; p.band_limited = j.band_limited;
+  p.bytes = qbytes;
+  CK(cudaMalloc(&p.kq, qbytes));
+  int rc = OSGPU_OK;
+  const bool prof = c.profiling;
+  {
+    ProfScope ps(c, st, PC_PLAN, 0.0);
+    c.profiling = false;  // the build's own passes are not counted as propagation passes
+    const size_t n = (size_t)nx * ny;
+    DBuf tmp;
+    cudaError_t e = tmp.alloc(2 * n * sizeof(double2), st);
+    double2* delta = reinterpret_cast<double2*>(tmp.p);
+    double2* hq = delta + n;
+    if (e == cudaSuccess) e = cudaMemsetAsync(delta, 0, n * sizeof(double2), st);
+    if (e == cudaSuccess) {
+      k_unit_sample<<<1, 1, 0, st>>>(delta);
+      ++launch_counter();
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "plan build");
+    } else {
+      PropJob jd;
+      std::memset(&jd, 0, sizeof(jd));
+      jd.engine = ENG_ASM;
+      jd.g = j.g;
+      jd.z = zabs;
+      jd.Px = j.Px;
+      jd.Py = j.Py;
+      jd.medium = j.medium;
+      jd.band_limited = j.band_limited;
+      jd.lim_x = j.lim_x;
+      jd.lim_y = j.lim_y;
+      jd.d_in = delta;
+      jd.in_c128 = 1;
+      jd.d_out = hq;
+      jd.out_c128 = 1;
+      rc = run_prop<double>(c, jd, st);
+    }
+    if (rc == OSGPU_OK) {
+      PropArgs b;
+      std::memset(&b, 0, sizeof(b));
+      const int Qx = (int)(2 * nx), Qy = (int)(2 * ny);
+      b.dx = j.g.dx;
+      b.dy = j.g.dy;
+      b.ax = make_axis((int)nx, Qx);
+      b.ay = make_axis((int)ny, Qy);
+      b.scale = 1.0 / ((double)Qx * (double)Qy);
+      if (b.ax.nst < 0 || b.ay.nst < 0 || smem_passA_bytes(b.ax, 1, 1) > kMaxSmem ||
+          smem_passB_bytes(b.ay, 1) > kMaxSmem) {
+        set_err("kernel-spectrum plan of %dx%d exceeds the shared-memory plan", Qx, Qy);
+        rc = OSGPU_E_UNSUPPORTED;
+      } else if ((rc = get_tw(c, b.ax.m, 1, &b.tw_mx)) == OSGPU_OK &&
+                 (rc = get_tw(c, b.ay.m, 1, &b.tw_my)) == OSGPU_OK &&
+                 (rc = get_tw(c, Qx, 1, &b.tw_Px)) == OSGPU_OK &&
+                 (rc = get_tw(c, Qy, 1, &b.tw_Py)) == OSGPU_OK) {
+        DBuf tmp2;
+        cudaError_t e = tmp2.alloc(((size_t)Qx * ny + (size_t)Qx * Qy) * sizeof(double2), st);
+        if (e == cudaSuccess) e = launch_even_kspec(b, hq, (int)nx, (int)ny, p.kq, tmp2.p, st);
+        if (e != cudaSuccess) rc = cuda_fail(e, "plan build");
+      }
+    }
+    c.profiling = prof;
+  }
+  if (rc != OSGPU_OK) {
+    cudaStreamSynchronize(st);
+    cudaFree(p.kq);
+    return rc;
+  }
+  p.last_use = ++c.plan_tick;
+  ++c.plan_builds;
+  c.plan_bytes += qbytes;
+  c.plans.push_back(p);
+  *kq = p.kq;
+  return OSGPU_OK;
+}
+
+template <typename T>
+int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
   const int is_d = sizeof(T) == 8;
   const size_t es = is_d ? 16 : 8;
+  PropJob jp;
+  const PropJob* jj = &j0;
+  if (!is_d) {  // f32 ASM with padding above 2n: the kernel-spectrum plan at 2n
+    const void* kq = nullptr;
+    const int prc = plan_lookup(c, j0, st, &kq);
+    if (prc) return prc;
+    if (kq) {
+      jp = j0;
+      jp.engine = ENG_KEVEN;
+      jp.Px = 2 * j0.g.nx;
+      jp.Py = 2 * j0.g.ny;
+      jp.kspec_ext = kq;
+      jp.conj_h = j0.z < 0.0;
+      jj = &jp;
+    }
+  }
+  const PropJob& j = *jj;
   PropArgs a;
   std::memset(&a, 0, sizeof(a));
   a.nx = (int)j.g.nx;
@@ -420,6 +584,8 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
     a.hy = base + o_hy;
     ProfScope ps(c, st, PC_KSPEC, 0.0);
     CK(launch_fresnel_ksep<T>(a, base + o_hx, base + o_hy, base + o_tmp, st));
+  } else if (j.engine == ENG_KEVEN) {
+    a.kspec = j.kspec_ext;
   } else if (j.engine == ENG_KSPEC) {
     PropArgs b = a;
     b.ax = make_axis((int)Px, (int)Px);
@@ -449,7 +615,8 @@ int run_prop(Context& c, const PropJob& j, cudaStream_t st) {
   }
   {
     ProfScope ps(c, st, PC_PASS_B,
-                 2 * nsp * es + (j.engine == ENG_KSPEC ? (double)Px * Py * es : 0.0));
+                 2 * nsp * es + (j.engine == ENG_KSPEC ? (double)Px * Py * es : 0.0) +
+                     (j.engine == ENG_KEVEN ? (double)(Px / 2 + 1) * (Py / 2 + 1) * 8 : 0.0));
     CK(launch_passB<T>(a, st));
   }
   {
@@ -2319,6 +2486,53 @@ int osgpu_gs_run_batch_device(osgpu_gs_item* items, int32_t n_items, const osgpu
 }
 
 // ------------------------------------------------------------ profiling
+
+int osgpu_plan_cache_config(int32_t enable, uint64_t max_bytes) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc = ensure_init(c);
+  if (rc) return rc;
+  c.plans_on = enable != 0;
+  c.plan_cap = (size_t)max_bytes;
+  if (c.plan_bytes > c.plan_cap) {
+    CK(cudaDeviceSynchronize());
+    while (c.plan_bytes > c.plan_cap && !c.plans.empty()) {
+      auto lru = std::min_element(c.plans.begin(), c.plans.end(),
+                                  [](const KPlan& a, const KPlan& b) { return a.last_use < b.last_use; });
+      cudaFree(lru->kq);
+      c.plan_bytes -= lru->bytes;
+      c.plans.erase(lru);
+    }
+  }
+  return OSGPU_OK;
+}
+
+int osgpu_plan_cache_clear(void) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc = ensure_init(c);
+  if (rc) return rc;
+  CK(cudaDeviceSynchronize());
+  for (KPlan& p : c.plans) cudaFree(p.kq);
+  c.plans.clear();
+  c.plan_bytes = 0;
+  c.plan_hits = c.plan_builds = 0;
+  return OSGPU_OK;
+}
+
+int osgpu_plan_cache_stats(osgpu_plan_stats* out) {
+  if (!out) {
+    set_err("null stats pointer");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  out->plans = c.plans.size();
+  out->bytes = c.plan_bytes;
+  out->hits = c.plan_hits;
+  out->builds = c.plan_builds;
+  return OSGPU_OK;
+}
 
 int osgpu_profile_begin(void) {
   Context& c = ctx();

@@ -32,6 +32,7 @@ enum EngineKind : int {
   ENG_KSPEC = 2,        // precomputed kernel spectrum (Fresnel conv, RS)
   ENG_KSEP = 3,         // separable kernel spectrum Hx[kx]*Hy[ky] (Fresnel conv)
   ENG_IDENTITY = 4,     // spectrum untouched (used to build 2D FFTs)
+  ENG_KEVEN = 5,        // even kernel spectrum, quarter table (kernel-spectrum plans, f32)
 };
 
 enum ElementKind : int {

@@ -161,6 +161,19 @@ __device__ __forceinline__ void build_htab(const PropArgs& a, int kx, float2* ht
                                            int nt) {
   constexpr int U = M / 2 + 1;
   const int Py = a.ay.P, ry = a.ay.r;
+  const int hh = Py / 2;
+  if (a.engine == ENG_KEVEN) {  // quarter table of a kernel-spectrum plan
+    const float2* kq = reinterpret_cast<const float2*>(a.kspec) + (size_t)kx * (hh + 1);
+    for (int idx = t0; idx < ry * U; idx += nt) {
+      const int rr = idx / U, u = idx - rr * U;
+      const int ak = ry * u + rr;
+      if (ak > hh) continue;
+      float2 h = __ldg(kq + ak);
+      if (a.conj_h) h.y = -h.y;
+      htab[idx] = h;
+    }
+    return;
+  }
   const bool asm_split = (a.engine == ENG_ASM);
   const float2 exc = a.Ex[kx];
   float cah = 0.f, cal = 0.f, sac = 0.f;
@@ -171,7 +184,6 @@ __device__ __forceinline__ void build_htab(const PropArgs& a, int kx, float2* ht
     sac = a.sa[kx];
     kmc = a.kmax[kx];
   }
-  const int hh = Py / 2;
   const float4* rt = reinterpret_cast<const float4*>(a.rowtab);
   constexpr int UNR = 4;
   for (int base = t0; base < ry * U; base += UNR * nt) {
@@ -269,6 +281,10 @@ __global__ void __launch_bounds__(Lay<M, G>::THREADS, Lay<M, G>::MINB)
         h = (q < 8) ? htab[hb_lo + T * q] : htab[hb_hi - T * q];
       } else if (a.engine == ENG_KSPEC) {
         h = __ldg(reinterpret_cast<const float2*>(a.kspec) + (size_t)kx * Py + ky);
+        if (a.conj_h) h.y = -h.y;
+      } else if (a.engine == ENG_KEVEN) {
+        const int kxq = min(kx, a.ax.P - kx), kyq = min(ky, Py - ky);
+        h = __ldg(reinterpret_cast<const float2*>(a.kspec) + (size_t)kxq * (Py / 2 + 1) + kyq);
         if (a.conj_h) h.y = -h.y;
       } else if (a.engine == ENG_KSEP) {
         h = cmul(__ldg(reinterpret_cast<const float2*>(a.hx) + kx),
@@ -788,7 +804,8 @@ size_t smem_pair(int r) {
 
 template <int M>
 cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
-  const bool even = (a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF) && a.h_mode == 1;
+  const bool even =
+      ((a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF) && a.h_mode == 1) || a.engine == ENG_KEVEN;
   if (even && (a.ax.P % 2) == 0 && smem_pair<M>(a.ay.r) <= kMaxSmemB && !getenv("OSGPU_NO_PAIR")) {
     const size_t smem = smem_pair<M>(a.ay.r);
     cudaError_t e = cudaFuncSetAttribute(k_passB_pair<M>,

@@ -582,6 +582,10 @@ __global__ void __launch_bounds__(kThreads) k_passB(PropArgs a, int fwd_only, vo
       if (a.engine == ENG_KSPEC) {
         h = reinterpret_cast<const V*>(a.kspec)[(size_t)kx * Py + ky];
         if (a.conj_h) h.y = -h.y;
+      } else if (a.engine == ENG_KEVEN) {
+        const int kxq = min(kx, a.ax.P - kx), kyq = min(ky, Py - ky);
+        const float2 k = reinterpret_cast<const float2*>(a.kspec)[(size_t)kxq * (Py / 2 + 1) + kyq];
+        h = mkc<V>((T)k.x, (T)(a.conj_h ? -k.y : k.y));
       } else if (a.engine == ENG_KSEP) {
         h = cmul(reinterpret_cast<const V*>(a.hx)[kx], reinterpret_cast<const V*>(a.hy)[ky]);
         if (a.conj_h) h.y = -h.y;
@@ -849,6 +853,74 @@ cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStr
   if (e != cudaSuccess) return e;
   COUNT_LAUNCH();
   k_cast_c128<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(spec, kspec, n);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------- kernel-spectrum plans
+//
+// A propagation out = crop_n(IFFT_P(H FFT_P(pad_n(u)))) only reaches kernel
+// offsets |d| < n of h = IFFT_P(H), so it equals the circular convolution of
+// period 2n with h restricted to those offsets.  For a transfer function
+// even in each axis (ASM: fx^2, fy^2 and |fx|, |fy| band limits), h is even
+// too: the quadrant h(y, x), 0 <= x, y < n, is the propagation of a unit
+// sample at the origin, and the spectrum of its 2n-periodic even extension
+// (zero at offset n, which no output reaches) is
+//   K(ky, kx) = sum over the four sign pairs of A(+-ky, +-kx),
+//   A = FFT_2n(pad_n(c_y c_x h)),  c_0 = 1/2, c_d = 1 otherwise,
+// (the halved first row and column are the offsets shared by two
+// reflections), so the pruned zero-padded passes give it directly.  K is
+// even; the quarter kx <= n, ky <= n is kept.
+
+// hq[y][x] *= (y == 0 ? 1/2 : 1) (x == 0 ? 1/2 : 1)
+__global__ void k_halve_axes(double2* hq, int hnx, int hny) {
+  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (idx >= (size_t)hnx * hny) return;
+  const int x = (int)(idx % hnx), y = (int)(idx / hnx);
+  const double w = (x == 0 ? 0.5 : 1.0) * (y == 0 ? 0.5 : 1.0);
+  if (w != 1.0) hq[idx] = make_double2(hq[idx].x * w, hq[idx].y * w);
+}
+
+// kq[kx (Py/2 + 1) + ky] = sum of the column-major spectrum A at (+-kx, +-ky).
+__global__ void k_quarter_fold(const double2* A, int Px, int Py, float2* kq) {
+  const int hx = Px / 2 + 1, hy = Py / 2 + 1;
+  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (idx >= (size_t)hx * hy) return;
+  const int kx = (int)(idx / hy), ky = (int)(idx % hy);
+  const int mx = kx == 0 ? 0 : Px - kx, my = ky == 0 ? 0 : Py - ky;
+  const double2 a = A[(size_t)kx * Py + ky], b = A[(size_t)mx * Py + ky];
+  const double2 c = A[(size_t)kx * Py + my], d = A[(size_t)mx * Py + my];
+  kq[idx] = make_float2((float)((a.x + b.x) + (c.x + d.x)), (float)((a.y + b.y) + (c.y + d.y)));
+}
+
+cudaError_t launch_even_kspec(const PropArgs& a, void* hq, int hnx, int hny, void* kq,
+                              void* tmp64, cudaStream_t st) {
+  const int Px = a.ax.P, Py = a.ay.P;
+  if (Px != 2 * hnx || Py != 2 * hny || a.ax.n != hnx || a.ay.n != hny) return cudaErrorInvalidValue;
+  double2* h = reinterpret_cast<double2*>(hq);
+  double2* work = reinterpret_cast<double2*>(tmp64);
+  double2* spec = work + (size_t)Px * hny;
+  const size_t n = (size_t)hnx * hny;
+  COUNT_LAUNCH();
+  k_halve_axes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h, hnx, hny);
+  PropArgs b = a;
+  b.nx = hnx;
+  b.ny = hny;
+  b.in = h;
+  b.in_c128 = 1;
+  b.work = work;
+  b.els.count = 0;
+  b.seed = nullptr;
+  b.adj = 0;
+  b.status = nullptr;
+  b.engine = ENG_IDENTITY;
+  cudaError_t e = launch_passA<double>(b, st);
+  if (e != cudaSuccess) return e;
+  e = launch_passB_impl<double>(b, 1, spec, st);
+  if (e != cudaSuccess) return e;
+  const size_t nq = (size_t)(Px / 2 + 1) * (Py / 2 + 1);
+  COUNT_LAUNCH();
+  k_quarter_fold<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(spec, Px, Py,
+                                                               reinterpret_cast<float2*>(kq));
   return cudaGetLastError();
 }
 

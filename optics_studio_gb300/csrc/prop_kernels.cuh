@@ -48,7 +48,9 @@ struct PropArgs {
   const void* rowtab;  // f32 split: per row {Ey.x, Ey.y, b_hi, b_lo} packed (float4)
   float Kf;            // kz as f32 (for the small residual term)
   // kernel spectra
-  const void* kspec;   // ENG_KSPEC: column-major Px x Py spectrum (type of engine)
+  const void* kspec;   // ENG_KSPEC: column-major Px x Py spectrum (type of engine);
+                       // ENG_KEVEN: f32 quarter table K[kx (Py/2 + 1) + ky], kx <= Px/2,
+                       // ky <= Py/2, of a spectrum even in both axes (scale folded in)
   const void* hx;      // ENG_KSEP: per-column spectrum factor (includes prefactor, scale)
   const void* hy;      // ENG_KSEP: per-row spectrum factor
   int* status;         // bit 0: non-finite input sample, bit 1: non-finite output
@@ -113,6 +115,13 @@ cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp
 // and stored as T.
 template <typename T>
 cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStream_t st);
+// Quarter table (ENG_KEVEN) of the spectrum of the 2n-periodic even extension
+// of a kernel quadrant hq (hny x hnx complex128, hq[y][x] = h(y, x); its
+// first row and column are halved in place): `a` carries the zero-padding
+// axis plans make_axis(hnx, 2 hnx), make_axis(hny, 2 hny), their FP64
+// twiddle tables and scale = 1 / (Px Py); tmp64 holds Px hny + Px Py double2.
+cudaError_t launch_even_kspec(const PropArgs& a, void* hq, int hnx, int hny, void* kq,
+                              void* tmp64, cudaStream_t st);
 
 // Standalone element application (Element::apply chain, no propagation).
 template <typename T>

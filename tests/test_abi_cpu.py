@@ -46,7 +46,7 @@ STRUCTS = {
     "osgpu_frame": "FrameC", "osgpu_adam_config": "AdamConfigC",
     "osgpu_gs_config": "GsConfigC", "osgpu_gs_record": "GsRecordC",
     "osgpu_gs_result": "GsResultC", "osgpu_gs_item": "GsItemC",
-    "osgpu_host_trace_item": "HostTraceItemC",
+    "osgpu_host_trace_item": "HostTraceItemC", "osgpu_plan_stats": "PlanStatsC",
 }
 
 

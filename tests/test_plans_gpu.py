@@ -1,0 +1,163 @@
+"""Kernel-spectrum plans (osgpu_plan_cache_*) against the oracle and the
+padded f32 path.
+
+A plan replaces an f32 ASM propagation padded above 2n by the circular
+convolution of period 2n with the same kernel (its spectrum built once in
+FP64), so its results match the f64 oracle (oracle/asm.py, restating
+src/propagation/asm.rs:438-538) to the f32 bounds of the padded path: 1e-5
+relative L2 for fields, 1e-4 for gradients.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle import adjoint as o_adj, asm as oasm, carrier as o_car, element as o_el
+from oracle import field as ofield, merit as o_merit, observe as o_obs
+
+from _util import rel_l2, rng_field, to_gpu_band
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+from optics_studio_gb300 import inverse as inv, element as el, plans  # noqa: E402
+from optics_studio_gb300.propagation import asm as gasm  # noqa: E402
+
+# strict densification pads this geometry 256 -> 1024 at 532 nm, 10 mm
+N, D, LAM, Z = 256, 3e-6, 532e-9, 10e-3
+
+
+@pytest.fixture
+def plans_on():
+    plans.clear()
+    plans.enable(1 << 30)
+    yield
+    plans.disable()
+    plans.clear()
+
+
+def band(seed=5, lam=LAM):
+    return ofield.BandField(rng_field(N, N, seed=seed), D, D, lam)
+
+
+def test_plan_propagation_matches_oracle_and_padded_path(plans_on):
+    ob = band()
+    assert oasm.resolve_report(ob, Z, oasm.AsmConfig()).padded_dims == (1024, 1024)
+    ref = oasm.propagate(ob, Z)
+    out1 = gasm.propagate(to_gpu_band(ob), Z, gasm.AsmConfig(), "f32")
+    assert (out1.report.nx_pad, out1.report.ny_pad) == (1024, 1024)  # the reference's report
+    st = plans.stats()
+    assert (st["plans"], st["builds"], st["hits"]) == (1, 1, 0)
+    assert st["bytes"] == (N + 1) * (N + 1) * 8
+    assert rel_l2(out1.samples, ref.samples) <= 1e-5
+    out2 = gasm.propagate(to_gpu_band(ob), Z, gasm.AsmConfig(), "f32")
+    assert plans.stats()["hits"] == 1
+    np.testing.assert_array_equal(out1.samples, out2.samples)
+    # the adjoint distance uses the conjugate of the same table
+    back = gasm.propagate(to_gpu_band(ob), -Z, gasm.AsmConfig(), "f32")
+    assert rel_l2(back.samples, oasm.propagate(ob, -Z).samples) <= 1e-5
+    assert plans.stats()["builds"] == 1
+    plans.disable()
+    padded = gasm.propagate(to_gpu_band(ob), Z, gasm.AsmConfig(), "f32")
+    assert rel_l2(out1.samples, padded.samples) <= 1e-5
+
+
+def test_plan_applies_only_to_f32_above_2n(plans_on):
+    ob = band(seed=9)
+    out64 = gasm.propagate(to_gpu_band(ob), Z, gasm.AsmConfig(), "f64")
+    assert rel_l2(out64.samples, oasm.propagate(ob, Z).samples) <= 1e-12
+    z2 = 5e-3  # pads 256 -> 512: already 2n
+    assert oasm.resolve_report(ob, z2, oasm.AsmConfig()).padded_dims == (512, 512)
+    gasm.propagate(to_gpu_band(ob), z2, gasm.AsmConfig(), "f32")
+    assert plans.stats()["builds"] == 0
+
+
+def test_plan_cache_evicts_least_recently_used():
+    table = (N + 1) * (N + 1) * 8
+    plans.clear()
+    plans.enable(table * 3 // 2)
+    try:
+        a, b = band(seed=1, lam=532e-9), band(seed=2, lam=580e-9)
+        za, zb = 10e-3, 8e-3  # both pad 256 -> 1024
+        assert oasm.resolve_report(b, zb, oasm.AsmConfig()).padded_dims == (1024, 1024)
+        ra = gasm.propagate(to_gpu_band(a), za, gasm.AsmConfig(), "f32")
+        rb = gasm.propagate(to_gpu_band(b), zb, gasm.AsmConfig(), "f32")
+        st = plans.stats()
+        assert (st["plans"], st["builds"], st["bytes"]) == (1, 2, table)
+        ra2 = gasm.propagate(to_gpu_band(a), za, gasm.AsmConfig(), "f32")
+        assert plans.stats()["builds"] == 3
+        np.testing.assert_array_equal(ra.samples, ra2.samples)
+        assert rel_l2(rb.samples, oasm.propagate(b, zb).samples) <= 1e-5
+    finally:
+        plans.disable()
+        plans.clear()
+
+
+# inverse design: [DOE, 2 mm] [aperture r 250 um, 10 mm]; at 532 nm the second
+# propagation pads to 4n (plan), at 580 nm to 2n (padded path)
+BANDS = [532e-9, 580e-9]
+Z1, Z2, R_AP = 2e-3, 10e-3, 250e-6
+
+
+def o_source(x0, y0, lam):
+    return ofield.gaussian(200e-6, 1.0, (x0, y0), 0.0, lam, N, N, D, D)
+
+
+def o_design(v, lam):
+    d = o_car.Design()
+    d.push(o_el.PhaseMask.sampled(v, (N, N), (D, D)), Z1)
+    d.push(o_el.EllipticalAperture.circle(R_AP), Z2)
+    return d
+
+
+def windows():
+    w = np.zeros((N, N), dtype=bool)
+    for cy in (96, 128, 160):
+        for cx in (96, 128, 160):
+            w[cy - 2:cy + 3, cx - 2:cx + 3] = True
+    return w
+
+
+def g_gradient(phi):
+    def source(x0, y0, lam):
+        return torch.from_numpy(o_source(x0, y0, lam).samples).to("cuda", torch.complex64)
+
+    def carrier(values, lam):
+        d = inv.Design()
+        d.push(inv.DevicePhaseMask(values, (N, N), (D, D)), Z1)
+        d.push(el.EllipticalAperture.circle(R_AP), Z2)
+        return d
+
+    rend = inv.Renderer(carrier, source, (D, D), bands=list(BANDS),
+                        asm_cfg=gasm.AsmConfig(), precision="f32")
+    p_in = [float(np.sum(np.abs(o_source(0.0, 0.0, lam).samples) ** 2)) for lam in BANDS]
+    m = inv.SpotArrayEfficiency(torch.from_numpy(windows()).cuda(), p_in)
+    g, val, obs = inv.grid_gradient(rend, torch.from_numpy(phi).cuda(), m)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in g.items()}, val, obs.data.cpu().numpy()
+
+
+def test_plan_gradients_match_oracle_and_padded_path(plans_on):
+    pads = [oasm.resolve_report(band(lam=lam), Z2, oasm.AsmConfig()).padded_dims[0]
+            for lam in BANDS]
+    assert pads == [1024, 512]
+    phi = np.random.default_rng(11).uniform(0.0, 2 * math.pi, (N, N))
+    got, val, obs = g_gradient(phi)
+    st = plans.stats()
+    assert st["builds"] == 1 and st["hits"] >= 1  # forward and adjoint share the table
+    car = o_car.Carrier.analytic(N * N, 0.0, 2 * math.pi, o_design)
+    p_in = [float(np.sum(np.abs(o_source(0.0, 0.0, lam).samples) ** 2)) for lam in BANDS]
+    o_m = o_merit.SpotArrayEfficiency(windows(), p_in)
+    rend = o_obs.Renderer(car, o_source, bands=list(BANDS), scenes=[(0.0, 0.0)],
+                          asm_cfg=oasm.AsmConfig())
+    want = o_adj.grid_gradient(rend, phi.reshape(-1), o_m)
+    for ei in (0, 1):
+        assert rel_l2(got[ei], want[ei].reshape(N, N)) <= 1e-4, ei
+    ref_obs = rend.render(phi.reshape(-1)).data
+    assert rel_l2(obs, ref_obs) <= 1e-5
+    plans.disable()
+    pad, pval, pobs = g_gradient(phi)
+    for ei in (0, 1):
+        assert rel_l2(got[ei], pad[ei]) <= 1e-4, ei
+    assert abs(val - pval) <= 1e-5 * abs(pval)
