@@ -699,6 +699,85 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(Pro
   }
 }
 
+// Pass C on R-row tiles: the CTA stages each sub-transform's R-row tile of
+// the column-major spectrum through shared memory, read in runs
+// W[kx * ny + iy0 .. iy0 + R - 1] of 8 R bytes (with R = 4 the two lanes of a
+// pair read the two halves of one 32-byte sector), then group g transforms
+// row iy0 + g and accumulates it in registers; the epilogue writes the
+// group's row directly (samples tid + T q).  Needs ny % R == 0.
+template <int M, int R, bool ADJ>
+__global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passC_tile(PropArgs a) {
+  constexpr int T = M / 16;
+  constexpr int SBT = tile_stride<M>();
+  constexpr int NT = R * T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = a.nx, ny = a.ny, rx = a.ax.r;
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  float2* tb = bufs + R * SBT;
+  float2* tq = tb + rx * T;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  const int iy0 = blockIdx.x * R;
+  float2* buf = bufs + g * SBT;
+  const float2* W = reinterpret_cast<const float2*>(a.work);
+  pdl_trigger();
+  copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
+  load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
+  pdl_wait();  // pass B's spectrum is complete
+  float2 acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
+  constexpr int HV = R / 2;
+  for (int s = 0; s < rx; ++s) {
+    // the tile of sub-transform s into row buffers (natural order, padded index)
+#pragma unroll 4
+    for (int h = threadIdx.x; h < HV * M; h += NT) {
+      const int p = h / HV, hf = h - p * HV;
+      const float4 v =
+          __ldg(reinterpret_cast<const float4*>(W + (size_t)(rx * p + s) * ny + iy0) + hf);
+      const int pp = p + (p >> 4);
+      bufs[2 * hf * SBT + pp] = make_float2(v.x, v.y);
+      bufs[(2 * hf + 1) * SBT + pp] = make_float2(v.z, v.w);
+    }
+    __syncthreads();
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int j = tid + T * q;
+      v[q] = buf[j + (j >> 4)];
+    }
+    fft1s<M, true>(v, buf, tws, tid, 1 + g, T);
+    const float2 wb = tb[s * T + tid];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      float2 y = v[q];
+      if (s > 0) y = cmulc(y, cmul(wb, tq[s * 16 + q]));
+      acc[q] = cadd(acc[q], y);
+    }
+    __syncthreads();  // every group is done with its buffer before the next tile
+  }
+  const int iy = iy0 + g;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = tid + T * q;
+    if (j >= nx) continue;
+    float2 v = acc[q];
+    const size_t o = (size_t)iy * nx + j;
+    if (ADJ) {  // adjoint element plane (a.adj)
+      const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
+      adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x, v.y);
+    }
+    if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
+    if (a.out) {
+      if (a.out_c128) reinterpret_cast<double2*>(a.out)[o] = make_double2(v.x, v.y);
+      else reinterpret_cast<float2*>(a.out)[o] = v;
+    }
+    if (a.out_intensity) a.out_intensity[o] = v.x * v.x + v.y * v.y;
+    if (a.out_intensity64) a.out_intensity64[o] = (double)v.x * v.x + (double)v.y * v.y;
+  }
+}
+
 template <int M>
 constexpr bool r4_ok() {
   return M >= 512 && M <= 2048;
@@ -826,8 +905,12 @@ cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
 template <int M>
 cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
   if constexpr (r4_ok<M>()) {
-    // 4-row tiles (2-row tiles measured the same on the 2048^2 workload)
-    if (a.ny % 4 == 0 && smem_tile<M, 4>(a.ax.r) <= kMaxSmemB) return launch_A_tile<M, 4>(a, st);
+    const char* e = getenv("OSGPU_PASSA_TILE");
+    const int R = e ? atoi(e) : 4;
+    if (R == 4 && a.ny % 4 == 0 && smem_tile<M, 4>(a.ax.r) <= kMaxSmemB)
+      return launch_A_tile<M, 4>(a, st);
+    if (R == 2 && a.ny % 2 == 0 && smem_tile<M, 2>(a.ax.r) <= kMaxSmemB)
+      return launch_A_tile<M, 2>(a, st);
   }
   const int g = pick_groups<M>(0, a.ax.r, 0, env_groups("OSGPU_GROUPS_A", 2));
   if (g == 4) return launchA_mg<M, 4>(a, st);
@@ -835,8 +918,38 @@ cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
   return launchA_mg<M, 1>(a, st);
 }
 
+template <int M, int R, bool ADJ>
+size_t smem_ctile(int r) {
+  constexpr int T = M / 16;
+  return ((size_t)TwLay<M>::SIZE + R * (size_t)tile_stride<M>() + (size_t)r * (T + 16)) *
+         sizeof(float2);
+}
+
+template <int M, int R, bool ADJ>
+cudaError_t launch_C_tile(const PropArgs& a, cudaStream_t st) {
+  const size_t smem = smem_ctile<M, R, ADJ>(a.ax.r);
+  cudaError_t e = cudaFuncSetAttribute(k_passC_tile<M, R, ADJ>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  return launch_pdl(k_passC_tile<M, R, ADJ>, dim3(a.ny / R), dim3(R * (M / 16)), smem, st, a);
+}
+
 template <int M>
 cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
+  if constexpr (r4_ok<M>()) {
+    // 2-row tiles (2 CTAs per SM) measured fastest on the 2048^2 workload
+    // without the adjoint epilogue (0.126 -> 0.118 ms per band); the adjoint
+    // epilogue spills in the tile kernels, so it keeps the one-row kernel
+    const char* e = getenv("OSGPU_PASSC_TILE");
+    const int R = e ? atoi(e) : (a.adj ? 0 : 2);
+    if ((R == 2 || R == 4) && a.ny % R == 0) {
+      if (R == 4 && smem_ctile<M, 4, false>(a.ax.r) <= kMaxSmemB)
+        return a.adj ? launch_C_tile<M, 4, true>(a, st) : launch_C_tile<M, 4, false>(a, st);
+      if (R == 2 && smem_ctile<M, 2, false>(a.ax.r) <= kMaxSmemB)
+        return a.adj ? launch_C_tile<M, 2, true>(a, st) : launch_C_tile<M, 2, false>(a, st);
+    }
+  }
   const int g = pick_groups<M>(2, a.ax.r, 0, env_groups("OSGPU_GROUPS_C", 2));
   if (g == 4) return launchC_mg<M, 4>(a, st);
   if (g == 2) return launchC_mg<M, 2>(a, st);
