@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(kThreads) k_passB(PropArgs a, int fwd_only, vo
           const float s = sac + bh;
           const float q = sqrtf(fmaxf(1.f - s, 0.f));
           const float opq = 1.f + q;
-          const float tau = a.Kf * (s * s * s) * (3.f + q) / (8.f * opq * opq * opq);
+          const float tau = __fdividef(a.Kf * (s * s * s) * (3.f + q), 8.f * opq * opq * opq);
           const float pr = cah * bh;
           const float er = fmaf(cah, bh, -pr);
           const float corr = er + (cah * blo + cal * bh);
