@@ -72,6 +72,7 @@ struct Context {
   int device = -1;
   cudaStream_t stream = nullptr;
   cudaStream_t copy_in = nullptr, copy_out = nullptr;  // host-buffer batch pipeline
+  cudaStream_t aux = nullptr;  // element tables of the next batch item
   int* d_status = nullptr;
   std::map<std::pair<int, int>, void*> tw;  // (n, is_double) -> twiddle table
   bool profiling = false;
@@ -1769,6 +1770,34 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
   cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   const int f32 = dtype == OSGPU_C64;
   const int c128 = dtype == OSGPU_C128;
+  // The element tables of item i are built on the auxiliary stream while item
+  // i - 1 runs on st (fork from st at entry, join at exit; also under graph
+  // capture).  Item i's tables are freed on the auxiliary stream once item i
+  // has completed on st.
+  if (!c.aux) CK(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
+  cudaStream_t ax = c.aux;
+  cudaEvent_t ev = pool_event(c);
+  CK(cudaEventRecord(ev, st));
+  CK(cudaStreamWaitEvent(ax, ev, 0));
+  std::vector<Elements> prevE;
+  cudaEvent_t prev_done = nullptr;
+  struct OnExit {  // an early return must not free tables that queued work still reads
+    std::vector<Elements>& e;
+    cudaEvent_t& done;
+    cudaStream_t ax;
+    ~OnExit() {
+      if (done) cudaStreamWaitEvent(ax, done, 0);
+      e.clear();
+    }
+  } on_exit{prevE, prev_done, ax};
+  auto release_prev = [&]() -> int {
+    if (!prev_done) return OSGPU_OK;
+    CK(cudaStreamWaitEvent(ax, prev_done, 0));
+    prevE.clear();  // frees stream-ordered on ax, after item i - 1 completed
+    c.event_pool.push_back(prev_done);
+    prev_done = nullptr;
+    return OSGPU_OK;
+  };
   for (int i = 0; i < n_items; ++i) {
     const osgpu_trace_item& it = items[i];
     if (!it.d_in || !it.d_out || it.n_steps < 0 || (it.n_steps > 0 && !it.steps))
@@ -1776,7 +1805,7 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
     if (it.grid.nx == 0 || it.grid.ny == 0) return OSGPU_E_EMPTY_GRID;
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
-    rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, st);
+    rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, ax);
     if (reports && reports_stride > 0)
       for (int s = 0; s < it.n_steps && s < reports_stride && s < (int)R.size(); ++s)
         reports[(size_t)i * reports_stride + s] = R[s];
@@ -1784,10 +1813,23 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
       set_err("batch item %d: %s", i, t_err);
       return rc;
     }
+    CK(cudaEventRecord(ev, ax));
+    CK(cudaStreamWaitEvent(st, ev, 0));
     if ((rc = run_trace(c, it.d_in, c128, it.d_out, c128, it.grid, it.steps, it.n_steps, E, R,
-                        *cfg, f32, st)))
+                        *cfg, f32, st))) {
+      cudaStreamSynchronize(st);  // E's tables may be read by what was queued
       return rc;
+    }
+    cudaEvent_t done = pool_event(c);
+    CK(cudaEventRecord(done, st));
+    if ((rc = release_prev())) return rc;
+    prevE = std::move(E);
+    prev_done = done;
   }
+  if ((rc = release_prev())) return rc;
+  CK(cudaEventRecord(ev, ax));
+  CK(cudaStreamWaitEvent(st, ev, 0));
+  c.event_pool.push_back(ev);
   return OSGPU_OK;
 }
 
