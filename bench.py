@@ -742,18 +742,24 @@ def main():
         dt = max_over_ranks((time.perf_counter() - t0) / nrep * 1e3, world) / 1e3
         e2e_clocks = eclk.stop()
         barrier()
-        # the host link's own pinned copy rates on this machine (one 2 GiB copy each way)
+        # the host link's own pinned copy rates on this machine (2 GiB each way; best of 3
+        # after one untimed pair)
         dev = torch.empty((NBANDS, N, N), dtype=torch.complex128, device="cuda")
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        dev.copy_(host_in, non_blocking=True)
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
-        host_out.copy_(dev, non_blocking=True)
-        torch.cuda.synchronize()
-        t3 = time.perf_counter()
         nb = float(NBANDS * N * N * 16)
-        link = {"h2d_gbs": nb / (t2 - t1) / 1e9, "d2h_gbs": nb / (t3 - t2) / 1e9}
+        best_in = best_out = 0.0
+        for rep in range(4):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            dev.copy_(host_in, non_blocking=True)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            host_out.copy_(dev, non_blocking=True)
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            if rep:
+                best_in = max(best_in, nb / (t2 - t1) / 1e9)
+                best_out = max(best_out, nb / (t3 - t2) / 1e9)
+        link = {"h2d_gbs": best_in, "d2h_gbs": best_out}
         del dev
         line["e2e"] = {"value": NBANDS * world / dt, "unit": "propagations/s",
                        "h2d_bytes_per_step": NBANDS * N * N * 16,

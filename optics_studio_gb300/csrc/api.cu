@@ -1691,29 +1691,42 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   }
   CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), cs));
   CK(cudaStreamSynchronize(cs));  // slots allocated before the copy streams use them
-  cudaEvent_t ev_in[2], ev_comp[2], ev_out[2];
+  // element tables of item i on the auxiliary stream, overlapped with item i - 1
+  if (!c.aux) CK(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
+  const cudaStream_t ax = c.aux;
+  cudaEvent_t ev_in[2], ev_comp[2], ev_out[2], ev_prep;
   for (int k = 0; k < 2; ++k) {
     CK(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_comp[k], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_out[k], cudaEventDisableTiming));
   }
+  CK(cudaEventCreateWithFlags(&ev_prep, cudaEventDisableTiming));
+  std::vector<Elements> prevE;  // tables of item i - 1, freed on ax after it completed
+  int prev_k = -1;
   auto release = [&]() {
     cudaStreamSynchronize(si);
     cudaStreamSynchronize(cs);
     cudaStreamSynchronize(so);
+    cudaStreamSynchronize(ax);
+    prevE.clear();
     for (int k = 0; k < 2; ++k) {
       cudaEventDestroy(ev_in[k]);
       cudaEventDestroy(ev_comp[k]);
       cudaEventDestroy(ev_out[k]);
     }
+    cudaEventDestroy(ev_prep);
   };
+  if (cudaEventRecord(ev_prep, cs) != cudaSuccess || cudaStreamWaitEvent(ax, ev_prep, 0) != cudaSuccess) {
+    release();
+    return cuda_fail(cudaGetLastError(), "batch fork");
+  }
   for (int i = 0; i < n_items; ++i) {
     const osgpu_host_trace_item& it = items[i];
     const int k = i & 1;
     const size_t bytes = (size_t)(it.grid.nx * it.grid.ny) * 16;
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
-    rc = prepare_trace(c, it.in, bytes / 16, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, cs);
+    rc = prepare_trace(c, it.in, bytes / 16, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, ax);
     if (reports && reports_stride > 0)
       for (int s = 0; s < it.n_steps && s < reports_stride && s < (int)R.size(); ++s)
         reports[(size_t)i * reports_stride + s] = R[s];
@@ -1722,8 +1735,9 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
       release();
       return rc;
     }
-    cudaError_t e = cudaSuccess;
-    if (i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
+    cudaError_t e = cudaEventRecord(ev_prep, ax);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_prep, 0);
+    if (e == cudaSuccess && i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
     if (e == cudaSuccess) e = cudaMemcpyAsync(din[k].p, it.in, bytes, cudaMemcpyHostToDevice, si);
     if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], si);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_in[k], 0);
@@ -1741,11 +1755,16 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
     if (e == cudaSuccess) e = cudaStreamWaitEvent(so, ev_comp[k], 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(it.out, dout[k].p, bytes, cudaMemcpyDeviceToHost, so);
     if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], so);
+    if (e == cudaSuccess && prev_k >= 0) e = cudaStreamWaitEvent(ax, ev_comp[prev_k], 0);
     if (e != cudaSuccess) {
       release();
       return cuda_fail(e, "batch copy out");
     }
+    prevE.clear();  // item i - 1 has completed on cs before ax reaches these frees
+    prevE = std::move(E);
+    prev_k = k;
   }
+  if (prev_k >= 0 && cudaStreamWaitEvent(ax, ev_comp[prev_k], 0) == cudaSuccess) prevE.clear();
   int status = 0;
   cudaError_t e = cudaStreamSynchronize(so);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, cs);
