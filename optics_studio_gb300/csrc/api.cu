@@ -202,6 +202,43 @@ struct Elements {
   DBuf tables;
 };
 
+// Element tables of the next batch item / frame are built on the auxiliary
+// stream while the previous one runs on the compute stream: fork() makes the
+// auxiliary stream follow the compute stream's work so far, ready() makes the
+// compute stream wait for the tables built so far (the last ready() also
+// joins the auxiliary stream back, as graph capture requires), and
+// free_after() moves the frees of a built item's buffers to the compute
+// stream, where they follow the kernels that read them.
+struct AuxTables {
+  cudaStream_t st = nullptr, ax = nullptr;
+  cudaEvent_t ev = nullptr;
+  int fork(Context& c, cudaStream_t compute);
+  int ready() {
+    CK(cudaEventRecord(ev, ax));
+    CK(cudaStreamWaitEvent(st, ev, 0));
+    return OSGPU_OK;
+  }
+  void free_after(std::vector<Elements>& E) const {
+    for (Elements& e : E) {
+      e.tables.s = st;
+      for (DBuf& l : e.lattices) l.s = st;
+    }
+  }
+  ~AuxTables() {
+    if (ev) cudaEventDestroy(ev);
+  }
+};
+
+int AuxTables::fork(Context& c, cudaStream_t compute) {
+  if (!c.aux) CK(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
+  st = compute;
+  ax = c.aux;
+  CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  CK(cudaEventRecord(ev, st));
+  CK(cudaStreamWaitEvent(ax, ev, 0));
+  return OSGPU_OK;
+}
+
 int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid& g,
                    Elements& E, cudaStream_t st) {
   std::memset(&E.list, 0, sizeof(E.list));
@@ -1692,41 +1729,33 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), cs));
   CK(cudaStreamSynchronize(cs));  // slots allocated before the copy streams use them
   // element tables of item i on the auxiliary stream, overlapped with item i - 1
-  if (!c.aux) CK(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
-  const cudaStream_t ax = c.aux;
-  cudaEvent_t ev_in[2], ev_comp[2], ev_out[2], ev_prep;
+  AuxTables aux;
+  if ((rc = aux.fork(c, cs))) return rc;
+  cudaEvent_t ev_in[2], ev_comp[2], ev_out[2];
   for (int k = 0; k < 2; ++k) {
     CK(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_comp[k], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_out[k], cudaEventDisableTiming));
   }
-  CK(cudaEventCreateWithFlags(&ev_prep, cudaEventDisableTiming));
-  std::vector<Elements> prevE;  // tables of item i - 1, freed on ax after it completed
-  int prev_k = -1;
   auto release = [&]() {
     cudaStreamSynchronize(si);
+    cudaStreamSynchronize(aux.ax);
     cudaStreamSynchronize(cs);
     cudaStreamSynchronize(so);
-    cudaStreamSynchronize(ax);
-    prevE.clear();
     for (int k = 0; k < 2; ++k) {
       cudaEventDestroy(ev_in[k]);
       cudaEventDestroy(ev_comp[k]);
       cudaEventDestroy(ev_out[k]);
     }
-    cudaEventDestroy(ev_prep);
   };
-  if (cudaEventRecord(ev_prep, cs) != cudaSuccess || cudaStreamWaitEvent(ax, ev_prep, 0) != cudaSuccess) {
-    release();
-    return cuda_fail(cudaGetLastError(), "batch fork");
-  }
   for (int i = 0; i < n_items; ++i) {
     const osgpu_host_trace_item& it = items[i];
     const int k = i & 1;
     const size_t bytes = (size_t)(it.grid.nx * it.grid.ny) * 16;
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
-    rc = prepare_trace(c, it.in, bytes / 16, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, ax);
+    rc = prepare_trace(c, it.in, bytes / 16, it.grid, it.steps, it.n_steps, *cfg, f32, E, R,
+                       aux.ax);
     if (reports && reports_stride > 0)
       for (int s = 0; s < it.n_steps && s < reports_stride && s < (int)R.size(); ++s)
         reports[(size_t)i * reports_stride + s] = R[s];
@@ -1735,9 +1764,13 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
       release();
       return rc;
     }
-    cudaError_t e = cudaEventRecord(ev_prep, ax);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_prep, 0);
-    if (e == cudaSuccess && i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
+    if ((rc = aux.ready())) {
+      release();
+      return rc;
+    }
+    aux.free_after(E);
+    cudaError_t e = cudaSuccess;
+    if (i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
     if (e == cudaSuccess) e = cudaMemcpyAsync(din[k].p, it.in, bytes, cudaMemcpyHostToDevice, si);
     if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], si);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_in[k], 0);
@@ -1755,16 +1788,11 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
     if (e == cudaSuccess) e = cudaStreamWaitEvent(so, ev_comp[k], 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(it.out, dout[k].p, bytes, cudaMemcpyDeviceToHost, so);
     if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], so);
-    if (e == cudaSuccess && prev_k >= 0) e = cudaStreamWaitEvent(ax, ev_comp[prev_k], 0);
     if (e != cudaSuccess) {
       release();
       return cuda_fail(e, "batch copy out");
     }
-    prevE.clear();  // item i - 1 has completed on cs before ax reaches these frees
-    prevE = std::move(E);
-    prev_k = k;
   }
-  if (prev_k >= 0 && cudaStreamWaitEvent(ax, ev_comp[prev_k], 0) == cudaSuccess) prevE.clear();
   int status = 0;
   cudaError_t e = cudaStreamSynchronize(so);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, cs);
@@ -1789,34 +1817,8 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
   cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   const int f32 = dtype == OSGPU_C64;
   const int c128 = dtype == OSGPU_C128;
-  // The element tables of item i are built on the auxiliary stream while item
-  // i - 1 runs on st (fork from st at entry, join at exit; also under graph
-  // capture).  Item i's tables are freed on the auxiliary stream once item i
-  // has completed on st.
-  if (!c.aux) CK(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
-  cudaStream_t ax = c.aux;
-  cudaEvent_t ev = pool_event(c);
-  CK(cudaEventRecord(ev, st));
-  CK(cudaStreamWaitEvent(ax, ev, 0));
-  std::vector<Elements> prevE;
-  cudaEvent_t prev_done = nullptr;
-  struct OnExit {  // an early return must not free tables that queued work still reads
-    std::vector<Elements>& e;
-    cudaEvent_t& done;
-    cudaStream_t ax;
-    ~OnExit() {
-      if (done) cudaStreamWaitEvent(ax, done, 0);
-      e.clear();
-    }
-  } on_exit{prevE, prev_done, ax};
-  auto release_prev = [&]() -> int {
-    if (!prev_done) return OSGPU_OK;
-    CK(cudaStreamWaitEvent(ax, prev_done, 0));
-    prevE.clear();  // frees stream-ordered on ax, after item i - 1 completed
-    c.event_pool.push_back(prev_done);
-    prev_done = nullptr;
-    return OSGPU_OK;
-  };
+  AuxTables aux;
+  if ((rc = aux.fork(c, st))) return rc;
   for (int i = 0; i < n_items; ++i) {
     const osgpu_trace_item& it = items[i];
     if (!it.d_in || !it.d_out || it.n_steps < 0 || (it.n_steps > 0 && !it.steps))
@@ -1824,7 +1826,7 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
     if (it.grid.nx == 0 || it.grid.ny == 0) return OSGPU_E_EMPTY_GRID;
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
-    rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, ax);
+    rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, aux.ax);
     if (reports && reports_stride > 0)
       for (int s = 0; s < it.n_steps && s < reports_stride && s < (int)R.size(); ++s)
         reports[(size_t)i * reports_stride + s] = R[s];
@@ -1832,24 +1834,13 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
       set_err("batch item %d: %s", i, t_err);
       return rc;
     }
-    CK(cudaEventRecord(ev, ax));
-    CK(cudaStreamWaitEvent(st, ev, 0));
+    if ((rc = aux.ready())) return rc;
+    aux.free_after(E);
     if ((rc = run_trace(c, it.d_in, c128, it.d_out, c128, it.grid, it.steps, it.n_steps, E, R,
-                        *cfg, f32, st))) {
-      cudaStreamSynchronize(st);  // E's tables may be read by what was queued
+                        *cfg, f32, st)))
       return rc;
-    }
-    cudaEvent_t done = pool_event(c);
-    CK(cudaEventRecord(done, st));
-    if ((rc = release_prev())) return rc;
-    prevE = std::move(E);
-    prev_done = done;
   }
-  if ((rc = release_prev())) return rc;
-  CK(cudaEventRecord(ev, ax));
-  CK(cudaStreamWaitEvent(st, ev, 0));
-  c.event_pool.push_back(ev);
-  return OSGPU_OK;
+  return aux.ready();  // join
 }
 
 // ------------------------------------------------------------ graphs
@@ -1981,12 +1972,14 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
       record = true;
     }
   }
+  AuxTables aux;
+  if ((rc = aux.fork(c, st))) return rc;
   for (int f = 0; f < n_frames; ++f) {
     const osgpu_frame& fr = frames[f];
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
     std::vector<Chain> ch;
-    rc = prepare_trace(c, nullptr, 0, fr.grid, fr.steps, fr.n_steps, *cfg, f32, E, R, st);
+    rc = prepare_trace(c, nullptr, 0, fr.grid, fr.steps, fr.n_steps, *cfg, f32, E, R, aux.ax);
     if (reports && reports_stride > 0)
       for (int s = 0; s < fr.n_steps && s < reports_stride && s < (int)R.size(); ++s)
         reports[(size_t)f * reports_stride + s] = R[s];
@@ -1994,6 +1987,8 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
       set_err("frame %d: %s", f, t_err);
       return rc;
     }
+    if ((rc = aux.ready())) return rc;
+    aux.free_after(E);
     if ((rc = make_chains(fr.steps, fr.n_steps, E, f32, ch))) return rc;
     const size_t pl = (fr.grid.nx * fr.grid.ny * es + 255) & ~(size_t)255;
     DBuf work;
@@ -2008,7 +2003,7 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
     tape->valid = 1;
     tape->dtype = dtype;
   }
-  return OSGPU_OK;
+  return aux.ready();  // join
 }
 
 int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
@@ -2041,16 +2036,20 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
   cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   const int f32 = dtype == OSGPU_C64, c128 = dtype == OSGPU_C128;
   const size_t es = c128 ? 16 : 8;
+  AuxTables aux;
+  if ((rc = aux.fork(c, st))) return rc;
   for (int f = 0; f < n_frames; ++f) {
     const osgpu_frame& fr = frames[f];
     const osgpu_grid& g = fr.grid;
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
     std::vector<Chain> ch;
-    if ((rc = prepare_trace(c, nullptr, 0, g, fr.steps, fr.n_steps, *cfg, f32, E, R, st))) {
+    if ((rc = prepare_trace(c, nullptr, 0, g, fr.steps, fr.n_steps, *cfg, f32, E, R, aux.ax))) {
       set_err("frame %d: %s", f, t_err);
       return rc;
     }
+    if ((rc = aux.ready())) return rc;
+    aux.free_after(E);
     if ((rc = make_chains(fr.steps, fr.n_steps, E, f32, ch))) return rc;
     const int K = (int)ch.size() - 1;
     const size_t pl = (g.nx * g.ny * es + 255) & ~(size_t)255;
@@ -2122,7 +2121,7 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
       if ((rc = run_prop_dispatch(c, j, f32, st))) return rc;
     }
   }
-  return OSGPU_OK;
+  return aux.ready();  // join
 }
 
 namespace {
