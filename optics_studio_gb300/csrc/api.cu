@@ -200,6 +200,7 @@ struct Elements {
   ElementList list;
   std::vector<DBuf> lattices;
   DBuf tables;
+  DBuf prop_tables;  // per-axis tables of the propagation after this step (prebuild_tables)
 };
 
 // Element tables of the next batch item / frame are built on the auxiliary
@@ -221,6 +222,7 @@ struct AuxTables {
   void free_after(std::vector<Elements>& E) const {
     for (Elements& e : E) {
       e.tables.s = st;
+      e.prop_tables.s = st;
       for (DBuf& l : e.lattices) l.s = st;
     }
   }
@@ -352,12 +354,107 @@ struct PropJob {
   int adj_uin_c128;
   void* adj_grad[kMaxElements];
   const void* kspec_ext;  // ENG_KEVEN: the plan's quarter table
+  const void* tables_pre;  // ASM / Fresnel TF: per-axis tables already built (prebuild_tables)
 };
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 template <typename T>
 int run_prop(Context& c, const PropJob& j, cudaStream_t st);
+
+// Per-axis transfer-function tables of an ASM / Fresnel TF propagation
+// (k_axis_prep): byte offsets within one allocation.
+struct TfLayout {
+  size_t fxv, fyv, Ex, Ey, cah, cal, sa, bh, bl, km, rt, total;
+};
+
+TfLayout tf_layout(size_t Px, size_t Py) {
+  TfLayout L;
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off += align256(bytes);
+    return o;
+  };
+  L.fxv = carve(Px * 8);
+  L.fyv = carve(Py * 8);
+  L.Ex = carve(Px * 8);
+  L.Ey = carve(Py * 8);
+  L.cah = carve(Px * 4);
+  L.cal = carve(Px * 4);
+  L.sa = carve(Px * 4);
+  L.bh = carve(Py * 4);
+  L.bl = carve(Py * 4);
+  L.km = carve(Px * 4);
+  L.rt = carve(Py * 16);
+  L.total = off;
+  return L;
+}
+
+void tf_bind(PropArgs& a, char* tb, const TfLayout& L) {
+  a.fxv = reinterpret_cast<const double*>(tb + L.fxv);
+  a.fyv = reinterpret_cast<const double*>(tb + L.fyv);
+  a.Ex = reinterpret_cast<const float2*>(tb + L.Ex);
+  a.Ey = reinterpret_cast<const float2*>(tb + L.Ey);
+  a.ca_hi = reinterpret_cast<const float*>(tb + L.cah);
+  a.ca_lo = reinterpret_cast<const float*>(tb + L.cal);
+  a.sa = reinterpret_cast<const float*>(tb + L.sa);
+  a.b_hi = reinterpret_cast<const float*>(tb + L.bh);
+  a.b_lo = reinterpret_cast<const float*>(tb + L.bl);
+  a.kmax = reinterpret_cast<const int*>(tb + L.km);
+  a.rowtab = tb + L.rt;
+}
+
+// Scalars of the transfer function shared by k_axis_prep and pass B.
+void tf_scalars(PropArgs& a, const PropJob& j, int is_d) {
+  if (j.engine == ENG_ASM) {
+    const double lam_n = j.g.lambda / j.medium;
+    a.lam_n = lam_n;
+    a.kz = (2.0 * PI / lam_n) * j.z;
+    a.band_limited = j.band_limited;
+    a.lim_x = j.lim_x;
+    a.lim_y = j.lim_y;
+    a.h_mode = is_d ? 0
+                    : asm_f32_split_ok(j.g, j.z, j.medium, j.Px, j.Py, j.band_limited != 0,
+                                       j.lim_x, j.lim_y);
+  } else {
+    a.kz = (2.0 * PI / j.g.lambda) * j.z;
+    a.cfr = PI * j.g.lambda * j.z;
+    a.h_mode = is_d ? 0 : 1;
+  }
+  a.Kf = (float)a.kz;
+}
+
+// Builds the per-axis tables of propagation j on stream st into `keep`
+// (prepare_trace: on the auxiliary stream, ahead of the item's passes).
+// Leaves `keep` empty when the job has no such tables or will take a
+// kernel-spectrum plan.
+int prebuild_tables(Context& c, const PropJob& j, int is_d, DBuf& keep, cudaStream_t st) {
+  if (j.engine != ENG_ASM && j.engine != ENG_FRESNEL_TF) return OSGPU_OK;
+  if (!is_d && c.plans_on && j.engine == ENG_ASM &&
+      (j.Px > 2 * j.g.nx || j.Py > 2 * j.g.ny))
+    return OSGPU_OK;
+  PropArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nx = (int)j.g.nx;
+  a.ny = (int)j.g.ny;
+  a.dx = j.g.dx;
+  a.dy = j.g.dy;
+  a.ax = make_axis(a.nx, (int)j.Px);
+  a.ay = make_axis(a.ny, (int)j.Py);
+  if (a.ax.nst < 0 || a.ay.nst < 0) return OSGPU_OK;  // run_prop reports it
+  a.engine = j.engine;
+  a.lam = j.g.lambda;
+  a.z = j.z;
+  a.scale = 1.0 / ((double)j.Px * (double)j.Py);
+  tf_scalars(a, j, is_d);
+  const TfLayout L = tf_layout(j.Px, j.Py);
+  CK(keep.alloc(L.total, st));
+  tf_bind(a, reinterpret_cast<char*>(keep.p), L);
+  ProfScope ps(c, st, PC_PREP, 0.0);
+  CK(is_d ? launch_asm_prep<double>(a, nullptr, st) : launch_asm_prep<float>(a, nullptr, st));
+  return OSGPU_OK;
+}
 
 __global__ void k_unit_sample(double2* p) { *p = make_double2(1.0, 0.0); }
 
@@ -560,21 +657,11 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
     return o;
   };
   const size_t o_work = carve(Px * ny * es);
-  size_t o_fxv = 0, o_fyv = 0, o_Ex = 0, o_Ey = 0, o_cah = 0, o_cal = 0, o_sa = 0, o_bh = 0,
-         o_bl = 0, o_km = 0, o_hx = 0, o_hy = 0, o_tmp = 0, o_ks = 0, o_rt = 0;
+  size_t o_tf = 0, o_hx = 0, o_hy = 0, o_tmp = 0, o_ks = 0;
   const bool tf = (j.engine == ENG_ASM || j.engine == ENG_FRESNEL_TF);
+  const TfLayout L = tf_layout(Px, Py);
   if (tf) {
-    o_fxv = carve(Px * 8);
-    o_fyv = carve(Py * 8);
-    o_Ex = carve(Px * 8);
-    o_Ey = carve(Py * 8);
-    o_cah = carve(Px * 4);
-    o_cal = carve(Px * 4);
-    o_sa = carve(Px * 4);
-    o_bh = carve(Py * 4);
-    o_bl = carve(Py * 4);
-    o_km = carve(Px * 4);
-    o_rt = carve(Py * 16);
+    if (!j.tables_pre) o_tf = carve(L.total);
   } else if (j.engine == ENG_KSEP) {
     o_hx = carve(Px * es);
     o_hy = carve(Py * es);
@@ -588,35 +675,13 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
   char* base = reinterpret_cast<char*>(ws.p);
   a.work = base + o_work;
   if (tf) {
-    a.fxv = reinterpret_cast<const double*>(base + o_fxv);
-    a.fyv = reinterpret_cast<const double*>(base + o_fyv);
-    a.Ex = reinterpret_cast<const float2*>(base + o_Ex);
-    a.Ey = reinterpret_cast<const float2*>(base + o_Ey);
-    a.ca_hi = reinterpret_cast<const float*>(base + o_cah);
-    a.ca_lo = reinterpret_cast<const float*>(base + o_cal);
-    a.sa = reinterpret_cast<const float*>(base + o_sa);
-    a.b_hi = reinterpret_cast<const float*>(base + o_bh);
-    a.b_lo = reinterpret_cast<const float*>(base + o_bl);
-    a.kmax = reinterpret_cast<const int*>(base + o_km);
-    a.rowtab = base + o_rt;
-    if (j.engine == ENG_ASM) {
-      const double lam_n = j.g.lambda / j.medium;
-      a.lam_n = lam_n;
-      a.kz = (2.0 * PI / lam_n) * j.z;
-      a.band_limited = j.band_limited;
-      a.lim_x = j.lim_x;
-      a.lim_y = j.lim_y;
-      a.h_mode = is_d ? 0
-                      : asm_f32_split_ok(j.g, j.z, j.medium, j.Px, j.Py, j.band_limited != 0,
-                                         j.lim_x, j.lim_y);
-    } else {
-      a.kz = (2.0 * PI / j.g.lambda) * j.z;
-      a.cfr = PI * j.g.lambda * j.z;
-      a.h_mode = is_d ? 0 : 1;
+    tf_bind(a, j.tables_pre ? reinterpret_cast<char*>(const_cast<void*>(j.tables_pre))
+                            : base + o_tf, L);
+    tf_scalars(a, j, is_d);
+    if (!j.tables_pre) {
+      ProfScope ps(c, st, PC_PREP, 0.0);
+      CK(launch_asm_prep<T>(a, nullptr, st));
     }
-    a.Kf = (float)a.kz;
-    ProfScope ps(c, st, PC_PREP, 0.0);
-    CK(launch_asm_prep<T>(a, nullptr, st));
   } else if (j.engine == ENG_KSEP) {
     a.hx = base + o_hx;
     a.hy = base + o_hy;
@@ -636,6 +701,12 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
     ProfScope ps(c, st, PC_KSPEC, 0.0);
     CK(launch_rs_kspec<T>(b, base + o_ks, base + o_tmp, st));
     a.kspec = base + o_ks;
+  }
+  // every engine's spectrum data must be in place before pass B reads it
+  if ((tf && (!a.fxv || !a.rowtab)) || (j.engine == ENG_KSEP && (!a.hx || !a.hy)) ||
+      ((j.engine == ENG_KSPEC || j.engine == ENG_KEVEN) && !a.kspec)) {
+    set_err("internal: transfer-function data of engine %d missing", j.engine);
+    return OSGPU_E_UNSUPPORTED;
   }
   const double nin = (double)j.g.nx * j.g.ny, nsp = (double)Px * ny;
   const double el_bytes = element_bytes(j.els, !is_d);
@@ -945,7 +1016,6 @@ int forward_frame(Context& c, const osgpu_frame& fr, const std::vector<Elements>
                   const std::vector<osgpu_asm_report>& R, const std::vector<Chain>& ch,
                   const osgpu_asm_config& cfg, int f32, int c128, PlaneFn plane,
                   bool want_last_field, cudaStream_t st) {
-  (void)E;
   const osgpu_grid& g = fr.grid;
   const void* src = fr.d_source;
   const int K = (int)ch.size() - 1;  // propagations
@@ -957,6 +1027,7 @@ int forward_frame(Context& c, const osgpu_frame& fr, const std::vector<Elements>
     sc.medium = fr.steps[s].medium;
     PropJob j;
     fill_asm_job(j, g, fr.steps[s].z_after, R[s], sc);
+    j.tables_pre = E[s].prop_tables.p;
     j.els = ch[k].list;
     j.d_in = src;
     j.in_c128 = c128;
@@ -1589,6 +1660,9 @@ int prepare_trace(Context& c, const double* host_in, size_t n, const osgpu_grid&
         return rc;
       }
       if (first_prop < 0) first_prop = s;
+      PropJob pj;
+      fill_asm_job(pj, g, steps[s].z_after, R[s], sc);
+      if ((rc = prebuild_tables(c, pj, !f32, E[s].prop_tables, st))) return rc;
     }
   }
   return OSGPU_OK;
@@ -1646,6 +1720,7 @@ int run_trace(Context& c, const void* d_in, int in_c128, void* d_out, int out_c1
       sc.medium = steps[s].medium;
       PropJob j;
       fill_asm_job(j, g, steps[s].z_after, R[s], sc);
+      j.tables_pre = E[s].prop_tables.p;
       pending.fast = f32 && pending_fast;
       j.els = pending;
       j.d_in = src;
