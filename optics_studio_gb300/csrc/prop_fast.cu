@@ -8,6 +8,7 @@
 // Pass B runs one CTA per spectral column kx: the transfer functions of the
 // engines it serves are even in fy, so one shared-memory table of
 // H(kx, |k_y|) for |k_y| <= Py/2 serves both halves of the column.
+#include <algorithm>
 #include <cstdlib>
 
 #include "fft_reg.cuh"
@@ -780,6 +781,98 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passC_tile(Pro
   }
 }
 
+// Pass C, persistent and software-pipelined: a CTA of two row groups walks
+// its 2-row tiles; the next sub-transform's tile (2 rows x M columns, 16 bytes
+// per column) is copied into a shared staging buffer with cp.async while the
+// groups transform the current one, so the strided spectrum reads overlap
+// the FFTs.  Needs ny % 2 == 0.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int M, bool ADJ>
+__global__ void __launch_bounds__(2 * (M / 16), 2) k_passC_pipe(PropArgs a) {
+  constexpr int T = M / 16;
+  constexpr int SBT = tile_stride<M>();
+  constexpr int NT = 2 * T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = a.nx, ny = a.ny, rx = a.ax.r;
+  const int n_tiles = ny / 2;
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  float4* stage = reinterpret_cast<float4*>(bufs + 2 * SBT);  // column p: (row 0, row 1)
+  float2* tb = reinterpret_cast<float2*>(stage + M);
+  float2* tq = tb + rx * T;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  float2* buf = bufs + g * SBT;
+  const float2* W = reinterpret_cast<const float2*>(a.work);
+  pdl_trigger();
+  copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
+  load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
+  pdl_wait();  // pass B's spectrum is complete
+  auto issue = [&](int tile, int s) {
+    const float2* src = W + (size_t)s * ny + 2 * tile;
+    for (int p = threadIdx.x; p < M; p += NT) cp_async16(stage + p, src + (size_t)rx * p * ny);
+    cp_async_commit();
+  };
+  int tile = blockIdx.x;
+  if (tile < n_tiles) issue(tile, 0);
+  for (; tile < n_tiles; tile += gridDim.x) {
+    float2 acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
+    for (int s = 0; s < rx; ++s) {
+      cp_async_wait_all();
+      __syncthreads();  // the tile of sub-transform s is in the staging buffer
+      float2 v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const float4 t = stage[tid + T * q];
+        v[q] = g ? make_float2(t.z, t.w) : make_float2(t.x, t.y);
+      }
+      __syncthreads();  // every group holds its row: the buffer takes the next tile
+      int ns = s + 1, nt = tile;
+      if (ns == rx) {
+        ns = 0;
+        nt = tile + gridDim.x;
+      }
+      if (nt < n_tiles) issue(nt, ns);
+      fft1s<M, true>(v, buf, tws, tid, 1 + g, T);
+      const float2 wb = tb[s * T + tid];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float2 y = v[q];
+        if (s > 0) y = cmulc(y, cmul(wb, tq[s * 16 + q]));
+        acc[q] = cadd(acc[q], y);
+      }
+    }
+    const int iy = 2 * tile + g;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int j = tid + T * q;
+      if (j >= nx) continue;
+      float2 v = acc[q];
+      const size_t o = (size_t)iy * nx + j;
+      if (ADJ) {  // adjoint element plane (a.adj)
+        const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
+        adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x, v.y);
+      }
+      if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
+      if (a.out) {
+        if (a.out_c128) reinterpret_cast<double2*>(a.out)[o] = make_double2(v.x, v.y);
+        else reinterpret_cast<float2*>(a.out)[o] = v;
+      }
+      if (a.out_intensity) a.out_intensity[o] = v.x * v.x + v.y * v.y;
+      if (a.out_intensity64) a.out_intensity64[o] = (double)v.x * v.x + (double)v.y * v.y;
+    }
+  }
+  cp_async_wait_all();  // no copy outlives the CTA
+}
+
 template <int M>
 constexpr bool r4_ok() {
   return M >= 512 && M <= 2048;
@@ -938,8 +1031,42 @@ cudaError_t launch_C_tile(const PropArgs& a, cudaStream_t st) {
 }
 
 template <int M>
+size_t smem_cpipe(int r) {
+  constexpr int T = M / 16;
+  return ((size_t)TwLay<M>::SIZE + 2 * (size_t)tile_stride<M>() + 2 * (size_t)M +
+          (size_t)r * (T + 16)) * sizeof(float2);
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+template <int M, bool ADJ>
+cudaError_t launch_C_pipe(const PropArgs& a, cudaStream_t st) {
+  const size_t smem = smem_cpipe<M>(a.ax.r);
+  cudaError_t e = cudaFuncSetAttribute(k_passC_pipe<M, ADJ>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int tiles = a.ny / 2;
+  const int grid = std::min(tiles, 2 * sm_count());
+  ++launch_counter();
+  return launch_pdl(k_passC_pipe<M, ADJ>, dim3(grid), dim3(2 * (M / 16)), smem, st, a);
+}
+
+template <int M>
 cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
   if constexpr (r4_ok<M>()) {
+    // persistent pipelined 2-row tiles: 0.120 -> 0.104 ms per 2048^2 band
+    const char* pe = getenv("OSGPU_PASSC_PIPE");
+    if ((!pe || atoi(pe) != 0) && a.ny % 2 == 0 && smem_cpipe<M>(a.ax.r) <= kMaxSmemB)
+      return a.adj ? launch_C_pipe<M, true>(a, st) : launch_C_pipe<M, false>(a, st);
     // 2-row tiles (2 CTAs per SM) measured fastest on the 2048^2 workload
     // without the adjoint epilogue (0.126 -> 0.118 ms per band); the adjoint
     // epilogue spills in the tile kernels, so it keeps the one-row kernel
