@@ -201,32 +201,83 @@ struct Elements {
   std::vector<DBuf> lattices;
   DBuf tables;
   DBuf prop_tables;  // per-axis tables of the propagation after this step (prebuild_tables)
+  DBuf trans;        // f32: transmission of the element chain in front of that propagation
 };
 
-// Element tables of the next batch item / frame are built on the auxiliary
-// stream while the previous one runs on the compute stream: fork() makes the
-// auxiliary stream follow the compute stream's work so far, ready() makes the
-// compute stream wait for the tables built so far (the last ready() also
-// joins the auxiliary stream back, as graph capture requires), and
-// free_after() moves the frees of a built item's buffers to the compute
-// stream, where they follow the kernels that read them.
+// Element tables (and per-axis propagation tables and chain transmissions)
+// of the next batch item / frame are built on the auxiliary stream while the
+// previous one runs on the compute stream.  fork() makes the auxiliary
+// stream follow the compute stream's work so far; ready() makes the compute
+// stream wait for the tables built so far (the one in finish() also joins the
+// auxiliary stream back, as graph capture requires).  An item's buffers are
+// allocated and freed on the auxiliary stream, so the pool reuses them in
+// stream order: take() hands them over for the item's passes, end() marks
+// the passes queued, and begin() of the item after next frees them once that
+// item has completed on the compute stream (two generations in flight keep
+// the tables of item i + 1 building while item i runs).  The destructor
+// covers early returns: it waits for everything queued so far.
 struct AuxTables {
   cudaStream_t st = nullptr, ax = nullptr;
-  cudaEvent_t ev = nullptr;
+  cudaEvent_t ev = nullptr, e0 = nullptr, e1 = nullptr;
+  std::vector<Elements> cur, gen0, gen1;
+  bool joined = false;
   int fork(Context& c, cudaStream_t compute);
   int ready() {
     CK(cudaEventRecord(ev, ax));
     CK(cudaStreamWaitEvent(st, ev, 0));
     return OSGPU_OK;
   }
-  void free_after(std::vector<Elements>& E) const {
-    for (Elements& e : E) {
-      e.tables.s = st;
-      e.prop_tables.s = st;
-      for (DBuf& l : e.lattices) l.s = st;
+  int begin() {
+    if (!e0) return OSGPU_OK;
+    CK(cudaStreamWaitEvent(ax, e0, 0));
+    gen0.clear();
+    cudaEventDestroy(e0);
+    e0 = nullptr;
+    return OSGPU_OK;
+  }
+  std::vector<Elements>& take(std::vector<Elements>& E) {
+    cur = std::move(E);
+    return cur;
+  }
+  int end() {
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaEventRecord(e, st));
+    if (e0) {  // begin() was skipped: keep the order of the frees
+      CK(cudaStreamWaitEvent(ax, e0, 0));
+      gen0.clear();
+      cudaEventDestroy(e0);
     }
+    gen0 = std::move(gen1);
+    e0 = e1;
+    gen1 = std::move(cur);
+    e1 = e;
+    cur.clear();
+    return OSGPU_OK;
+  }
+  int finish() {
+    int rc;
+    if ((rc = begin())) return rc;
+    if (e1) {
+      CK(cudaStreamWaitEvent(ax, e1, 0));
+      gen1.clear();
+      cudaEventDestroy(e1);
+      e1 = nullptr;
+    }
+    if ((rc = ready())) return rc;
+    joined = true;
+    return OSGPU_OK;
   }
   ~AuxTables() {
+    if (ev && ax && !joined) {  // early return: free only after what was queued on st
+      cudaEventRecord(ev, st);
+      cudaStreamWaitEvent(ax, ev, 0);
+    }
+    cur.clear();
+    gen0.clear();
+    gen1.clear();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
     if (ev) cudaEventDestroy(ev);
   }
 };
@@ -355,6 +406,7 @@ struct PropJob {
   void* adj_grad[kMaxElements];
   const void* kspec_ext;  // ENG_KEVEN: the plan's quarter table
   const void* tables_pre;  // ASM / Fresnel TF: per-axis tables already built (prebuild_tables)
+  const float2* trans;     // f32: precomputed transmission of els (prepare_trace)
 };
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -641,6 +693,7 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
   a.adj_uin = j.adj_uin;
   a.adj_uin_c128 = j.adj_uin_c128;
   for (int q = 0; q < kMaxElements; ++q) a.adj_grad[q] = j.adj_grad[q];
+  a.trans = is_d ? nullptr : j.trans;
   int rc;
   if ((rc = get_tw(c, a.ax.m, is_d, &a.tw_mx))) return rc;
   if ((rc = get_tw(c, a.ay.m, is_d, &a.tw_my))) return rc;
@@ -1028,6 +1081,7 @@ int forward_frame(Context& c, const osgpu_frame& fr, const std::vector<Elements>
     PropJob j;
     fill_asm_job(j, g, fr.steps[s].z_after, R[s], sc);
     j.tables_pre = E[s].prop_tables.p;
+    j.trans = reinterpret_cast<const float2*>(E[s].trans.p);
     j.els = ch[k].list;
     j.d_in = src;
     j.in_c128 = c128;
@@ -1665,6 +1719,35 @@ int prepare_trace(Context& c, const double* host_in, size_t n, const osgpu_grid&
       if ((rc = prebuild_tables(c, pj, !f32, E[s].prop_tables, st))) return rc;
     }
   }
+  // f32: the element chain in front of each propagation as one transmission
+  // per sample (built here, on the preparing stream; pass A multiplies by it)
+  if (f32) {
+    ElementList pend;
+    std::memset(&pend, 0, sizeof(pend));
+    bool ok = true;
+    for (int s = 0; s < n_steps; ++s) {
+      for (int q = 0; q < E[s].list.count; ++q) {
+        if (pend.count == kMaxElements) {  // run_trace applies these on their own
+          ok = false;
+          pend.count = 0;
+        }
+        pend.el[pend.count++] = E[s].list.el[q];
+        ok = ok && E[s].list.fast;
+      }
+      if (steps[s].z_after != 0.0) {
+        if (ok && pend.count > 0) {
+          pend.fast = 1;
+          const size_t ns = (size_t)g.nx * g.ny;
+          CK(E[s].trans.alloc(ns * sizeof(float2), st));
+          ProfScope ps(c, st, PC_ELEMENTS, 0.0);
+          CK(launch_transmission(pend, (int)g.nx, (int)g.ny,
+                                 reinterpret_cast<float2*>(E[s].trans.p), st));
+        }
+        pend.count = 0;
+        ok = true;
+      }
+    }
+  }
   return OSGPU_OK;
 }
 
@@ -1721,6 +1804,7 @@ int run_trace(Context& c, const void* d_in, int in_c128, void* d_out, int out_c1
       PropJob j;
       fill_asm_job(j, g, steps[s].z_after, R[s], sc);
       j.tables_pre = E[s].prop_tables.p;
+      j.trans = reinterpret_cast<const float2*>(E[s].trans.p);
       pending.fast = f32 && pending_fast;
       j.els = pending;
       j.d_in = src;
@@ -1827,6 +1911,10 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
     const osgpu_host_trace_item& it = items[i];
     const int k = i & 1;
     const size_t bytes = (size_t)(it.grid.nx * it.grid.ny) * 16;
+    if ((rc = aux.begin())) {
+      release();
+      return rc;
+    }
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
     rc = prepare_trace(c, it.in, bytes / 16, it.grid, it.steps, it.n_steps, *cfg, f32, E, R,
@@ -1843,7 +1931,7 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
       release();
       return rc;
     }
-    aux.free_after(E);
+    std::vector<Elements>& Ei = aux.take(E);
     cudaError_t e = cudaSuccess;
     if (i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
     if (e == cudaSuccess) e = cudaMemcpyAsync(din[k].p, it.in, bytes, cudaMemcpyHostToDevice, si);
@@ -1854,7 +1942,7 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
       release();
       return cuda_fail(e, "batch copy in");
     }
-    if ((rc = run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, E, R, *cfg,
+    if ((rc = run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, Ei, R, *cfg,
                         f32, cs))) {
       release();
       return rc;
@@ -1863,10 +1951,18 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
     if (e == cudaSuccess) e = cudaStreamWaitEvent(so, ev_comp[k], 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(it.out, dout[k].p, bytes, cudaMemcpyDeviceToHost, so);
     if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], so);
+    if (e == cudaSuccess && (rc = aux.end())) {
+      release();
+      return rc;
+    }
     if (e != cudaSuccess) {
       release();
       return cuda_fail(e, "batch copy out");
     }
+  }
+  if ((rc = aux.finish())) {
+    release();
+    return rc;
   }
   int status = 0;
   cudaError_t e = cudaStreamSynchronize(so);
@@ -1899,6 +1995,7 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
     if (!it.d_in || !it.d_out || it.n_steps < 0 || (it.n_steps > 0 && !it.steps))
       return OSGPU_E_BAD_ARGUMENT;
     if (it.grid.nx == 0 || it.grid.ny == 0) return OSGPU_E_EMPTY_GRID;
+    if ((rc = aux.begin())) return rc;
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
     rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, aux.ax);
@@ -1910,12 +2007,13 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
       return rc;
     }
     if ((rc = aux.ready())) return rc;
-    aux.free_after(E);
-    if ((rc = run_trace(c, it.d_in, c128, it.d_out, c128, it.grid, it.steps, it.n_steps, E, R,
+    std::vector<Elements>& Ei = aux.take(E);
+    if ((rc = run_trace(c, it.d_in, c128, it.d_out, c128, it.grid, it.steps, it.n_steps, Ei, R,
                         *cfg, f32, st)))
       return rc;
+    if ((rc = aux.end())) return rc;
   }
-  return aux.ready();  // join
+  return aux.finish();
 }
 
 // ------------------------------------------------------------ graphs
@@ -2051,10 +2149,11 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
   if ((rc = aux.fork(c, st))) return rc;
   for (int f = 0; f < n_frames; ++f) {
     const osgpu_frame& fr = frames[f];
-    std::vector<Elements> E;
+    if ((rc = aux.begin())) return rc;
+    std::vector<Elements> E0;
     std::vector<osgpu_asm_report> R;
     std::vector<Chain> ch;
-    rc = prepare_trace(c, nullptr, 0, fr.grid, fr.steps, fr.n_steps, *cfg, f32, E, R, aux.ax);
+    rc = prepare_trace(c, nullptr, 0, fr.grid, fr.steps, fr.n_steps, *cfg, f32, E0, R, aux.ax);
     if (reports && reports_stride > 0)
       for (int s = 0; s < fr.n_steps && s < reports_stride && s < (int)R.size(); ++s)
         reports[(size_t)f * reports_stride + s] = R[s];
@@ -2063,7 +2162,7 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
       return rc;
     }
     if ((rc = aux.ready())) return rc;
-    aux.free_after(E);
+    std::vector<Elements>& E = aux.take(E0);
     if ((rc = make_chains(fr.steps, fr.n_steps, E, f32, ch))) return rc;
     const size_t pl = (fr.grid.nx * fr.grid.ny * es + 255) & ~(size_t)255;
     DBuf work;
@@ -2073,12 +2172,13 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
       return record ? static_cast<void*>(base + (size_t)k * pl) : work.p;
     };
     if ((rc = forward_frame(c, fr, E, R, ch, *cfg, f32, c128, plane, record, st))) return rc;
+    if ((rc = aux.end())) return rc;
   }
   if (record) {
     tape->valid = 1;
     tape->dtype = dtype;
   }
-  return aux.ready();  // join
+  return aux.finish();
 }
 
 int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
@@ -2116,15 +2216,16 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
   for (int f = 0; f < n_frames; ++f) {
     const osgpu_frame& fr = frames[f];
     const osgpu_grid& g = fr.grid;
-    std::vector<Elements> E;
+    if ((rc = aux.begin())) return rc;
+    std::vector<Elements> E0;
     std::vector<osgpu_asm_report> R;
     std::vector<Chain> ch;
-    if ((rc = prepare_trace(c, nullptr, 0, g, fr.steps, fr.n_steps, *cfg, f32, E, R, aux.ax))) {
+    if ((rc = prepare_trace(c, nullptr, 0, g, fr.steps, fr.n_steps, *cfg, f32, E0, R, aux.ax))) {
       set_err("frame %d: %s", f, t_err);
       return rc;
     }
     if ((rc = aux.ready())) return rc;
-    aux.free_after(E);
+    std::vector<Elements>& E = aux.take(E0);
     if ((rc = make_chains(fr.steps, fr.n_steps, E, f32, ch))) return rc;
     const int K = (int)ch.size() - 1;
     const size_t pl = (g.nx * g.ny * es + 255) & ~(size_t)255;
@@ -2195,8 +2296,9 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
       j.out_c128 = c128;
       if ((rc = run_prop_dispatch(c, j, f32, st))) return rc;
     }
+    if ((rc = aux.end())) return rc;
   }
-  return aux.ready();  // join
+  return aux.finish();
 }
 
 namespace {

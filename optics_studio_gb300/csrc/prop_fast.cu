@@ -640,7 +640,16 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(Pro
 #pragma unroll
     for (int k = 0; k < KS; ++k) bad = bad || !isfinite(xs[k].x) || !isfinite(xs[k].y);
     // per-sample stage, each kind for all KS samples at once (loads in flight together)
-    if (a.seed) {
+    if (a.trans && !a.seed && !a.adj) {  // precomputed chain transmission
+      float2 tr[KS];
+#pragma unroll
+      for (int k = 0; k < KS; ++k)
+        tr[k] = (inb >> k & 1u) ? __ldg(a.trans + (size_t)jy[k] * nx + jx[k])
+                                : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < KS; ++k)
+        if (inb >> k & 1u) xs[k] = cmul(xs[k], tr[k]);
+    } else if (a.seed) {
 #pragma unroll
       for (int k = 0; k < KS; ++k)
         if (inb >> k & 1u) xs[k] = pass_a_sample(a, jx[k], jy[k], xs[k]);

@@ -216,6 +216,20 @@ __global__ void k_screen_table(const double* v64, const float* v32, double depth
   out[i] = make_float2(c, s);
 }
 
+__global__ void k_transmission(ElementList L, int nx, int ny, float2* t) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)nx * ny) return;
+  const int ix = (int)(i % nx), iy = (int)(i / nx);
+  t[i] = apply_elements_fast(L, ix, iy, make_float2(1.f, 0.f));
+}
+
+cudaError_t launch_transmission(const ElementList& L, int nx, int ny, float2* t, cudaStream_t st) {
+  const size_t n = (size_t)nx * ny;
+  COUNT_LAUNCH();
+  k_transmission<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(L, nx, ny, t);
+  return cudaGetLastError();
+}
+
 size_t element_tables_bytes(const DevElement& e, int nx, int ny) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t b = al((size_t)ny * sizeof(int2));

@@ -67,6 +67,10 @@ struct PropArgs {
   const void* adj_uin;
   int adj_uin_c128;
   void* adj_grad[kMaxElements];
+  // f32 engine: the element chain of els precomputed as one complex
+  // transmission per sample (row-major ny x nx, launch_transmission); pass A
+  // multiplies by it instead of evaluating the chain
+  const float2* trans;
 };
 
 // Fraunhofer arguments (no padding; two passes).
@@ -132,6 +136,9 @@ cudaError_t launch_apply_elements(const void* in, int in_c128, void* out, int ou
 // f32 fast element tables (psi == 0 elements): bytes of scratch needed and
 // the build; fills e.span / tabx / taby / bilx / bily / latf.
 size_t element_tables_bytes(const DevElement& e, int nx, int ny);
+// t[iy nx + ix] = the f32 transmission of the chain L (fast tables) at each
+// sample: apply_elements_fast applied to 1.
+cudaError_t launch_transmission(const ElementList& L, int nx, int ny, float2* t, cudaStream_t st);
 cudaError_t launch_element_tables(DevElement& e, int nx, int ny, double dx, double dy,
                                   void* scratch, cudaStream_t st);
 
