@@ -2288,6 +2288,7 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
       }
       j.in_c128 = c128;
       j.els = cn.list;
+      j.trans = reinterpret_cast<const float2*>(E[s].trans.p);
       j.adj = cn.list.count > 0;
       j.adj_uin = uin(k);
       j.adj_uin_c128 = c128;

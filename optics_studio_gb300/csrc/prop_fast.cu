@@ -868,7 +868,18 @@ __global__ void __launch_bounds__(2 * (M / 16), 2) k_passC_pipe(PropArgs a) {
       const size_t o = (size_t)iy * nx + j;
       if (ADJ) {  // adjoint element plane (a.adj)
         const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
-        adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x, v.y);
+        if (a.trans && a.els.count == 1) {
+          // one element with its precomputed transmission t: v = t u,
+          // grad += -2 Im(conj(mu) v), mu <- conj(t) mu (adjoint_plane's steps)
+          const float2 t = __ldg(a.trans + o);
+          const float vr = u.x * t.x - u.y * t.y, vi = u.x * t.y + u.y * t.x;
+          if (a.adj_grad[0]) reinterpret_cast<float*>(a.adj_grad[0])[o] += -2.f * (v.x * vi + (-v.y) * vr);
+          const float nr = v.x * t.x - v.y * (-t.y), ni = v.x * (-t.y) + v.y * t.x;
+          v = make_float2(nr, ni);
+        } else {
+          adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x,
+                               v.y);
+        }
       }
       if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
       if (a.out) {
