@@ -223,10 +223,37 @@ __global__ void k_transmission(ElementList L, int nx, int ny, float2* t) {
   t[i] = apply_elements_fast(L, ix, iy, make_float2(1.f, 0.f));
 }
 
+// Four consecutive samples of a row per thread (nx % 4 == 0): the chain is
+// evaluated element by element for the four, so their table and lattice loads
+// are in flight together, and the result leaves as two 16-byte stores.
+__global__ void k_transmission4(ElementList L, int nx, int ny, float2* t) {
+  const size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const int nq = nx / 4;
+  if (q >= (size_t)nq * ny) return;
+  const int iy = (int)(q / nq), ix0 = 4 * (int)(q % nq);
+  int ix[4], iyv[4];
+  float2 v[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    ix[k] = ix0 + k;
+    iyv[k] = iy;
+    v[k] = make_float2(1.f, 0.f);
+  }
+  apply_elements_fast_k<4>(L, ix, iyv, 0xfu, v);
+  float4* o = reinterpret_cast<float4*>(t + (size_t)iy * nx + ix0);
+  o[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+  o[1] = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
+}
+
 cudaError_t launch_transmission(const ElementList& L, int nx, int ny, float2* t, cudaStream_t st) {
   const size_t n = (size_t)nx * ny;
   COUNT_LAUNCH();
-  k_transmission<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(L, nx, ny, t);
+  if (nx % 4 == 0) {
+    const size_t nq = n / 4;
+    k_transmission4<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(L, nx, ny, t);
+  } else {
+    k_transmission<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(L, nx, ny, t);
+  }
   return cudaGetLastError();
 }
 
