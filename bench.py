@@ -671,6 +671,26 @@ def main():
         with open(tpath) as f:
             traffic = json.load(f).get(dname)
 
+    # Pass B is bound by FP32 instruction issue, not by HBM: its FFT arithmetic
+    # against the nominal FP32 rate of this GPU (SMs x 128 lanes x 2 flops x
+    # max SM clock), counting 5 m log2 m flops per m-point transform (2 r
+    # transforms per spectral column: Px columns of a band).
+    props = torch.cuda.get_device_properties(local)
+    sm_clock_mhz = clk.get("sm_max_mhz") or 2070.0
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_clock_mhz * 1e6 / 1e12
+    m_fft, r_fft = N, 8192 // N
+    fft_flops = 8192 * 2 * r_fft * 5.0 * m_fft * math.log2(m_fft)
+    b_ms = kstats.get("pass_b_columns", {"total_ms": 0.0, "launches": 1})
+    b_ms = b_ms["total_ms"] / max(1, b_ms["launches"])
+    compute = None
+    if b_ms > 0:
+        compute = {"kernel": "pass_b_columns", "bound": "fp32 issue",
+                   "fft_tflops": fft_flops / (b_ms / 1e3) / 1e12,
+                   "fp32_peak_tflops": fp32_peak, "peak_source": "nominal (SMs x 128 x 2 x max clock)",
+                   "frac": fft_flops / (b_ms / 1e3) / 1e12 / fp32_peak,
+                   "note": "5 m log2 m flops per transform, 2 r transforms of m = 2048 per column; "
+                           "twiddles, H and recombination not counted"}
+
     line = {"metric": METRIC, "value": value, "unit": "propagations/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -682,7 +702,7 @@ def main():
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_src,
                          "bytes_per_launch": per_launch_bytes,
-                         "ms_per_launch": per_launch_ms},
+                         "ms_per_launch": per_launch_ms, "compute": compute},
             "kernels": kstats,
             "whole_step_hbm_gbs": all_bytes / prof_steps / (ms_step / 1e3) / 1e9,
             "kernel_stats_steps": prof_steps,

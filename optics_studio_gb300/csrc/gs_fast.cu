@@ -72,8 +72,12 @@ struct GsLay {
   static constexpr int T = M / 16;
   static constexpr int THREADS = G * T;
   static constexpr int MINB = THREADS >= 512 ? 1 : 2;  // 128 registers per thread
+  // exchange-buffer stride: the transform's padded size plus 4 entries, so
+  // that buffers 0..3 start 0, 8, 16 and 24 banks apart (the paired-lane
+  // tile gather / scatter of the row kernel reads two buffers per lane pair)
+  static constexpr int SB = Plan<M>::SMEM + 4;
   static constexpr size_t SMEM =
-      ((size_t)TwLay<M>::SIZE + (size_t)G * Plan<M>::SMEM) * sizeof(float2) + 32 * sizeof(double);
+      ((size_t)TwLay<M>::SIZE + (size_t)G * SB) * sizeof(float2) + 32 * sizeof(double);
 };
 
 template <int M, int G>
@@ -85,11 +89,11 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tws = reinterpret_cast<float2*>(smem_raw);
   float2* bufs = tws + TwLay<M>::SIZE;
-  double* red = reinterpret_cast<double*>(bufs + G * Plan<M>::SMEM);
+  double* red = reinterpret_cast<double*>(bufs + G * GsLay<M, G>::SB);
   const int g = threadIdx.x / T, tid = threadIdx.x - g * T;
   const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
   const int BAR_N = (T % 32 == 0) ? T : GsLay<M, G>::THREADS;
-  float2* buf = bufs + g * Plan<M>::SMEM;
+  float2* buf = bufs + g * GsLay<M, G>::SB;
   {  // stage-ordered table stored behind the M-point table
     const float2* twm = reinterpret_cast<const float2*>(a.tw);
     for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
@@ -157,11 +161,11 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tws = reinterpret_cast<float2*>(smem_raw);
   float2* bufs = tws + TwLay<M>::SIZE;
-  double* red = reinterpret_cast<double*>(bufs + G * Plan<M>::SMEM);
+  double* red = reinterpret_cast<double*>(bufs + G * GsLay<M, G>::SB);
   const int g = threadIdx.x / T, tid = threadIdx.x - g * T;
   const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
   const int BAR_N = (T % 32 == 0) ? T : GsLay<M, G>::THREADS;
-  float2* buf = bufs + g * Plan<M>::SMEM;
+  float2* buf = bufs + g * GsLay<M, G>::SB;
   {  // stage-ordered table stored behind the M-point table
     const float2* twm = reinterpret_cast<const float2*>(a.tw);
     for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
@@ -177,13 +181,13 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
   float d2 = 0.f;
   if (iterate) {
     if (kTile) {
-      for (int p = threadIdx.x; p < M; p += blockDim.x) {
-        const float4* src = reinterpret_cast<const float4*>(it.W + (size_t)p * M + iy0);
-        const float4 a0 = src[0], a1 = src[1];
-        bufs[p] = make_float2(a0.x, a0.y);
-        bufs[Plan<M>::SMEM + p] = make_float2(a0.z, a0.w);
-        bufs[2 * Plan<M>::SMEM + p] = make_float2(a1.x, a1.y);
-        bufs[3 * Plan<M>::SMEM + p] = make_float2(a1.z, a1.w);
+      // the two lanes of a pair read the two 16-byte halves of one 32-byte run
+      constexpr int SB = GsLay<M, G>::SB;
+      for (int h = threadIdx.x; h < 2 * M; h += blockDim.x) {
+        const int p = h >> 1, hf = h & 1;
+        const float4 a0 = reinterpret_cast<const float4*>(it.W + (size_t)p * M + iy0)[hf];
+        bufs[2 * hf * SB + p] = make_float2(a0.x, a0.y);
+        bufs[(2 * hf + 1) * SB + p] = make_float2(a0.z, a0.w);
       }
     } else {
 #pragma unroll
@@ -231,12 +235,11 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
 #pragma unroll
     for (int q = 0; q < 16; ++q) buf[tid + T * q] = v[q];
     __syncthreads();
-    for (int p = threadIdx.x; p < M; p += blockDim.x) {
-      float4* dst = reinterpret_cast<float4*>(it.W + (size_t)p * M + iy0);
-      const float2 r0 = bufs[p], r1 = bufs[Plan<M>::SMEM + p], r2 = bufs[2 * Plan<M>::SMEM + p],
-                   r3 = bufs[3 * Plan<M>::SMEM + p];
-      dst[0] = make_float4(r0.x, r0.y, r1.x, r1.y);
-      dst[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
+    constexpr int SB = GsLay<M, G>::SB;
+    for (int h = threadIdx.x; h < 2 * M; h += blockDim.x) {  // whole sectors per lane pair
+      const int p = h >> 1, hf = h & 1;
+      const float2 r0 = bufs[2 * hf * SB + p], r1 = bufs[(2 * hf + 1) * SB + p];
+      reinterpret_cast<float4*>(it.W + (size_t)p * M + iy0)[hf] = make_float4(r0.x, r0.y, r1.x, r1.y);
     }
   } else {
 #pragma unroll
