@@ -1880,10 +1880,16 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   const int f32 = precision == OSGPU_F32;
   const cudaStream_t cs = c.stream, si = c.copy_in, so = c.copy_out;
   // two device slots each way; the copy streams run ahead of the compute stream
-  DBuf din[2], dout[2];
+  // f32: complex64 slots beside the complex128 ones; the conversions run on
+  // the copy streams, so the passes read and write complex64
+  DBuf din[2], dout[2], din64[2], dout64[2];
   for (int k = 0; k < 2; ++k) {
     CK(din[k].alloc(max_n * 16, cs));
     CK(dout[k].alloc(max_n * 16, cs));
+    if (f32) {
+      CK(din64[k].alloc(max_n * 8, cs));
+      CK(dout64[k].alloc(max_n * 8, cs));
+    }
   }
   CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), cs));
   CK(cudaStreamSynchronize(cs));  // slots allocated before the copy streams use them
@@ -1935,6 +1941,7 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
     cudaError_t e = cudaSuccess;
     if (i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
     if (e == cudaSuccess) e = cudaMemcpyAsync(din[k].p, it.in, bytes, cudaMemcpyHostToDevice, si);
+    if (e == cudaSuccess && f32) e = launch_c128_to_c64(din[k].p, din64[k].p, bytes / 16, si);
     if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], si);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_in[k], 0);
     if (e == cudaSuccess && i >= 2) e = cudaStreamWaitEvent(cs, ev_out[k], 0);  // out slot drained
@@ -1942,13 +1949,16 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
       release();
       return cuda_fail(e, "batch copy in");
     }
-    if ((rc = run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, Ei, R, *cfg,
-                        f32, cs))) {
+    if ((rc = f32 ? run_trace(c, din64[k].p, 0, dout64[k].p, 0, it.grid, it.steps, it.n_steps,
+                              Ei, R, *cfg, f32, cs)
+                  : run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, Ei, R,
+                              *cfg, f32, cs))) {
       release();
       return rc;
     }
     e = cudaEventRecord(ev_comp[k], cs);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(so, ev_comp[k], 0);
+    if (e == cudaSuccess && f32) e = launch_c64_to_c128(dout64[k].p, dout[k].p, bytes / 16, so);
     if (e == cudaSuccess) e = cudaMemcpyAsync(it.out, dout[k].p, bytes, cudaMemcpyDeviceToHost, so);
     if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], so);
     if (e == cudaSuccess && (rc = aux.end())) {

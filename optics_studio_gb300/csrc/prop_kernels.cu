@@ -257,6 +257,57 @@ cudaError_t launch_transmission(const ElementList& L, int nx, int ny, float2* t,
   return cudaGetLastError();
 }
 
+__global__ void k_c128_to_c64(const double2* src, float4* dst, size_t n2) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const double2 a = src[2 * i], b = src[2 * i + 1];  // two samples
+  dst[i] = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+}
+
+__global__ void k_c64_to_c128(const float4* src, double2* dst, size_t n2) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const float4 v = src[i];
+  dst[2 * i] = make_double2(v.x, v.y);
+  dst[2 * i + 1] = make_double2(v.z, v.w);
+}
+
+__global__ void k_c128_to_c64_1(const double2* src, float2* dst, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = make_float2((float)src[i].x, (float)src[i].y);
+}
+
+__global__ void k_c64_to_c128_1(const float2* src, double2* dst, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = make_double2(src[i].x, src[i].y);
+}
+
+cudaError_t launch_c128_to_c64(const void* src, void* dst, size_t n, cudaStream_t st) {
+  COUNT_LAUNCH();
+  if (n % 2 == 0) {
+    const size_t n2 = n / 2;
+    k_c128_to_c64<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(
+        reinterpret_cast<const double2*>(src), reinterpret_cast<float4*>(dst), n2);
+  } else {
+    k_c128_to_c64_1<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        reinterpret_cast<const double2*>(src), reinterpret_cast<float2*>(dst), n);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_c64_to_c128(const void* src, void* dst, size_t n, cudaStream_t st) {
+  COUNT_LAUNCH();
+  if (n % 2 == 0) {
+    const size_t n2 = n / 2;
+    k_c64_to_c128<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(
+        reinterpret_cast<const float4*>(src), reinterpret_cast<double2*>(dst), n2);
+  } else {
+    k_c64_to_c128_1<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        reinterpret_cast<const float2*>(src), reinterpret_cast<double2*>(dst), n);
+  }
+  return cudaGetLastError();
+}
+
 size_t element_tables_bytes(const DevElement& e, int nx, int ny) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t b = al((size_t)ny * sizeof(int2));

@@ -136,6 +136,10 @@ cudaError_t launch_apply_elements(const void* in, int in_c128, void* out, int ou
 // f32 fast element tables (psi == 0 elements): bytes of scratch needed and
 // the build; fills e.span / tabx / taby / bilx / bily / latf.
 size_t element_tables_bytes(const DevElement& e, int nx, int ny);
+// complex128 <-> complex64 conversion of n samples (host-buffer batch: on the
+// copy streams, so the passes read and write complex64)
+cudaError_t launch_c128_to_c64(const void* src, void* dst, size_t n, cudaStream_t st);
+cudaError_t launch_c64_to_c128(const void* src, void* dst, size_t n, cudaStream_t st);
 // t[iy nx + ix] = the f32 transmission of the chain L (fast tables) at each
 // sample: apply_elements_fast applied to 1.
 cudaError_t launch_transmission(const ElementList& L, int nx, int ny, float2* t, cudaStream_t st);
