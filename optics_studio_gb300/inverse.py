@@ -180,6 +180,11 @@ class Renderer:
     scene_step: float = 1e-6
     lambda_step: float = 1e-9
     stream: object = None
+    # d(phase)/d(parameter) per band for band-dependent phase laws (a
+    # GridThickness carrier: 2 pi (n(lam) - 1) / lam); push_back then weights
+    # each frame's contribution by it, so grid_gradient returns dM/dparameter
+    # (adjoint.rs:255-262).  None: the phase is the parameter (weight 1).
+    param_slope: Callable = None
 
     def _stream_ptr(self):
         return _stream_handle(self.stream)
@@ -196,9 +201,10 @@ class Renderer:
             sarr, ns, order = _c_steps(design, lam, keep)
             self._designs.append((design, order))
             g = _ffi.Grid(nx, ny, self.pitch[0], self.pitch[1], lam)
+            slope = float(self.param_slope(lam)) if (seeds is not None and self.param_slope) else 1.0
             fr = _ffi.FrameC(g, src.data_ptr(), sarr, ns,
                              outs[i].data_ptr() if outs is not None else None,
-                             seeds[i].data_ptr() if seeds is not None else None, 1.0, None)
+                             seeds[i].data_ptr() if seeds is not None else None, slope, None)
             if grads is not None:
                 ga = (C.c_void_p * max(len(order), 1))(
                     *[grads[ei].data_ptr() if ei in grads else None for ei in order])
@@ -280,6 +286,37 @@ class Renderer:
     def push_back_frames(self, values, jobs, seeds, grads, tape=None):
         """adjoint.rs:140-246 per job, accumulated into grads {element index: tensor}."""
         self.launch_push_back(self.prepare_push_back(values, jobs, seeds, grads), tape)
+
+
+def grid_thickness(dims, pitch, index, aperture=ClearAperture.field(), center=(0.0, 0.0),
+                   z_after=0.0, rest=None):
+    """carrier.rs:247-275 + 338-354: a sampled relief-thickness carrier (m).
+    The phase at band lam is 2 pi (n(lam) - 1) h / lam with n = index(lam)
+    (a callable, or a constant index).  Returns (carrier, slope): the
+    Renderer's ``carrier(values, lam)`` (a PhaseMask design built on the
+    device from the thickness tensor, followed by z_after and by whatever
+    ``rest(design, lam)`` appends) and its ``param_slope``, the per-band
+    factor by which push_back weights each frame so that grid_gradient gives
+    dM/dh."""
+    n_at = index if callable(index) else (lambda lam, n0=float(index): n0)
+
+    def slope(lam):
+        if not (math.isfinite(lam) and lam > 0.0):
+            raise _ffi.OsgpuError(102)
+        n = float(n_at(lam))
+        if not math.isfinite(n):
+            raise _ffi.OsgpuError(102)
+        return 2.0 * math.pi * (n - 1.0) / lam
+
+    def carrier(values, lam):
+        d = Design()
+        d.push(DevicePhaseMask((values * slope(lam)).contiguous(), dims, pitch, aperture, center),
+               z_after)
+        if rest is not None:
+            rest(d, lam)
+        return d
+
+    return carrier, slope
 
 
 def push_back(renderer, values, lam, x0, y0, dmdi):

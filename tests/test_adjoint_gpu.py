@@ -245,3 +245,55 @@ def test_field_power_compensated():
     u = rng.normal(size=(256, 256)) + 1j * rng.normal(size=(256, 256))
     p = inv.field_power(torch.from_numpy(u).cuda())
     assert p == pytest.approx(float(np.sum(np.abs(u) ** 2)), rel=1e-13)
+
+
+def thickness_renderer(precision, index):
+    cdt = torch.complex128 if precision == "f64" else torch.complex64
+
+    def source(x0, y0, lam):
+        return torch.from_numpy(o_source(x0, y0, lam).samples).to("cuda", cdt)
+
+    carrier, slope = inv.grid_thickness(
+        (N, N), (D, D), index, z_after=Z1,
+        rest=lambda d, lam: d.push(el.EllipticalAperture.circle(R_AP), Z2))
+    rend = inv.Renderer(carrier, source, (D, D), bands=list(BANDS), asm_cfg=AsmConfig(),
+                        precision=precision, param_slope=slope)
+    return rend, slope
+
+
+def test_grid_thickness_gradient_chain_rule():
+    """carrier.rs:247-354 GridThickness: phase 2 pi (n(lam) - 1) h / lam per band.
+    grid_gradient with the carrier's per-band slope returns dM/dh: checked
+    against central differences in h (FP64 engine), against the weighted sum
+    over bands of single-band dM/dphi that adjoint.rs:255-262 prescribes, and
+    the f32 engine against the FP64 one (1e-4)."""
+    index = lambda lam: 1.46 + 3.0e-15 / lam ** 2  # dispersive (Cauchy form)
+    h0 = np.random.default_rng(21).uniform(0.0, 1.2e-6, (N, N))
+    g_m = inv.SpotArrayEfficiency(torch.from_numpy(windows()).cuda(), p_in())
+    rend, slope = thickness_renderer("f64", index)
+    got, _, _ = inv.grid_gradient(rend, torch.from_numpy(h0).cuda(), g_m)
+    g = got[0].cpu().numpy()
+    # weighted sum of per-band phase gradients, each from a one-band render
+    want = np.zeros((N, N))
+    for b, lam in enumerate(BANDS):
+        one = inv.Renderer(rend.carrier, rend.source, (D, D), bands=[lam], asm_cfg=AsmConfig(),
+                           precision="f64")
+        mb = inv.SpotArrayEfficiency(torch.from_numpy(windows()).cuda(), [p_in()[b]])
+        gb, _, _ = inv.grid_gradient(one, torch.from_numpy(h0).cuda(), mb)
+        want += slope(lam) * gb[0].cpu().numpy()
+    assert rel_l2(g, want) <= 1e-12
+    # central differences in h
+    flat = g.reshape(-1)
+    idx = np.random.default_rng(5).choice(np.flatnonzero(np.abs(flat) > 1e-3 * np.abs(flat).max()),
+                                          6, replace=False)
+    dh = 1e-11  # m (about 1e-4 rad of phase)
+    for i in idx:
+        hp = h0.reshape(-1).copy(); hp[i] += dh
+        hm = h0.reshape(-1).copy(); hm[i] -= dh
+        fp = g_m.evaluate(rend.render(torch.from_numpy(hp.reshape(N, N)).cuda()))
+        fm = g_m.evaluate(rend.render(torch.from_numpy(hm.reshape(N, N)).cuda()))
+        fd = (fp - fm) / (2 * dh)
+        assert abs(flat[i] - fd) <= 1e-4 * abs(fd), (i, flat[i], fd)
+    r32, _ = thickness_renderer("f32", index)
+    g32, _, _ = inv.grid_gradient(r32, torch.from_numpy(h0).cuda().float(), g_m)
+    assert rel_l2(g32[0].cpu().numpy(), g) <= 1e-4
