@@ -562,6 +562,27 @@ typedef struct {
 int osgpu_profile_begin(void);
 int osgpu_profile_end(osgpu_kernel_stat* out, int32_t max_out, int32_t* n_out);
 
+/* ------------------------------------------------------- detector metrics */
+/* src/analysis.rs on a device intensity grid (real, row-major ny x nx:
+ * double for OSGPU_F64, float for OSGPU_F32; grid pitch dx, dy; lambda
+ * unused), sums FP64-compensated, results on the host.
+ *   spot_rms: sqrt(sum I rho^2 / sum I) (m), rho at the centred pixel
+ *             coordinates (analysis.rs:111-124; 0 for a zero grid).
+ *   mtf:      |F{I}(fx, 0)| / max(|F{I}(0, 0)|, MIN_POSITIVE), capped at 1,
+ *             for fx = k / (nx dx), k = 0..nx/2: freqs and values hold
+ *             nx/2 + 1 entries (analysis.rs:136-150).
+ *   strehl:   (max I_m / P_m) / (max I_r / P_r), P = sum I dx dy; 0 when a
+ *             power is not positive (analysis.rs:159-168).
+ * marechal_strehl (a closed form of a scalar) and the encircled-energy curve
+ * (a radius-sorted walk) stay in the caller's code. */
+int osgpu_psf_spot_rms_device(const void* d_int, int32_t real_dtype, const osgpu_grid* g,
+                              void* stream, double* out_m);
+int osgpu_psf_mtf_device(const void* d_int, int32_t real_dtype, const osgpu_grid* g,
+                         void* stream, double* freqs, double* values);
+int osgpu_psf_strehl_device(const void* d_meas, const osgpu_grid* g_meas, const void* d_ref,
+                            const osgpu_grid* g_ref, int32_t real_dtype, void* stream,
+                            double* out);
+
 /* ------------------------------------------------- kernel-spectrum plans */
 /* No counterpart in the reference (its ASM recomputes H on every call,
  * src/propagation/asm.rs:505-522).  An f32 ASM propagation whose padded grid

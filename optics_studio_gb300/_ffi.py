@@ -253,6 +253,14 @@ SIGNATURES = [
     ("osgpu_asm_propagate_noalloc", C.c_int,
      [C.c_void_p, C.c_void_p, C.POINTER(Grid), C.c_double, C.POINTER(AsmConfigC), C.c_void_p,
       C.POINTER(AsmReportC)]),
+    ("osgpu_psf_spot_rms_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.POINTER(Grid), C.c_void_p, C.POINTER(C.c_double)]),
+    ("osgpu_psf_mtf_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.POINTER(Grid), C.c_void_p, C.POINTER(C.c_double),
+      C.POINTER(C.c_double)]),
+    ("osgpu_psf_strehl_device", C.c_int,
+     [C.c_void_p, C.POINTER(Grid), C.c_void_p, C.POINTER(Grid), C.c_int32, C.c_void_p,
+      C.POINTER(C.c_double)]),
     ("osgpu_plan_cache_config", C.c_int, [C.c_int32, C.c_uint64]),
     ("osgpu_plan_cache_clear", C.c_int, []),
     ("osgpu_plan_cache_stats", C.c_int, [C.POINTER(PlanStatsC)]),

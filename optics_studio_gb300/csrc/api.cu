@@ -2339,6 +2339,109 @@ int osgpu_field_power_device(const void* d_field, int32_t dtype, uint64_t n, voi
   return OSGPU_OK;
 }
 
+namespace {
+int psf_check(const void* d, int32_t real_dtype, const osgpu_grid* g) {
+  if (!d || !g || (real_dtype != OSGPU_F64 && real_dtype != OSGPU_F32)) {
+    set_err("bad detector grid arguments");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  if (g->nx == 0 || g->ny == 0) {
+    set_err("empty detector grid");
+    return OSGPU_E_EMPTY_GRID;
+  }
+  if (!(g->dx > 0.0) || !(g->dy > 0.0) || !std::isfinite(g->dx) || !std::isfinite(g->dy)) {
+    set_err("detector pitch must be positive and finite");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  return OSGPU_OK;
+}
+}  // namespace
+
+int osgpu_psf_spot_rms_device(const void* d_int, int32_t real_dtype, const osgpu_grid* g,
+                              void* stream, double* out_m) {
+  int rc;
+  if ((rc = psf_check(d_int, real_dtype, g))) return rc;
+  if (!out_m) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  DBuf scr;
+  const size_t sb = reduce_scratch_bytes(2);
+  CK(scr.alloc(sb, st));
+  double* part = reinterpret_cast<double*>(scr.p);
+  double* res = part + (sb / sizeof(double) - 4);
+  CK(launch_psf_moments(d_int, real_dtype == OSGPU_F64, (int)g->nx, (int)g->ny, g->dx, g->dy,
+                        part, res, st));
+  double h[2];
+  CK(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *out_m = h[0] > 0.0 ? std::sqrt(h[1] / h[0]) : 0.0;  // analysis.rs:124
+  return OSGPU_OK;
+}
+
+int osgpu_psf_mtf_device(const void* d_int, int32_t real_dtype, const osgpu_grid* g,
+                         void* stream, double* freqs, double* values) {
+  int rc;
+  if ((rc = psf_check(d_int, real_dtype, g))) return rc;
+  if (!freqs || !values) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int nx = (int)g->nx, half = nx / 2;
+  const void* tw = nullptr;
+  if ((rc = get_tw(c, nx, 1, &tw))) return rc;
+  DBuf scr;
+  CK(scr.alloc((size_t)nx * sizeof(double) + (size_t)(half + 1) * sizeof(double2), st));
+  double* colsum = reinterpret_cast<double*>(scr.p);
+  double2* X = reinterpret_cast<double2*>(colsum + nx);
+  CK(launch_row_mtf(d_int, real_dtype == OSGPU_F64, nx, (int)g->ny, tw, colsum, X, st));
+  std::vector<double2> hx(half + 1);
+  CK(cudaMemcpyAsync(hx.data(), X, hx.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  // analysis.rs:141-150: |X[k]| / max(|X[0]|, MIN_POSITIVE), capped at 1
+  const double dc = std::max(std::hypot(hx[0].x, hx[0].y), 2.2250738585072014e-308);
+  for (int k = 0; k <= half; ++k) {
+    freqs[k] = (double)k / ((double)nx * g->dx);
+    values[k] = std::min(std::hypot(hx[k].x, hx[k].y) / dc, 1.0);
+  }
+  return OSGPU_OK;
+}
+
+int osgpu_psf_strehl_device(const void* d_meas, const osgpu_grid* g_meas, const void* d_ref,
+                            const osgpu_grid* g_ref, int32_t real_dtype, void* stream,
+                            double* out) {
+  int rc;
+  if ((rc = psf_check(d_meas, real_dtype, g_meas)) || (rc = psf_check(d_ref, real_dtype, g_ref)))
+    return rc;
+  if (!out) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  // per grid: moment partials (2 frames), then the max partials (1216), results at the tail
+  const size_t sb = reduce_scratch_bytes(3);
+  DBuf scr;
+  CK(scr.alloc(2 * sb, st));
+  double h[2][3];
+  for (int q = 0; q < 2; ++q) {
+    const void* d = q ? d_ref : d_meas;
+    const osgpu_grid* g = q ? g_ref : g_meas;
+    double* part = reinterpret_cast<double*>(static_cast<char*>(scr.p) + q * sb);
+    double* res = part + (sb / sizeof(double) - 4);
+    const int f64 = real_dtype == OSGPU_F64;
+    CK(launch_psf_moments(d, f64, (int)g->nx, (int)g->ny, g->dx, g->dy, part, res, st));
+    CK(launch_psf_max(d, f64, g->nx * g->ny, part + 2 * 1216 * 2, res + 2, st));
+    CK(cudaMemcpyAsync(h[q], res, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  // analysis.rs:159-168: (peak_m / P_m) / (peak_r / P_r), P = sum I dx dy
+  const double pm = h[0][0] * g_meas->dx * g_meas->dy, pr = h[1][0] * g_ref->dx * g_ref->dy;
+  *out = (pm <= 0.0 || pr <= 0.0) ? 0.0 : (h[0][2] / pm) / (h[1][2] / pr);
+  return OSGPU_OK;
+}
+
 int osgpu_merit_spot_efficiency_device(const void* d_obs, int32_t real_dtype, int32_t n_frames,
                                        uint64_t frame_len, const uint8_t* d_windows,
                                        const double* p_in, void* d_seed, void* stream,

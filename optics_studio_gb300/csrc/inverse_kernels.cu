@@ -699,6 +699,108 @@ cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, doubl
   return cudaGetLastError();
 }
 
+// ------------------------------------------------- detector metrics
+// (reference src/analysis.rs)
+
+// part frame 0 = sum I, frame 1 = sum I (x^2 + y^2) at the centred pixel
+// coordinates of field.rs:490-495 (spot_rms_radius, analysis.rs:111-124).
+__global__ void k_psf_moments(const void* img, int f64, int nx, int ny, double dx, double dy,
+                              double* part) {
+  const uint64_t len = (uint64_t)nx * ny;
+  Acc sw, swr2;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(k % nx), iy = (int)(k / nx);
+    const double x = ((double)ix - ((double)nx - 1.0) / 2.0) * dx;
+    const double y = ((double)iy - ((double)ny - 1.0) / 2.0) * dy;
+    const double i = ld_real(img, f64, k);
+    sw.add(i);
+    swr2.add(i * (x * x + y * y));
+  }
+  write_part(part, 0, block_fold(sw));
+  write_part(part, 1, block_fold(swr2));
+}
+
+// Per-block maximum of a real grid (analysis.rs:167, fold from 0.0).
+__global__ void k_psf_max(const void* img, int f64, uint64_t len, double* part) {
+  __shared__ double sm[kRedThreads / 32];
+  double m = 0.0;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x)
+    m = fmax(m, ld_real(img, f64, k));
+  for (int d = 16; d > 0; d >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, d));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kRedThreads / 32; ++w) m = fmax(m, sm[w]);
+    part[blockIdx.x] = m;
+  }
+}
+
+__global__ void k_fold_max(const double* part, int nb, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double m = 0.0;
+    for (int b = 0; b < nb; ++b) m = fmax(m, part[b]);
+    *out = m;
+  }
+}
+
+// Column sums s[ix] = sum_y I[y][ix] (compensated): row 0 of the 2D DFT of I
+// is the 1D DFT of s (the MTF along +fx, analysis.rs:136-150).
+__global__ void k_col_sums(const void* img, int f64, int nx, int ny, double* s) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix >= nx) return;
+  Acc a;
+  for (int iy = 0; iy < ny; ++iy) a.add(ld_real(img, f64, (size_t)iy * nx + ix));
+  s[ix] = a.value();
+}
+
+// X[k] = sum_x s[x] W_nx^{k x}, k <= nx / 2, one block per bin, twiddles
+// from the FP64 table tw[e] = W_nx^e.
+__global__ void k_row_dft(const double* s, int nx, const double2* tw, double2* X) {
+  const int k = blockIdx.x;
+  Acc re, im;
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+    const double2 w = tw[(int)(((long long)k * x) % nx)];
+    re.add(s[x] * w.x);
+    im.add(s[x] * w.y);
+  }
+  re = block_fold(re);
+  im = block_fold(im);
+  if (threadIdx.x == 0) X[k] = make_double2(re.value(), im.value());
+}
+
+cudaError_t launch_psf_moments(const void* img, int f64, int nx, int ny, double dx, double dy,
+                               double* scratch, double* out2, cudaStream_t st) {
+  const uint64_t n = (uint64_t)nx * ny;
+  const int blocks = red_blocks(n);
+  OSGPU_LAUNCH;
+  k_psf_moments<<<blocks, kRedThreads, 0, st>>>(img, f64, nx, ny, dx, dy, scratch);
+  OSGPU_LAUNCH;
+  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 2, out2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_psf_max(const void* img, int f64, uint64_t n, double* scratch, double* out,
+                           cudaStream_t st) {
+  const int blocks = red_blocks(n);
+  OSGPU_LAUNCH;
+  k_psf_max<<<blocks, kRedThreads, 0, st>>>(img, f64, n, scratch);
+  OSGPU_LAUNCH;
+  k_fold_max<<<1, 32, 0, st>>>(scratch, blocks, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_row_mtf(const void* img, int f64, int nx, int ny, const void* tw64,
+                           double* colsum, double2* X, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_col_sums<<<(nx + 127) / 128, 128, 0, st>>>(img, f64, nx, ny, colsum);
+  OSGPU_LAUNCH;
+  k_row_dft<<<nx / 2 + 1, kRedThreads, 0, st>>>(colsum, nx, reinterpret_cast<const double2*>(tw64),
+                                                X);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_power(const void* u, int c128, uint64_t n, double* scratch, double* out,
                          cudaStream_t st) {
   const int blocks = red_blocks(n);

@@ -97,6 +97,14 @@ cudaError_t launch_mse(const void* obs, int f64, uint64_t len, int nb, int ns, i
 cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, double dy,
                       double radius, int nb, int ns, int band, int scene, void* seed,
                       double* scratch, double* out, cudaStream_t st);
+// detector metrics (analysis.rs): out2 = {sum I, sum I rho^2}; out = max I;
+// X[k] (k <= nx/2) = DFT of the column sums (tw64: FP64 nx-point twiddles)
+cudaError_t launch_psf_moments(const void* img, int f64, int nx, int ny, double dx, double dy,
+                               double* scratch, double* out2, cudaStream_t st);
+cudaError_t launch_psf_max(const void* img, int f64, uint64_t n, double* scratch, double* out,
+                           cudaStream_t st);
+cudaError_t launch_row_mtf(const void* img, int f64, int nx, int ny, const void* tw64,
+                           double* colsum, double2* X, cudaStream_t st);
 cudaError_t launch_power(const void* u, int c128, uint64_t n, double* scratch, double* out,
                          cudaStream_t st);
 cudaError_t launch_adam(double* x, float* x32, const void* g, int g_f64, double* m, double* v,

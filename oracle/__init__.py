@@ -29,4 +29,4 @@ Parity pins (see ``tests/test_oracle_pins.py``):
 """
 
 from . import fft, field, asm, fresnel, fraunhofer, rs, element, beamline  # noqa: F401
-from . import carrier, observe, merit, gs, adjoint, adam  # noqa: F401
+from . import carrier, observe, merit, gs, adjoint, adam, analysis  # noqa: F401

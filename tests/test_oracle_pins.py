@@ -348,3 +348,45 @@ def test_adam_first_step_by_hand():
     # |10 g| = 5 > clip 1: g is rescaled to 2 g before the moments
     xc, _, _ = adam.adam_step(x, g * 10, np.zeros(3), np.zeros(3), 1, 0.0, 4.0, lr_frac=0.1)
     np.testing.assert_allclose(xc, x - 0.1 * 4.0 * (2 * g) / (np.abs(2 * g) + 1e-8), rtol=1e-12)
+
+
+# ---- analysis.rs restatement ---------------------------------------------------
+
+def _gaussian_psf(w, n, d):
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    return np.exp(-(c[None, :] ** 2 + c[:, None] ** 2) / (w * w))
+
+
+def test_analysis_encircled_energy_of_airy():
+    """analysis.rs:444-474: EE(r1) = 0.84 +- 0.02 at the first dark ring."""
+    from oracle import analysis, fraunhofer
+    lam, a, z = 500e-9, 0.5e-3, 0.5
+    band = field.uniform(1.0, 0.0, 128, 128, 50e-6, 50e-6, lam)
+    masked = element.EllipticalAperture.circle(a).apply(band)
+    far = fraunhofer.propagate(masked, z, fraunhofer.FraunhoferConfig(aperture_extent=a))
+    psf = np.abs(far.samples) ** 2
+    ee = analysis.encircled_energy(psf, (far.dx, far.dy))
+    r1 = 1.22 * lam * z / (2.0 * a)
+    assert abs(ee.value_at(r1) - 0.84) < 0.02, ee.value_at(r1)
+    assert ee.radius_for_fraction(1.0) == pytest.approx(float(ee.radii[-1]))
+
+
+def test_analysis_gaussian_anchors_and_strehl():
+    """analysis.rs:475-505: spot RMS = w (1 %), MTF = exp(-pi^2 w^2 f^2) (0.02 below
+    0.8 f_nyq), Strehl of a PSF with itself 1, wide vs narrow in (0.2, 0.6),
+    Marechal bounds."""
+    from oracle import analysis
+    w, d = 100e-6, 10e-6
+    psf = _gaussian_psf(w, 512, d)
+    assert abs(analysis.spot_rms_radius(psf, (d, d)) / w - 1.0) < 0.01
+    freqs, vals = analysis.mtf(psf, (d, d))
+    assert abs(vals[0] - 1.0) < 1e-12
+    err = max(abs(v - math.exp(-math.pi ** 2 * w * w * f * f))
+              for f, v in zip(freqs[1:], vals[1:]) if f <= 800e3)
+    assert err < 0.02
+    narrow, wide = _gaussian_psf(80e-6, 256, 10e-6), _gaussian_psf(160e-6, 256, 10e-6)
+    assert abs(analysis.strehl(narrow, (d, d), narrow, (d, d)) - 1.0) < 1e-12
+    s = analysis.strehl(wide, (d, d), narrow, (d, d))
+    assert 0.2 < s < 0.6
+    assert 0.67 < analysis.marechal_strehl(0.1) < 0.68
+    assert analysis.marechal_strehl(0.0) == 1.0
