@@ -133,6 +133,15 @@ class Observation:
     def frame_len(self):
         return self.dims[0] * self.dims[1]
 
+    # Zero-copy export of the [channel][band][scene][row][col] array (the
+    # numpy layout of observe.rs:10-16) through DLPack: any DLPack consumer
+    # (numpy for host data, or a GPU array library) views `data` in place.
+    def __dlpack__(self, stream=None):
+        return self.data.__dlpack__() if stream is None else self.data.__dlpack__(stream=stream)
+
+    def __dlpack_device__(self):
+        return self.data.__dlpack_device__()
+
     def channel_index(self, ch):
         return self.channels.index(ch) if ch in self.channels else None
 

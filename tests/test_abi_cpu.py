@@ -186,3 +186,16 @@ def test_host_validation_errors_without_device():
     assert L.osgpu_asm_propagate(src.ctypes.data_as(_ffi.c_double_p),
                                  out.ctypes.data_as(_ffi.c_double_p), g, 0.0,
                                  gasm.AsmConfig().c(), 0, None) == 5
+
+
+def test_observation_dlpack_export_is_zero_copy():
+    """observe.rs:10-16 layout [C][B][S][Ny][Nx] exported through DLPack in place."""
+    torch = pytest.importorskip("torch")
+    from optics_studio_gb300.inverse import Observation
+    data = torch.arange(2 * 3 * 1 * 4 * 5, dtype=torch.float64).reshape(2, 3, 1, 4, 5)
+    obs = Observation(["intensity", "d_dx"], [5e-7, 6e-7, 7e-7], [(0.0, 0.0)], (5, 4),
+                      (1e-6, 1e-6), data)
+    view = np.from_dlpack(obs)
+    assert view.shape == (2, 3, 1, 4, 5)
+    data[1, 2, 0, 3, 4] = -1.0
+    assert view[1, 2, 0, 3, 4] == -1.0  # same memory
