@@ -15,6 +15,8 @@
 // says stop.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "fft_reg.cuh"
 #include "gs_fast.cuh"
 #include "inverse_kernels.cuh"
@@ -51,7 +53,8 @@ __device__ __forceinline__ float encode_f(float p, const GsFastArgs& a) {
 
 // Sum of one float per thread over the CTA into part[(f * gridDim.x + blockIdx.x) * 2]
 // (compensation slot 0), the layout of the GS fold kernels.
-__device__ __forceinline__ void cta_sum(float x, double* part, int f, double* red) {
+__device__ __forceinline__ void cta_sum(float x, double* part, int f, double* red, int blk,
+                                        int nblk) {
   double v = (double)x;
   for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
   const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
@@ -61,7 +64,7 @@ __device__ __forceinline__ void cta_sum(float x, double* part, int f, double* re
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int i = 0; i < nw; ++i) s += red[i];
-    const size_t o = ((size_t)f * gridDim.x + blockIdx.x) * 2;
+    const size_t o = ((size_t)f * nblk + blk) * 2;
     part[o] = s;
     part[o + 1] = 0.0;
   }
@@ -82,10 +85,9 @@ struct GsLay {
 
 template <int M, int G>
 __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
-    k_gs_cols(const GsFastItem* __restrict__ items, GsFastArgs a) {
+    k_gs_cols(const GsFastItem* __restrict__ items, GsFastArgs a, int n_items) {
   constexpr int T = M / 16;
-  const GsFastItem& it = items[blockIdx.y];
-  if (a.intensity_only ? !it.out_intensity : it.state->stop) return;
+  constexpr int NB = M / G;  // CTAs' worth of columns per item
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tws = reinterpret_cast<float2*>(smem_raw);
   float2* bufs = tws + TwLay<M>::SIZE;
@@ -98,7 +100,12 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     const float2* twm = reinterpret_cast<const float2*>(a.tw);
     for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
   }
-  const int kx = blockIdx.x * G + g;
+  // persistent: the CTA walks (item, column block) units, the twiddles loaded once
+  for (int u = blockIdx.x; u < NB * n_items; u += gridDim.x) {
+  const GsFastItem& it = items[u / NB];
+  const int blk = u - (u / NB) * NB;
+  if (a.intensity_only ? !it.out_intensity : it.state->stop) continue;
+  const int kx = blk * G + g;
   float2* col = it.W + (size_t)kx * M;
   float2 v[16];
   float tq[16];
@@ -117,7 +124,7 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
       const float m2q = v[q].x * v[q].x + v[q].y * v[q].y;
       it.out_intensity[(size_t)(tid + T * q) * M + kx] = c * c * m2q;
     }
-    return;
+    continue;
   }
   float e2 = 0.f, m2 = 0.f;
 #pragma unroll
@@ -148,16 +155,16 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
   fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
 #pragma unroll
   for (int q = 0; q < 16; ++q) col[tid + T * q] = v[q];
-  cta_sum(e2, it.part_col, 0, red);
-  cta_sum(m2, it.part_col, 1, red);
+  cta_sum(e2, it.part_col, 0, red, blk, NB);
+  cta_sum(m2, it.part_col, 1, red, blk, NB);
+  }
 }
 
 template <int M, int G>
 __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
-    k_gs_rows(const GsFastItem* __restrict__ items, GsFastArgs a, int iterate) {
+    k_gs_rows(const GsFastItem* __restrict__ items, GsFastArgs a, int iterate, int n_items) {
   constexpr int T = M / 16;
-  const GsFastItem& it = items[blockIdx.y];
-  if (iterate && it.state->stop) return;
+  constexpr int NB = M / G;  // CTAs' worth of rows per item
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tws = reinterpret_cast<float2*>(smem_raw);
   float2* bufs = tws + TwLay<M>::SIZE;
@@ -170,7 +177,12 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     const float2* twm = reinterpret_cast<const float2*>(a.tw);
     for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
   }
-  const int iy0 = blockIdx.x * G, iy = iy0 + g;
+  // persistent: the CTA walks (item, row block) units, the twiddles loaded once
+  for (int u = blockIdx.x; u < NB * n_items; u += gridDim.x) {
+  const GsFastItem& it = items[u / NB];
+  const int blk = u - (u / NB) * NB;
+  if (iterate && it.state->stop) continue;
+  const int iy0 = blk * G, iy = iy0 + g;
   const float2 py = __ldg(it.pry + iy);
   float* __restrict__ prow = it.phase + (size_t)iy * M;
   // 4-row tiles: the spectrum moves through the groups' exchange buffers in
@@ -245,7 +257,9 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
 #pragma unroll
     for (int q = 0; q < 16; ++q) it.W[(size_t)(tid + T * q) * M + iy] = v[q];
   }
-  if (iterate) cta_sum(d2, it.part_row, 0, red);
+  if (iterate) cta_sum(d2, it.part_row, 0, red, blk, NB);
+  __syncthreads();  // the next unit's tile gather rewrites the exchange buffers
+  }
 }
 
 // Column-major copy of a real M x M array (32 x 32 tiles through shared memory).
@@ -270,8 +284,14 @@ cudaError_t launch_cols(const GsFastItem* items, int n_items, const GsFastArgs& 
   cudaError_t e = cudaFuncSetAttribute(k_gs_cols<M, kG>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM);
   if (e != cudaSuccess) return e;
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs_cols<M, kG>, L::THREADS, L::SMEM);
+  const int units = (M / kG) * n_items;
+  const int grid = std::max(1, std::min(units, std::max(1, per_sm) * std::max(1, sms)));
   ++launch_counter();
-  k_gs_cols<M, kG><<<dim3(M / kG, n_items), L::THREADS, L::SMEM, st>>>(items, a);
+  k_gs_cols<M, kG><<<grid, L::THREADS, L::SMEM, st>>>(items, a, n_items);
   return cudaGetLastError();
 }
 
@@ -283,8 +303,14 @@ cudaError_t launch_rows(const GsFastItem* items, int n_items, const GsFastArgs& 
   cudaError_t e = cudaFuncSetAttribute(k_gs_rows<M, G>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM);
   if (e != cudaSuccess) return e;
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs_rows<M, G>, L::THREADS, L::SMEM);
+  const int units = (M / G) * n_items;
+  const int grid = std::max(1, std::min(units, std::max(1, per_sm) * std::max(1, sms)));
   ++launch_counter();
-  k_gs_rows<M, G><<<dim3(M / G, n_items), L::THREADS, L::SMEM, st>>>(items, a, iterate);
+  k_gs_rows<M, G><<<grid, L::THREADS, L::SMEM, st>>>(items, a, iterate, n_items);
   return cudaGetLastError();
 }
 
