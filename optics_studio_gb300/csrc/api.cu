@@ -1121,7 +1121,8 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
                o_ta = o_op + al(n), o_ti = o_ta + al(n * 4), o_tab = o_ti + al(n * 4),
                o_am = o_tab + al((size_t)4 * M * 8), o_pc = o_am + al(n * 4),
                o_pr = o_pc + al((size_t)4 * nb * 8),
-               o_hi = o_pr + al((size_t)2 * nb * 8), per = o_hi + al(sizeof(GsRecordDev) * max_it);
+               o_hi = o_pr + al((size_t)2 * nb * 8), o_te = o_hi + al(sizeof(GsRecordDev) * max_it),
+               per = o_te + al(n * 4);  // o_te: |U| - T column-major, transposed at the end
   DBuf mem, dstates, ditems, dfolds;
   CK(mem.alloc(per * n_items, st));
   CK(dstates.alloc(sizeof(GsState) * n_items, st));
@@ -1178,7 +1179,7 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
     f.qx = f.prx + 2 * M;
     f.qy = f.prx + 3 * M;
     f.c = (float)(w / lz);
-    f.terr = reinterpret_cast<float*>(it.d_target_error);
+    f.terr = it.d_target_error ? reinterpret_cast<float*>(b + o_te) : nullptr;
     f.perr = reinterpret_cast<float*>(it.d_phase_error);
     f.state = S + i;
     f.part_col = reinterpret_cast<double*>(b + o_pc);
@@ -1255,6 +1256,9 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
     char* b = base + per * i;
     if (it.d_last_phase)
       CK(cudaMemcpyAsync(it.d_last_phase, b + o_ph, n * 4, cudaMemcpyDeviceToDevice, st));
+    if (it.d_target_error)
+      CK(launch_transpose_real(reinterpret_cast<const float*>(b + o_te),
+                               reinterpret_cast<float*>(it.d_target_error), M, st));
     if (it.d_illumination)
       CK(cudaMemcpyAsync(it.d_illumination, b + o_il, n * 4, cudaMemcpyDeviceToDevice, st));
     want_int = want_int || it.d_best_intensity;

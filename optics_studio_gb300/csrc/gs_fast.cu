@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     const float inten = amp * amp;
     e2 = fmaf(err, err, e2);
     m2 = fmaf(inten - ti, inten - ti, m2);
-    if (it.terr) it.terr[(size_t)ky * M + kx] = err;
+    if (it.terr) it.terr[kt] = err;  // column-major, coalesced; transposed after the loop
     const float aa = (1.f - bf) * amp + bf * t;
     float2 gq;
     if (m > 0.f) {

@@ -19,7 +19,7 @@ struct GsFastItem {
   const float2* qx;           // D = qx[ix] qy[iy]
   const float2* qy;
   float c;                    // |D|
-  float* terr;                // optional: |U| - T of the last iteration (row-major)
+  float* terr;                // optional: |U| - T of the last iteration (column-major)
   float* perr;                // optional: phase update of the last iteration
   GsState* state;
   double* part_col;           // 2 frames x gs_fast_blocks(M) pairs

@@ -108,6 +108,11 @@ def test_gs_f64_follows_oracle(engine):
                                want.illumination_amplitude, rtol=1e-12, atol=1e-12)
     bi = got.target_intensity.cpu().numpy()
     assert np.linalg.norm(bi - want.target_intensity) / np.linalg.norm(want.target_intensity) <= 1e-9
+    te = got.target_amplitude_error.cpu().numpy()
+    assert (np.linalg.norm(te - want.target_amplitude_error)
+            <= 1e-9 * np.linalg.norm(want.target_amplitude_error))
+    pe = got.phase_error.cpu().numpy()
+    assert np.linalg.norm(pe - want.phase_error) <= 1e-9 * np.linalg.norm(want.phase_error)
 
 
 def test_gs_f32_fraunhofer_follows_oracle_merit():
@@ -194,6 +199,10 @@ def test_gs_fused_f32_follows_oracle_at_256():
     assert got.best_iteration == want.best_iteration
     bi = got.target_intensity.cpu().numpy()
     assert np.linalg.norm(bi - want.target_intensity) / np.linalg.norm(want.target_intensity) <= 1e-4
+    # |U| - T of the last iteration (written column-major in the loop, transposed at the end)
+    te = got.target_amplitude_error.cpu().numpy()
+    assert (np.linalg.norm(te - want.target_amplitude_error)
+            <= 1e-4 * np.linalg.norm(want.target_amplitude_error))
 
 
 def test_gs_fused_matches_generic_path_and_patience(monkeypatch):
