@@ -573,12 +573,22 @@ int osgpu_profile_end(osgpu_kernel_stat* out, int32_t max_out, int32_t* n_out);
  *             nx/2 + 1 entries (analysis.rs:136-150).
  *   strehl:   (max I_m / P_m) / (max I_r / P_r), P = sum I dx dy; 0 when a
  *             power is not positive (analysis.rs:159-168).
- * marechal_strehl (a closed form of a scalar) and the encircled-energy curve
- * (a radius-sorted walk) stay in the caller's code. */
+ *   encircled_energy: the cumulative power fraction at the end of each group
+ *             of equal pixel radius, radii ascending (analysis.rs:81-108);
+ *             *n_out = number of points (0 for a zero grid); radii and
+ *             fraction must hold cap >= *n_out entries (nx * ny always
+ *             suffices).  The radius order, a function of the geometry only,
+ *             is sorted on the host once per geometry; the walk itself is a
+ *             gather and an FP64 prefix sum on the device.
+ * marechal_strehl (a closed form of a scalar) and the curve's interpolation
+ * stay in the caller's code. */
 int osgpu_psf_spot_rms_device(const void* d_int, int32_t real_dtype, const osgpu_grid* g,
                               void* stream, double* out_m);
 int osgpu_psf_mtf_device(const void* d_int, int32_t real_dtype, const osgpu_grid* g,
                          void* stream, double* freqs, double* values);
+int osgpu_psf_encircled_energy_device(const void* d_int, int32_t real_dtype,
+                                      const osgpu_grid* g, void* stream, double* radii,
+                                      double* fraction, uint64_t cap, uint64_t* n_out);
 int osgpu_psf_strehl_device(const void* d_meas, const osgpu_grid* g_meas, const void* d_ref,
                             const osgpu_grid* g_ref, int32_t real_dtype, void* stream,
                             double* out);

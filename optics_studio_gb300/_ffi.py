@@ -258,6 +258,9 @@ SIGNATURES = [
     ("osgpu_psf_mtf_device", C.c_int,
      [C.c_void_p, C.c_int32, C.POINTER(Grid), C.c_void_p, C.POINTER(C.c_double),
       C.POINTER(C.c_double)]),
+    ("osgpu_psf_encircled_energy_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.POINTER(Grid), C.c_void_p, C.POINTER(C.c_double),
+      C.POINTER(C.c_double), C.c_uint64, C.POINTER(C.c_uint64)]),
     ("osgpu_psf_strehl_device", C.c_int,
      [C.c_void_p, C.POINTER(Grid), C.c_void_p, C.POINTER(Grid), C.c_int32, C.c_void_p,
       C.POINTER(C.c_double)]),

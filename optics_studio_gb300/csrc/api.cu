@@ -79,6 +79,14 @@ struct Context {
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> event_pool;
   std::map<const void*, float*> lattices;  // osgpu_lattice_create handle -> f32 copy
+  // encircled-energy walk order of the last detector geometry (radius sort on the host)
+  struct EeOrder {
+    uint64_t nx = 0, ny = 0;
+    double dx = 0.0, dy = 0.0;
+    std::vector<double> radii;  // one per tied-radius group, ascending
+    void* d = nullptr;          // device: perm (n u32) then group ends (ng u32)
+    uint64_t ng = 0;
+  } ee;
   // kernel-spectrum plans (osgpu_plan_cache_config); off by default
   bool plans_on = false;
   size_t plan_cap = 0, plan_bytes = 0;
@@ -2381,6 +2389,89 @@ int osgpu_psf_spot_rms_device(const void* d_int, int32_t real_dtype, const osgpu
   CK(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   *out_m = h[0] > 0.0 ? std::sqrt(h[1] / h[0]) : 0.0;  // analysis.rs:124
+  return OSGPU_OK;
+}
+
+int osgpu_psf_encircled_energy_device(const void* d_int, int32_t real_dtype,
+                                      const osgpu_grid* g, void* stream, double* radii,
+                                      double* fraction, uint64_t cap, uint64_t* n_out) {
+  int rc;
+  if ((rc = psf_check(d_int, real_dtype, g))) return rc;
+  if (!n_out || (cap > 0 && (!radii || !fraction))) return OSGPU_E_BAD_ARGUMENT;
+  const uint64_t n = g->nx * g->ny;
+  if (n >= 0xffffffffull) {
+    set_err("detector grid too large for the encircled-energy walk");
+    return OSGPU_E_UNSUPPORTED;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  Context::EeOrder& E = c.ee;
+  if (!(E.d && E.nx == g->nx && E.ny == g->ny && E.dx == g->dx && E.dy == g->dy)) {
+    // pixel radii at the centred coordinates (field.rs:490-495), stable sort by
+    // radius, one group per run of equal radii (analysis.rs:84-106)
+    std::vector<std::pair<double, unsigned>> px(n);
+    for (uint64_t iy = 0; iy < g->ny; ++iy) {
+      const double y = ((double)iy - ((double)g->ny - 1.0) / 2.0) * g->dy;
+      for (uint64_t ix = 0; ix < g->nx; ++ix) {
+        const double x = ((double)ix - ((double)g->nx - 1.0) / 2.0) * g->dx;
+        px[iy * g->nx + ix] = {std::sqrt(x * x + y * y), (unsigned)(iy * g->nx + ix)};
+      }
+    }
+    std::stable_sort(px.begin(), px.end(),
+                     [](const std::pair<double, unsigned>& a, const std::pair<double, unsigned>& b) {
+                       return a.first < b.first;
+                     });
+    std::vector<unsigned> host(n);
+    std::vector<unsigned> ends;
+    std::vector<double> radii_g;
+    for (uint64_t k = 0; k < n; ++k) {
+      host[k] = px[k].second;
+      if (k + 1 == n || px[k + 1].first != px[k].first) {
+        ends.push_back((unsigned)k);
+        radii_g.push_back(px[k].first);
+      }
+    }
+    if (E.d) {
+      CK(cudaDeviceSynchronize());
+      cudaFree(E.d);
+      E.d = nullptr;
+    }
+    CK(cudaMalloc(&E.d, (n + ends.size()) * sizeof(unsigned)));
+    CK(cudaMemcpy(E.d, host.data(), n * sizeof(unsigned), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(static_cast<unsigned*>(E.d) + n, ends.data(), ends.size() * sizeof(unsigned),
+                  cudaMemcpyHostToDevice));
+    E.nx = g->nx;
+    E.ny = g->ny;
+    E.dx = g->dx;
+    E.dy = g->dy;
+    E.ng = ends.size();
+    E.radii = std::move(radii_g);
+  }
+  const uint64_t nb = (n + 1023) / 1024;
+  DBuf scr;
+  CK(scr.alloc((n + nb + E.ng) * sizeof(double), st));
+  double* v = reinterpret_cast<double*>(scr.p);
+  double* tot = v + n;
+  double* frac = tot + nb;
+  const unsigned* perm = static_cast<const unsigned*>(E.d);
+  double total = 0.0;
+  CK(launch_ee_curve(d_int, real_dtype == OSGPU_F64, perm, n, perm + n, E.ng, v, tot, frac,
+                     &total, st));
+  if (!(total > 0.0)) {  // analysis.rs:95: an empty curve
+    *n_out = 0;
+    return OSGPU_OK;
+  }
+  *n_out = E.ng;
+  if (cap < E.ng) {
+    set_err("curve has %llu points, buffers hold %llu", (unsigned long long)E.ng,
+            (unsigned long long)cap);
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  CK(cudaMemcpyAsync(fraction, frac, E.ng * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::copy(E.radii.begin(), E.radii.end(), radii);
   return OSGPU_OK;
 }
 

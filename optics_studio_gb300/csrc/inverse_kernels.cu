@@ -770,6 +770,103 @@ __global__ void k_row_dft(const double* s, int nx, const double2* tw, double2* X
   if (threadIdx.x == 0) X[k] = make_double2(re.value(), im.value());
 }
 
+// Encircled-energy walk (analysis.rs:81-108): v[k] = I[perm[k]] in radius
+// order, inclusive prefix sums in FP64 (block scans of 1024, then the block
+// totals, then the offsets), fraction at the end of each tied-radius group.
+constexpr int kScan = 1024;
+
+__device__ __forceinline__ double warp_incl_scan(double v) {
+  const int l = threadIdx.x & 31;
+  for (int d = 1; d < 32; d <<= 1) {
+    const double o = __shfl_up_sync(0xffffffffu, v, d);
+    if (l >= d) v += o;
+  }
+  return v;
+}
+
+// Inclusive scan of one 1024-element block in place; block total to tot[b].
+__device__ void block_incl_scan(double* data, uint64_t n, double* tot) {
+  __shared__ double ws[kScan / 32];
+  const uint64_t i = (uint64_t)blockIdx.x * kScan + threadIdx.x;
+  double v = i < n ? data[i] : 0.0;
+  v = warp_incl_scan(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 31) ws[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = ws[l];
+    t = warp_incl_scan(t);
+    ws[l] = t;
+  }
+  __syncthreads();
+  if (w > 0) v += ws[w - 1];
+  if (i < n) data[i] = v;
+  if (threadIdx.x == kScan - 1 && tot) tot[blockIdx.x] = v;
+}
+
+__global__ void k_ee_gather_scan(const void* img, int f64, const unsigned* perm, uint64_t n,
+                                 double* v, double* tot) {
+  const uint64_t i = (uint64_t)blockIdx.x * kScan + threadIdx.x;
+  if (i < n) v[i] = ld_real(img, f64, perm[i]);
+  __syncthreads();
+  block_incl_scan(v, n, tot);
+}
+
+// exclusive prefix of the block totals, serial per 1024-chunk inside one block
+__global__ void k_scan_totals(double* tot, int nb) {
+  __shared__ double carry;
+  if (threadIdx.x == 0) carry = 0.0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += kScan) {
+    const int i = base + threadIdx.x;
+    double v = i < nb ? tot[i] : 0.0;
+    v = warp_incl_scan(v);
+    __shared__ double ws[kScan / 32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 31) ws[w] = v;
+    __syncthreads();
+    if (w == 0) ws[l] = warp_incl_scan(ws[l]);
+    __syncthreads();
+    if (w > 0) v += ws[w - 1];
+    const double c = carry;
+    if (i < nb) tot[i] = c + v;  // inclusive prefix including the earlier chunks
+    __syncthreads();
+    if (threadIdx.x == kScan - 1) carry = c + v;
+    __syncthreads();
+  }
+}
+
+__global__ void k_ee_fraction(const double* v, const double* tot_incl, uint64_t n,
+                              const unsigned* group_end, uint64_t ng, double total,
+                              double* frac) {
+  const uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  const uint64_t k = group_end[g];
+  const uint64_t b = k / kScan;
+  const double acc = v[k] + (b > 0 ? tot_incl[b - 1] : 0.0);
+  frac[g] = acc / total;
+}
+
+cudaError_t launch_ee_curve(const void* img, int f64, const unsigned* perm, uint64_t n,
+                            const unsigned* group_end, uint64_t ng, double* v, double* tot,
+                            double* frac, double* total_out, cudaStream_t st) {
+  const unsigned nb = (unsigned)((n + kScan - 1) / kScan);
+  OSGPU_LAUNCH;
+  k_ee_gather_scan<<<nb, kScan, 0, st>>>(img, f64, perm, n, v, tot);
+  OSGPU_LAUNCH;
+  k_scan_totals<<<1, kScan, 0, st>>>(tot, (int)nb);
+  cudaError_t e = cudaMemcpyAsync(total_out, tot + nb - 1, sizeof(double),
+                                  cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (!(*total_out > 0.0)) return cudaSuccess;
+  OSGPU_LAUNCH;
+  k_ee_fraction<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(v, tot, n, group_end, ng,
+                                                               *total_out, frac);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_psf_moments(const void* img, int f64, int nx, int ny, double dx, double dy,
                                double* scratch, double* out2, cudaStream_t st) {
   const uint64_t n = (uint64_t)nx * ny;

@@ -101,6 +101,13 @@ cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, doubl
 // X[k] (k <= nx/2) = DFT of the column sums (tw64: FP64 nx-point twiddles)
 cudaError_t launch_psf_moments(const void* img, int f64, int nx, int ny, double dx, double dy,
                                double* scratch, double* out2, cudaStream_t st);
+// encircled-energy curve: perm = pixel order by radius, group_end = last
+// index of each tied-radius group; v (n doubles) and tot (ceil(n/1024)) are
+// scratch; frac[g] = cumulative power at group g / total (total_out, host;
+// frac untouched when total <= 0).  Synchronises st.
+cudaError_t launch_ee_curve(const void* img, int f64, const unsigned* perm, uint64_t n,
+                            const unsigned* group_end, uint64_t ng, double* v, double* tot,
+                            double* frac, double* total_out, cudaStream_t st);
 cudaError_t launch_psf_max(const void* img, int f64, uint64_t n, double* scratch, double* out,
                            cudaStream_t st);
 cudaError_t launch_row_mtf(const void* img, int f64, int nx, int ny, const void* tw64,

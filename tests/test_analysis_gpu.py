@@ -60,3 +60,35 @@ def test_strehl_and_anchors_match_oracle():
     assert abs(gan.spot_rms_radius(torch.from_numpy(g).cuda(), (10e-6, 10e-6)) / 100e-6 - 1) < 0.01
     assert gan.spot_rms_radius(torch.zeros((8, 8), dtype=torch.float64, device="cuda"),
                                (1e-6, 1e-6)) == 0.0
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_encircled_energy_curve_matches_oracle(k):
+    img, pitch = list(grids())[k]
+    t = torch.from_numpy(img).cuda()
+    got = gan.encircled_energy(t, pitch)
+    want = oan.encircled_energy(img, pitch)
+    assert len(got.radii) == want.radii.size
+    np.testing.assert_array_equal(np.array(got.radii), want.radii)  # same sort, same groups
+    np.testing.assert_allclose(got.fraction, want.fraction, rtol=1e-10, atol=1e-13)
+    for r in (0.0, float(want.radii[len(want.radii) // 3]), 1.5 * float(want.radii[-1]) / 3):
+        assert got.value_at(r) == pytest.approx(want.value_at(r), rel=1e-10, abs=1e-13)
+    assert got.radius_for_fraction(0.5) == pytest.approx(want.radius_for_fraction(0.5), rel=1e-9)
+    # again on the same geometry (cached radius order), float32 samples
+    t32 = t.float()
+    g32 = gan.encircled_energy(t32, pitch)
+    w32 = oan.encircled_energy(t32.double().cpu().numpy(), pitch)
+    np.testing.assert_allclose(g32.fraction, w32.fraction, rtol=1e-10, atol=1e-13)
+    assert gan.encircled_energy(torch.zeros_like(t), pitch).radii == []
+
+
+def test_encircled_energy_of_airy_on_device():
+    """analysis.rs:444-474 on the device: EE(r1) = 0.84 +- 0.02."""
+    from oracle import field as ofield, element as oel, fraunhofer as ofr
+    lam, a, z = 500e-9, 0.5e-3, 0.5
+    band = ofield.uniform(1.0, 0.0, 128, 128, 50e-6, 50e-6, lam)
+    far = ofr.propagate(oel.EllipticalAperture.circle(a).apply(band), z,
+                        ofr.FraunhoferConfig(aperture_extent=a))
+    psf = torch.from_numpy(np.abs(far.samples) ** 2).cuda()
+    ee = gan.encircled_energy(psf, (far.dx, far.dy))
+    assert abs(ee.value_at(1.22 * lam * z / (2.0 * a)) - 0.84) < 0.02
