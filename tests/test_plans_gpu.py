@@ -161,3 +161,60 @@ def test_plan_gradients_match_oracle_and_padded_path(plans_on):
     for ei in (0, 1):
         assert rel_l2(got[ei], pad[ei]) <= 1e-4, ei
     assert abs(val - pval) <= 1e-5 * abs(pval)
+
+
+@pytest.mark.parametrize("ny,nx,lam,z", [(256, 512, 532e-9, 10e-3), (512, 256, 580e-9, 8e-3)])
+def test_plan_non_square_grid(plans_on, ny, nx, lam, z):
+    ob = ofield.BandField(rng_field(ny, nx, seed=ny + nx), D, D, lam)
+    py, px = oasm.resolve_report(ob, z, oasm.AsmConfig()).padded_dims[::-1]
+    assert px > 2 * nx or py > 2 * ny
+    out = gasm.propagate(to_gpu_band(ob), z, gasm.AsmConfig(), "f32")
+    assert plans.stats()["builds"] == 1
+    assert plans.stats()["bytes"] == (nx + 1) * (ny + 1) * 8
+    assert rel_l2(out.samples, oasm.propagate(ob, z).samples) <= 1e-5
+
+
+def test_plans_with_graph_capture_and_host_batch(plans_on):
+    """A captured batch takes the padded path inside the graph (no plan is
+    built or used under capture) and still matches the oracle; the host-buffer
+    batch uses the plan."""
+    import ctypes as C
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import _ffi as ffi
+    L = og.lib()
+    obs_ = [band(seed=s) for s in (3, 4)]
+    refs = [oasm.propagate(b, Z).samples for b in obs_]
+    arr = (ffi.TraceItemC * 2)()
+    keep, outs = [], []
+    for i, b in enumerate(obs_):
+        tin = torch.from_numpy(b.samples).to("cuda", torch.complex64)
+        tout = torch.zeros_like(tin)
+        steps = (ffi.StepC * 1)(ffi.StepC(None, 0, Z, 1.0))
+        keep += [tin, steps]
+        outs.append(tout)
+        arr[i] = ffi.TraceItemC(tin.data_ptr(), tout.data_ptr(), ffi.Grid(N, N, D, D, LAM), steps, 1)
+    cfg = ffi.AsmConfigC(2, 1, 1, 8, 1)
+    g = C.c_void_p()
+    ffi.check(L.osgpu_beamline_trace_batch_graph(arr, 2, cfg, ffi.C64, C.byref(g)))
+    built = plans.stats()["builds"]  # the warm-up run before capture may build the plan
+    for o in outs:
+        o.zero_()
+    ffi.check(L.osgpu_graph_launch(g, None))
+    torch.cuda.synchronize()
+    ffi.check(L.osgpu_graph_destroy(g))
+    assert plans.stats()["builds"] == built
+    for o, r in zip(outs, refs):
+        assert rel_l2(o.cpu().numpy().astype(np.complex128), r) <= 1e-5
+    # host buffers (complex128), f32 engine: the plan is used
+    hits0 = plans.stats()["hits"]
+    hitems = (ffi.HostTraceItemC * 2)()
+    hout = [np.zeros((N, N), dtype=np.complex128) for _ in obs_]
+    hin = [np.ascontiguousarray(b.samples, dtype=np.complex128) for b in obs_]
+    for i in range(2):
+        hitems[i] = ffi.HostTraceItemC(hin[i].ctypes.data_as(ffi.c_double_p),
+                                       hout[i].ctypes.data_as(ffi.c_double_p),
+                                       ffi.Grid(N, N, D, D, LAM), arr[i].steps, 1)
+    ffi.check(L.osgpu_beamline_trace_batch(hitems, 2, cfg, ffi.F32, None, 0))
+    assert plans.stats()["hits"] >= hits0 + 2
+    for o, r in zip(hout, refs):
+        assert rel_l2(o, r) <= 1e-5
