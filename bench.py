@@ -520,18 +520,22 @@ def reference_arm(args):
     except (OSError, IndexError, ValueError):
         mem_workers = 4
     workers = max(1, min(cores, mem_workers, NBANDS))
+    # each step is ~6-7 s of CPU work on 16 cores: bounded so that the whole
+    # run stays within a couple of minutes whatever --steps asks for
+    steps, warmup = max(1, min(args.steps, 8)), max(1, min(args.warmup, 1))
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             pool.map(_ref_worker, range(workers))
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             pool.map(_ref_worker, range(workers))
         dt = time.perf_counter() - t0
-    props = workers * args.steps
+    props = workers * steps
     val = props / dt
     line = {"metric": METRIC, "value": val, "unit": "propagations/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "steps": steps, "warmup": warmup, "ms_per_step": dt / steps * 1e3,
+            "steps_requested": args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD, "step": f"{workers} bands, one per worker process"},
