@@ -70,6 +70,17 @@ __device__ __forceinline__ void cta_sum(float x, double* part, int f, double* re
   }
 }
 
+// e^{-i pi q / 16}, q = 0..15 (cos and -sin of pi q / 16)
+__device__ __constant__ float2 kW32[16] = {
+    {1.000000000e+00f, -0.000000000e+00f}, {9.807852804e-01f, -1.950903220e-01f},
+    {9.238795325e-01f, -3.826834324e-01f}, {8.314696123e-01f, -5.555702330e-01f},
+    {7.071067812e-01f, -7.071067812e-01f}, {5.555702330e-01f, -8.314696123e-01f},
+    {3.826834324e-01f, -9.238795325e-01f}, {1.950903220e-01f, -9.807852804e-01f},
+    {0.000000000e+00f, -1.000000000e+00f}, {-1.950903220e-01f, -9.807852804e-01f},
+    {-3.826834324e-01f, -9.238795325e-01f}, {-5.555702330e-01f, -8.314696123e-01f},
+    {-7.071067812e-01f, -7.071067812e-01f}, {-8.314696123e-01f, -5.555702330e-01f},
+    {-9.238795325e-01f, -3.826834324e-01f}, {-9.807852804e-01f, -1.950903220e-01f}};
+
 template <int M, int G>
 struct GsLay {
   static constexpr int T = M / 16;
@@ -221,11 +232,15 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
   }
   const bool keep = iterate && it.state->improved;
+  // pre-phase of column ix = tid + T q: prx[ix] = e^{i pi (M - 1) ix / M}
+  // = prx[tid] e^{-i pi q / 16} (T even), so one load per thread and the
+  // 32nd roots of unity replace sixteen loads behind the stores below
+  const float2 p0 = __ldg(it.prx + tid);
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int ix = tid + T * q;
     const size_t k = (size_t)iy * M + ix;
-    const float2 pre = cmul(__ldg(it.prx + ix), py);
+    const float2 pre = cmul(cmul(p0, kW32[q]), py);
     float p = ph[q];
     if (iterate) {
       const float2 w = cmulc(v[q], pre);  // conj(pre) v
