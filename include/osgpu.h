@@ -338,8 +338,8 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
  * layout), e.g. every band of Renderer::render_frame (observe.rs:195-210):
  * the host->device copy of band i+1 and the device->host copy of band i-1
  * run on their own streams while band i is traced (two device slots each
- * way).  Page-locked host buffers overlap fully; pageable ones are copied
- * by the driver.  Synchronous: outputs are on the host when it returns; a
+ * way).  Page-locked host buffers overlap fully; pageable ones are staged
+ * by the CUDA runtime.  Synchronous: outputs are on the host when it returns; a
  * non-finite input sample anywhere returns OSGPU_E_NON_FINITE_SAMPLE. */
 typedef struct {
   const double* in;

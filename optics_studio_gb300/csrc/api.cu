@@ -677,7 +677,7 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
   }
   if (smem_passA_bytes(a.ax, is_d, 1) > kMaxSmem || smem_passB_bytes(a.ay, is_d) > kMaxSmem ||
       (2 * ((size_t)a.ax.m + 1) + (size_t)a.ax.n) * es > kMaxSmem) {
-    set_err("grid %dx%d (sub-FFT %d x %d) exceeds the shared-memory plan of this build",
+    set_err("grid %dx%d (sub-FFT %d x %d) exceeds the shared-memory plan of this library",
             a.nx, a.ny, a.ax.m, a.ay.m);
     return OSGPU_E_UNSUPPORTED;
   }
@@ -813,7 +813,7 @@ int run_fft2(Context& c, const void* d_in, int in_c128, void* d_out, int out_c12
   a.ay = make_axis(ny, ny);
   if (a.ax.nst < 0 || a.ay.nst < 0 || smem_passA_bytes(a.ax, is_d, 1) > kMaxSmem ||
       smem_passB_bytes(a.ay, is_d) > kMaxSmem) {
-    set_err("fft2 of %dx%d exceeds the shared-memory plan of this build", nx, ny);
+    set_err("fft2 of %dx%d exceeds the shared-memory plan of this library", nx, ny);
     return OSGPU_E_UNSUPPORTED;
   }
   int rc;
