@@ -447,6 +447,28 @@ int osgpu_merit_encircled_energy_device(const void* d_obs, int32_t real_dtype, i
                                         int32_t n_scenes, uint64_t nx, uint64_t ny, double dx,
                                         double dy, double radius, int32_t band, int32_t scene,
                                         void* d_seed, void* stream, double* value);
+/* SpotRmsMerit (merit.rs:248-321): sqrt(sum I rho^2 / sum I) of the selected
+ * frame (0 when sum I <= 0); the seed (rho^2 - R^2) / (2 R sum I) goes to the
+ * selected frames and 0 to the others.  A seed request with sum I <= 0 or
+ * R <= 0 returns OSGPU_E_ADJOINT (obs_gradient is None). */
+int osgpu_merit_spot_rms_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                                int32_t n_scenes, uint64_t nx, uint64_t ny, double dx, double dy,
+                                int32_t band, int32_t scene, void* d_seed, void* stream,
+                                double* value);
+/* StrehlMerit (merit.rs:323-352): -((max I / sum I) / (max R / sum R)) of the
+ * selected frame against d_reference (FP64, nx ny samples, the frame's
+ * grid); 0 when either sum is <= 0.  No obs gradient. */
+int osgpu_merit_strehl_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                              int32_t n_scenes, uint64_t nx, uint64_t ny,
+                              const double* d_reference, int32_t band, int32_t scene,
+                              void* stream, double* value);
+/* MtfMerit (merit.rs:354-400): -|DFT_x(I)[m]| / sum I of the selected frame
+ * (summed over rows) at the bin m = freq nx dx.  freq < 0, 2 freq dx >= 1
+ * or m more than 1e-9 from an integer returns OSGPU_E_RENDER.  No obs
+ * gradient. */
+int osgpu_merit_mtf_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                           int32_t n_scenes, uint64_t nx, uint64_t ny, double dx, double freq,
+                           int32_t band, int32_t scene, void* stream, double* value);
 
 /* Adam update of fd.rs:186-257 (AdamConfig, fd.rs:63-110): optional global
  * gradient-norm clip, bias-corrected moments, x -= lr_frac (hi - lo) m^ /

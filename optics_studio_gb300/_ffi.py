@@ -244,6 +244,15 @@ SIGNATURES = [
      [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_double,
       C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
       C.POINTER(C.c_double)]),
+    ("osgpu_merit_spot_rms_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_double,
+      C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    ("osgpu_merit_strehl_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_void_p,
+      C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_double)]),
+    ("osgpu_merit_mtf_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_double,
+      C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_double)]),
     ("osgpu_adam_step_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64,
       C.POINTER(AdamConfigC), C.c_int32, C.c_double, C.c_double, C.c_void_p]),

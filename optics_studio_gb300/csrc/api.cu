@@ -2631,6 +2631,158 @@ int osgpu_merit_encircled_energy_device(const void* d_obs, int32_t real_dtype, i
   return OSGPU_OK;
 }
 
+namespace {
+int merit_args(const void* d_obs, int32_t real_dtype, int32_t nb, int32_t ns, uint64_t nx,
+               uint64_t ny, int32_t band, int32_t scene) {
+  if (!d_obs || nb <= 0 || ns <= 0 || nx == 0 || ny == 0 || band >= nb || scene >= ns ||
+      (real_dtype != OSGPU_F64 && real_dtype != OSGPU_F32) || nx > INT32_MAX || ny > INT32_MAX)
+    return OSGPU_E_BAD_ARGUMENT;
+  return OSGPU_OK;
+}
+
+// The frame a merit reads (Selector::frame, merit.rs:47-80): the
+// observation's own frame when the selector picks exactly one, else the FP64
+// sum of the selected frames, materialised in `buf`.
+int merit_frame(const void* d_obs, int f64, int nb, int ns, uint64_t len, int band, int scene,
+                DBuf& buf, cudaStream_t st, const void** img, int* img_f64) {
+  if ((band >= 0 || nb == 1) && (scene >= 0 || ns == 1)) {
+    const size_t f = (size_t)(band >= 0 ? band : 0) * ns + (scene >= 0 ? scene : 0);
+    *img = static_cast<const char*>(d_obs) + f * len * (f64 ? sizeof(double) : sizeof(float));
+    *img_f64 = f64;
+    return OSGPU_OK;
+  }
+  CK(buf.alloc(len * sizeof(double), st));
+  CK(launch_sel_frame(d_obs, f64, len, nb, ns, band, scene, reinterpret_cast<double*>(buf.p),
+                      st));
+  *img = buf.p;
+  *img_f64 = 1;
+  return OSGPU_OK;
+}
+}  // namespace
+
+int osgpu_merit_spot_rms_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                                int32_t n_scenes, uint64_t nx, uint64_t ny, double dx, double dy,
+                                int32_t band, int32_t scene, void* d_seed, void* stream,
+                                double* value) {
+  int rc;
+  if ((rc = merit_args(d_obs, real_dtype, n_bands, n_scenes, nx, ny, band, scene))) return rc;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f64 = real_dtype == OSGPU_F64;
+  DBuf frame, scr;
+  const void* img;
+  int img_f64;
+  if ((rc = merit_frame(d_obs, f64, n_bands, n_scenes, nx * ny, band, scene, frame, st, &img,
+                        &img_f64)))
+    return rc;
+  const size_t sb = reduce_scratch_bytes(2);
+  CK(scr.alloc(sb, st));
+  double* part = reinterpret_cast<double*>(scr.p);
+  double* res = part + (sb / sizeof(double) - 4);
+  CK(launch_psf_moments(img, img_f64, (int)nx, (int)ny, dx, dy, part, res, st));
+  double h[2];
+  CK(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const double sw = h[0];
+  if (value) *value = sw <= 0.0 ? 0.0 : std::sqrt(h[1] / sw);
+  if (d_seed) {
+    const double rr = h[1] / sw, root = std::sqrt(rr);
+    if (sw <= 0.0 || root <= 0.0) {  // obs_gradient is None (merit.rs:291-299)
+      set_err("spot rms: total intensity or radius is not positive, no obs gradient");
+      return OSGPU_E_ADJOINT;
+    }
+    CK(launch_spot_seed(d_seed, f64, (int)nx, (int)ny, dx, dy, n_bands, n_scenes, band, scene,
+                        rr, 2.0 * root * sw, st));
+  }
+  return OSGPU_OK;
+}
+
+int osgpu_merit_strehl_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                              int32_t n_scenes, uint64_t nx, uint64_t ny,
+                              const double* d_reference, int32_t band, int32_t scene,
+                              void* stream, double* value) {
+  int rc;
+  if ((rc = merit_args(d_obs, real_dtype, n_bands, n_scenes, nx, ny, band, scene))) return rc;
+  if (!d_reference || !value) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f64 = real_dtype == OSGPU_F64;
+  DBuf frame, scr;
+  const void* img;
+  int img_f64;
+  if ((rc = merit_frame(d_obs, f64, n_bands, n_scenes, nx * ny, band, scene, frame, st, &img,
+                        &img_f64)))
+    return rc;
+  // per grid: moment partials (2 frames), then the max partials, results at the tail
+  const size_t sb = reduce_scratch_bytes(3);
+  CK(scr.alloc(2 * sb, st));
+  double h[2][3];
+  for (int q = 0; q < 2; ++q) {
+    double* part = reinterpret_cast<double*>(static_cast<char*>(scr.p) + q * sb);
+    double* res = part + (sb / sizeof(double) - 4);
+    const void* d = q ? static_cast<const void*>(d_reference) : img;
+    const int df = q ? 1 : img_f64;
+    CK(launch_psf_moments(d, df, (int)nx, (int)ny, 1.0, 1.0, part, res, st));
+    CK(launch_psf_max(d, df, nx * ny, part + 2 * 1216 * 2, res + 2, st));
+    CK(cudaMemcpyAsync(h[q], res, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  const double pm = h[0][0], pr = h[1][0];
+  *value = (pm <= 0.0 || pr <= 0.0) ? 0.0 : -((h[0][2] / pm) / (h[1][2] / pr));
+  return OSGPU_OK;
+}
+
+int osgpu_merit_mtf_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
+                           int32_t n_scenes, uint64_t nx, uint64_t ny, double dx, double freq,
+                           int32_t band, int32_t scene, void* stream, double* value) {
+  int rc;
+  if ((rc = merit_args(d_obs, real_dtype, n_bands, n_scenes, nx, ny, band, scene))) return rc;
+  if (!value) return OSGPU_E_BAD_ARGUMENT;
+  if (freq < 0.0 || 2.0 * freq * dx >= 1.0) {
+    set_err("MTF frequency beyond Nyquist");
+    return OSGPU_E_RENDER;
+  }
+  // the bin, with the saturating float-to-integer cast of the reference
+  // (a NaN frequency lands on bin 0)
+  const double kf = freq * (double)nx * dx;
+  const double kr = std::round(kf);
+  const long long m = std::isnan(kr) ? 0 : (long long)kr;
+  if (std::fabs(kf - (double)m) > 1e-9) {
+    set_err("MTF frequency must land on a DFT bin (f = m / (nx dx))");
+    return OSGPU_E_RENDER;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f64 = real_dtype == OSGPU_F64;
+  DBuf frame, scr;
+  const void* img;
+  int img_f64;
+  if ((rc = merit_frame(d_obs, f64, n_bands, n_scenes, nx * ny, band, scene, frame, st, &img,
+                        &img_f64)))
+    return rc;
+  const int half = (int)(nx / 2);
+  if (m > half) return OSGPU_E_RENDER;  // excluded by the Nyquist test above
+  const void* tw = nullptr;
+  if ((rc = get_tw(c, (int)nx, 1, &tw))) return rc;
+  CK(scr.alloc(nx * sizeof(double) + (size_t)(half + 1) * sizeof(double2), st));
+  double* colsum = reinterpret_cast<double*>(scr.p);
+  double2* X = reinterpret_cast<double2*>(colsum + nx);
+  CK(launch_row_mtf(img, img_f64, (int)nx, (int)ny, tw, colsum, X, st));
+  double2 h[2];
+  CK(cudaMemcpyAsync(&h[0], X, sizeof(double2), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&h[1], X + m, sizeof(double2), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const double dc = h[0].x;  // the frame sum
+  *value = dc <= 0.0 ? 0.0 : -(std::hypot(h[1].x, h[1].y) / dc);
+  return OSGPU_OK;
+}
+
 int osgpu_adam_step_device(double* d_x, float* d_x32, const void* d_g, int32_t g_real_dtype,
                            double* d_m, double* d_v, uint64_t n, const osgpu_adam_config* cfg,
                            int32_t t, double lo, double hi, void* stream) {

@@ -272,6 +272,36 @@ __global__ void k_ee_seed(void* seed, int f64, int nx, int ny, double dx, double
   }
 }
 
+// The selected frame (Selector::frame, merit.rs:47-80) materialised in FP64:
+// out[k] = sum over the selected (band, scene) frames, band-major, from 0.0.
+__global__ void k_sel_frame(const void* obs, int f64, uint64_t len, int nb, int ns, int band,
+                            int scene, double* out) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x)
+    out[k] = selected_sum(obs, f64, len, nb, ns, band, scene, k);
+}
+
+// Spot RMS seed (merit.rs:285-320): (rho_k^2 - R^2) / (2 R sum I) on the
+// selected frames, 0 elsewhere; rr = R^2, denom = 2 R sum I.
+__global__ void k_spot_seed(void* seed, int f64, int nx, int ny, double dx, double dy, int ns,
+                            int band, int scene, double rr, double denom) {
+  const uint64_t len = (uint64_t)nx * ny;
+  const int f = blockIdx.y;
+  const int b = f / ns, s = f - b * ns;
+  const bool sel = (band < 0 || b == band) && (scene < 0 || s == scene);
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x) {
+    double g = 0.0;
+    if (sel) {
+      const int ix = (int)(k % nx), iy = (int)(k / nx);
+      const double y = ((double)iy - ((double)ny - 1.0) / 2.0) * dy;
+      const double x = ((double)ix - ((double)nx - 1.0) / 2.0) * dx;
+      g = ((x * x + y * y) - rr) / denom;
+    }
+    st_real(seed, f64, (size_t)f * len + k, g);
+  }
+}
+
 // Field power sum |u|^2.
 __global__ void k_power(const void* u, int c128, uint64_t n, double* part) {
   Acc a;
@@ -696,6 +726,22 @@ cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, doubl
     k_ee_seed<<<dim3(blocks, nb * ns), kRedThreads, 0, st>>>(seed, f64, nx, ny, dx, dy, radius,
                                                              ns, band, scene, out);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sel_frame(const void* obs, int f64, uint64_t len, int nb, int ns, int band,
+                             int scene, double* out, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_sel_frame<<<red_blocks(len), kRedThreads, 0, st>>>(obs, f64, len, nb, ns, band, scene, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spot_seed(void* seed, int f64, int nx, int ny, double dx, double dy, int nb,
+                             int ns, int band, int scene, double rr, double denom,
+                             cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_spot_seed<<<dim3(red_blocks((uint64_t)nx * ny), nb * ns), kRedThreads, 0, st>>>(
+      seed, f64, nx, ny, dx, dy, ns, band, scene, rr, denom);
   return cudaGetLastError();
 }
 

@@ -97,6 +97,14 @@ cudaError_t launch_mse(const void* obs, int f64, uint64_t len, int nb, int ns, i
 cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, double dy,
                       double radius, int nb, int ns, int band, int scene, void* seed,
                       double* scratch, double* out, cudaStream_t st);
+// the selected frame of an observation summed in FP64 (Selector::frame)
+cudaError_t launch_sel_frame(const void* obs, int f64, uint64_t len, int nb, int ns, int band,
+                             int scene, double* out, cudaStream_t st);
+// spot-RMS merit seed on every (band, scene) frame: selected ones get
+// (rho^2 - rr) / denom, the others 0
+cudaError_t launch_spot_seed(void* seed, int f64, int nx, int ny, double dx, double dy, int nb,
+                             int ns, int band, int scene, double rr, double denom,
+                             cudaStream_t st);
 // detector metrics (analysis.rs): out2 = {sum I, sum I rho^2}; out = max I;
 // X[k] (k <= nx/2) = DFT of the column sums (tw64: FP64 nx-point twiddles)
 cudaError_t launch_psf_moments(const void* img, int f64, int nx, int ny, double dx, double dy,

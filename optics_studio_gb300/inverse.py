@@ -482,6 +482,95 @@ class EncircledEnergyMerit:
         return v, True
 
 
+def _sel(v):
+    return -1 if v is None else v
+
+
+class SpotRmsMerit:
+    """merit.rs:248-321: the spot RMS radius sqrt(sum I rho^2 / sum I) of the
+    selected frame, with its analytic obs gradient."""
+
+    def __init__(self, band=None, scene=None):
+        self.band, self.scene = band, scene
+
+    def _call(self, obs, seed):
+        v = C.c_double()
+        B, S = len(obs.bands), len(obs.scenes)
+        nx, ny = obs.dims
+        code = _ffi.lib().osgpu_merit_spot_rms_device(
+            obs.data[0].data_ptr(), _real_code(obs.data), B, S, nx, ny, obs.pitch[0],
+            obs.pitch[1], _sel(self.band), _sel(self.scene),
+            seed.data_ptr() if seed is not None else None, _sptr(), C.byref(v))
+        return code, v.value
+
+    def evaluate(self, obs):
+        code, v = self._call(obs, None)
+        _ffi.check(code)
+        return v
+
+    def obs_gradient(self, obs):
+        g = _torch().zeros_like(obs.data)
+        code, _ = self._call(obs, g[0])
+        if code == 44:
+            return None
+        _ffi.check(code)
+        return g
+
+    def value_and_seed(self, obs, seed):
+        code, v = self._call(obs, seed[0])
+        if code == 44:
+            return v, False
+        _ffi.check(code)
+        return v, True
+
+
+class StrehlMerit:
+    """merit.rs:323-352: the negative power-equalised peak ratio of the
+    selected frame against a reference frame (device, the frame's grid).  No
+    obs gradient: grid_gradient rejects it, as the reference does."""
+
+    def __init__(self, reference, band=None, scene=None):
+        torch = _torch()
+        self.reference = torch.as_tensor(reference, dtype=torch.float64).contiguous()
+        self.band, self.scene = band, scene
+
+    def evaluate(self, obs):
+        if self.reference.numel() != obs.frame_len():
+            raise _ffi.OsgpuError(43)  # the frame and the reference differ in length
+        ref = self.reference.to(obs.data.device)
+        v = C.c_double()
+        nx, ny = obs.dims
+        _ffi.check(_ffi.lib().osgpu_merit_strehl_device(
+            obs.data[0].data_ptr(), _real_code(obs.data), len(obs.bands), len(obs.scenes), nx,
+            ny, ref.data_ptr(), _sel(self.band), _sel(self.scene), _sptr(), C.byref(v)))
+        return v.value
+
+    def obs_gradient(self, obs):
+        return None
+
+
+class MtfMerit:
+    """merit.rs:354-400: the negative MTF of the selected frame at one DFT bin
+    along x (freq in cycles/m, freq nx dx an integer below Nyquist).  No obs
+    gradient."""
+
+    def __init__(self, freq, band=None, scene=None):
+        self.freq = freq
+        self.band, self.scene = band, scene
+
+    def evaluate(self, obs):
+        v = C.c_double()
+        nx, ny = obs.dims
+        _ffi.check(_ffi.lib().osgpu_merit_mtf_device(
+            obs.data[0].data_ptr(), _real_code(obs.data), len(obs.bands), len(obs.scenes), nx,
+            ny, obs.pitch[0], self.freq, _sel(self.band), _sel(self.scene), _sptr(),
+            C.byref(v)))
+        return v.value
+
+    def obs_gradient(self, obs):
+        return None
+
+
 class SpotArrayEfficiency:
     """Negative summed efficiency into a set of spot windows (the merit of the
     spot-array inverse design; no reference counterpart):

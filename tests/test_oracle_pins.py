@@ -390,3 +390,74 @@ def test_analysis_gaussian_anchors_and_strehl():
     assert 0.2 < s < 0.6
     assert 0.67 < analysis.marechal_strehl(0.1) < 0.68
     assert analysis.marechal_strehl(0.0) == 1.0
+
+
+# ---- merit.rs built-ins over the analysis metrics -----------------------------
+
+def _merit_obs(frame, pitch=10e-6, bands=(500e-9,)):
+    n = frame.shape[-1]
+    data = np.asarray(frame, dtype=np.float64).reshape(1, len(bands), 1, n, n)
+    return observe.Observation(["intensity"], list(bands), [(0.0, 0.0)], (n, n),
+                               (pitch, pitch), data, (1e-6, 1e-9))
+
+
+def _merit_gaussian(n):
+    """merit.rs:427-438: exp(-2 rho^2 / w^2), w = n 10 um / 6."""
+    w = n * 10e-6 / 6.0
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * 10e-6
+    return np.exp(-2.0 * (c[None, :] ** 2 + c[:, None] ** 2) / (w * w))
+
+
+def test_spot_strehl_mtf_merits_match_analysis():
+    """merit.rs:474-520 and 556-576: SpotRmsMerit = spot_rms_radius (1e-9),
+    StrehlMerit of a frame against itself = -1 (1e-12), MtfMerit at the fifth
+    MTF bin = -mtf (2e-3)."""
+    from oracle import analysis
+    frame = _merit_gaussian(32)
+    obs = _merit_obs(frame)
+    want = analysis.spot_rms_radius(frame, (10e-6, 10e-6))
+    got = merit.SpotRmsMerit().evaluate(obs)
+    assert abs(got - want) / want < 1e-9
+    assert abs(merit.StrehlMerit(frame).evaluate(obs) + 1.0) < 1e-12
+    freqs, vals = analysis.mtf(frame, (10e-6, 10e-6))
+    assert abs(merit.MtfMerit(freqs[4]).evaluate(obs) + vals[4]) < 2e-3
+    assert merit.StrehlMerit(frame).obs_gradient(obs) is None
+    assert merit.MtfMerit(freqs[4]).obs_gradient(obs) is None
+
+
+def test_spot_rms_merit_gradient_fd():
+    """merit.rs:522-554: the analytic obs gradient against central differences
+    (eps 1e-9) at samples 0, 68, 255 of a 16 x 16 Gaussian frame."""
+    frame = _merit_gaussian(16)
+    obs = _merit_obs(frame)
+    m = merit.SpotRmsMerit()
+    g = m.obs_gradient(obs).reshape(-1)
+    eps = 1e-9
+    for k in (0, 68, 255):
+        up, dn = frame.copy().reshape(-1), frame.copy().reshape(-1)
+        up[k] += eps
+        dn[k] -= eps
+        fd = (m.evaluate(_merit_obs(up.reshape(16, 16)))
+              - m.evaluate(_merit_obs(dn.reshape(16, 16)))) / (2 * eps)
+        assert abs(fd - g[k]) < 1e-4 * (abs(fd) + 1.0), (k, fd, g[k])
+
+
+def test_merit_selector_and_errors():
+    """merit.rs:578-600: a selector over two bands sums them; an out-of-range band
+    and an off-bin or super-Nyquist MTF frequency are errors; a dark frame
+    gives 0 and no spot gradient."""
+    ones = np.ones((2, 4, 4))
+    obs = _merit_obs(ones, bands=(450e-9, 550e-9))
+    assert merit.SpotRmsMerit().evaluate(obs) == pytest.approx(
+        merit.SpotRmsMerit(band=0).evaluate(obs), rel=1e-15)
+    with pytest.raises(ValueError):
+        merit.SpotRmsMerit(band=5).evaluate(obs)
+    with pytest.raises(ValueError):
+        merit.MtfMerit(0.6 / 10e-6).evaluate(obs)  # above Nyquist
+    with pytest.raises(ValueError):
+        merit.MtfMerit(1.5 / (4 * 10e-6)).evaluate(obs)  # between bins
+    dark = _merit_obs(np.zeros((4, 4)))
+    assert merit.SpotRmsMerit().evaluate(dark) == 0.0
+    assert merit.SpotRmsMerit().obs_gradient(dark) is None
+    assert merit.StrehlMerit(np.ones(16)).evaluate(dark) == 0.0
+    assert merit.MtfMerit(0.0).evaluate(dark) == 0.0
