@@ -304,7 +304,8 @@ def adjoint_leg(args, stream):
                 "build_ms": build_ms,
                 "note": "kernel-spectrum plans: the 80 mm propagations (padded 8192^2) run "
                         "as 4096^2 circular convolutions with a kernel spectrum built once "
-                        "per band in FP64; the 20 mm ones (4096^2) are unchanged",
+                        "per band (kernel by the f32 engine, spectrum folded in FP64); the "
+                        "20 mm ones (4096^2) are unchanged",
                 f"rate_over_{ADJ_STEPS}_steps": ADJ_STEPS / ((ADJ_STEPS * ms + build_ms) / 1e3)}
             out["no_plan"] = no_plan
         tape.close()
@@ -797,7 +798,7 @@ def main():
                        "median_call_rate": round(statistics.median(calls) * world, 1)}
 
     # the same batch with kernel-spectrum plans (opt-in, not the headline): the
-    # first call builds one FP64 kernel table per band, later calls run every
+    # first call builds one kernel table per band, later calls run every
     # band as a circular convolution of period 2n (4096^2 instead of 8192^2)
     if not args.no_plans:
         from optics_studio_gb300 import plans
@@ -832,7 +833,7 @@ def main():
             "break_even_steps": (first_ms - pms) / gain if gain > 0 else None,
             "rel_l2_vs_padded_band0": rel,
             "note": "osgpu_plan_cache_config on: the first call builds the 32 kernel tables "
-                    "(FP64, one per band) and is timed apart (first_call_ms); value is the "
+                    "(one per band) and is timed apart (first_call_ms); value is the "
                     "steady rate of the later calls; the headline value runs without plans"}
         plans.disable()
         plans.clear()

@@ -602,7 +602,12 @@ int plan_lookup(Context& c, const PropJob& j, cudaStream_t st, const void** kq) 
       jd.in_c128 = 1;
       jd.d_out = hq;
       jd.out_c128 = 1;
-      rc = run_prop<double>(c, jd, st);
+      // the kernel quadrant from the f32 engine on the padded path (its
+      // rounding, ~3e-7 of the kernel, stays far inside the f32 bound of the
+      // propagations that use the table); the fold below runs in FP64
+      c.plans_on = false;
+      rc = run_prop<float>(c, jd, st);
+      c.plans_on = true;
     }
     if (rc == OSGPU_OK) {
       PropArgs b;

@@ -5,7 +5,8 @@ every call (src/propagation/asm.rs:505-522).  When a padded grid exceeds twice
 the field (strict densification often pads 2048^2 to 8192^2), the output
 only reaches kernel offsets |d| < n, so the same propagation is a circular
 convolution of period 2n.  With plans enabled, the first f32 ASM propagation
-of a geometry builds that kernel's spectrum once (in FP64) and later ones,
+of a geometry builds that kernel's spectrum once (the kernel by the f32
+engine on the padded path, its spectrum folded in FP64) and later ones,
 forward or adjoint, run at 2n: worth it when one geometry is propagated
 many times (an optimisation loop, a renderer over scenes).  Off by default.
 """

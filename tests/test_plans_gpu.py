@@ -2,8 +2,8 @@
 padded f32 path.
 
 A plan replaces an f32 ASM propagation padded above 2n by the circular
-convolution of period 2n with the same kernel (its spectrum built once in
-FP64), so its results match the f64 oracle (oracle/asm.py, restating
+convolution of period 2n with the same kernel (built once: the kernel by the
+f32 engine, its spectrum in FP64), so its results match the f64 oracle (oracle/asm.py, restating
 src/propagation/asm.rs:438-538) to the f32 bounds of the padded path: 1e-5
 relative L2 for fields, 1e-4 for gradients.
 """
