@@ -1,0 +1,289 @@
+"""The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
+engines, restated against the oracle (CPU; pins the oracle to the reference's
+known answers).
+
+Each test cites the test of src/propagation/fresnel.rs, fraunhofer.rs or
+rayleigh_sommerfeld.rs it restates and keeps its geometry and tolerance.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle import field as ofield, fraunhofer as ofh, fresnel as ofr, rs as ors
+
+LAMBDA = 500e-9
+
+
+def uniform(a, n, d):
+    return ofield.uniform(a, 0.0, n, n, d, d, LAMBDA)
+
+
+def gaussian(n, d, sigma, c=(0.0, 0.0)):
+    x = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d - c[0]
+    y = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d - c[1]
+    u = np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / (2.0 * sigma * sigma))
+    return ofield.BandField(u.astype(np.complex128), d, d, LAMBDA)
+
+
+def power(b):
+    return float(np.sum(np.abs(b.samples) ** 2)) * b.dx * b.dy
+
+
+# ---- src/propagation/fresnel.rs ---------------------------------------------------
+
+def test_fresnel_closed_form_step_is_the_sweep_maximum():
+    """fresnel.rs closed_form_step_is_the_exact_sweep_maximum."""
+    nx_pad, ny_pad, d, z = 12, 8, 2e-6, 0.037
+    fx = np.fft.fftfreq(nx_pad, d)
+    fy = np.fft.fftfreq(ny_pad, d)
+    ph = -math.pi * LAMBDA * z * (fx[None, :] ** 2 + fy[:, None] ** 2)
+    sweep = float(np.max(np.abs(ph - np.roll(ph, -1, axis=1))))
+    assert abs(sweep - ofr.worst_axis_step(nx_pad, d, LAMBDA, z)) < 1e-9
+
+
+def test_fresnel_z_zero_and_invalid_inputs():
+    """fresnel.rs z_zero_is_identity, convolution_z_zero_is_identity,
+    invalid_inputs_rejected."""
+    b = uniform(1.5, 16, 20e-6)
+    np.testing.assert_array_equal(ofr.propagate(b, 0.0).samples, b.samples)
+    b2 = uniform(2.0, 16, 20e-6)
+    np.testing.assert_array_equal(ofr.propagate_convolution(b2, 0.0).samples, b2.samples)
+    small = uniform(1.0, 8, 20e-6)
+    with pytest.raises(ofr.FresnelError) as e:
+        ofr.propagate(small, math.inf)
+    assert e.value.variant == "InvalidDistance"
+    with pytest.raises(ofr.FresnelError) as e:
+        ofr.propagate_convolution(small, math.nan)
+    assert e.value.variant == "InvalidDistance"
+
+
+def test_fresnel_plane_wave_bins_pick_up_exact_quadratic_phase():
+    """fresnel.rs plane_wave_bins_pick_up_exact_quadratic_phase."""
+    n, d, z, m = 32, 20e-6, 1e-3, 2.0
+    alpha = m * LAMBDA / (n * d)
+    b = ofield.plane_wave(math.asin(alpha), 0.0, 1.0, n, n, d, d, LAMBDA)
+    out = ofr.propagate(b, z, ofr.FresnelConfig(1.0, False, 1.0))
+    k = 2.0 * math.pi / LAMBDA
+    fx = m / (n * d)
+    want = np.exp(1j * (k * z - math.pi * LAMBDA * z * fx * fx))
+    for iy in (0, 16, 31):
+        assert abs(out.samples[iy, 10] / b.samples[iy, 10] - want) < 1e-9
+
+
+def test_fresnel_round_trip_on_periodic_grid_is_exact():
+    """fresnel.rs round_trip_on_periodic_grid_is_exact."""
+    b = uniform(1.0, 16, 20e-6)
+    cfg = ofr.FresnelConfig(1.0, False, 1.0)
+    rt = ofr.propagate(ofr.propagate(b, 2e-3, cfg), -2e-3, cfg)
+    assert float(np.max(np.abs(rt.samples - b.samples))) < 1e-9
+
+
+def test_fresnel_strict_mode_flags_undersampled_chirp_and_mitigates():
+    """fresnel.rs strict_mode_flags_undersampled_chirp_and_mitigates."""
+    b = uniform(1.0, 32, 1e-6)
+    z = 3e-4
+    risk = ofr.FresnelConfig(1.0, True, 1.0)
+    rep = ofr.sampling_report(b, z, risk)
+    assert not rep.nyquist_ok and rep.max_phase_step_x > math.pi
+    with pytest.raises(ofr.FresnelError) as e:
+        ofr.propagate(b, z, risk)
+    assert e.value.variant == "AliasingRisk"
+    ofr.propagate(b, z, ofr.FresnelConfig(1.0, False, 1.0))
+    fix = ofr.FresnelConfig(1.0, True, 8.0)
+    assert not ofr.sampling_report(b, z, fix).nyquist_ok
+    assert ofr.propagate(b, z, fix).samples.shape == b.samples.shape
+    at8 = ofr.sampling_report(b, z, ofr.FresnelConfig(8.0, True, 8.0))
+    assert at8.nyquist_ok and at8.max_phase_step_x < math.pi
+
+
+def test_fresnel_paraxial_flag_tracks_grid_angular_extent():
+    """fresnel.rs paraxial_flag_tracks_grid_angular_extent."""
+    rep = ofr.sampling_report(uniform(1.0, 32, 1e-3), 0.1, ofr.FresnelConfig())
+    assert rep.paraxial_ok and rep.max_phase_error_vs_asm < 0.01
+    rep = ofr.sampling_report(uniform(1.0, 32, 1e-6), 0.05, ofr.FresnelConfig())
+    assert not rep.paraxial_ok and rep.max_phase_error_vs_asm > 0.01
+
+
+def test_fresnel_convolution_guard_is_reciprocal_to_transfer_guard():
+    """fresnel.rs convolution_guard_is_reciprocal_to_transfer_guard."""
+    b = uniform(1.0, 64, 1e-6)
+    z = 5e-4
+    cfg = ofr.FresnelConfig(1.0, True, 1.0)
+    rep = ofr.sampling_report(b, z, cfg)
+    assert rep.kernel_nyquist_ok and rep.max_kernel_step_x < math.pi
+    assert not rep.nyquist_ok and rep.max_phase_step_x > math.pi
+    ofr.propagate_convolution(b, z, cfg)
+    with pytest.raises(ofr.FresnelError) as e:
+        ofr.propagate(b, z, cfg)
+    assert e.value.variant == "AliasingRisk"
+    ofr.propagate(b, z, ofr.FresnelConfig(1.0, True, 8.0))
+
+
+def test_fresnel_convolution_matches_tf_at_critical_sampling():
+    """fresnel.rs convolution_matches_tf_at_critical_sampling: n d^2 = lambda z,
+    the two forms agree within 1e-6."""
+    n, z = 256, 2e-3
+    d = math.sqrt(LAMBDA * z / n)
+    b = gaussian(n, d, 50.0 * d)
+    cfg = ofr.FresnelConfig(1.0, True, 1.0)
+    rep = ofr.sampling_report(b, z, cfg)
+    assert rep.nyquist_ok and rep.kernel_nyquist_ok
+    tf = ofr.propagate(b, z, cfg).samples
+    conv = ofr.propagate_convolution(b, z, cfg).samples
+    assert np.linalg.norm(tf - conv) / np.linalg.norm(tf) < 1e-6
+
+
+# ---- src/propagation/fraunhofer.rs ------------------------------------------------
+
+def test_fraunhofer_uniform_input_concentrates_at_dc():
+    """fraunhofer.rs uniform_input_concentrates_at_dc: |U(0)| = a (n d)^2 /
+    (lambda z), every other bin below 1e-9."""
+    n, d, z, a = 15, 2e-5, 4.0, 0.75
+    out = ofh.propagate(ofield.uniform(a, 0.0, n, n, d, d, LAMBDA), z)
+    mag = np.abs(out.samples).reshape(-1)
+    c = (n // 2) * n + n // 2
+    assert abs(mag[c] - a * (n * d) ** 2 / (LAMBDA * z)) < 1e-9
+    assert float(np.max(np.delete(mag, c))) < 1e-9
+
+
+def test_fraunhofer_power_regime_gate_and_mirror():
+    """fraunhofer.rs far_field_power_equals_input_power,
+    regime_gate_blocks_near_field_geometry, negative_z_mirrors_the_pattern,
+    invalid_inputs_rejected."""
+    n, d = 64, 1e-5
+    b = gaussian(n, d, 5.0 * d)
+    assert ofh.regime_report(b, 2.0, ofh.FraunhoferConfig()).regime_ok
+    out = ofh.propagate(b, 2.0)
+    assert abs(power(out) - power(b)) / power(b) < 1e-9
+    with pytest.raises(ofh.FraunhoferError) as e:
+        ofh.propagate(b, 0.01)
+    assert e.value.variant == "RegimeViolation"
+    assert not e.value.report.regime_ok and e.value.report.n_f_x > 1.0
+    loose = ofh.FraunhoferConfig(strict=False)
+    assert ofh.propagate(b, 0.01, loose).samples.shape == (n, n)
+    assert not ofh.regime_report(b, 0.01, loose).regime_ok
+    tight = ofh.FraunhoferConfig(max_n_f=0.05)
+    assert not ofh.regime_report(b, 2.0, tight).regime_ok
+    assert ofh.regime_report(b, 5.0, tight).regime_ok
+    back = ofh.propagate(b, -2.0)
+    assert float(np.max(np.abs(np.abs(out.samples) - np.abs(back.samples[::-1, ::-1])))) < 1e-12
+    small = ofield.uniform(1.0, 0.0, 8, 8, 20e-6, 20e-6, LAMBDA)
+    for z in (0.0, math.nan):
+        with pytest.raises(ofh.FraunhoferError) as e:
+            ofh.propagate(small, z, loose)
+        assert e.value.variant == "InvalidDistance"
+
+
+def test_fraunhofer_source_position_and_off_axis_power():
+    """fraunhofer.rs source_pos_none_equals_explicit_origin,
+    off_axis_propagation_conserves_power."""
+    b = gaussian(64, 1e-5, 5e-5)
+    a = ofh.propagate(b, 2.0, ofh.FraunhoferConfig(source_pos=None))
+    o = ofh.propagate(b, 2.0, ofh.FraunhoferConfig(source_pos=(0.0, 0.0)))
+    np.testing.assert_array_equal(a.samples, o.samples)
+    s = (1e-4, -5e-5)
+    cfg = ofh.FraunhoferConfig(source_pos=s)
+    shifted = gaussian(64, 1e-5, 5e-5, s)
+    assert ofh.regime_report(shifted, 2.0, cfg).regime_ok
+    out_s = ofh.propagate(shifted, 2.0, cfg)
+    assert abs(power(out_s) - power(shifted)) / power(shifted) < 1e-9
+    assert abs(power(out_s) - power(a)) / power(a) < 1e-9
+
+
+def test_fraunhofer_aperture_extent_declares_true_source_size():
+    """fraunhofer.rs aperture_extent_declares_true_source_size."""
+    b = gaussian(64, 1e-5, 2.0e-5)
+    z = 0.05
+    win = ofh.regime_report(b, z, ofh.FraunhoferConfig())
+    assert not win.regime_ok and not win.extent_is_aperture
+    with pytest.raises(ofh.FraunhoferError) as e:
+        ofh.propagate(b, z)
+    assert e.value.variant == "RegimeViolation"
+    cfg = ofh.FraunhoferConfig(aperture_extent=1e-4)
+    rep = ofh.regime_report(b, z, cfg)
+    assert rep.regime_ok and rep.extent_is_aperture
+    assert abs(rep.extent_used - 1e-4) < 1e-15
+    assert abs(rep.n_f_x - 0.4) < 1e-9
+    assert ofh.propagate(b, z, cfg).samples.shape == (64, 64)
+    with pytest.raises(ofh.FraunhoferError) as e:
+        ofh.propagate(b, z, ofh.FraunhoferConfig(aperture_extent=0.0))
+    assert e.value.variant == "RegimeViolation"
+
+
+# ---- src/propagation/rayleigh_sommerfeld.rs ---------------------------------------
+
+def _dft_coord(i, n, d):
+    return (i if i <= n // 2 else i - n) * d
+
+
+def test_rs_kernel_reduces_to_fresnel_paraxially_and_conjugates_for_minus_z():
+    """rayleigh_sommerfeld.rs kernel_reduces_to_fresnel_paraxially (1e-6),
+    negative_z_kernel_is_conjugate (exact)."""
+    n, d, z = 64, 10e-6, 5.0
+    k = 2.0 * math.pi / LAMBDA
+    worst = 0.0
+    for iy in (0, 16, 31, 32, 48, 63):
+        for ix in (0, 16, 31, 32, 48, 63):
+            x, y = _dft_coord(ix, n, d), _dft_coord(iy, n, d)
+            rs = complex(ors.kernel_value(x, y, LAMBDA, z))
+            fr = (complex(math.cos(k * z), math.sin(k * z)) / (1j * LAMBDA * z)
+                  * np.exp(1j * math.pi * (x * x + y * y) / (LAMBDA * z)))
+            worst = max(worst, abs(rs / fr - 1.0))
+    assert worst < 1e-6
+    fwd = ors.impulse_response(32, 32, 10e-6, 10e-6, LAMBDA, 2e-3)
+    bwd = ors.impulse_response(32, 32, 10e-6, 10e-6, LAMBDA, -2e-3)
+    np.testing.assert_array_equal(bwd, np.conj(fwd))
+
+
+def test_rs_engine_agrees_with_asm_on_smooth_band():
+    """rayleigh_sommerfeld.rs engine_agrees_with_asm_on_smooth_band (5e-2)."""
+    from oracle import asm as oasm
+    b = gaussian(200, 2e-6, 30e-6)
+    cfg = ors.RayleighSommerfeldConfig(2.0, True)
+    assert ors.sampling_report(b, 5e-3, cfg).kernel_nyquist_ok
+    rs = ors.propagate(b, 5e-3, cfg).samples
+    asm = oasm.propagate(b, 5e-3, oasm.AsmConfig(padding=2.0)).samples
+    assert np.linalg.norm(rs - asm) / np.linalg.norm(asm) < 5e-2
+
+
+def test_rs_kernel_step_closed_form_brackets_sweep():
+    """rayleigh_sommerfeld.rs kernel_step_closed_form_brackets_sweep."""
+    n, d, z = 64, 2e-6, 3e-4
+    k = 2.0 * math.pi / LAMBDA
+    c = np.array([_dft_coord(i, n, d) for i in range(n)])
+    r = np.sqrt(c[None, :] ** 2 + c[:, None] ** 2 + z * z)
+    ph = k * r - np.arctan(k * r)
+    sweep = float(np.max(np.abs(ph - np.roll(ph, -1, axis=1))))
+    closed = ors.worst_kernel_axis_step(n, d, LAMBDA, z)
+    assert sweep <= closed + 1e-12
+    assert closed < 2.0 * sweep + 1e-12
+
+
+def test_rs_strict_guard_invalid_inputs_and_back_propagation():
+    """rayleigh_sommerfeld.rs strict_guard_raises_immediately_and_padding_worsens_it,
+    z_zero_and_invalid_inputs_rejected, back_propagation_inverts_on_smooth_band."""
+    b = uniform(1.0, 64, 10e-6)
+    cfg = ors.RayleighSommerfeldConfig(1.0, True)
+    rep = ors.sampling_report(b, 1e-3, cfg)
+    assert not rep.kernel_nyquist_ok and rep.max_kernel_step_x > math.pi
+    with pytest.raises(ors.RayleighSommerfeldError) as e:
+        ors.propagate(b, 1e-3, cfg)
+    assert e.value.variant == "AliasingRisk"
+    rep4 = ors.sampling_report(b, 1e-3, ors.RayleighSommerfeldConfig(4.0, True))
+    assert rep4.max_kernel_step_x > rep.max_kernel_step_x
+    ors.propagate(b, 1e-3, ors.RayleighSommerfeldConfig(1.0, False))
+    ok = ors.sampling_report(b, 0.5, ors.RayleighSommerfeldConfig(2.0, True))
+    assert ok.kernel_nyquist_ok and ok.paraxial_ok
+    small = uniform(1.0, 8, 20e-6)
+    for z in (0.0, math.inf, math.nan):
+        with pytest.raises(ors.RayleighSommerfeldError) as e:
+            ors.propagate(small, z)
+        assert e.value.variant == "InvalidDistance"
+    g = gaussian(128, 10e-6, 80e-6)
+    cfg2 = ors.RayleighSommerfeldConfig(2.0, True)
+    rep = ors.sampling_report(g, 0.2, cfg2)
+    assert rep.kernel_nyquist_ok and rep.paraxial_ok
+    rt = ors.propagate(ors.propagate(g, 0.2, cfg2), -0.2, cfg2).samples
+    assert np.linalg.norm(rt - g.samples) / np.linalg.norm(g.samples) < 1e-2
