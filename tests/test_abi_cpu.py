@@ -199,3 +199,59 @@ def test_observation_dlpack_export_is_zero_copy():
     assert view.shape == (2, 3, 1, 4, 5)
     data[1, 2, 0, 3, 4] = -1.0
     assert view[1, 2, 0, 3, 4] == -1.0  # same memory
+
+
+# the reference unit tests' guard geometries (fresnel.rs, fraunhofer.rs,
+# rayleigh_sommerfeld.rs): the product's host decision (status before any
+# device work) equals the oracle's outcome
+ERR = {"AliasingRisk": 6, "RegimeViolation": 7, "InvalidDistance": 1}
+GUARD_CASES = [
+    ("fresnel", 32, 1e-6, 3e-4, (1.0, True, 1.0)),
+    ("fresnel", 32, 1e-6, 3e-4, (1.0, False, 1.0)),
+    ("fresnel", 32, 1e-6, 3e-4, (1.0, True, 8.0)),
+    ("fresnel", 64, 1e-6, 5e-4, (1.0, True, 1.0)),
+    ("fresnel_conv", 64, 1e-6, 5e-4, (1.0, True, 1.0)),
+    ("fresnel", 8, 20e-6, math.inf, (2.0, True, 8.0)),
+    ("fresnel_conv", 8, 20e-6, math.nan, (2.0, True, 8.0)),
+    ("rs", 64, 10e-6, 1e-3, (1.0, True)),
+    ("rs", 64, 10e-6, 1e-3, (1.0, False)),
+    ("rs", 8, 20e-6, 0.0, (2.0, True)),
+    ("fraunhofer", 64, 1e-5, 0.01, (True, 1.0, None, None)),
+    ("fraunhofer", 64, 1e-5, 0.01, (False, 1.0, None, None)),
+    ("fraunhofer", 64, 1e-5, 0.05, (True, 1.0, None, 1e-4)),
+    ("fraunhofer", 64, 1e-5, 0.05, (True, 1.0, None, 0.0)),
+    ("fraunhofer", 8, 20e-6, 0.0, (False, 1.0, None, None)),
+]
+
+
+@pytest.mark.parametrize("case", GUARD_CASES)
+def test_guard_decisions_match_oracle(case):
+    from optics_studio_gb300.propagation import rayleigh_sommerfeld as grs
+    from oracle import rs as ors
+    engine, n, d, z, cargs = case
+    lam = 500e-9
+    ob = ofield.BandField(np.ones((n, n), complex), d, d, lam)
+    o_fn, o_cfg, g_fn, g_cfg = {
+        "fresnel": (ofr.propagate, ofr.FresnelConfig, og.lib().osgpu_fresnel_propagate,
+                    gfr.FresnelConfig),
+        "fresnel_conv": (ofr.propagate_convolution, ofr.FresnelConfig,
+                         og.lib().osgpu_fresnel_propagate_convolution, gfr.FresnelConfig),
+        "rs": (ors.propagate, ors.RayleighSommerfeldConfig, og.lib().osgpu_rs_propagate,
+               grs.RayleighSommerfeldConfig),
+        "fraunhofer": (ofh.propagate, ofh.FraunhoferConfig, og.lib().osgpu_fraunhofer_propagate,
+                       gfh.FraunhoferConfig),
+    }[engine]
+    try:
+        o_fn(ob, z, o_cfg(*cargs))
+        want = None
+    except Exception as e:  # the oracle's typed error
+        want = ERR[e.variant]
+    rep = {"fresnel": _ffi.FresnelReportC, "fresnel_conv": _ffi.FresnelReportC,
+           "rs": _ffi.RsReportC, "fraunhofer": _ffi.FraunhoferReportC}[engine]()
+    buf = np.ones((n, n), complex)
+    code = g_fn(buf.ctypes.data_as(_ffi.c_double_p), buf.ctypes.data_as(_ffi.c_double_p),
+                _ffi.Grid(n, n, d, d, lam), z, g_cfg(*cargs).c(), 0, rep)
+    if want is None:
+        assert code in (0, 103)  # 103 = no device here
+    else:
+        assert code == want
