@@ -1,9 +1,10 @@
 """The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
-engines, restated against the oracle (CPU; pins the oracle to the reference's
-known answers).
+engines and its two golden Gerchberg-Saxton tests, restated against the
+oracle (CPU; pins the oracle to the reference's known answers).
 
-Each test cites the test of src/propagation/fresnel.rs, fraunhofer.rs or
-rayleigh_sommerfeld.rs it restates and keeps its geometry and tolerance.
+Each test cites the test of src/propagation/fresnel.rs, fraunhofer.rs,
+rayleigh_sommerfeld.rs or crates/optics-inverse/src/gs.rs it restates and
+keeps its geometry and tolerance.
 """
 
 import math
@@ -287,3 +288,76 @@ def test_rs_strict_guard_invalid_inputs_and_back_propagation():
     assert rep.kernel_nyquist_ok and rep.paraxial_ok
     rt = ors.propagate(ors.propagate(g, 0.2, cfg2), -0.2, cfg2).samples
     assert np.linalg.norm(rt - g.samples) / np.linalg.norm(g.samples) < 1e-2
+
+
+# ---- crates/optics-inverse/src/gs.rs ----------------------------------------------
+
+def _gs_asm(n, d, z_total, lam=LAMBDA):
+    """gs.rs tests' asm_plain (no band limit, not strict): half transforms of
+    z_total / 2 and the back-propagation."""
+    from oracle import asm as oasm
+    cfg = oasm.AsmConfig(band_limited=False, strict=False)
+    half = z_total / 2.0
+    fwd = lambda s: oasm.propagate(ofield.BandField(s, d, d, lam), half, cfg).samples
+    back = lambda s: oasm.propagate(ofield.BandField(s, d, d, lam), -half, cfg).samples
+    return fwd, back
+
+
+def _mse_merit(target):
+    tint = target * target  # gs.rs tests' mse_merit: MseToTarget on the squared target
+    return lambda inten: float(np.sum((inten - tint) ** 2) / inten.size)
+
+
+def test_gs_golden_lens_phase_recovered_from_target_intensity():
+    """gs.rs golden_lens_phase_recovered_from_target_intensity (zero start, so
+    fully deterministic): a 150 um lens aperture, f = 12 mm; GS over 2 f
+    brings the merit below 0.1 of the first and recovers the lens phase
+    (cos-score > 0.9 inside 0.9 of the radius)."""
+    from oracle import gs as ogs
+    n, d, f, radius = 128, 5e-6, 12e-3, 150e-6
+    k = 2.0 * math.pi / LAMBDA
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    r2 = c[None, :] ** 2 + c[:, None] ** 2
+    true_phase = ogs.wrap_pi(-k * r2 / (2.0 * f))
+    inside = r2 <= radius * radius
+    mask = np.where(inside, np.exp(1j * true_phase), 0.0)
+    from oracle import asm as oasm
+    u_true = oasm.propagate(ofield.BandField(mask, d, d, LAMBDA), f,
+                            oasm.AsmConfig(band_limited=False, strict=False)).samples
+    target = np.abs(u_true)
+    u_in = ofield.plane_wave(0.0, 0.0, 1.0, n, n, d, d, LAMBDA).samples
+    fwd, back = _gs_asm(n, d, 2.0 * f)
+    sol = ogs.run(u_in, inside, target, -math.pi, math.pi, np.zeros((n, n)), fwd, back,
+                  _mse_merit(target), max_iterations=60, patience=10, merit_tolerance=1e-5)
+    first = sol.history[0].merit
+    assert sol.merit < 0.1 * max(first, 1e-30)
+    sel = r2 <= (0.9 * radius) ** 2
+    diff = ogs.wrap_pi(np.asarray(sol.phase).reshape(n, n)[sel] - true_phase[sel])
+    assert float(np.mean(np.cos(diff - diff.mean()))) > 0.9
+
+
+def test_gs_golden_tophat_shaper_is_flat_and_best_merit_monotone():
+    """gs.rs golden_tophat_shaper_is_flat_and_mse_monotone: a 150 um Gaussian
+    shaped into a 250 um disk over 8 mm: best-so-far merit monotone, final
+    merit below half the first, interior (0.7 r) coefficient of variation
+    below 0.35.  The reference starts from rand's StdRng (seed 7), which only
+    Rust reproduces; a seeded uniform start in [-pi, pi) stands in."""
+    from oracle import gs as ogs
+    n, d, z_total, target_r = 128, 8e-6, 8e-3, 250e-6
+    u_in = ofield.gaussian(150e-6, 1.0, (0.0, 0.0), 0.0, LAMBDA, n, n, d, d).samples
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    r2 = c[None, :] ** 2 + c[:, None] ** 2
+    disk = r2 <= target_r * target_r
+    amp = math.sqrt(float(np.sum(np.abs(u_in) ** 2)) / float(np.sum(disk)))
+    target = np.where(disk, amp, 0.0)
+    init = np.random.default_rng(7).uniform(-math.pi, math.pi, (n, n))
+    fwd, back = _gs_asm(n, d, z_total)
+    sol = ogs.run(u_in, np.ones((n, n), bool), target, -math.pi, math.pi, init, fwd, back,
+                  _mse_merit(target), max_iterations=120, patience=10, merit_tolerance=1e-4)
+    best = [r.best_merit for r in sol.history]
+    assert all(b1 <= b0 + 1e-15 for b0, b1 in zip(best, best[1:]))
+    assert sol.merit < 0.5 * sol.history[0].merit
+    v = np.asarray(sol.target_intensity).reshape(n, n)[r2 <= (0.7 * target_r) ** 2]
+    assert float(np.std(v) / np.mean(v)) < 0.35
+    assert all(math.isfinite(r.target_error_rms) and math.isfinite(r.phase_update_rms)
+               for r in sol.history)
