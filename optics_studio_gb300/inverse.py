@@ -244,6 +244,12 @@ class Renderer:
         """observe.rs:213-314 (frames band-major, scenes inner)."""
         if not self.bands or not self.scenes:
             raise _ffi.OsgpuError(43)
+        # observe.rs:219-230: the finite-difference steps of the requested channels
+        if (self.deriv_x or self.deriv_y) and not (math.isfinite(self.scene_step)
+                                                   and self.scene_step > 0.0):
+            raise _ffi.OsgpuError(43)
+        if self.deriv_lambda and not (math.isfinite(self.lambda_step) and self.lambda_step > 0.0):
+            raise _ffi.OsgpuError(43)
         chans = [INTENSITY]
         if self.deriv_x:
             chans.append(DX)

@@ -6,6 +6,7 @@ Restates ``crates/optics-inverse/src/observe.rs``: the flat
 differences (213-314).
 """
 
+import math
 from dataclasses import dataclass, field, replace
 from typing import Callable, List
 
@@ -59,6 +60,11 @@ class Renderer:
         """observe.rs:213-314."""
         if not self.bands or not self.scenes:
             raise InverseError("Render", "renderer needs at least one band and one scene")
+        if (self.deriv_x or self.deriv_y) and not (math.isfinite(self.scene_step)
+                                                   and self.scene_step > 0.0):
+            raise InverseError("Render", "scene_step must be positive and finite")
+        if self.deriv_lambda and not (math.isfinite(self.lambda_step) and self.lambda_step > 0.0):
+            raise InverseError("Render", "lambda_step must be positive and finite")
         chans = [INTENSITY]
         if self.deriv_x:
             chans.append(DX)

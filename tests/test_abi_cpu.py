@@ -255,3 +255,23 @@ def test_guard_decisions_match_oracle(case):
         assert code in (0, 103)  # 103 = no device here
     else:
         assert code == want
+
+
+def test_renderer_rejects_empty_axes_and_bad_steps_before_device_work():
+    """observe.rs:214-230: no band or scene, or a non-positive / non-finite
+    finite-difference step of a requested channel, is a Render error raised
+    before the source or any device call."""
+    pytest.importorskip("torch")
+    from optics_studio_gb300 import inverse as inv
+
+    def never(*_):
+        raise AssertionError("the renderer must validate before building frames")
+
+    for kw in ({"bands": []}, {"scenes": []}, {"deriv_x": True, "scene_step": 0.0},
+               {"deriv_y": True, "scene_step": math.inf},
+               {"deriv_lambda": True, "lambda_step": -1e-9},
+               {"deriv_lambda": True, "lambda_step": math.nan}):
+        r = inv.Renderer(never, never, (1e-6, 1e-6), **kw)
+        with pytest.raises(og.OsgpuError) as e:
+            r.render(None)
+        assert e.value.variant == "Render"

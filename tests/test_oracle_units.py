@@ -1,10 +1,11 @@
 """The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
-engines and its two golden Gerchberg-Saxton tests, restated against the
-oracle (CPU; pins the oracle to the reference's known answers).
+engines, its two golden Gerchberg-Saxton tests and its renderer tests,
+restated against the oracle (CPU; pins the oracle to the reference's known
+answers).
 
 Each test cites the test of src/propagation/fresnel.rs, fraunhofer.rs,
-rayleigh_sommerfeld.rs or crates/optics-inverse/src/gs.rs it restates and
-keeps its geometry and tolerance.
+rayleigh_sommerfeld.rs, crates/optics-inverse/src/gs.rs or observe.rs it
+restates and keeps its geometry and tolerance.
 """
 
 import math
@@ -361,3 +362,120 @@ def test_gs_golden_tophat_shaper_is_flat_and_best_merit_monotone():
     assert float(np.std(v) / np.mean(v)) < 0.35
     assert all(math.isfinite(r.target_error_rms) and math.isfinite(r.phase_update_rms)
                for r in sol.history)
+
+
+# ---- crates/optics-inverse/src/observe.rs -----------------------------------------
+
+def _obs_mods():
+    from oracle import asm as oasm, carrier as ocar, element as oel, observe as oobs
+    return oasm, ocar, oel, oobs
+
+
+def _gauss_src(w0, n=64, d=10e-6):
+    return lambda x0, y0, lam: ofield.gaussian(w0, 1.0, (x0, y0), 0.0, lam, n, n, d, d)
+
+
+def _plane_src(n=64, d=10e-6):
+    return lambda x0, y0, lam: ofield.plane_wave(0.0, 0.0, 1.0, n, n, d, d, lam)
+
+
+def _relay_carrier(dist, n_idx):
+    """observe.rs relay_carrier: defocus -d, a uniform phase 2 pi (n - 1) h /
+    lambda, refocus +d."""
+    oasm, ocar, oel, _ = _obs_mods()
+
+    def build(v, lam):
+        phase = 2.0 * math.pi * (n_idx - 1.0) * v[0] / lam
+        d = ocar.Design()
+        d.gap(-dist, 1.0)
+        d.push(oel.PhaseMask.sampled(np.full(64 * 64, phase), (64, 64), (10e-6, 10e-6)), 0.0, 1.0)
+        d.gap(dist, 1.0)
+        return d
+    return ocar.Carrier.analytic(1, 0.0, 20e-6, build)
+
+
+def test_observe_piston_chain_zero_xy_channels_and_round_trip():
+    """observe.rs defocus_mask_defocus_chain_is_pure_piston (1e-6 of peak),
+    plane_wave_x_y_channels_are_exactly_zero, round_trip_propagation_preserves_gaussian
+    (power and overlap within 1e-6)."""
+    oasm, ocar, oel, oobs = _obs_mods()
+    plain = oasm.AsmConfig(band_limited=False, strict=False)
+    r = oobs.Renderer(_relay_carrier(5e-3, 1.5), _gauss_src(80e-6), asm_cfg=plain)
+    obs = r.render(np.array([2e-6]))
+    i_in = np.abs(_gauss_src(80e-6)(0.0, 0.0, LAMBDA).samples) ** 2
+    assert float(np.max(np.abs(obs.data[0, 0, 0] - i_in))) < 1e-6 * float(np.max(i_in))
+    r = oobs.Renderer(_relay_carrier(5e-3, 1.5), _plane_src(), deriv_x=True, deriv_y=True)
+    obs = r.render(np.array([2e-6]))
+    assert np.all(obs.data[1:, 0, 0] == 0.0)
+    d = ocar.Design()
+    d.gap(2e-3, 1.0)
+    d.gap(-2e-3, 1.0)
+    u = _gauss_src(100e-6)(0.0, 0.0, LAMBDA)
+    out = d.beamline().trace(u, lambda b, z, m: oasm.propagate(
+        b, z, oasm.AsmConfig(band_limited=False, strict=False, medium=m)))
+    s_in = float(np.sum(np.abs(u.samples) ** 2))
+    s_out = float(np.sum(np.abs(out.samples) ** 2))
+    assert abs(s_out / s_in - 1.0) < 1e-6
+    ip = abs(np.sum(u.samples * np.conj(out.samples)))
+    assert abs(ip / math.sqrt(s_in * s_out) - 1.0) < 1e-6
+
+
+def test_observe_dx_channel_matches_translation_invariance():
+    """observe.rs dx_channel_matches_translation_invariance: after a 3 mm gap
+    dI/dx0 = -dI/dx (five-point stencil), within 0.02 of peak / w0 over the
+    pixels above 2 % of the peak."""
+    oasm, ocar, oel, oobs = _obs_mods()
+
+    def build(v, lam):
+        d = ocar.Design()
+        d.gap(3e-3, 1.0)
+        return d
+    r = oobs.Renderer(ocar.Carrier.analytic(0, 0.0, 1.0, build), _gauss_src(80e-6),
+                      asm_cfg=oasm.AsmConfig(band_limited=False, strict=False), deriv_x=True,
+                      scene_step=1e-6)
+    obs = r.render(np.zeros(0))
+    i, dx = obs.data[0, 0, 0], obs.data[1, 0, 0]
+    peak = float(np.max(i))
+    scale = peak / 80e-6
+    gx = (i[:, :-4] - 8.0 * i[:, 1:-3] + 8.0 * i[:, 3:-1] - i[:, 4:]) / (12.0 * obs.pitch[0])
+    core = i[1:-1, 2:-2] >= 0.02 * peak
+    err = np.abs(dx[1:-1, 2:-2] + gx[1:-1]) / scale
+    assert int(np.sum(core)) > 100
+    assert float(np.max(err[core])) < 0.02
+
+
+def test_observe_lambda_channel_detects_chromatic_focus():
+    """observe.rs lambda_channel_detects_chromatic_focus: a diffractive lens
+    (f = f0 lambda0 / lambda, 300 um stop) at f0: max |dI/dlambda| at the
+    middle band exceeds 1e5 times that band's peak intensity."""
+    oasm, ocar, oel, oobs = _obs_mods()
+    lam0, f0 = 500e-9, 50e-3
+
+    def build(v, lam):
+        f = v[0] * lam0 / lam
+        d = ocar.Design()
+        d.push(oel.ThinLens(lambda _l: f, None, oel.ClearAperture.circle(300e-6)), v[0], 1.0)
+        return d
+    r = oobs.Renderer(ocar.Carrier.analytic(1, 0.01, 1.0, build), _plane_src(128),
+                      bands=[450e-9, 500e-9, 550e-9], deriv_lambda=True, lambda_step=5e-9,
+                      asm_cfg=oasm.AsmConfig(band_limited=False, strict=False))
+    obs = r.render(np.array([f0]))
+    assert float(np.max(np.abs(obs.data[1, 1, 0]))) > 1.0e5 * float(np.max(obs.data[0, 1, 0]))
+
+
+def test_observe_layout_and_rejections():
+    """observe.rs observation_layout_is_contiguous_frames,
+    renderer_rejects_empty_axes_and_bad_steps (observe.rs:214-230)."""
+    oasm, ocar, oel, oobs = _obs_mods()
+    car = _relay_carrier(5e-3, 1.5)
+    r = oobs.Renderer(car, _plane_src(), bands=[450e-9, 550e-9],
+                      scenes=[(0.0, 0.0), (20e-6, 0.0)], deriv_x=True, deriv_lambda=True)
+    obs = r.render(np.array([1e-6]))
+    assert obs.data.shape == (3, 2, 2, 64, 64)
+    assert obs.channels[1:] == [oobs.DX, oobs.DLAMBDA]
+    assert obs.channel_index(oobs.DY) is None
+    for kw in ({"bands": []}, {"scenes": []}, {"deriv_x": True, "scene_step": 0.0},
+               {"deriv_y": True, "scene_step": math.nan},
+               {"deriv_lambda": True, "lambda_step": -1e-9}):
+        with pytest.raises(ocar.InverseError):
+            oobs.Renderer(car, _plane_src(), **kw).render(np.array([1e-6]))
