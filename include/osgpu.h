@@ -651,6 +651,26 @@ const char* osgpu_version(void);
 /* Number of kernel launches issued by the library since load. */
 uint64_t osgpu_launch_count(void);
 
+/* ------------------------------------------------- device-resident fields
+ * For callers without a device allocator of their own (the Rust binding): a
+ * handle owns the nx x ny samples of one field on the device, stored as
+ * complex128 (OSGPU_C128) or complex64 (OSGPU_C64), so that a beamline's
+ * planes stay on the device between the *_device calls.  Host buffers are
+ * interleaved complex128 (the reference's Vec<Complex64>, field.rs:100);
+ * a complex64 handle converts on the device.  Upload and download are
+ * synchronous: they return when the copy is complete. */
+typedef struct osgpu_field_s* osgpu_field;
+/* A zero-filled field. */
+int osgpu_field_create(uint64_t nx, uint64_t ny, int32_t dtype, osgpu_field* out);
+int osgpu_field_upload(osgpu_field f, const double* host_c128, void* stream);
+int osgpu_field_download(osgpu_field f, double* host_c128, void* stream);
+/* The device buffer (d_in / d_out of the *_device entry points) and shape;
+ * any output pointer may be NULL. */
+int osgpu_field_info(osgpu_field f, void** d_samples, uint64_t* nx, uint64_t* ny,
+                     int32_t* dtype);
+/* Frees the samples after the work queued on them (NULL: no-op). */
+int osgpu_field_destroy(osgpu_field f);
+
 #ifdef __cplusplus
 }
 #endif

@@ -168,6 +168,13 @@ SIGNATURES = [
     ("osgpu_sync_status", C.c_int, []),
     ("osgpu_version", C.c_char_p, []),
     ("osgpu_launch_count", C.c_uint64, []),
+    ("osgpu_field_create", C.c_int, [C.c_uint64, C.c_uint64, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("osgpu_field_upload", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("osgpu_field_download", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("osgpu_field_info", C.c_int,
+     [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+      C.POINTER(C.c_int32)]),
+    ("osgpu_field_destroy", C.c_int, [C.c_void_p]),
     ("osgpu_asm_sampling_report", C.c_int,
      [C.POINTER(Grid), C.c_double, C.POINTER(AsmConfigC), C.POINTER(AsmReportC)]),
     ("osgpu_asm_propagate", C.c_int,

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <new>
 #include <utility>
 #include <vector>
 
@@ -1337,6 +1338,100 @@ int osgpu_init(int32_t device) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
   }
   return ensure_init(c);
+}
+
+struct osgpu_field_s {
+  void* p;
+  uint64_t nx, ny;
+  int32_t dtype;
+};
+
+int osgpu_field_create(uint64_t nx, uint64_t ny, int32_t dtype, osgpu_field* out) {
+  if (!out) return OSGPU_E_BAD_ARGUMENT;
+  *out = nullptr;
+  if (nx == 0 || ny == 0 || (dtype != OSGPU_C128 && dtype != OSGPU_C64) ||
+      nx > (uint64_t)INT32_MAX || ny > (uint64_t)INT32_MAX) {
+    set_err("field handle: bad shape or dtype");
+    return OSGPU_E_BAD_ARGUMENT;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  const size_t bytes = (size_t)(nx * ny) * (dtype == OSGPU_C128 ? 16 : 8);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e == cudaSuccess) e = cudaMemset(p, 0, bytes);
+  if (e != cudaSuccess) {
+    if (p) cudaFree(p);
+    return cuda_fail(e, "field handle allocation");
+  }
+  osgpu_field f = new (std::nothrow) osgpu_field_s{p, nx, ny, dtype};
+  if (!f) {
+    cudaFree(p);
+    return OSGPU_E_OUT_OF_MEMORY;
+  }
+  *out = f;
+  return OSGPU_OK;
+}
+
+int osgpu_field_upload(osgpu_field f, const double* host_c128, void* stream) {
+  if (!f || !host_c128) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const size_t n = (size_t)(f->nx * f->ny);
+  if (f->dtype == OSGPU_C128) {
+    CK(cudaMemcpyAsync(f->p, host_c128, n * 16, cudaMemcpyHostToDevice, st));
+  } else {
+    DBuf tmp;
+    CK(tmp.alloc(n * 16, st));
+    CK(cudaMemcpyAsync(tmp.p, host_c128, n * 16, cudaMemcpyHostToDevice, st));
+    CK(launch_c128_to_c64(tmp.p, f->p, n, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  return OSGPU_OK;
+}
+
+int osgpu_field_download(osgpu_field f, double* host_c128, void* stream) {
+  if (!f || !host_c128) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const size_t n = (size_t)(f->nx * f->ny);
+  if (f->dtype == OSGPU_C128) {
+    CK(cudaMemcpyAsync(host_c128, f->p, n * 16, cudaMemcpyDeviceToHost, st));
+  } else {
+    DBuf tmp;
+    CK(tmp.alloc(n * 16, st));
+    CK(launch_c64_to_c128(f->p, tmp.p, n, st));
+    CK(cudaMemcpyAsync(host_c128, tmp.p, n * 16, cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  return OSGPU_OK;
+}
+
+int osgpu_field_info(osgpu_field f, void** d_samples, uint64_t* nx, uint64_t* ny,
+                     int32_t* dtype) {
+  if (!f) return OSGPU_E_BAD_ARGUMENT;
+  if (d_samples) *d_samples = f->p;
+  if (nx) *nx = f->nx;
+  if (ny) *ny = f->ny;
+  if (dtype) *dtype = f->dtype;
+  return OSGPU_OK;
+}
+
+int osgpu_field_destroy(osgpu_field f) {
+  if (!f) return OSGPU_OK;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  const cudaError_t e = cudaFree(f->p);  // waits for the work queued on the samples
+  delete f;
+  return e == cudaSuccess ? OSGPU_OK : cuda_fail(e, "field handle free");
 }
 
 int osgpu_last_error(char* buf, size_t len) {

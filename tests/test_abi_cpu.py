@@ -275,3 +275,26 @@ def test_renderer_rejects_empty_axes_and_bad_steps_before_device_work():
         with pytest.raises(og.OsgpuError) as e:
             r.render(None)
         assert e.value.variant == "Render"
+
+
+def test_field_handles_validate_without_device():
+    """osgpu_field_*: argument checks come before any device call; without a
+    GPU a well-formed create reports NoDevice."""
+    L = og.lib()
+    h = ctypes.c_void_p()
+    assert L.osgpu_field_create(0, 4, 0, ctypes.byref(h)) == 102
+    assert L.osgpu_field_create(4, 4, 7, ctypes.byref(h)) == 102
+    assert L.osgpu_field_create(4, 4, 0, None) == 102
+    assert h.value is None
+    assert L.osgpu_field_upload(None, None, None) == 102
+    assert L.osgpu_field_download(None, None, None) == 102
+    assert L.osgpu_field_info(None, None, None, None, None) == 102
+    assert L.osgpu_field_destroy(None) == 0
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = False
+    if not has_gpu:
+        assert L.osgpu_field_create(4, 4, 0, ctypes.byref(h)) == 103
+        assert h.value is None
