@@ -1,11 +1,11 @@
 """The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
-engines, its two golden Gerchberg-Saxton tests and its renderer tests,
-restated against the oracle (CPU; pins the oracle to the reference's known
-answers).
+engines, the ASM Airy test, the Gerchberg-Saxton convention pins and golden
+tests and the renderer tests, restated against the oracle (CPU; pins the
+oracle to the reference's known answers).
 
 Each test cites the test of src/propagation/fresnel.rs, fraunhofer.rs,
-rayleigh_sommerfeld.rs, crates/optics-inverse/src/gs.rs or observe.rs it
-restates and keeps its geometry and tolerance.
+rayleigh_sommerfeld.rs, tests/asm.rs, crates/optics-inverse/src/gs.rs or
+observe.rs it restates and keeps its geometry and tolerance.
 """
 
 import math
@@ -479,3 +479,79 @@ def test_observe_layout_and_rejections():
                {"deriv_lambda": True, "lambda_step": -1e-9}):
         with pytest.raises(ocar.InverseError):
             oobs.Renderer(car, _plane_src(), **kw).render(np.array([1e-6]))
+
+
+def _plain(u, n, d, z):
+    from oracle import asm as oasm
+    return oasm.propagate(ofield.BandField(u, d, d, LAMBDA), z,
+                          oasm.AsmConfig(band_limited=False, strict=False)).samples
+
+
+def test_gs_convention_pins():
+    """gs.rs asm_roundtrip_is_identity (1e-9), two_half_transforms_compose_to_full_transform
+    (1e-6 of the mean modulus), converging_lens_phase_focuses_at_positive_z (peak
+    above 5x the bare propagation, centroid within 10 um of the axis),
+    blaze_phase_steers_spot_to_positive_x (centroid at lambda z / period within 15 %)."""
+    n, d, z = 64, 10e-6, 2e-3
+    g = ofield.gaussian(60e-6, 1.0, (0.0, 0.0), 0.0, LAMBDA, n, n, d, d).samples
+    back = _plain(_plain(g, n, d, z), n, d, -z)
+    assert float(np.max(np.abs(back - g))) < 1e-9
+    full = _plain(g, n, d, 2.0 * z)
+    half = _plain(_plain(g, n, d, z), n, d, z)
+    assert float(np.max(np.abs(full - half))) < 1e-6 * float(np.mean(np.abs(full)))
+
+    n, d, f = 128, 5e-6, 12e-3
+    k = 2.0 * math.pi / LAMBDA
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    r2 = c[None, :] ** 2 + c[:, None] ** 2
+    pw = ofield.plane_wave(0.0, 0.0, 1.0, n, n, d, d, LAMBDA).samples
+    focused = _plain(pw * np.exp(-1j * k * r2 / (2.0 * f)), n, d, f)
+    bare = _plain(pw, n, d, f)
+    w = np.abs(focused) ** 2
+    assert float(np.max(w)) > 5.0 * float(np.max(np.abs(bare) ** 2))
+    assert abs(float(np.sum(w * c[None, :])) / float(np.sum(w))) < 10e-6
+
+    z, period = 4e-3, 60e-6
+    gb = ofield.gaussian(120e-6, 1.0, (0.0, 0.0), 0.0, LAMBDA, n, n, d, d).samples
+    out = _plain(gb * np.exp(1j * 2.0 * math.pi * c[None, :] / period), n, d, z)
+    w = np.abs(out) ** 2
+    shift = float(np.sum(w * c[None, :])) / float(np.sum(w))
+    want = LAMBDA * z / period
+    assert abs(shift - want) < 0.15 * want
+
+
+# ---- tests/asm.rs -----------------------------------------------------------------
+
+def test_asm_airy_pattern_far_field():
+    """tests/asm.rs airy_pattern_far_field: a 1 mm circular aperture on a 1536^2
+    grid (20 um) propagated 40 m by ASM; the ring-binned profile (bins of 2 dx)
+    follows [2 J1(v)/v]^2 within 2 % of the on-axis value out to 12.6 mm and the
+    first zero lies within 2 % of 1.22 lambda z / 2a."""
+    from scipy import special
+    from oracle import asm as oasm, element as oel
+    n, dx, a, z = 1536, 20e-6, 1.0e-3, 40.0
+    band = ofield.uniform(1.0, 0.0, n, n, dx, dx, LAMBDA)
+    far = oasm.propagate(oel.EllipticalAperture.circle(a).apply(band), z)
+    dr, r_max = 2.0 * dx, 12.6e-3
+    nbins = int(r_max / dr)
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * dx
+    r = np.sqrt(c[None, :] ** 2 + c[:, None] ** 2)
+    b = (r / dr).astype(np.int64).reshape(-1)
+    keep = b < nbins
+    i = (np.abs(far.samples) ** 2).reshape(-1)
+    prof = (np.bincount(b[keep], weights=i[keep], minlength=nbins)
+            / np.maximum(np.bincount(b[keep], minlength=nbins), 1))
+    i0 = float(np.mean(prof[:3]))
+    rc = (np.arange(nbins) + 0.5) * dr
+    v = 2.0 * math.pi / LAMBDA * a * rc / z
+    airy = (2.0 * special.j1(v) / v) ** 2
+    sel = rc <= r_max - dr
+    assert float(np.max(np.abs(prof[sel] / i0 - airy[sel]))) <= 0.02
+    r1 = 1.22 * LAMBDA * z / (2.0 * a)
+    lo, hi = int(8.0e-3 / dr), int(12.4e-3 / dr)
+    bm = lo + int(np.argmin(prof[lo:hi]))
+    y0, ym, y1 = prof[bm - 1], prof[bm], prof[bm + 1]
+    d2 = y0 - 2.0 * ym + y1
+    frac = 0.5 * (y0 - y1) / d2 if d2 != 0.0 else 0.0
+    r_zero = (bm + min(max(frac, -0.5), 0.5)) * dr
+    assert abs(r_zero - r1) / r1 <= 0.02
