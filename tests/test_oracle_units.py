@@ -1,10 +1,11 @@
 """The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
-engines, the ASM Airy test, the Gerchberg-Saxton convention pins and golden
+engines, the ASM Airy test, the element-transmission probe, the
+Gerchberg-Saxton convention pins and golden
 tests and the renderer tests, restated against the oracle (CPU; pins the
 oracle to the reference's known answers).
 
 Each test cites the test of src/propagation/fresnel.rs, fraunhofer.rs,
-rayleigh_sommerfeld.rs, tests/asm.rs, crates/optics-inverse/src/gs.rs or
+rayleigh_sommerfeld.rs, tests/asm.rs, crates/optics-inverse/src/adjoint.rs, gs.rs or
 observe.rs it restates and keeps its geometry and tolerance.
 """
 
@@ -555,3 +556,37 @@ def test_asm_airy_pattern_far_field():
     frac = 0.5 * (y0 - y1) / d2 if d2 != 0.0 else 0.0
     r_zero = (bm + min(max(frac, -0.5), 0.5)) * dr
     assert abs(r_zero - r1) / r1 <= 0.02
+
+
+# ---- crates/optics-inverse/src/adjoint.rs -----------------------------------------
+
+def _chirp(n, d):
+    """adjoint.rs tests' chirp_field: a Gaussian envelope (60 um) with a tilt and
+    a quadratic phase."""
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    x, y = c[None, :], c[:, None]
+    r2 = x * x + y * y
+    ph = 3.7 * x / 1e-3 + 2.1 * y / 1e-3 + 9.0e6 * r2
+    return ofield.BandField(np.exp(-r2 / (2.0 * 60e-6 ** 2)) * np.exp(1j * ph), d, d, LAMBDA)
+
+
+def test_adjoint_element_transmission_probe_and_identity():
+    """adjoint.rs element_transmission_probe_and_adjoint_identity: the probe of a
+    sampled phase mask behind a 120 um stop is e^{i phase} inside, 0 outside
+    (1e-12), equals apply(1), and <w, t d> = <conj(t) w, d> (1e-12)."""
+    from oracle import element as oel
+    n, d = 32, 10e-6
+    phase = np.sin(np.arange(n * n, dtype=np.float64) * 0.37)
+    mask = oel.PhaseMask.sampled(phase, (n, n), (d, d), None, oel.ClearAperture.circle(120e-6))
+    like = _chirp(n, d)
+    t = oel.transmission(mask, like)
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    inside = c[None, :] ** 2 + c[:, None] ** 2 <= 120e-6 ** 2
+    want = np.where(inside, np.exp(1j * phase.reshape(n, n)), 0.0)
+    assert float(np.max(np.abs(t - want))) < 1e-12
+    ones = ofield.BandField(np.ones((n, n), complex), d, d, LAMBDA)
+    np.testing.assert_array_equal(mask.apply(ones).samples, t)
+    dvec, w = _chirp(n, d).samples, _chirp(n, d).samples
+    lhs = np.vdot(w, t * dvec)
+    rhs = np.vdot(np.conj(t) * w, dvec)
+    assert abs(lhs - rhs) / abs(lhs) < 1e-12
