@@ -1,12 +1,13 @@
 """The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
 engines, the ASM Airy test, the element-transmission probe, the
-Gerchberg-Saxton convention pins and golden
-tests and the renderer tests, restated against the oracle (CPU; pins the
-oracle to the reference's known answers).
+Gerchberg-Saxton convention pins and golden tests and the renderer tests,
+restated against the oracle (CPU; pins the oracle to the reference's known
+answers).
 
-Each test cites the test of src/propagation/fresnel.rs, fraunhofer.rs,
-rayleigh_sommerfeld.rs, tests/asm.rs, crates/optics-inverse/src/adjoint.rs, gs.rs or
-observe.rs it restates and keeps its geometry and tolerance.
+Each test cites the test it restates (src/propagation/fresnel.rs,
+fraunhofer.rs, rayleigh_sommerfeld.rs, tests/asm.rs, or
+crates/optics-inverse/src/adjoint.rs, gs.rs, observe.rs) and keeps its
+geometry and tolerance.
 """
 
 import math
