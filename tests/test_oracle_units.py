@@ -1,11 +1,11 @@
 """The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
-engines, the ASM Airy test, the element-transmission probe, the
-Gerchberg-Saxton convention pins and golden tests and the renderer tests,
-restated against the oracle (CPU; pins the oracle to the reference's known
-answers).
+engines, the ASM Airy test, element tests (lens, ramp, blaze, wedge, rotated
+stop, sag), the element-transmission probe, the Gerchberg-Saxton convention
+pins and golden tests and the renderer tests, restated against the oracle
+(CPU; pins the oracle to the reference's known answers).
 
 Each test cites the test it restates (src/propagation/fresnel.rs,
-fraunhofer.rs, rayleigh_sommerfeld.rs, tests/asm.rs, or
+fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, tests/asm.rs, or
 crates/optics-inverse/src/adjoint.rs, gs.rs, observe.rs) and keeps its
 geometry and tolerance.
 """
@@ -591,3 +591,97 @@ def test_adjoint_element_transmission_probe_and_identity():
     lhs = np.vdot(w, t * dvec)
     rhs = np.vdot(np.conj(t) * w, dvec)
     assert abs(lhs - rhs) / abs(lhs) < 1e-12
+
+
+# ---- src/element.rs ---------------------------------------------------------------
+
+def _wrap(p):
+    return (p + math.pi) % (2.0 * math.pi) - math.pi
+
+
+def _xy(n, d):
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    return c[None, :], c[:, None]
+
+
+def test_element_thin_lens_phase_and_diverging_conjugate():
+    """element.rs phase_profile_is_the_negative_quadratic (|t| = 1 to 1e-12, phase
+    -k r^2 / 2f to 1e-9), diverging_lens_conjugates_the_converging_phase (1e-12)."""
+    from oracle import element as oel
+    n, d, f = 128, 1e-5, 0.1
+    band = ofield.uniform(2.0, 0.0, n, n, d, d, LAMBDA)
+    out = oel.ThinLens.fixed(f).apply(band).samples
+    k = 2.0 * math.pi / LAMBDA
+    x, y = _xy(n, d)
+    for ix, iy in ((0, 0), (63, 64), (127, 127), (10, 120)):
+        s = out[iy, ix]
+        assert abs(abs(s) - 2.0) < 1e-12
+        want = -k * (x[0, ix] ** 2 + y[iy, 0] ** 2) / (2.0 * f)
+        assert abs(_wrap(np.angle(s) - want)) < 1e-9
+    b = ofield.uniform(1.0, 0.0, 64, 64, 1e-5, 1e-5, LAMBDA)
+    conv = oel.ThinLens.fixed(0.1).apply(b).samples
+    div = oel.ThinLens.fixed(-0.1).apply(b).samples
+    assert float(np.max(np.abs(np.conj(conv) - div))) < 1e-12
+
+
+def test_element_linear_ramp_and_blazes():
+    """element.rs linear_ramp_reproduces_a_tilted_plane_wave (1e-9),
+    blaze_integer_2pi_depth_is_a_pure_tilted_plane_wave (phase 1e-9, modulus
+    1e-12), orientation_rotates_the_grating_vector (a kinoform at pi/2 follows
+    2 pi frac(y / period), 1e-9)."""
+    from oracle import element as oel
+    theta = 0.02
+    k = 2.0 * math.pi / LAMBDA
+    alpha = math.sin(theta)
+    b = ofield.uniform(1.0, 0.0, 101, 101, 1e-3, 1e-3, LAMBDA)
+    out = oel.PhaseMask(lambda x, y: k * alpha * x).apply(b).samples
+    want = ofield.plane_wave(theta, 0.0, 1.0, 101, 101, 1e-3, 1e-3, LAMBDA).samples
+    assert float(np.max(np.abs(out - want))) < 1e-9
+    period = 100e-6
+    b = ofield.uniform(1.0, 0.0, 64, 64, 5e-6, 5e-6, LAMBDA)
+    x, y = _xy(64, 5e-6)
+    for m in (1.0, 2.0):
+        s = oel.BlazedGrating(period, 2.0 * math.pi * m, 0.0).apply(b).samples
+        kg = 2.0 * math.pi * m / period
+        assert float(np.max(np.abs(_wrap(np.angle(s) - kg * x)))) < 1e-9
+        assert float(np.max(np.abs(np.abs(s) - 1.0))) < 1e-12
+    s = oel.BlazedGrating(period, 2.0 * math.pi, math.pi / 2.0).apply(b).samples
+    for ix, iy in ((0, 0), (63, 17), (40, 5), (12, 63)):
+        u = y[iy, 0] / period
+        assert abs(_wrap(np.angle(s[iy, ix]) - 2.0 * math.pi * (u - math.floor(u)))) < 1e-9
+
+
+def test_element_wedge_convention_and_rotated_ellipse():
+    """element.rs wedge_ramp_piston_and_deflection_convention (centre phase
+    pi/3 + k (n - 1) t0, 10 samples to the right k (n - 1) tan(alpha) 0.01
+    lower, 1e-9), rotated_ellipse_aperture (45 deg: (85, 85) passes, (100, 50)
+    blocked; a rotated circle equals the plain one exactly)."""
+    from oracle import element as oel
+    band = ofield.uniform(1.0, math.pi / 3.0, 101, 101, 1e-3, 1e-3, LAMBDA)
+    alpha, t0 = 1e-3, 1e-3
+    w = oel.Wedge(alpha, 1.5, t0, 0.0, oel.ClearAperture.circle(20e-3))
+    out = w.apply(band).samples
+    k = 2.0 * math.pi / LAMBDA
+    centre = np.angle(out[50, 50])
+    assert abs(_wrap(centre - (math.pi / 3.0 + k * 0.5 * t0))) < 1e-9
+    assert abs(_wrap(np.angle(out[50, 60]) - (centre - k * 0.5 * math.tan(alpha) * 0.01))) < 1e-9
+    ap = oel.EllipticalAperture((50e-3, 20e-3), math.pi / 4.0)
+    o = ap.apply(band).samples
+    assert o[85, 85] == band.samples[50, 50] and o[50, 100] == 0.0
+    circ = oel.EllipticalAperture((31.7e-3, 31.7e-3), math.pi / 2.0).apply(band).samples
+    plain = oel.EllipticalAperture.circle(31.7e-3).apply(band).samples
+    np.testing.assert_array_equal(circ, plain)
+
+
+def test_element_sag_matches_standard_surface():
+    """element.rs sag_matches_zemax_standard_surface: sphere (1e-12 relative),
+    paraboloid r^2 / 2R (1e-15), even asphere with 2e9 r^4 - 3e13 r^6 (1e-15)."""
+    from oracle import element as oel
+    r = 3.0e-3
+    geo = 5e-3 - math.sqrt(5e-3 ** 2 - r * r)
+    assert abs(oel.conic_sag(r, 5e-3, 0.0) - geo) / geo < 1e-12
+    for r in (1e-3, 7e-3, 30e-3):
+        assert abs(oel.conic_sag(r, 0.1, -1.0) - r * r / 0.2) < 1e-15
+    r, c = 4e-3, 10.0
+    want = c * r * r / (1.0 + math.sqrt(1.0 - c * c * r * r)) + 2.0e9 * r ** 4 - 3.0e13 * r ** 6
+    assert abs(oel.conic_sag(r, 0.1, 0.0, (2.0e9, -3.0e13)) - want) < 1e-15
