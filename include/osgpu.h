@@ -642,6 +642,12 @@ int osgpu_plan_cache_stats(osgpu_plan_stats* out);
 
 /* ---------------------------------------------------------------- runtime */
 int osgpu_init(int32_t device);
+/* Waits for all queued work and releases the library's cached device memory
+ * (kernel-spectrum plans, the encircled-energy order, the pooled scratch).
+ * Streams, twiddle tables, lattices, field handles and captured graphs stay
+ * valid; later calls rebuild what they need (the plan-cache setting is
+ * kept). */
+int osgpu_shutdown(void);
 /* Copies the last error message (NUL-terminated, truncated to len). */
 int osgpu_last_error(char* buf, size_t len);
 /* Waits for the library stream; returns a pending device-side status

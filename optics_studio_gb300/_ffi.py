@@ -164,6 +164,7 @@ class PlanStatsC(C.Structure):
 # (name, restype, argtypes) for every symbol of include/osgpu.h
 SIGNATURES = [
     ("osgpu_init", C.c_int, [C.c_int32]),
+    ("osgpu_shutdown", C.c_int, []),
     ("osgpu_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
     ("osgpu_sync_status", C.c_int, []),
     ("osgpu_version", C.c_char_p, []),

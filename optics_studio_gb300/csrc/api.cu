@@ -1434,6 +1434,25 @@ int osgpu_field_destroy(osgpu_field f) {
   return e == cudaSuccess ? OSGPU_OK : cuda_fail(e, "field handle free");
 }
 
+int osgpu_shutdown(void) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  if (c.device < 0) return OSGPU_OK;  // nothing was initialised
+  CK(cudaDeviceSynchronize());  // no queued work reads what is freed below
+  // twiddle tables stay: captured graphs (osgpu_beamline_trace_batch_graph)
+  // hold their addresses; plans and the encircled-energy order are never
+  // used under capture
+  for (KPlan& p : c.plans) cudaFree(p.kq);
+  c.plans.clear();
+  c.plan_bytes = 0;
+  if (c.ee.d) cudaFree(c.ee.d);
+  c.ee = Context::EeOrder();
+  cudaMemPool_t pool;
+  CK(cudaDeviceGetDefaultMemPool(&pool, c.device));
+  CK(cudaMemPoolTrimTo(pool, 0));  // scratch returned by the stream-ordered frees
+  return OSGPU_OK;
+}
+
 int osgpu_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return OSGPU_E_BAD_ARGUMENT;
   std::snprintf(buf, len, "%s", t_err);

@@ -290,6 +290,7 @@ def test_field_handles_validate_without_device():
     assert L.osgpu_field_download(None, None, None) == 102
     assert L.osgpu_field_info(None, None, None, None, None) == 102
     assert L.osgpu_field_destroy(None) == 0
+    assert L.osgpu_shutdown() == 0  # nothing initialised: a no-op
     try:
         import torch
         has_gpu = torch.cuda.is_available()
