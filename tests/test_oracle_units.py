@@ -1,13 +1,14 @@
-"""The reference's unit tests of the Fresnel, Fraunhofer and Rayleigh-Sommerfeld
-engines, the ASM Airy test, element tests (lens, ramp, blaze, wedge, rotated
-stop, sag), the element-transmission probe, the Gerchberg-Saxton convention
-pins and golden tests and the renderer tests, restated against the oracle
-(CPU; pins the oracle to the reference's known answers).
+"""The reference's unit and golden tests restated against the oracle (CPU;
+pins the oracle to the reference's known answers): the Fresnel, Fraunhofer
+and Rayleigh-Sommerfeld engine tests, the ASM Airy test, element tests
+(lens, ramp, blaze, wedge, rotated stop, sag), the Gaussian source tests,
+the element-transmission probe, the Gerchberg-Saxton convention pins and
+golden tests, and the renderer tests.
 
 Each test cites the test it restates (src/propagation/fresnel.rs,
-fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, tests/asm.rs, or
-crates/optics-inverse/src/adjoint.rs, gs.rs, observe.rs) and keeps its
-geometry and tolerance.
+fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, src/sources.rs,
+tests/asm.rs, or crates/optics-inverse/src/adjoint.rs, gs.rs, observe.rs)
+and keeps its geometry and tolerance.
 """
 
 import math
@@ -685,3 +686,54 @@ def test_element_sag_matches_standard_surface():
     r, c = 4e-3, 10.0
     want = c * r * r / (1.0 + math.sqrt(1.0 - c * c * r * r)) + 2.0e9 * r ** 4 - 3.0e13 * r ** 6
     assert abs(oel.conic_sag(r, 0.1, 0.0, (2.0e9, -3.0e13)) - want) < 1e-15
+
+
+# ---- src/sources.rs ---------------------------------------------------------------
+
+def test_gaussian_source_pins():
+    """sources.rs waist_plane_is_real_gaussian_with_analytic_power (real,
+    exp(-r^2 / w0^2) to 1e-12, power pi w0^2 / 2 to 1e-3),
+    on_axis_amplitude_and_gouy_match_q_form (1e-12, phase 1e-9),
+    negative_z_is_complex_conjugate (1e-12),
+    off_center_waist_translates_by_integer_samples (1e-15),
+    analytic_beam_matches_own_engines (ASM and Fresnel TF within 1e-3)."""
+    g = ofield.gaussian
+    w0 = 1e-3
+    d = w0 / 20.0
+    b = g(w0, 1.0, (0.0, 0.0), 0.0, LAMBDA, 201, 201, d, d)
+    x, y = (np.arange(201) - 100.0) * d, (np.arange(201) - 100.0) * d
+    for ix, iy in ((0, 0), (100, 100), (200, 200), (37, 160)):
+        s = b.samples[iy, ix]
+        assert abs(s.imag) < 1e-15
+        assert abs(s.real - math.exp(-(x[ix] ** 2 + y[iy] ** 2) / (w0 * w0))) < 1e-12
+    p = float(np.sum(np.abs(b.samples) ** 2)) * d * d
+    assert abs(p - math.pi * w0 * w0 / 2.0) / (math.pi * w0 * w0 / 2.0) < 1e-3
+
+    w0, z, n = 0.5e-3, 0.25, 129
+    d = w0 / 20.0
+    c = g(w0, 2.0, (0.0, 0.0), z, LAMBDA, n, n, d, d).samples[n // 2, n // 2]
+    z_r = math.pi * w0 * w0 / LAMBDA
+    w_z = w0 * math.sqrt(1.0 + (z / z_r) ** 2)
+    assert abs(abs(c) - 2.0 * w0 / w_z) / (2.0 * w0 / w_z) < 1e-12
+    ph = 2.0 * math.pi * z / LAMBDA - math.atan(z / z_r)
+    assert abs((np.angle(c) - ph + math.pi) % (2.0 * math.pi) - math.pi) < 1e-9
+
+    pos = g(0.5e-3, 1.0, (0.0, 0.0), 0.2, LAMBDA, 64, 64, 1e-5, 1e-5).samples
+    neg = g(0.5e-3, 1.0, (0.0, 0.0), -0.2, LAMBDA, 64, 64, 1e-5, 1e-5).samples
+    assert float(np.max(np.abs(np.conj(pos) - neg))) < 1e-12
+
+    w0, n = 1e-3, 161
+    d = w0 / 20.0
+    on = g(w0, 1.0, (0.0, 0.0), 0.0, LAMBDA, n, n, d, d).samples
+    sh = g(w0, 1.0, (3.0 * d, -2.0 * d), 0.0, LAMBDA, n, n, d, d).samples
+    # shifted(ix, iy) = on_axis(ix - 3, iy + 2) over the interior
+    assert float(np.max(np.abs(sh[5:n - 5, 5:n - 5] - on[7:n - 3, 2:n - 8]))) < 1e-15
+
+    from oracle import asm as oasm
+    w0, z, n, d = 0.15e-3, 0.1, 255, 1e-5
+    analytic = g(w0, 1.0, (0.0, 0.0), z, LAMBDA, n, n, d, d).samples
+    waist = g(w0, 1.0, (0.0, 0.0), 0.0, LAMBDA, n, n, d, d)
+    fr = ofr.propagate(waist, z, ofr.FresnelConfig(2.0, False, 8.0)).samples
+    asm = oasm.propagate(waist, z).samples
+    assert np.linalg.norm(fr - analytic) / np.linalg.norm(analytic) < 1e-3
+    assert np.linalg.norm(asm - analytic) / np.linalg.norm(analytic) < 1e-3
