@@ -620,6 +620,64 @@ def field_power(u):
 
 
 @dataclass
+class Param:
+    """params.rs:30-105: one bounded design slot with an optional
+    finite-difference step."""
+    name: str
+    lo: float
+    hi: float
+    value: float = 0.0
+    fd_step: float = None
+
+    def step(self):
+        """params.rs:62-71: the explicit step, else 1e-4 of the span (1e-9 for a
+        point bound)."""
+        if self.fd_step is not None:
+            return self.fd_step
+        rel = (self.hi - self.lo) * 1.0e-4
+        return rel if rel > 0.0 else 1.0e-9
+
+    def check(self, v):
+        """params.rs:79-104 on the value v."""
+        if not (math.isfinite(self.lo) and math.isfinite(self.hi)) or not math.isfinite(v):
+            raise _ffi.OsgpuError(41)  # NotFinite
+        if v < self.lo or v > self.hi:
+            raise _ffi.OsgpuError(42)  # OutOfBounds
+
+
+def fd_gradient(params, objective, x):
+    """fd.rs:139-179: central-difference gradient of ``objective(values) ->
+    float`` (typically a render plus a merit) at ``x``.  Probes are clamped
+    into the bounds, so a slot at a bound gets the one-sided slope over the
+    effective separation; zero-width slots are skipped (gradient 0).  Returns
+    (gradient list, objective evaluations)."""
+    if len(x) != len(params):
+        raise _ffi.OsgpuError(40)  # WrongDimension
+    for p, v in zip(params, x):
+        p.check(v)
+    g = [0.0] * len(params)
+    evaluations = 0
+    for i, p in enumerate(params):
+        if p.lo == p.hi:
+            continue
+        s = p.step()
+        up, dn = list(x), list(x)
+        up[i] = min(max(x[i] + s, p.lo), p.hi)
+        dn[i] = min(max(x[i] - s, p.lo), p.hi)
+        fu = objective(up)
+        fd = objective(dn)
+        evaluations += 2
+        d = up[i] - dn[i]
+        if not d > 0.0:
+            raise _ffi.OsgpuError(43)  # the step collapses to zero separation
+        gi = (fu - fd) / d
+        if not math.isfinite(gi):
+            raise _ffi.OsgpuError(43)
+        g[i] = gi
+    return g, evaluations
+
+
+@dataclass
 class AdamConfig:
     """fd.rs:63-91 (defaults as the reference)."""
     lr_frac: float = 0.02

@@ -299,3 +299,30 @@ def test_field_handles_validate_without_device():
     if not has_gpu:
         assert L.osgpu_field_create(4, 4, 0, ctypes.byref(h)) == 103
         assert h.value is None
+
+
+def test_fd_gradient_matches_reference_unit_tests():
+    """fd.rs fd_gradient_matches_closed_form (1e-6), fd_gradient_uses_params_steps_and_clamps_probes
+    (1.75 exactly), zero_width_slot_is_ignored, gradient_rejects_bad_inputs."""
+    pytest.importorskip("torch")
+    from optics_studio_gb300 import inverse as inv
+    unit = [inv.Param(f"x{i}", -1.0, 1.0) for i in range(3)]
+    t = [0.3, -0.2, 0.5]
+    bowl = lambda v: sum((a - b) ** 2 for a, b in zip(v, t)) + v[0] * v[1]
+    x = [0.1, 0.05, -0.4]
+    g, ev = inv.fd_gradient(unit, bowl, x)
+    want = [2 * (a - b) for a, b in zip(x, t)]
+    want[0] += x[1]
+    want[1] += x[0]
+    assert ev == 6
+    assert all(abs(a - b) < 1e-6 * (1 + abs(b)) for a, b in zip(g, want))
+    g, ev = inv.fd_gradient([inv.Param("x", 0.0, 1.0, 1.0, 0.25)], lambda v: v[0] * v[0], [1.0])
+    assert ev == 2 and abs(g[0] - 1.75) < 1e-12
+    g, ev = inv.fd_gradient([inv.Param("k", 2.0, 2.0, 2.0), inv.Param("x", 0.0, 1.0, 0.5)],
+                            lambda v: v[0] + v[1] * v[1], [2.0, 0.5])
+    assert ev == 2 and g[0] == 0.0 and abs(g[1] - 1.0) < 1e-9
+    two = unit[:2]
+    for bad, code in (([0.0], 40), ([math.nan, 0.0], 41), ([0.0, 2.0], 42)):
+        with pytest.raises(og.OsgpuError) as e:
+            inv.fd_gradient(two, lambda v: 1.0, bad)
+        assert e.value.code == code
