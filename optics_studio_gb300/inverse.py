@@ -23,7 +23,7 @@ device memory and streams.  Arrays are real float64 for ``precision="f64"``
 
 import ctypes as C
 import math
-from dataclasses import dataclass, field, replace
+from dataclasses import dataclass, field
 from typing import Callable, List
 
 from . import _ffi

@@ -12,7 +12,6 @@ from dataclasses import dataclass, replace
 import numpy as np
 
 from .fft import fft2, ifft2, fftfreq, padded_len, embed_centered, crop_centered
-from .field import BandField
 
 PI = math.pi
 

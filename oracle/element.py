@@ -12,7 +12,7 @@ wrapping (``src/common.rs:25-40``).
 
 import math
 from dataclasses import dataclass
-from typing import Callable, Optional
+from typing import Callable
 
 import numpy as np
 

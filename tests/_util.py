@@ -2,7 +2,6 @@
 
 import numpy as np
 
-import optics_studio_gb300 as og
 from optics_studio_gb300.field import BandField
 
 

@@ -19,7 +19,6 @@ from oracle import field as o_field, merit as o_merit, observe as o_obs, adam as
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
-import optics_studio_gb300 as og  # noqa: E402
 from optics_studio_gb300 import inverse as inv, element as el  # noqa: E402
 from optics_studio_gb300.propagation.asm import AsmConfig  # noqa: E402
 

@@ -2,7 +2,6 @@
 restatement of src/analysis.rs (oracle/analysis.py): FP64 grids to 1e-12
 relative (MTF values to 1e-12 of the DC term), float32 grids to 1e-6."""
 
-import math
 
 import numpy as np
 import pytest
