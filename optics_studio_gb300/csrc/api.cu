@@ -1350,7 +1350,8 @@ int osgpu_field_create(uint64_t nx, uint64_t ny, int32_t dtype, osgpu_field* out
   if (!out) return OSGPU_E_BAD_ARGUMENT;
   *out = nullptr;
   if (nx == 0 || ny == 0 || (dtype != OSGPU_C128 && dtype != OSGPU_C64) ||
-      nx > (uint64_t)INT32_MAX || ny > (uint64_t)INT32_MAX) {
+      nx > (uint64_t)INT32_MAX || ny > (uint64_t)INT32_MAX ||
+      nx * ny > ((uint64_t)1 << 40)) {  // 16 TiB of complex128: beyond any device
     set_err("field handle: bad shape or dtype");
     return OSGPU_E_BAD_ARGUMENT;
   }
