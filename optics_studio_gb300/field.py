@@ -41,10 +41,46 @@ class BandField:
         return BandField(s, self.dx if dx is None else dx, self.dy if dy is None else dy, self.lam)
 
     def intensities(self):
-        return np.abs(self.samples) ** 2
+        """|u|^2 as re^2 + im^2 (Complex64::norm_sqr, field.rs)."""
+        return self.samples.real ** 2 + self.samples.imag ** 2
 
     def power(self):
         return float(np.sum(self.intensities()) * self.dx * self.dy)
+
+
+class Psf:
+    """A real intensity grid with its pitch (field.rs:404-420): ``samples`` is
+    (ny, nx) float64."""
+
+    def __init__(self, samples, dx, dy):
+        self.samples = np.ascontiguousarray(samples, dtype=np.float64)
+        self.dx = float(dx)
+        self.dy = float(dy)
+
+    def total_power(self):
+        """field.rs:499-501: sum I dx dy."""
+        return float(np.sum(self.samples)) * self.dx * self.dy
+
+
+def sum_intensity(bands):
+    """field.rs:554-578: the incoherent sum of the bands' intensities on their
+    shared grid (the results of host-buffer propagations, already on the
+    host).  Raises ValueError("EmptyGrid") for no band,
+    ValueError("GeometryMismatch") for differing dims or pitch and
+    ValueError("NonFiniteSample") for a non-finite sum."""
+    if not bands:
+        raise ValueError("EmptyGrid")
+    first = bands[0]
+    geom = (first.nx, first.ny, first.dx, first.dy)
+    for b in bands[1:]:
+        if (b.nx, b.ny, b.dx, b.dy) != geom:
+            raise ValueError("GeometryMismatch")
+    acc = first.intensities().copy()
+    for b in bands[1:]:
+        acc += b.intensities()
+    if not np.all(np.isfinite(acc)):
+        raise ValueError("NonFiniteSample")
+    return Psf(acc, first.dx, first.dy)
 
 
 def ptr(a):

@@ -109,3 +109,28 @@ def test_oracle_trace_matches_manual_chain_and_slab_piston():
     with pytest.raises(Exception) as e:
         bl.trace(band(), lambda x, z, m: x)
     assert "OutsideField" in str(e.value) or getattr(e.value, "variant", "") == "OutsideField"
+
+
+def test_sum_intensity_matches_reference_tests():
+    """field.rs sum_intensity_adds_powers_without_cross_terms (|1|^2 + |2|^2 = 5
+    per sample, powers add, phases do not matter) and sum_intensity_validation."""
+    from optics_studio_gb300.field import BandField, sum_intensity
+
+    def band_at(a, phase, lam, d=1e-3):
+        return BandField(np.full((4, 4), a * np.exp(1j * phase)), d, d, lam)
+
+    red, blue = band_at(1.0, 0.0, 650e-9), band_at(2.0, math.pi / 3.0, 450e-9)
+    s = sum_intensity([red, blue])
+    assert float(np.max(np.abs(s.samples - 5.0))) < 1e-15
+    assert abs(s.total_power() - (red.power() + blue.power())) < 1e-15
+    np.testing.assert_array_equal(s.samples,
+                                  sum_intensity([red, band_at(2.0, -1.2, 450e-9)]).samples)
+    assert abs(sum_intensity([red, red]).total_power() - 2.0 * red.power()) < 1e-15
+    with pytest.raises(ValueError, match="EmptyGrid"):
+        sum_intensity([])
+    with pytest.raises(ValueError, match="GeometryMismatch"):
+        sum_intensity([red, band_at(1.0, 0.0, 650e-9, 2e-3)])
+    bad = band_at(1.0, 0.0, 650e-9)
+    bad.samples[1, 1] = complex(math.nan, 0.0)
+    with pytest.raises(ValueError, match="NonFiniteSample"):
+        sum_intensity([bad])
