@@ -1,14 +1,15 @@
 """The reference's unit and golden tests restated against the oracle (CPU;
 pins the oracle to the reference's known answers): the Fresnel, Fraunhofer
 and Rayleigh-Sommerfeld engine tests, the ASM Airy test, element tests
-(lens, ramp, blaze, wedge, rotated stop, sag), the Gaussian source tests,
-the element-transmission probe, the Gerchberg-Saxton convention pins and
-golden tests, and the renderer tests.
+(lens, ramp, blaze, wedge, rotated stop, sag), the Gaussian source and
+field tests, the element-transmission probe, the Gerchberg-Saxton convention
+pins and golden tests, and the renderer tests.  The field test also checks
+the product's host-side BandField validation.
 
 Each test cites the test it restates (src/propagation/fresnel.rs,
 fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, src/sources.rs,
-tests/asm.rs, or crates/optics-inverse/src/adjoint.rs, gs.rs, observe.rs)
-and keeps its geometry and tolerance.
+src/field.rs, tests/asm.rs, or crates/optics-inverse/src/adjoint.rs, gs.rs,
+observe.rs) and keeps its geometry and tolerance.
 """
 
 import math
@@ -737,3 +738,34 @@ def test_gaussian_source_pins():
     asm = oasm.propagate(waist, z).samples
     assert np.linalg.norm(fr - analytic) / np.linalg.norm(analytic) < 1e-3
     assert np.linalg.norm(asm - analytic) / np.linalg.norm(analytic) < 1e-3
+
+
+# ---- src/field.rs -----------------------------------------------------------------
+
+def test_field_pins():
+    """field.rs plane_wave_phase_ramp_matches_direction_cosines (1e-9, a flat wave
+    exactly A), coordinates_are_centered_on_origin (exact), uniform_field_power
+    (1e-6; amplitude, phase, intensity 1e-12), band_field_validates_wavelength;
+    the product's BandField rejects the same wavelengths."""
+    from optics_studio_gb300.field import BandField
+    lam = 500e-9
+    b = ofield.plane_wave(0.05, 0.0, 1.0, 16, 16, 10e-6, 10e-6, lam).samples
+    step = np.exp(1j * 2.0 * math.pi / lam * math.sin(0.05) * 10e-6)
+    for iy in (0, 7, 15):
+        assert abs(b[iy, 8] / b[iy, 7] - step) < 1e-9
+    flat = ofield.plane_wave(0.0, 0.0, 3.0, 16, 16, 10e-6, 10e-6, lam).samples
+    assert np.all(flat == 3.0 + 0.0j)
+    x = (np.arange(5) - 2.0) * 1e-3
+    y = (np.arange(3) - 1.0) * 1e-3
+    assert (x[2], y[1]) == (0.0, 0.0) and (x[0], y[0]) == (-2e-3, -1e-3)
+    assert (x[4], y[2]) == (2e-3, 1e-3)
+    u = ofield.uniform(2.0, math.pi / 3.0, 8, 4, 1e-3, 5e-4, lam)
+    want = 4.0 * 8 * 4 * 1e-3 * 5e-4
+    assert abs(power(u) - want) < 1e-6 * want
+    assert float(np.max(np.abs(np.abs(u.samples) - 2.0))) < 1e-12
+    assert float(np.max(np.abs(np.angle(u.samples) - math.pi / 3.0))) < 1e-12
+    for lam_bad in (0.0, math.nan, -1.0):
+        with pytest.raises(Exception):
+            ofield.uniform(1.0, 0.0, 2, 2, 1e-3, 1e-3, lam_bad)
+        with pytest.raises(ValueError):
+            BandField(np.zeros((2, 2), complex), 1e-3, 1e-3, lam_bad)
