@@ -3,8 +3,9 @@ pins the oracle to the reference's known answers): the Fresnel, Fraunhofer
 and Rayleigh-Sommerfeld engine tests, the ASM Airy test, element tests
 (lens, ramp, blaze, wedge, rotated stop, sag), the Gaussian source and
 field tests, the element-transmission probe, the Gerchberg-Saxton convention
-pins and golden tests, and the renderer tests.  The field test also checks
-the product's host-side BandField validation.
+pins and golden tests, and the renderer tests.  The field and ASM-analysis
+tests also check the product's host side (BandField validation, the C
+library's padded sizes, band limits and phase steps).
 
 Each test cites the test it restates (src/propagation/fresnel.rs,
 fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, src/sources.rs,
@@ -769,3 +770,54 @@ def test_field_pins():
             ofield.uniform(1.0, 0.0, 2, 2, 1e-3, 1e-3, lam_bad)
         with pytest.raises(ValueError):
             BandField(np.zeros((2, 2), complex), 1e-3, 1e-3, lam_bad)
+
+
+# ---- src/propagation/asm.rs (host analysis: oracle and product) -------------------
+
+def _product_asm_report(n, d, z, cfg):
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import _ffi
+    rep = _ffi.AsmReportC()
+    assert og.lib().osgpu_asm_sampling_report(_ffi.Grid(n, n, d, d, LAMBDA), z, cfg.c(), rep) == 0
+    return rep
+
+
+def test_asm_padding_band_limit_and_medium_pins():
+    """asm.rs padding_rounds_up_and_clamps, band_limit_uses_padded_width_and_shrinks_with_z,
+    medium_scales_band_limit_and_guard, medium_round_trip_inverts (1e-9),
+    invalid_inputs_rejected; the product's host analysis gives the same padded
+    sizes, band limits and steps as the oracle."""
+    from oracle import asm as oasm
+    from oracle.fft import padded_len
+    from optics_studio_gb300.propagation import asm as gasm
+    for pad, want in ((2.0, 200), (1.5, 150), (1.0, 100), (0.5, 100)):
+        assert padded_len(100, pad) == want
+        rep = _product_asm_report(100, 10e-6, 1e-3, gasm.AsmConfig(pad, True, False, 8.0, 1.0))
+        assert rep.nx_pad == want
+    lp = 200.0 * 10e-6
+    f0 = oasm.axis_band_limit(LAMBDA, 0.0, lp, True, 1.0)
+    assert abs(f0 - 1.0 / LAMBDA) < 1e-6
+    assert oasm.axis_band_limit(LAMBDA, 0.05, lp, True, 1.0) < f0
+    assert abs(oasm.axis_band_limit(LAMBDA, 1.0, lp, False, 1.0) - 1.0 / LAMBDA) < 1e-9
+    rep = _product_asm_report(100, 10e-6, 0.05, gasm.AsmConfig(2.0, True, False, 8.0, 1.0))
+    assert rep.band_limit_fx == oasm.axis_band_limit(LAMBDA, 0.05, lp, True, 1.0)
+
+    b = uniform(1.0, 32, 1e-6)
+    base = oasm.AsmConfig(2.0, False, False, 8.0, 1.0)
+    dense = oasm.AsmConfig(2.0, False, False, 8.0, 1.5)
+    r1, r2 = oasm.sampling_report(b, 0.5, base), oasm.sampling_report(b, 0.5, dense)
+    assert abs(r2.band_limit_fx - 1.5 * r1.band_limit_fx) < 1e-9
+    assert 0.55 < r2.max_phase_step_x / r1.max_phase_step_x < 1.0 and r2.medium == 1.5
+    p1 = _product_asm_report(32, 1e-6, 0.5, gasm.AsmConfig(2.0, False, False, 8.0, 1.0))
+    p2 = _product_asm_report(32, 1e-6, 0.5, gasm.AsmConfig(2.0, False, False, 8.0, 1.5))
+    assert (p1.band_limit_fx, p1.max_phase_step_x) == (r1.band_limit_fx, r1.max_phase_step_x)
+    assert (p2.band_limit_fx, p2.max_phase_step_x, p2.medium) == (
+        r2.band_limit_fx, r2.max_phase_step_x, 1.5)
+
+    b = uniform(1.0, 16, 20e-6)
+    cfg = oasm.AsmConfig(padding=1.0, medium=2.0)
+    rt = oasm.propagate(oasm.propagate(b, 1e-3, cfg), -1e-3, cfg)
+    assert float(np.max(np.abs(rt.samples - b.samples))) < 1e-9
+    with pytest.raises(oasm.PropagationError) as e:
+        oasm.propagate(uniform(1.0, 8, 20e-6), math.nan)
+    assert e.value.variant == "InvalidDistance"
