@@ -821,3 +821,27 @@ def test_asm_padding_band_limit_and_medium_pins():
     with pytest.raises(oasm.PropagationError) as e:
         oasm.propagate(uniform(1.0, 8, 20e-6), math.nan)
     assert e.value.variant == "InvalidDistance"
+
+
+def test_fraunhofer_regime_extent_is_measured_from_the_axis():
+    """fraunhofer.rs regime_extent_is_measured_from_the_axis: with max N_F 0.15
+    the centred Gaussian passes (N_F 0.099); declared 0.2 mm off axis it fails
+    (0.265), reports the position and the strict propagation refuses; the
+    product's host regime report agrees."""
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import _ffi
+    from optics_studio_gb300.propagation import fraunhofer as gfh
+    b = gaussian(64, 1e-5, 5e-5)
+    assert ofh.regime_report(b, 2.0, ofh.FraunhoferConfig(max_n_f=0.15)).regime_ok
+    off = ofh.FraunhoferConfig(max_n_f=0.15, source_pos=(2e-4, 0.0))
+    rep = ofh.regime_report(b, 2.0, off)
+    assert not rep.regime_ok and tuple(rep.source_pos) == (2e-4, 0.0)
+    with pytest.raises(ofh.FraunhoferError) as e:
+        ofh.propagate(b, 2.0, off)
+    assert e.value.variant == "RegimeViolation"
+    for cfg, ok in ((gfh.FraunhoferConfig(max_n_f=0.15), True),
+                    (gfh.FraunhoferConfig(max_n_f=0.15, source_pos=(2e-4, 0.0)), False)):
+        r = _ffi.FraunhoferReportC()
+        og.lib().osgpu_fraunhofer_regime_report(_ffi.Grid(64, 64, 1e-5, 1e-5, LAMBDA), 2.0,
+                                                cfg.c(), r)
+        assert bool(r.regime_ok) == ok
