@@ -3,14 +3,15 @@ pins the oracle to the reference's known answers): the Fresnel, Fraunhofer
 and Rayleigh-Sommerfeld engine tests, the ASM Airy test, element tests
 (lens, ramp, blaze, wedge, rotated stop, sag), the Gaussian source and
 field tests, the element-transmission probe, the Gerchberg-Saxton convention
-pins and golden tests, and the renderer tests.  The field and ASM-analysis
+pins and golden tests, the carrier tests and the renderer tests.  The field
+and ASM-analysis
 tests also check the product's host side (BandField validation, the C
 library's padded sizes, band limits and phase steps).
 
 Each test cites the test it restates (src/propagation/fresnel.rs,
 fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, src/sources.rs,
-src/field.rs, tests/asm.rs, or crates/optics-inverse/src/adjoint.rs, gs.rs,
-observe.rs) and keeps its geometry and tolerance.
+src/field.rs, tests/asm.rs, or crates/optics-inverse/src/adjoint.rs,
+carrier.rs, gs.rs, observe.rs) and keeps its geometry and tolerance.
 """
 
 import math
@@ -845,3 +846,40 @@ def test_fraunhofer_regime_extent_is_measured_from_the_axis():
         og.lib().osgpu_fraunhofer_regime_report(_ffi.Grid(64, 64, 1e-5, 1e-5, LAMBDA), 2.0,
                                                 cfg.c(), r)
         assert bool(r.regime_ok) == ok
+
+
+# ---- crates/optics-inverse/src/carrier.rs -----------------------------------------
+
+def test_carrier_pins():
+    """carrier.rs grid_phase_roundtrip_matches_manual_mask (the built design
+    traced without propagation equals the sampled mask exactly),
+    grid_carriers_validate_before_building, analytic_rejects_bad_values_at_apply."""
+    from oracle import carrier as ocar, element as oel
+    values = np.arange(16, dtype=np.float64) * 0.2
+    car = ocar.Carrier.grid_phase((4, 4), (20e-6, 20e-6), oel.ClearAperture.field(), (0.0, 0.0),
+                                  0.0, math.pi)
+    assert car.dim == 16 and car.slot_bounds() == (0.0, math.pi)
+    b = ofield.uniform(1.0, 0.0, 32, 32, 20e-6, 20e-6, LAMBDA)
+    out = car.build(values, LAMBDA).beamline().trace(b, lambda x, z, m: x)
+    manual = oel.PhaseMask.sampled(values, (4, 4), (20e-6, 20e-6)).apply(b)
+    np.testing.assert_array_equal(out.samples, manual.samples)
+    g = ocar.Carrier.grid_phase((2, 2), (1e-5, 1e-5), oel.ClearAperture.field(), (0.0, 0.0),
+                                0.0, 1.0)
+    for vals, variant in (([0.5, 0.5, 0.5, 1.5], "OutOfBounds"), ([0.5] * 3, "WrongDimension")):
+        with pytest.raises(ocar.InverseError) as e:
+            g.build(np.array(vals), LAMBDA)
+        assert e.value.variant == variant
+    with pytest.raises(ocar.InverseError):
+        ocar.Carrier.grid_phase((0, 4), (1e-5, 1e-5), oel.ClearAperture.field(), (0.0, 0.0),
+                                0.0, 1.0)
+
+    def build(v, lam):
+        d = ocar.Design()
+        d.gap(v[0], 1.0)
+        return d
+    an = ocar.Carrier.analytic(1, 0.01, 1.0, build)
+    for vals, variant in (([5.0], "OutOfBounds"), ([math.nan], "NotFinite"),
+                          ([], "WrongDimension")):
+        with pytest.raises(ocar.InverseError) as e:
+            an.build(np.array(vals), LAMBDA)
+        assert e.value.variant == variant
