@@ -326,3 +326,23 @@ def test_fd_gradient_matches_reference_unit_tests():
         with pytest.raises(og.OsgpuError) as e:
             inv.fd_gradient(two, lambda v: 1.0, bad)
         assert e.value.code == code
+
+
+def test_gs_setup_validation_before_device_work():
+    """gs.rs run_rejects_invalid_setup (GsVariant::validate, gs.rs:165-178):
+    DVR beta outside (0, 2), FPR beta outside (0, 1] and zero iterations are
+    Render errors, an unknown variant or engine a bad argument - all decided
+    before any device call."""
+    L = og.lib()
+    items = (_ffi.GsItemC * 1)()
+    asm_c = gasm.AsmConfig().c()
+    fr_c = gfh.FraunhoferConfig().c()
+
+    def run(variant, beta, iters=10, engine=0):
+        cfg = _ffi.GsConfigC(iters, 10, 1e-4, variant, beta, -math.pi, math.pi, engine)
+        return L.osgpu_gs_run_batch_device(items, 1, cfg, asm_c, fr_c, 0, None)
+
+    assert run(1, 3.0) == 43 and run(1, 0.0) == 43 and run(1, math.nan) == 43
+    assert run(2, 0.0) == 43 and run(2, 1.5) == 43
+    assert run(0, 1.0, iters=0) == 43
+    assert run(7, 1.0) == 102 and run(0, 1.0, engine=5) == 102
