@@ -346,3 +346,24 @@ def test_gs_setup_validation_before_device_work():
     assert run(2, 0.0) == 43 and run(2, 1.5) == 43
     assert run(0, 1.0, iters=0) == 43
     assert run(7, 1.0) == 102 and run(0, 1.0, engine=5) == 102
+
+
+def test_adam_config_validation_before_device_work():
+    """fd.rs adam_config_validation_errors (AdamConfig::validate, fd.rs:95-121):
+    lr_frac 0 or NaN, beta1 = 1, beta2 < 0, infinite eps and a zero clip norm
+    are Render errors, decided before any device access (the device pointers
+    below are never dereferenced)."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("host-only check: its placeholder device pointers stay off a real device")
+    L = og.lib()
+    fake = ctypes.c_void_p(16)
+
+    def step(lr=0.02, b1=0.9, b2=0.999, eps=1e-8, clip_norm=1.0, clip=1):
+        cfg = _ffi.AdamConfigC(lr, b1, b2, eps, clip_norm, clip)
+        return L.osgpu_adam_step_device(fake, None, fake, 0, fake, fake, 4, ctypes.byref(cfg), 1,
+                                        -1.0, 1.0, None)
+
+    for kw in ({"lr": 0.0}, {"lr": math.nan}, {"b1": 1.0}, {"b2": -0.1}, {"eps": math.inf},
+               {"clip_norm": 0.0}):
+        assert step(**kw) == 43, kw
