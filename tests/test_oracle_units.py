@@ -882,3 +882,16 @@ def test_carrier_pins():
         with pytest.raises(ocar.InverseError) as e:
             an.build(np.array(vals), LAMBDA)
         assert e.value.variant == variant
+
+
+def test_fresnel_transfer_matches_asm_at_low_frequencies():
+    """fresnel.rs transfer_function_matches_asm_at_low_frequencies: at
+    (lambda f)^2 = s = 1e-4 the Fresnel transfer differs from the ASM one by
+    at most 2 k z s^2 / 8, and the DC bin is e^{ikz} (1e-12)."""
+    z, s = 0.1, 1e-4
+    k = 2.0 * math.pi / LAMBDA
+    f = math.sqrt(s) / LAMBDA
+    h = ofr.transfer_function(2, 1, 1.0 / (2.0 * f), 1.0, LAMBDA, z)  # bins 0 and -f
+    h_asm = np.exp(1j * k * z * math.sqrt(1.0 - s))
+    assert abs(h[0, 1] - h_asm) < 2.0 * k * z * s * s / 8.0 + 1e-12
+    assert abs(h[0, 0] - np.exp(1j * k * z)) < 1e-12
