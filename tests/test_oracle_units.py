@@ -933,3 +933,39 @@ def test_adjoint_gs_phase_error_is_negative_mse_gradient():
     assert corr > 0.9, corr
     ls = -float(np.sum(g * pred)) / float(np.sum(pred * pred))
     assert abs(ls / (2.0 / npx) - 1.0) < 0.25, ls
+
+
+def _disk_target(u_in, n, d, r, amp=None):
+    c = (np.arange(n, dtype=np.float64) - (n - 1.0) / 2.0) * d
+    disk = c[None, :] ** 2 + c[:, None] ** 2 <= r * r
+    if amp is None:
+        amp = math.sqrt(float(np.sum(np.abs(u_in) ** 2)) / float(np.sum(disk)))
+    return np.where(disk, amp, 0.0)
+
+
+def test_gs_dvr_and_fpr_variants():
+    """gs.rs dvr_variant_converges_on_tophat (DVR = phase relaxation beta 0.7:
+    best-so-far monotone, final merit below half the first) and
+    fpr_variant_stops_on_merit_seam (FPR = Fourier-plane relaxation beta 0.8
+    stops by the patience rule within 120 iterations).  Seeded uniform starts
+    stand in for rand's StdRng."""
+    from oracle import gs as ogs
+    n, d = 96, 8e-6
+    u = ofield.gaussian(140e-6, 1.0, (0.0, 0.0), 0.0, LAMBDA, n, n, d, d).samples
+    t = _disk_target(u, n, d, 220e-6)
+    fwd, back = _gs_asm(n, d, 8e-3)
+    init = np.random.default_rng(11).uniform(-math.pi, math.pi, (n, n))
+    sol = ogs.run(u, np.ones((n, n), bool), t, -math.pi, math.pi, init, fwd, back, _mse_merit(t),
+                  max_iterations=150, patience=10, merit_tolerance=1e-4, beta_p=0.7)
+    best = [r.best_merit for r in sol.history]
+    assert all(b1 <= b0 + 1e-15 for b0, b1 in zip(best, best[1:]))
+    assert sol.merit < 0.5 * sol.history[0].merit
+
+    n, d = 64, 10e-6
+    u = ofield.gaussian(120e-6, 1.0, (0.0, 0.0), 0.0, LAMBDA, n, n, d, d).samples
+    t = _disk_target(u, n, d, 180e-6, amp=1.0)
+    fwd, back = _gs_asm(n, d, 6e-3)
+    init = np.random.default_rng(3).uniform(-math.pi, math.pi, (n, n))
+    sol = ogs.run(u, np.ones((n, n), bool), t, -math.pi, math.pi, init, fwd, back, _mse_merit(t),
+                  max_iterations=120, patience=5, merit_tolerance=1e-3, beta_f=0.8)
+    assert sol.converged and sol.iterations <= 120
