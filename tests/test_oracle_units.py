@@ -3,13 +3,15 @@ pins the oracle to the reference's known answers): the Fresnel, Fraunhofer
 and Rayleigh-Sommerfeld engine tests, the ASM Airy test, element tests
 (lens, ramp, blaze, wedge, rotated stop, sag), the Gaussian source and
 field tests, the element-transmission probe, the Gerchberg-Saxton convention
-pins and golden tests, the carrier tests and the renderer tests.  The field
+pins and golden tests, the carrier tests, the renderer tests and the
+detector-metric safety test.  The field
 and ASM-analysis tests also check the product's host side (BandField
 validation, the C library's padded sizes, band limits and phase steps).
 
 Each test cites the test it restates (src/propagation/fresnel.rs,
 fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, src/sources.rs,
-src/field.rs, tests/asm.rs, or crates/optics-inverse/src/adjoint.rs,
+src/field.rs, src/analysis.rs, tests/asm.rs, or
+crates/optics-inverse/src/adjoint.rs,
 carrier.rs, gs.rs, observe.rs) and keeps its geometry and tolerance.
 """
 
@@ -969,3 +971,18 @@ def test_gs_dvr_and_fpr_variants():
     sol = ogs.run(u, np.ones((n, n), bool), t, -math.pi, math.pi, init, fwd, back, _mse_merit(t),
                   max_iterations=120, patience=5, merit_tolerance=1e-3, beta_f=0.8)
     assert sol.converged and sol.iterations <= 120
+
+
+# ---- src/analysis.rs --------------------------------------------------------------
+
+def test_analysis_mtf_dc_and_zero_field_safety():
+    """analysis.rs mtf_dc_and_zero_field_safety: a flat PSF's MTF vanishes off
+    DC (1e-9); a dark PSF has spot RMS 0, Strehl 0 and an encircled energy of
+    0 everywhere."""
+    from oracle import analysis as oan
+    flat, zero = np.ones((8, 8)), np.zeros((8, 8))
+    _, vals = oan.mtf(flat, (1e-3, 1e-3))
+    assert max(vals[1:]) < 1e-9
+    assert oan.spot_rms_radius(zero, (1e-3, 1e-3)) == 0.0
+    assert oan.strehl(zero, (1e-3, 1e-3), flat, (1e-3, 1e-3)) == 0.0
+    assert oan.encircled_energy(zero, (1e-3, 1e-3)).value_at(1.0) == 0.0
