@@ -4,15 +4,15 @@ and Rayleigh-Sommerfeld engine tests, the ASM Airy test, element tests
 (lens, ramp, blaze, wedge, rotated stop, sag), the Gaussian source and
 field tests, the element-transmission probe, the Gerchberg-Saxton convention
 pins and golden tests, the carrier tests, the renderer tests and the
-detector-metric safety test.  The field
-and ASM-analysis tests also check the product's host side (BandField
-validation, the C library's padded sizes, band limits and phase steps).
+detector-metric safety test.  The field and ASM-analysis tests also check
+the product's host side (BandField validation, the C library's padded
+sizes, band limits and phase steps).
 
 Each test cites the test it restates (src/propagation/fresnel.rs,
 fraunhofer.rs, rayleigh_sommerfeld.rs, src/element.rs, src/sources.rs,
 src/field.rs, src/analysis.rs, tests/asm.rs, or
-crates/optics-inverse/src/adjoint.rs,
-carrier.rs, gs.rs, observe.rs) and keeps its geometry and tolerance.
+crates/optics-inverse/src/adjoint.rs, carrier.rs, gs.rs, observe.rs) and
+keeps its geometry and tolerance.
 """
 
 import math
