@@ -436,6 +436,16 @@ int osgpu_merit_spot_efficiency_device(const void* d_obs, int32_t real_dtype, in
                                        uint64_t frame_len, const uint8_t* d_windows,
                                        const double* p_in, void* d_seed, void* stream,
                                        double* value);
+/* Weighted spot-array efficiency (no reference counterpart: the merit of the
+ * inverse-design workload with a Gaussian spot-array target):
+ * M = -sum_f sum_k w[k] I_f[k] / p_in[f], with d_weights a device array of
+ * frame_len real weights in the observation's real dtype (e.g. a sum of
+ * Gaussian spots of peak 1) and p_in the positive input power of each frame.
+ * The seed is dM/dI_f[k] = -w[k] / p_in[f]. */
+int osgpu_merit_weighted_efficiency_device(const void* d_obs, int32_t real_dtype,
+                                           int32_t n_frames, uint64_t frame_len,
+                                           const void* d_weights, const double* p_in,
+                                           void* d_seed, void* stream, double* value);
 /* MseToTarget (merit.rs:112-164); band/scene -1 selects all (Selector). */
 int osgpu_merit_mse_device(const void* d_obs, int32_t real_dtype, int32_t n_bands,
                            int32_t n_scenes, uint64_t frame_len, const double* d_target,
@@ -551,19 +561,22 @@ int osgpu_gs_run_batch_device(osgpu_gs_item* items, int32_t n_items, const osgpu
 /* ------------------------------------------------------- allocation-free */
 /* ASM propagation that allocates no device memory, on any call.  No
  * counterpart in the reference: it exists for callers that must not have a
- * library allocate, such as code running during CUDA graph capture,
- * applications whose device memory is owned by another allocator, and
- * latency-critical loops that cannot absorb cudaMalloc's synchronisation.
+ * library allocate, such as applications whose device memory is owned by
+ * another allocator that reserved it up front, latency-critical loops that
+ * cannot absorb cudaMalloc's synchronisation, and plugins hosted by a
+ * process that forbids a library from allocating.
  * d_in/d_out: caller-owned device complex64 fields (f32 engine); stream: a
  * cudaStream_t (NULL: the default stream).  All other scratch (spectrum
  * buffer, transfer-function and twiddle tables) comes from one static
  * device array of 32 MiB that every GPU loading the library holds until
- * exit; sizes needing more return OSGPU_E_UNSUPPORTED before any GPU work
- * (a 1024 x 1024 field at padding 2 fits, 2048 x 2048 padded to 4096 does
- * not).  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress, with that device current): make it before any
- * stream capture.  Calls share the array, so calls whose GPU work overlaps
- * race: serialise them on one stream.  Input finiteness is not checked. */
+ * exit; sizes needing more, or more shared memory than a block has, return
+ * OSGPU_E_UNSUPPORTED before any GPU work (a 1024 x 1024 field at padding 2
+ * fits, 2048 x 2048 padded to 4096 does not).  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress, with that device
+ * current): make it before any stream capture.  After a cudaDeviceReset,
+ * call osgpu_shutdown() before the next call so the address is looked up
+ * again.  Calls share the array, so calls whose GPU work overlaps race:
+ * serialise them on one stream.  Input finiteness is not checked. */
 int osgpu_asm_propagate_noalloc(const void* d_in, void* d_out, const osgpu_grid* g, double z,
                                 const osgpu_asm_config* cfg, void* stream,
                                 osgpu_asm_report* report);

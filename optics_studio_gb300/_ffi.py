@@ -245,6 +245,9 @@ SIGNATURES = [
     ("osgpu_merit_spot_efficiency_device", C.c_int,
      [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p, c_double_p, C.c_void_p,
       C.c_void_p, C.POINTER(C.c_double)]),
+    ("osgpu_merit_weighted_efficiency_device", C.c_int,
+     [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p, c_double_p, C.c_void_p,
+      C.c_void_p, C.POINTER(C.c_double)]),
     ("osgpu_merit_mse_device", C.c_int,
      [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p, C.c_int32, C.c_int32,
       C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),

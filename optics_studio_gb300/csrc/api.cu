@@ -681,8 +681,7 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
     set_err("padded length has too many prime factors");
     return OSGPU_E_UNSUPPORTED;
   }
-  if (smem_passA_bytes(a.ax, is_d, 1) > kMaxSmem || smem_passB_bytes(a.ay, is_d) > kMaxSmem ||
-      (2 * ((size_t)a.ax.m + 1) + (size_t)a.ax.n) * es > kMaxSmem) {
+  if (!prop_smem_fits(a.ax, a.ay, is_d, kMaxSmem)) {
     set_err("grid %dx%d (sub-FFT %d x %d) exceeds the shared-memory plan of this library",
             a.nx, a.ny, a.ax.m, a.ay.m);
     return OSGPU_E_UNSUPPORTED;
@@ -1325,6 +1324,13 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
 
 }  // namespace
 
+void osgpu::set_last_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(t_err, sizeof(t_err), fmt, ap);
+  va_end(ap);
+}
+
 // ====================================================================== ABI
 
 extern "C" {
@@ -1436,9 +1442,10 @@ int osgpu_field_destroy(osgpu_field f) {
 }
 
 int osgpu_shutdown(void) {
+  noalloc_forget_scratch();  // looked up again by the next allocation-free call
   Context& c = ctx();
   std::lock_guard<std::recursive_mutex> lk(c.mu);
-  if (c.device < 0) return OSGPU_OK;  // nothing was initialised
+  if (c.device < 0) return OSGPU_OK;  // nothing else was initialised
   CK(cudaDeviceSynchronize());  // no queued work reads what is freed below
   // twiddle tables stay: captured graphs (osgpu_beamline_trace_batch_graph)
   // hold their addresses; plans and the encircled-energy order are never
@@ -2683,6 +2690,48 @@ int osgpu_merit_spot_efficiency_device(const void* d_obs, int32_t real_dtype, in
     CK(cudaMemcpyAsync(sums + n_frames, coef.data(), sizeof(double) * n_frames,
                        cudaMemcpyHostToDevice, st));
     CK(launch_window_seed(d_seed, f64, n_frames, frame_len, d_windows, sums + n_frames, st));
+  }
+  std::vector<double> h(n_frames);
+  if ((rc = merit_sync(st, res, h.data(), n_frames))) return rc;
+  if (value) {
+    double tot = 0.0;
+    for (int f = 0; f < n_frames; ++f) tot += h[f] / p_in[f];
+    *value = -tot;
+  }
+  return OSGPU_OK;
+}
+
+int osgpu_merit_weighted_efficiency_device(const void* d_obs, int32_t real_dtype,
+                                           int32_t n_frames, uint64_t frame_len,
+                                           const void* d_weights, const double* p_in,
+                                           void* d_seed, void* stream, double* value) {
+  if (!d_obs || !d_weights || !p_in || n_frames <= 0 || frame_len == 0 ||
+      (real_dtype != OSGPU_F64 && real_dtype != OSGPU_F32))
+    return OSGPU_E_BAD_ARGUMENT;
+  for (int f = 0; f < n_frames; ++f)
+    if (!(p_in[f] > 0.0) || !std::isfinite(p_in[f])) {
+      set_err("frame %d: input power must be positive and finite", f);
+      return OSGPU_E_BAD_ARGUMENT;
+    }
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const int f64 = real_dtype == OSGPU_F64;
+  const size_t sb = reduce_scratch_bytes(n_frames);
+  DBuf scr, res;
+  CK(scr.alloc(sb, st));
+  CK(res.alloc(sizeof(double) * 2 * n_frames, st));
+  double* sums = reinterpret_cast<double*>(res.p);
+  CK(launch_weighted_sums(d_obs, f64, n_frames, frame_len, d_weights,
+                          reinterpret_cast<double*>(scr.p), sums, st));
+  if (d_seed) {
+    std::vector<double> coef(n_frames);
+    for (int f = 0; f < n_frames; ++f) coef[f] = -1.0 / p_in[f];
+    CK(cudaMemcpyAsync(sums + n_frames, coef.data(), sizeof(double) * n_frames,
+                       cudaMemcpyHostToDevice, st));
+    CK(launch_weighted_seed(d_seed, f64, n_frames, frame_len, d_weights, sums + n_frames, st));
   }
   std::vector<double> h(n_frames);
   if ((rc = merit_sync(st, res, h.data(), n_frames))) return rc;

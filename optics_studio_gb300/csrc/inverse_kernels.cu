@@ -190,6 +190,30 @@ __global__ void k_window_seed(void* seed, int f64, uint64_t len, const unsigned 
     st_real(seed, f64, (size_t)f * len + k, win[k] ? c : 0.0);
 }
 
+// sum of w[k] I_f[k] over each frame (w in the observation's real dtype).
+__global__ void k_weighted_sums(const void* obs, int f64, uint64_t len, const void* w,
+                                double* part) {
+  const int f = blockIdx.y;
+  const size_t base = (size_t)f * len;
+  Acc a;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const double wk = ld_real(w, f64, k);
+    if (wk != 0.0) a.add(wk * ld_real(obs, f64, base + k));
+  }
+  write_part(part, f, block_fold(a));
+}
+
+// seed_f[k] = coef[f] w[k]
+__global__ void k_weighted_seed(void* seed, int f64, uint64_t len, const void* w,
+                                const double* coef) {
+  const int f = blockIdx.y;
+  const double c = coef[f];
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+       k += (size_t)gridDim.x * blockDim.x)
+    st_real(seed, f64, (size_t)f * len + k, c * ld_real(w, f64, k));
+}
+
 // Sum of the selected frames at sample k (reference merit.rs:44-81: bands
 // outer, scenes inner, from 0).
 __device__ __forceinline__ double selected_sum(const void* obs, int f64, uint64_t len, int nb,
@@ -692,6 +716,23 @@ cudaError_t launch_window_seed(void* seed, int f64, int nf, uint64_t len,
                                const unsigned char* win, const double* coef, cudaStream_t st) {
   OSGPU_LAUNCH;
   k_window_seed<<<dim3(red_blocks(len), nf), kRedThreads, 0, st>>>(seed, f64, len, win, coef);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_weighted_sums(const void* obs, int f64, int nf, uint64_t len, const void* w,
+                                 double* scratch, double* out, cudaStream_t st) {
+  const int nb = red_blocks(len);
+  OSGPU_LAUNCH;
+  k_weighted_sums<<<dim3(nb, nf), kRedThreads, 0, st>>>(obs, f64, len, w, scratch);
+  OSGPU_LAUNCH;
+  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, nb, nf, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_weighted_seed(void* seed, int f64, int nf, uint64_t len, const void* w,
+                                 const double* coef, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_weighted_seed<<<dim3(red_blocks(len), nf), kRedThreads, 0, st>>>(seed, f64, len, w, coef);
   return cudaGetLastError();
 }
 

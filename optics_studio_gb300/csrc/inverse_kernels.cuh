@@ -89,6 +89,12 @@ cudaError_t launch_window_sums(const void* obs, int f64, int nf, uint64_t len,
                                cudaStream_t st);
 cudaError_t launch_window_seed(void* seed, int f64, int nf, uint64_t len,
                                const unsigned char* win, const double* coef, cudaStream_t st);
+// out[f] = sum_k w[k] I_f[k]; w has the observation's real dtype
+cudaError_t launch_weighted_sums(const void* obs, int f64, int nf, uint64_t len, const void* w,
+                                 double* scratch, double* out, cudaStream_t st);
+// seed_f[k] = coef[f] w[k]
+cudaError_t launch_weighted_seed(void* seed, int f64, int nf, uint64_t len, const void* w,
+                                 const double* coef, cudaStream_t st);
 // out[0] = sum (selected frame - target)^2; seed (optional) per frame
 cudaError_t launch_mse(const void* obs, int f64, uint64_t len, int nb, int ns, int band,
                        int scene, const double* target, void* seed, double* scratch,

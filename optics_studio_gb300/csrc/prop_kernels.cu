@@ -509,6 +509,13 @@ size_t smem_passA_bytes(const AxisPlan& ax, int is_double, int rows) {
   return (2 * ld + (ax.r > 1 ? (size_t)ax.n : 0)) * rows * es;
 }
 
+bool prop_smem_fits(const AxisPlan& ax, const AxisPlan& ay, int is_double, size_t max_smem) {
+  const size_t es = is_double ? 16 : 8;
+  return smem_passA_bytes(ax, is_double, 1) <= max_smem &&
+         smem_passB_bytes(ay, is_double) <= max_smem &&
+         (2 * ((size_t)ax.m + 1) + (size_t)ax.n) * es <= max_smem;  // pass C, one row
+}
+
 int rows_per_cta(const AxisPlan& ax, int is_double) {
   int rows = 16;
   while (rows > 1 && smem_passA_bytes(ax, is_double, rows) > kSmemBudgetRows) rows /= 2;

@@ -159,5 +159,15 @@ unsigned long long launch_count();
 size_t smem_passA_bytes(const AxisPlan& ax, int is_double, int rows);
 size_t smem_passB_bytes(const AxisPlan& ay, int is_double);
 int rows_per_cta(const AxisPlan& ax, int is_double);
+// Whether the three passes of a propagation on these axis plans fit the
+// per-block shared memory `max_smem` (every entry point checks this before
+// its first launch).
+bool prop_smem_fits(const AxisPlan& ax, const AxisPlan& ay, int is_double, size_t max_smem);
+
+// The message osgpu_last_error returns on this thread (printf format).
+void set_last_error(const char* fmt, ...);
+// Forget the cached device addresses of the allocation-free entry point's
+// static scratch (their contexts may have been reset).
+void noalloc_forget_scratch();
 
 }  // namespace osgpu

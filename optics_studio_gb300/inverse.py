@@ -609,6 +609,67 @@ class SpotArrayEfficiency:
         return self._call(obs, seed[0]), True
 
 
+def gaussian_spot_array(shape, count, pitch, sigma):
+    """Target weights of a centred count x count array of Gaussian spots (peak 1,
+    standard deviation ``sigma`` samples, ``pitch`` samples apart) on a
+    (ny, nx) detector grid, as a float64 numpy array (host-side target
+    preparation)."""
+    import numpy as np
+    ny, nx = shape
+    w = np.zeros((ny, nx))
+    half = int(math.ceil(5.0 * sigma))
+    for i in range(count):
+        for j in range(count):
+            cy = ny // 2 + pitch * (i - (count - 1) / 2.0)
+            cx = nx // 2 + pitch * (j - (count - 1) / 2.0)
+            y0, y1 = max(0, math.floor(cy) - half), min(ny, math.ceil(cy) + half + 1)
+            x0, x1 = max(0, math.floor(cx) - half), min(nx, math.ceil(cx) + half + 1)
+            yy = np.arange(y0, y1, dtype=np.float64)[:, None] - cy
+            xx = np.arange(x0, x1, dtype=np.float64)[None, :] - cx
+            w[y0:y1, x0:x1] += np.exp(-(yy * yy + xx * xx) / (2.0 * sigma * sigma))
+    return w
+
+
+class WeightedSpotEfficiency:
+    """Negative summed efficiency into a weighted spot-array target (the merit
+    of the spot-array inverse design with Gaussian spots; no reference
+    counterpart): M = -sum_frames sum_k w[k] I[k] / p_in[frame], with ``weights``
+    a device (ny, nx) real array (e.g. ``gaussian_spot_array``), converted to
+    the observation's real dtype, and ``p_in`` the input power of each band."""
+
+    def __init__(self, weights, p_in):
+        self.weights = weights.contiguous()
+        self.p_in = [float(p) for p in p_in]  # per band
+        self._w = {}
+
+    def _weights(self, obs):
+        dt = obs.data.dtype
+        if dt not in self._w:
+            self._w[dt] = self.weights.to(dt).contiguous()
+        return self._w[dt]
+
+    def _call(self, obs, seed):
+        B, S = len(obs.bands), len(obs.scenes)
+        pin = (C.c_double * (B * S))(*[self.p_in[b] for b in range(B) for _ in range(S)])
+        v = C.c_double()
+        _ffi.check(_ffi.lib().osgpu_merit_weighted_efficiency_device(
+            obs.data[0].data_ptr(), _real_code(obs.data), B * S, obs.frame_len(),
+            self._weights(obs).data_ptr(), pin, seed.data_ptr() if seed is not None else None,
+            _sptr(), C.byref(v)))
+        return v.value
+
+    def evaluate(self, obs):
+        return self._call(obs, None)
+
+    def obs_gradient(self, obs):
+        g = _torch().zeros_like(obs.data)
+        self._call(obs, g[0])
+        return g
+
+    def value_and_seed(self, obs, seed):
+        return self._call(obs, seed[0]), True
+
+
 def field_power(u):
     """sum |u|^2 of a device field in FP64."""
     torch = _torch()

@@ -70,6 +70,30 @@ class SpotArrayEfficiency:
         return g
 
 
+class WeightedSpotEfficiency:
+    """M = -sum_b sum_k w[k] I_b[k] / P_in_b (project-defined: the efficiency into
+    a weighted spot-array target, e.g. a 9 x 9 array of Gaussian spots of peak
+    1); dM/dI_b = -w / P_in_b."""
+
+    def __init__(self, weights, p_in):
+        self.weights = np.asarray(weights, dtype=np.float64)
+        self.p_in = np.asarray(p_in, dtype=np.float64)
+
+    def evaluate(self, obs):
+        tot = 0.0
+        for b in range(len(obs.bands)):
+            for s in range(len(obs.scenes)):
+                tot += math.fsum((self.weights * obs.data[0, b, s]).ravel()) / self.p_in[b]
+        return -float(tot)
+
+    def obs_gradient(self, obs):
+        g = np.zeros_like(obs.data)
+        for b in range(len(obs.bands)):
+            for s in range(len(obs.scenes)):
+                g[0, b, s] = -self.weights / self.p_in[b]
+        return g
+
+
 class EncircledEnergyMerit:
     """merit.rs:167-245: M = -S_in / S_tot over a centred circle of ``radius``."""
 

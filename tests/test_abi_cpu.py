@@ -367,3 +367,16 @@ def test_adam_config_validation_before_device_work():
     for kw in ({"lr": 0.0}, {"lr": math.nan}, {"b1": 1.0}, {"b2": -0.1}, {"eps": math.inf},
                {"clip_norm": 0.0}):
         assert step(**kw) == 43, kw
+
+
+def test_gaussian_spot_array_target():
+    """Host-side target of the spot-array merit: peak 1 at every centre of the
+    centred count x count array, mirror-symmetric about the grid centre for
+    an odd count on an odd grid."""
+    from optics_studio_gb300.inverse import gaussian_spot_array
+    w = gaussian_spot_array((129, 129), 3, 20, 2.0)
+    for i in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            assert abs(w[64 + 20 * i, 64 + 20 * j] - 1.0) < 1e-9
+    assert np.allclose(w, w[::-1, ::-1])
+    assert w.min() >= 0.0 and w.max() <= 1.0 + 1e-9
