@@ -872,6 +872,8 @@ int host_call(Context& c, const double* in, double* out, size_t n, F&& fn) {
   CK(cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (status) {
+    // reported here: clear it, so a later osgpu_sync_status does not see it again
+    CK(cudaMemset(c.d_status, 0, sizeof(int)));
     set_err("field contains non-finite samples");
     return OSGPU_E_NON_FINITE_SAMPLE;
   }
@@ -2119,6 +2121,8 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   release();
   if (e != cudaSuccess) return cuda_fail(e, "batch sync");
   if (status & 1) {
+    // reported here: clear it, so a later osgpu_sync_status does not see it again
+    CK(cudaMemset(c.d_status, 0, sizeof(int)));
     set_err("a field of the batch contains non-finite samples");
     return OSGPU_E_NON_FINITE_SAMPLE;
   }

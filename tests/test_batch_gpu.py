@@ -194,3 +194,5 @@ def test_host_batch_pipeline_equals_single_calls(pinned):
     items[0].in_ = bad.ctypes.data_as(ffi.c_double_p)
     code = L.osgpu_beamline_trace_batch(items, 1, ffi.AsmConfigC(2, 1, 1, 8, 1), ffi.F32, None, 0)
     assert ffi.STATUS_NAMES[code] == "NonFiniteSample"
+    # reported once: the device-resident status check afterwards is clean
+    ffi.check(L.osgpu_sync_status())
