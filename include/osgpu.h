@@ -47,6 +47,8 @@ enum {
   OSGPU_E_INVALID_GRID_PITCH = 27,
   OSGPU_E_INVALID_GRATING = 28,
   OSGPU_E_INVALID_SAG = 29, /* raised by bindings that evaluate a sag (RefractiveSurface) */
+  OSGPU_E_INVALID_THICKNESS = 30, /* ThickLens central thickness (bindings, element.rs:207) */
+  OSGPU_E_INVALID_SURFACE = 31,   /* surface profile parameters or conic domain (element.rs:177) */
   /* InverseError (crates/optics-inverse/src/error.rs:11-85) */
   OSGPU_E_WRONG_DIMENSION = 40,
   OSGPU_E_NOT_FINITE = 41,
@@ -586,7 +588,9 @@ int osgpu_asm_propagate_noalloc(const void* d_in, void* d_out, const osgpu_grid*
  * osgpu_profile_begin and osgpu_profile_end every pass launch is bracketed by
  * events; _end synchronises and returns, per class, the launch count, total
  * device time and the algorithmic bytes those launches move (reads of the
- * inputs they must read + writes of their outputs). */
+ * inputs they must read + writes of their outputs).  While profiling, the
+ * per-item table builds that normally overlap on an auxiliary stream run on
+ * the launching stream, so every class's events time its own kernels. */
 typedef struct {
   char name[32];
   uint64_t launches;

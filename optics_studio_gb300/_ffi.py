@@ -17,7 +17,7 @@ STATUS_NAMES = {
     5: "NonFiniteSample", 6: "AliasingRisk", 7: "RegimeViolation",
     20: "InvalidAperture", 21: "OutsideField", 22: "InvalidAxis", 23: "InvalidFocal",
     24: "InvalidOrientation", 25: "InvalidPhase", 26: "InvalidGrid", 27: "InvalidGridPitch",
-    28: "InvalidGrating", 29: "InvalidSag",
+    28: "InvalidGrating", 29: "InvalidSag", 30: "InvalidThickness", 31: "InvalidSurface",
     40: "WrongDimension", 41: "NotFinite", 42: "OutOfBounds", 43: "Render", 44: "Adjoint",
     100: "Unsupported", 101: "Cuda", 102: "BadArgument", 103: "NoDevice", 104: "OutOfMemory",
 }

@@ -74,6 +74,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   cudaStream_t copy_in = nullptr, copy_out = nullptr;  // host-buffer batch pipeline
   cudaStream_t aux = nullptr;  // element tables of the next batch item
+  cudaStream_t lane2 = nullptr, aux2 = nullptr;  // second lane of the device batch
   int* d_status = nullptr;
   std::map<std::pair<int, int>, void*> tw;  // (n, is_double) -> twiddle table
   bool profiling = false;
@@ -230,7 +231,8 @@ struct AuxTables {
   cudaEvent_t ev = nullptr, e0 = nullptr, e1 = nullptr;
   std::vector<Elements> cur, gen0, gen1;
   bool joined = false;
-  int fork(Context& c, cudaStream_t compute);
+  // `second`: the auxiliary stream of the device batch's second lane
+  int fork(Context& c, cudaStream_t compute, bool second = false);
   int ready() {
     CK(cudaEventRecord(ev, ax));
     CK(cudaStreamWaitEvent(st, ev, 0));
@@ -291,10 +293,14 @@ struct AuxTables {
   }
 };
 
-int AuxTables::fork(Context& c, cudaStream_t compute) {
-  if (!c.aux) CK(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
+int AuxTables::fork(Context& c, cudaStream_t compute, bool second) {
+  cudaStream_t& own = second ? c.aux2 : c.aux;
+  if (!own) CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
   st = compute;
-  ax = c.aux;
+  // While profiling, the table builds run on the compute stream: events on
+  // an overlapped auxiliary stream would time its waits for free SMs, not
+  // the kernels.
+  ax = c.profiling ? compute : own;
   CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   CK(cudaEventRecord(ev, st));
   CK(cudaStreamWaitEvent(ax, ev, 0));
@@ -2141,32 +2147,69 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
   cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   const int f32 = dtype == OSGPU_C64;
   const int c128 = dtype == OSGPU_C128;
-  AuxTables aux;
-  if ((rc = aux.fork(c, st))) return rc;
   for (int i = 0; i < n_items; ++i) {
     const osgpu_trace_item& it = items[i];
     if (!it.d_in || !it.d_out || it.n_steps < 0 || (it.n_steps > 0 && !it.steps))
       return OSGPU_E_BAD_ARGUMENT;
     if (it.grid.nx == 0 || it.grid.ny == 0) return OSGPU_E_EMPTY_GRID;
-    if ((rc = aux.begin())) return rc;
+  }
+  // Items are independent: two lanes (the caller's stream and a second
+  // stream forked from it and joined back at the end) take alternate items,
+  // so one item's passes fill the SMs that the other's leave idle at the
+  // ends of their grids.  Each lane has its own scratch and its own
+  // auxiliary stream for the per-item tables.  One lane while profiling
+  // (per-kernel events) or when OSGPU_LANES=1.
+  const char* lenv = getenv("OSGPU_LANES");
+  const int lanes = (n_items > 1 && !c.profiling && !(lenv && atoi(lenv) == 1)) ? 2 : 1;
+  cudaStream_t ls[2] = {st, nullptr};
+  if (lanes == 2) {
+    if (!c.lane2) CK(cudaStreamCreateWithFlags(&c.lane2, cudaStreamNonBlocking));
+    ls[1] = c.lane2;
+    cudaEvent_t fk = nullptr;
+    CK(cudaEventCreateWithFlags(&fk, cudaEventDisableTiming));
+    CK(cudaEventRecord(fk, st));
+    CK(cudaStreamWaitEvent(ls[1], fk, 0));
+    cudaEventDestroy(fk);
+  }
+  AuxTables aux[2];
+  for (int l = 0; l < lanes; ++l)
+    if ((rc = aux[l].fork(c, ls[l], l == 1))) return rc;
+  // on an error return the second lane is still joined back into `st`
+  auto join = [&](int rc0) {
+    if (lanes == 2) {
+      cudaEvent_t jn = nullptr;
+      if (cudaEventCreateWithFlags(&jn, cudaEventDisableTiming) == cudaSuccess) {
+        cudaEventRecord(jn, ls[1]);
+        cudaStreamWaitEvent(st, jn, 0);
+        cudaEventDestroy(jn);
+      }
+    }
+    return rc0;
+  };
+  for (int i = 0; i < n_items; ++i) {
+    const osgpu_trace_item& it = items[i];
+    AuxTables& ax = aux[i % lanes];
+    if ((rc = ax.begin())) return join(rc);
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
-    rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, aux.ax);
+    rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, ax.ax);
     if (reports && reports_stride > 0)
       for (int s = 0; s < it.n_steps && s < reports_stride && s < (int)R.size(); ++s)
         reports[(size_t)i * reports_stride + s] = R[s];
     if (rc) {
       set_err("batch item %d: %s", i, t_err);
-      return rc;
+      return join(rc);
     }
-    if ((rc = aux.ready())) return rc;
-    std::vector<Elements>& Ei = aux.take(E);
+    if ((rc = ax.ready())) return join(rc);
+    std::vector<Elements>& Ei = ax.take(E);
     if ((rc = run_trace(c, it.d_in, c128, it.d_out, c128, it.grid, it.steps, it.n_steps, Ei, R,
-                        *cfg, f32, st)))
-      return rc;
-    if ((rc = aux.end())) return rc;
+                        *cfg, f32, ls[i % lanes])))
+      return join(rc);
+    if ((rc = ax.end())) return join(rc);
   }
-  return aux.finish();
+  for (int l = lanes - 1; l >= 0; --l)
+    if ((rc = aux[l].finish())) return join(rc);
+  return join(OSGPU_OK);
 }
 
 // ------------------------------------------------------------ graphs

@@ -19,8 +19,35 @@
 namespace osgpu {
 namespace regfft {
 
+#ifndef OSGPU_NO_F32X2
+// Complex add / subtract as one packed f32x2 instruction (sm_100+): each lane
+// rounds like the scalar add, so results are bit-identical; it halves the
+// issue slots of the butterflies' additions (OSGPU_NO_F32X2 builds the
+// scalar form for comparison).
+__device__ __forceinline__ unsigned long long pk2(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(unsigned long long r) {
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(r));
+  return d;
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+  return upk2(d);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+  return upk2(d);
+}
+#else
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -45,11 +72,17 @@ __device__ __forceinline__ void dft2(float2& a, float2& b) {
 template <bool INV>
 __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
   float2 b0 = cadd(a0, a2), b1 = csub(a0, a2);
-  float2 b2 = cadd(a1, a3), b3 = rot<INV>(csub(a1, a3));
+  float2 b2 = cadd(a1, a3), d = csub(a1, a3);
   a0 = cadd(b0, b2);
   a2 = csub(b0, b2);
-  a1 = cadd(b1, b3);
-  a3 = csub(b1, b3);
+  // b1 +- rot(d), rot(d) = -i d (fwd) or +i d (inv), componentwise
+  if (INV) {
+    a1 = make_float2(b1.x - d.y, b1.y + d.x);
+    a3 = make_float2(b1.x + d.y, b1.y - d.x);
+  } else {
+    a1 = make_float2(b1.x + d.y, b1.y - d.x);
+    a3 = make_float2(b1.x - d.y, b1.y + d.x);
+  }
 }
 
 // multiply by W8^1 = e^{-i pi/4} (fwd) or its conjugate (inv)

@@ -245,6 +245,42 @@ def _index(n, lam):
     return float(n(lam)) if callable(n) else float(n)
 
 
+class SurfaceProfile:
+    """SurfaceProfile (element.rs:1760-1870): spherical / conic / even asphere
+    (vertex radius, conic constant, coefficients of r^4, r^6, ...) or an
+    analytic sag callable z(r), evaluated on the host."""
+
+    def __init__(self, radius=None, conic=0.0, coeffs=(), analytic=None):
+        self.radius, self.conic, self.coeffs, self.analytic = radius, conic, tuple(coeffs), analytic
+
+    @staticmethod
+    def spherical(radius):
+        return SurfaceProfile(radius)
+
+    def validate(self):
+        """element.rs:1800-1822: finite parameters and a nonzero vertex radius."""
+        if self.analytic is not None:
+            return
+        if (not math.isfinite(self.radius) or self.radius == 0.0 or not math.isfinite(self.conic)
+                or any(not math.isfinite(a) for a in self.coeffs)):
+            raise _ffi.OsgpuError(31)
+
+    def check_domain(self, r_max):
+        """element.rs:1828-1845: the conic square root must stay real over the stop."""
+        if self.analytic is None:
+            c = 1.0 / self.radius
+            if (1.0 + self.conic) * c * c * r_max * r_max > 1.0:
+                raise _ffi.OsgpuError(31)
+
+    def sag(self, r):
+        if self.analytic is not None:
+            return np.asarray(self.analytic(r), dtype=np.float64)
+        return conic_sag(r, self.radius, self.conic, self.coeffs)
+
+    def vertex_curvature(self):
+        return None if self.analytic is not None else 1.0 / self.radius
+
+
 class RefractiveSurface(Element):
     """element.rs:1910-2123: exp(i k (n1 - n2) z) inside the stop, z = conic /
     even-asphere sag plus a linear tilt.  The sag is evaluated on the host at
@@ -253,8 +289,7 @@ class RefractiveSurface(Element):
 
     def __init__(self, radius, conic=0.0, coeffs=(), n_front=1.0, n_back=1.5, tilt=(0.0, 0.0),
                  orientation=None, aperture=ClearAperture.field(), center=(0.0, 0.0)):
-        if not (math.isfinite(radius) and radius != 0.0):
-            raise _ffi.OsgpuError(23)
+        SurfaceProfile(radius, conic, coeffs).validate()
         self.radius, self.conic, self.coeffs = radius, conic, tuple(coeffs)
         self.n_front, self.n_back, self.tilt = n_front, n_back, tilt
         self.psi = 0.0 if orientation is None else orientation
@@ -299,3 +334,94 @@ class Wedge(Element):
         v = self.values(band)
         return _screen_desc(v, k * (_index(self.n, band.lam) - 1.0), self.aperture, self.psi,
                             self.center), v
+
+
+def _validate_stop(ap, center):
+    """ClearAperture::validate (element.rs:415-430) on the host: a finite centre
+    for the full field, else positive finite semi-axes and a finite centre."""
+    cx, cy = center
+    if ap.kind == STOP_FIELD:
+        if not (math.isfinite(cx) and math.isfinite(cy)):
+            raise _ffi.OsgpuError(22)
+    elif not (math.isfinite(ap.a) and ap.a > 0.0 and math.isfinite(ap.b) and ap.b > 0.0
+              and math.isfinite(cx) and math.isfinite(cy)):
+        raise _ffi.OsgpuError(20)
+
+
+def _check_footprint(ap, psi, center, band):
+    """The OutsideField check of Element::apply (element.rs:2310-2322): the
+    stop's rotated footprint plus the centre offset within the grid's half
+    extents."""
+    if ap.kind == STOP_FIELD:
+        return
+    if ap.kind == STOP_CIRCLE:
+        fx, fy = ap.a, ap.b
+    else:
+        o = wrap_angle(psi)
+        c, s = abs(math.cos(o)), abs(math.sin(o))
+        fx, fy = ap.a * c + ap.b * s, ap.a * s + ap.b * c
+    gx = (float(band.nx) - 1.0) / 2.0 * band.dx
+    gy = (float(band.ny) - 1.0) / 2.0 * band.dy
+    if abs(center[0]) + fx > gx or abs(center[1]) + fy > gy:
+        raise _ffi.OsgpuError(21)
+
+
+class ThickLens(Element):
+    """element.rs:2159-2360: exp(i k (n - 1) t(rho)) inside the stop, with the
+    glass thickness t = t0 - z_front(rho) + z_back(rho) at the element-frame
+    radius (no tilt term: a common tilt cancels in the difference).  The
+    thickness is evaluated on the host per field sample and bound as a grid
+    screen with depth k (n - 1); the index is a number or a callable n(lam).
+    Construction raises InvalidOrientation, InvalidSurface, InvalidThickness
+    and the aperture errors in the reference's order; apply raises
+    OutsideField, InvalidMedium and InvalidSag."""
+
+    def __init__(self, front, back, n, thickness, orientation=None,
+                 aperture=ClearAperture.field(), center=(0.0, 0.0)):
+        if orientation is not None and not math.isfinite(orientation):
+            raise _ffi.OsgpuError(24)
+        front.validate()
+        back.validate()
+        if not math.isfinite(thickness) or thickness < 0.0:
+            raise _ffi.OsgpuError(30)
+        _validate_stop(aperture, center)
+        if aperture.kind != STOP_FIELD:
+            r_max = max(aperture.a, aperture.b)  # ClearAperture::extent_radius
+            front.check_domain(r_max)
+            back.check_domain(r_max)
+        self.front, self.back, self.n, self.t0 = front, back, n, thickness
+        self.psi = 0.0 if orientation is None else orientation
+        self.aperture, self.center = aperture, center
+
+    def thickness_profile(self, r):
+        """element.rs:2215-2217."""
+        return self.t0 - self.front.sag(r) + self.back.sag(r)
+
+    def power_at(self, lam):
+        """element.rs:2221-2225: (n(lam) - 1)(c1 - c2); None for analytic profiles."""
+        c1, c2 = self.front.vertex_curvature(), self.back.vertex_curvature()
+        if c1 is None or c2 is None:
+            return None
+        return (_index(self.n, lam) - 1.0) * (c1 - c2)
+
+    def focal_at(self, lam):
+        p = self.power_at(lam)
+        return None if p is None or p == 0.0 else 1.0 / p
+
+    def values(self, band):
+        _, _, fx, fy = frame_coords(band, self.center, self.psi)
+        inside = ap_contains(self.aperture, fx, fy)
+        t = self.thickness_profile(np.hypot(fx, fy))
+        if not np.all(np.isfinite(t[inside])):
+            raise _ffi.OsgpuError(29)
+        return np.ascontiguousarray(np.where(inside, t, 0.0))
+
+    def descriptor(self, band):
+        _check_footprint(self.aperture, self.psi, self.center, band)
+        n = _index(self.n, band.lam)
+        if not math.isfinite(n) or n <= 0.0:
+            raise _ffi.OsgpuError(3)
+        k = 2.0 * math.pi / band.lam
+        v = self.values(band)
+        return _screen_desc(v, k * (n - 1.0), self.aperture, self.psi, self.center), v
+

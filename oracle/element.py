@@ -374,3 +374,98 @@ class Wedge(Element):
         k = 2.0 * math.pi / band.lam
         dn = self.n - 1.0
         return np.where(inside, np.exp(1j * ((k * dn) * self.thickness_at(fx, fy))), 0.0)
+
+
+class SurfaceProfile:
+    """SurfaceProfile (element.rs:1760-1870): spherical / conic / even asphere
+    (vertex radius, conic constant, coefficients of r^4, r^6, ...) or an
+    analytic sag callable z(r)."""
+
+    def __init__(self, radius=None, conic=0.0, coeffs=(), analytic=None):
+        self.radius, self.conic, self.coeffs, self.analytic = radius, conic, tuple(coeffs), analytic
+
+    @staticmethod
+    def spherical(radius):
+        return SurfaceProfile(radius)
+
+    def validate(self):
+        """element.rs:1800-1822."""
+        if self.analytic is not None:
+            return
+        r, k = self.radius, self.conic
+        if (not math.isfinite(r) or r == 0.0 or not math.isfinite(k)
+                or any(not math.isfinite(a) for a in self.coeffs)):
+            raise OpticsError("InvalidSurface", radius=r, conic=k, r=math.nan)
+
+    def check_domain(self, r_max):
+        """element.rs:1828-1845: 1 - (1 + k) c^2 r^2 >= 0 over the stop."""
+        if self.analytic is not None:
+            return
+        c = 1.0 / self.radius
+        if (1.0 + self.conic) * c * c * r_max * r_max > 1.0:
+            raise OpticsError("InvalidSurface", radius=self.radius, conic=self.conic, r=r_max)
+
+    def sag(self, r):
+        if self.analytic is not None:
+            return self.analytic(r)
+        return conic_sag(r, self.radius, self.conic, self.coeffs)
+
+    def vertex_curvature(self):
+        return None if self.analytic is not None else 1.0 / self.radius
+
+
+class ThickLens(Element):
+    """element.rs:2159-2360: exp(i (k (n - 1)) t(rho)) inside the stop,
+    t = t0 - z_front(rho) + z_back(rho) at the element-frame radius; the glass
+    index ``n`` is a number or a callable n(lam)."""
+
+    def __init__(self, front, back, n, thickness, orientation=None,
+                 aperture=ClearAperture.field(), center=(0.0, 0.0)):
+        self.psi = resolve_orientation(orientation)
+        front.validate()
+        back.validate()
+        if not math.isfinite(thickness) or thickness < 0.0:
+            raise OpticsError("InvalidThickness", thickness=thickness)
+        aperture.validate(center)
+        if aperture.kind != "field":
+            r_max = max(aperture.a, aperture.b)
+            front.check_domain(r_max)
+            back.check_domain(r_max)
+        self.front, self.back, self.n, self.t0 = front, back, n, thickness
+        self.aperture, self.center = aperture, center
+
+    def index_at(self, lam):
+        return float(self.n(lam)) if callable(self.n) else float(self.n)
+
+    def thickness_profile(self, r):
+        """element.rs:2215-2217."""
+        return self.t0 - self.front.sag(r) + self.back.sag(r)
+
+    def power_at(self, lam):
+        """element.rs:2221-2225: (n - 1)(c1 - c2), None for analytic profiles."""
+        c1, c2 = self.front.vertex_curvature(), self.back.vertex_curvature()
+        if c1 is None or c2 is None:
+            return None
+        return (self.index_at(lam) - 1.0) * (c1 - c2)
+
+    def focal_at(self, lam):
+        p = self.power_at(lam)
+        return None if p is None or p == 0.0 else 1.0 / p
+
+    def transmission(self, band):
+        """element.rs:2305-2358."""
+        _check_footprint(self.aperture.footprint_at(self.psi), self.center, band)
+        n = self.index_at(band.lam)
+        if not math.isfinite(n) or n <= 0.0:
+            raise OpticsError("InvalidMedium", n_front=n, n_back=n)
+        _, _, fx, fy = _frame_coords(band, self.center, self.psi)
+        inside = self.aperture.contains(fx, fy)
+        k = 2.0 * math.pi / band.lam
+        dn = n - 1.0
+        t = self.thickness_profile(np.hypot(fx, fy))
+        bad = inside & ~np.isfinite(t)
+        if np.any(bad):
+            raise OpticsError("InvalidSag", r=float(np.hypot(fx, fy)[bad][0]),
+                              sag=float(t[bad][0]))
+        return np.where(inside, np.exp(1j * ((k * dn) * t)), 0.0)
+

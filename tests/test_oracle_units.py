@@ -21,6 +21,7 @@ import numpy as np
 import pytest
 
 from oracle import field as ofield, fraunhofer as ofh, fresnel as ofr, rs as ors
+from oracle import element as oel
 
 LAMBDA = 500e-9
 
@@ -986,3 +987,97 @@ def test_analysis_mtf_dc_and_zero_field_safety():
     assert oan.spot_rms_radius(zero, (1e-3, 1e-3)) == 0.0
     assert oan.strehl(zero, (1e-3, 1e-3), flat, (1e-3, 1e-3)) == 0.0
     assert oan.encircled_energy(zero, (1e-3, 1e-3)).value_at(1.0) == 0.0
+
+
+def _wrap(p):
+    return (p + math.pi) % (2 * math.pi) - math.pi
+
+
+def test_thick_lens_paraxial_matches_thin_lens_with_piston():
+    """element.rs thick_lens_paraxial_matches_thin_lens_with_piston: biconvex
+    R1 = +0.1, R2 = -0.1, n = 1.5 gives f = 0.1 m; the vertex phase is the
+    piston k (n - 1) t0; at rho = 2 mm the relative phase equals the exact
+    two-sphere sag to 1e-9 and differs from the paraxial quadratic by the r^4
+    residual (~ -0.025 rad).  The product's host-evaluated thickness screen
+    takes the same values."""
+    from optics_studio_gb300 import element as gel
+    lam, t0 = 500e-9, 2e-3
+    lens = oel.ThickLens(oel.SurfaceProfile.spherical(0.1), oel.SurfaceProfile.spherical(-0.1),
+                         1.5, t0, None, oel.ClearAperture.circle(2e-2))
+    f = lens.focal_at(lam)
+    assert abs(f - 0.1) < 1e-12
+    k = 2 * math.pi / lam
+    band = ofield.uniform(1.0, math.pi / 3.0, 101, 101, 1e-3, 1e-3, lam)
+    out = lens.apply(band).samples
+    center = np.angle(out[50, 50])
+    assert abs(_wrap(center - (math.pi / 3.0 + k * 0.5 * t0))) < 1e-9
+    rho = 2e-3
+    rel = _wrap(np.angle(out[50, 52]) - center)
+    exact = -k * 0.5 * 2.0 * (0.1 - math.sqrt(0.1 ** 2 - rho * rho))
+    assert abs(_wrap(rel - exact)) < 1e-9
+    paraxial = -k * rho * rho / (2.0 * f)
+    assert abs(_wrap(rel - paraxial) - (-0.025)) < 0.005
+    assert abs(lens.thickness_profile(0.0) - t0) < 1e-18
+    assert lens.thickness_profile(1e-2) < t0
+    g = gel.ThickLens(gel.SurfaceProfile.spherical(0.1), gel.SurfaceProfile.spherical(-0.1),
+                      1.5, t0, None, gel.ClearAperture.circle(2e-2))
+    assert g.focal_at(lam) == f
+    from optics_studio_gb300.field import BandField
+    d, v = g.descriptor(BandField(band.samples, 1e-3, 1e-3, lam))
+    xs = ofield.axis_coords(101, 1e-3)
+    r = np.hypot(xs[None, :], xs[:, None])
+    inside = r <= 2e-2
+    assert np.array_equal(v[inside], lens.thickness_profile(r)[inside])
+    assert d.depth == k * (1.5 - 1.0)
+
+
+def test_thick_lens_validation_matches_reference_errors():
+    """element.rs thick_lens_validation: negative thickness -> InvalidThickness;
+    a back surface whose conic domain the stop exceeds -> InvalidSurface;
+    analytic profiles have no power; zero thickness adds no piston.  The
+    product's binding raises the same variants (host-side construction and
+    apply checks: OutsideField, InvalidMedium, InvalidSag)."""
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import element as gel
+    from optics_studio_gb300.field import BandField
+    lam = 500e-9
+    sph = oel.SurfaceProfile.spherical
+    with pytest.raises(oel.OpticsError) as e:
+        oel.ThickLens(sph(0.1), sph(-0.1), 1.5, -1e-3, None, oel.ClearAperture.circle(2e-2))
+    assert e.value.variant == "InvalidThickness"
+    with pytest.raises(oel.OpticsError) as e:
+        oel.ThickLens(sph(0.1), sph(1e-3), 1.5, 1e-3, None, oel.ClearAperture.circle(2e-3))
+    assert e.value.variant == "InvalidSurface"
+    an = oel.ThickLens(oel.SurfaceProfile(analytic=lambda r: r * r), sph(0.1), 1.5, 0.0, None,
+                       oel.ClearAperture.circle(1e-3))
+    assert an.power_at(lam) is None and an.focal_at(lam) is None
+    flat = oel.ThickLens(sph(0.1), sph(-0.1), 1.5, 0.0, None, oel.ClearAperture.circle(1e-3))
+    band = ofield.uniform(1.0, math.pi / 3.0, 101, 101, 1e-3, 1e-3, lam)
+    assert abs(_wrap(np.angle(flat.apply(band).samples[50, 50]) - math.pi / 3.0)) < 1e-12
+
+    gs = gel.SurfaceProfile.spherical
+    for args, variant in [
+        ((gs(0.1), gs(-0.1), 1.5, -1e-3, None, gel.ClearAperture.circle(2e-2)), "InvalidThickness"),
+        ((gs(0.1), gs(1e-3), 1.5, 1e-3, None, gel.ClearAperture.circle(2e-3)), "InvalidSurface"),
+        ((gs(0.0), gs(-0.1), 1.5, 1e-3, None, gel.ClearAperture.circle(2e-3)), "InvalidSurface"),
+        ((gs(0.1), gs(-0.1), 1.5, 1e-3, None, gel.ClearAperture.circle(-1.0)), "InvalidAperture"),
+        ((gs(0.1), gs(-0.1), 1.5, 1e-3, math.nan), "InvalidOrientation"),
+    ]:
+        with pytest.raises(og.OsgpuError) as e:
+            gel.ThickLens(*args)
+        assert e.value.variant == variant
+    gb = BandField(band.samples, 1e-3, 1e-3, lam)
+    big = gel.ThickLens(gs(1.0), gs(-1.0), 1.5, 1e-3, None, gel.ClearAperture.circle(60e-3))
+    with pytest.raises(og.OsgpuError) as e:
+        big.descriptor(gb)
+    assert e.value.variant == "OutsideField"
+    bad_n = gel.ThickLens(gs(0.1), gs(-0.1), lambda l: -1.0, 1e-3, None,
+                          gel.ClearAperture.circle(2e-2))
+    with pytest.raises(og.OsgpuError) as e:
+        bad_n.descriptor(gb)
+    assert e.value.variant == "InvalidMedium"
+    nan_sag = gel.ThickLens(gel.SurfaceProfile(analytic=lambda r: np.where(r > 5e-3, np.nan, 0.0)),
+                            gs(-0.1), 1.5, 1e-3, None, gel.ClearAperture.circle(2e-2))
+    with pytest.raises(og.OsgpuError) as e:
+        nan_sag.descriptor(gb)
+    assert e.value.variant == "InvalidSag"

@@ -272,8 +272,9 @@ def test_fresnel_f32_register_fft(z):
 
 def screen_pairs():
     """Elements bound as grid screens (host-evaluated values): refractive
-    surfaces (conic + asphere + tilt), wedges and an analytic phase mask,
-    rotated and unrotated (unrotated ones take the f32 table path)."""
+    surfaces (conic + asphere + tilt), wedges, an analytic phase mask and
+    thick lenses, rotated and unrotated (unrotated ones take the f32 table
+    path)."""
     prof = lambda x, y: 3e8 * x * y + 2e4 * x - 1e9 * y * y
     return [
         (gel.RefractiveSurface(2e-3, -0.5, (1e3, -2e6), 1.0, 1.52, (1e-3, -2e-3), 0.3,
@@ -289,6 +290,18 @@ def screen_pairs():
         (gel.Wedge(-0.02, 1.6, 5e-5, 0.0), oel.Wedge(-0.02, 1.6, 5e-5, 0.0)),
         (gel.PhaseMask.new(prof, 0.2, gel.ClearAperture.circle(85e-6)),
          oel.PhaseMask(prof, 0.2, oel.ClearAperture.circle(85e-6))),
+        # thick lenses (element.rs:2159-2360): biconvex spheres, and an asphere
+        # against a conic, rotated, off-centre, elliptical stop, dispersive glass
+        (gel.ThickLens(gel.SurfaceProfile.spherical(2e-3), gel.SurfaceProfile.spherical(-3e-3),
+                       1.52, 40e-6, None, gel.ClearAperture.circle(80e-6)),
+         oel.ThickLens(oel.SurfaceProfile.spherical(2e-3), oel.SurfaceProfile.spherical(-3e-3),
+                       1.52, 40e-6, None, oel.ClearAperture.circle(80e-6))),
+        (gel.ThickLens(gel.SurfaceProfile(1.5e-3, -0.6, (2e3, -1e6)),
+                       gel.SurfaceProfile(-4e-3, 0.3), lambda lam: 1.45 + 4e-15 / lam ** 2, 25e-6,
+                       0.4, gel.ClearAperture.ellipse(70e-6, 50e-6), (3e-6, -4e-6)),
+         oel.ThickLens(oel.SurfaceProfile(1.5e-3, -0.6, (2e3, -1e6)),
+                       oel.SurfaceProfile(-4e-3, 0.3), lambda lam: 1.45 + 4e-15 / lam ** 2, 25e-6,
+                       0.4, oel.ClearAperture.ellipse(70e-6, 50e-6), (3e-6, -4e-6))),
     ]
 
 
