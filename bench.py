@@ -253,6 +253,36 @@ def hbm_peak():
     return 6800.0, "fallback"
 
 
+KERNEL_SOURCES = ("optics_studio_gb300/csrc/prop_fast.cu", "optics_studio_gb300/csrc/fft_reg.cuh")
+
+
+def kernel_sources_sha():
+    """SHA-256 (first 16 hex digits) of the sources of the f32 passes."""
+    import hashlib
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def traffic_of(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu capture
+    (profiles/traffic.json: dram__bytes_read.sum + dram__bytes_write.sum of one
+    full-size launch), with where it came from and whether the kernel sources
+    changed since that capture (then the figure is stale and not reported)."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as f:
+        t = json.load(f)
+    src = {"profile": t.get("profile"), "captured_sources_sha": t.get("sources_sha"),
+           "current_sources_sha": kernel_sources_sha()}
+    src["stale"] = src["captured_sources_sha"] != src["current_sources_sha"]
+    val = t.get("kernels", {}).get(kernel)
+    return (None if src["stale"] else val), src
+
+
 def prop_bytes(n, p, s=8):
     """Algorithmic bytes of one pruned padded propagation of an n x n field on a
     p x p grid (element fused in, crop out): s (2 n^2 + 4 n p)."""
@@ -455,6 +485,117 @@ def ragged_leg(args, stream):
                         "50-500 um, dx 3 um, 450-650 nm, complex64, one captured CUDA graph"}
 
 
+# Single-plane engine sweep at 1024^2 (dx 4 um, 532 nm): unit plane wave x
+# 8-level quantised random DOE phase (levels k 2 pi / 8, seeded) x thin lens
+# f 50 mm, then Fresnel transfer function 50 mm and Fresnel convolution
+# 200 mm (strict; both pass at padding 2, P = 2048), Fraunhofer 50 mm and
+# Rayleigh-Sommerfeld 5 mm (strict off: the reference's strict guards reject
+# both; the reports are recorded).  Each engine through its reference-facing
+# host-buffer entry point (complex128 in and out) on the plain FP64 and the
+# f32 engines.
+C2_N, C2_DX, C2_LAM, C2_F, C2_SEED = 1024, 4e-6, 532e-9, 50e-3, 808
+
+
+def c2_input():
+    """Host complex128 input of the sweep: the elements applied on the device
+    (FP64 engine), so both precisions propagate the same samples."""
+    from optics_studio_gb300 import element as gel
+    from optics_studio_gb300.field import BandField
+    lat = np.floor(np.random.default_rng(C2_SEED).uniform(0, 8, (C2_N, C2_N))) * (2 * math.pi / 8)
+    b = BandField(np.ones((C2_N, C2_N), complex), C2_DX, C2_DX, C2_LAM)
+    return gel.apply_elements(b, [gel.PhaseMask.sampled(lat, (C2_N, C2_N), (C2_DX, C2_DX)),
+                                  gel.ThinLens.fixed(C2_F)], "f64"), lat
+
+
+def c2_engines():
+    from optics_studio_gb300.propagation import fresnel, fraunhofer, rayleigh_sommerfeld as rs
+    n, P = C2_N, 2 * C2_N
+    # algorithmic bytes per call (s = bytes per complex): pruned padded
+    # propagation s (2 n^2 + 4 n P), plus the kernel spectrum P^2 for the
+    # convolution engines; Fraunhofer is unpadded, s 4 n^2 (two passes)
+    return {
+        "fresnel_tf": (lambda b, p: fresnel.propagate(b, 50e-3, fresnel.FresnelConfig(), p),
+                       lambda s: s * (2 * n * n + 4 * n * P)),
+        "fresnel_conv": (lambda b, p: fresnel.propagate_convolution(
+            b, 200e-3, fresnel.FresnelConfig(), p), lambda s: s * (2 * n * n + 4 * n * P + P * P)),
+        "fraunhofer": (lambda b, p: fraunhofer.propagate(
+            b, 50e-3, fraunhofer.FraunhoferConfig(strict=False), p), lambda s: s * 4 * n * n),
+        "rayleigh_sommerfeld": (lambda b, p: rs.propagate(
+            b, 5e-3, rs.RayleighSommerfeldConfig(strict=False), p),
+            lambda s: s * (2 * n * n + 4 * n * P + P * P)),
+    }
+
+
+def c2_oracle(samples):
+    from oracle import field as ofield, fresnel as ofr, fraunhofer as ofh, rs as ors
+    ob = ofield.BandField(samples, C2_DX, C2_DX, C2_LAM)
+    return {"fresnel_tf": ofr.propagate(ob, 50e-3, ofr.FresnelConfig()).samples,
+            "fresnel_conv": ofr.propagate_convolution(ob, 200e-3, ofr.FresnelConfig()).samples,
+            "fraunhofer": ofh.propagate(ob, 50e-3, ofh.FraunhoferConfig(strict=False)).samples,
+            "rayleigh_sommerfeld": ors.propagate(
+                ob, 5e-3, ors.RayleighSommerfeldConfig(strict=False)).samples}
+
+
+def c2_leg(args):
+    import ctypes as C
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import _ffi as ffi
+    from optics_studio_gb300.propagation import fraunhofer, rayleigh_sommerfeld as rs
+    L = og.lib()
+    band, _ = c2_input()
+    peak, src = hbm_peak()
+    reps = max(5, args.steps)
+    out = {"workload": "1024^2, dx 4 um, 532 nm, plane wave x 8-level DOE x lens f 50 mm; "
+                       "Fresnel TF 50 mm, Fresnel conv 200 mm, Fraunhofer 50 mm (strict off), "
+                       "RS 5 mm (strict off)",
+           "api": "host-buffer entry points (complex128 in/out, copies in the timed call)",
+           "engines": {}}
+    results = {}
+    for name, (fn, nbytes) in c2_engines().items():
+        row = {}
+        for prec in ("f64", "f32"):
+            fn(band, prec)  # warm-up: twiddle tables, kernel attributes
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                r = fn(band, prec)
+            dt = (time.perf_counter() - t0) / reps
+            results[(name, prec)] = r.samples
+            # device time of the kernels of one call (events on the launching stream)
+            ffi.check(L.osgpu_profile_begin())
+            fn(band, prec)
+            stats = (ffi.KernelStatC * 16)()
+            nst = C.c_int32()
+            ffi.check(L.osgpu_profile_end(stats, 16, C.byref(nst)))
+            kms = sum(stats[i].total_ms for i in range(nst.value))
+            b = nbytes(16 if prec == "f64" else 8)
+            row[prec] = {"value": 1.0 / dt, "unit": "propagations/s", "ms_per_call": dt * 1e3,
+                         "kernel_ms": kms,
+                         "roofline": {"bound": "hbm", "bytes": b,
+                                      "achieved": b / (kms / 1e3) / 1e9 if kms > 0 else None,
+                                      "peak": peak, "unit": "GB/s", "peak_source": src,
+                                      "frac": b / (kms / 1e3) / 1e9 / peak if kms > 0 else None}}
+        row["f32_speedup_vs_f64"] = row["f32"]["value"] / row["f64"]["value"]
+        out["engines"][name] = row
+    # the strict guards the reference would apply (reports of the rejected runs)
+    try:
+        rs.propagate(band, 5e-3, rs.RayleighSommerfeldConfig(strict=True))
+        out["rs_strict"] = "passed"
+    except og.OsgpuError as e:
+        out["rs_strict"] = {"error": e.variant,
+                            "max_kernel_step_x": e.report.max_kernel_step_x if e.report else None}
+    fr = fraunhofer.regime_report(band, 50e-3, fraunhofer.FraunhoferConfig())
+    out["fraunhofer_regime"] = {"n_f_x": fr.n_f_x, "max_n_f": fr.max_n_f,
+                                "regime_ok": bool(fr.regime_ok)}
+    if not args.no_cpu_baseline:
+        ref = c2_oracle(band.samples)
+        for name in out["engines"]:
+            for prec in ("f64", "f32"):
+                got = results[(name, prec)]
+                out["engines"][name][prec]["rel_l2_vs_oracle"] = float(
+                    np.linalg.norm(got - ref[name]) / np.linalg.norm(ref[name]))
+    return out
+
+
 # Gerchberg-Saxton batch: 16 targets at 2048^2, each an N x N array (N uniform
 # in 4-16) of Gaussian spots (sigma 2 samples, amplitudes uniform 0.5-1) on a
 # centred pitch of 3/4 of the frame / N; uniform input amplitude, seeded
@@ -625,6 +766,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-gs", action="store_true")
     ap.add_argument("--no-ragged", action="store_true")
+    ap.add_argument("--no-c2", action="store_true", help="no 1024^2 engine-sweep leg")
     ap.add_argument("--no-plans", action="store_true",
                     help="no kernel-spectrum plan legs (the batch with plans, the adjoint "
                          "leg's plans)")
@@ -727,11 +869,7 @@ def main():
     per_launch_ms = d["total_ms"] / d["launches"]
     achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
     all_bytes = sum(v["bytes"] for v in kstats.values())
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(dname)
+    traffic, traffic_src = traffic_of(dname)
 
     # Pass B is bound by FP32 instruction issue, not by HBM: its FFT arithmetic
     # against the nominal FP32 rate of this GPU (SMs x 128 lanes x 2 flops x
@@ -762,7 +900,7 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "peak_source": peak_src,
+                         "traffic_source": traffic_src, "peak_source": peak_src,
                          "bytes_per_launch": per_launch_bytes,
                          "ms_per_launch": per_launch_ms, "compute": compute},
             "kernels": kstats,
@@ -904,6 +1042,10 @@ def main():
     # Gerchberg-Saxton batch
     if not args.no_gs:
         line["gs"] = gs_leg(args, stream)
+
+    # single-plane engine sweep at 1024^2
+    if not args.no_c2:
+        line["c2"] = c2_leg(args)
 
     # accuracy of band 0 against the f64 oracle + bounded CPU baseline
     if rank == 0 and not args.no_cpu_baseline:

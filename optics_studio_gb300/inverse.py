@@ -609,6 +609,37 @@ class SpotArrayEfficiency:
         return self._call(obs, seed[0]), True
 
 
+def shard_bands(n_bands, rank, world):
+    """Band indices of one rank when the bands of a gradient are split over
+    `world` ranks: rank r takes bands r, r + world, ... (independent units;
+    every band lands on exactly one rank)."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank must lie in [0, world)")
+    return list(range(rank, n_bands, world))
+
+
+def grid_gradient_sharded(partial, n_bands, group=None):
+    """grid_gradient (adjoint.rs:268-340) with its bands split over the ranks
+    of a torch.distributed process group: the merit and every frame's
+    contribution are sums over bands, so each rank computes the partial
+    gradient of its own bands (``partial(band_indices) -> ({element: tensor},
+    merit value)``, e.g. ``grid_gradient`` of a renderer and merit built for
+    those bands) and one sum all-reduce per element grid (and one for the
+    merit) gives every rank the gradient of all bands.  The exchange is the
+    only collective of the inverse-design step; it runs on the backend of the
+    group (NCCL on GPUs, gloo on CPUs)."""
+    import torch
+    import torch.distributed as dist
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    grads, value = partial(shard_bands(n_bands, rank, world))
+    for key in sorted(grads):
+        dist.all_reduce(grads[key], op=dist.ReduceOp.SUM, group=group)
+    dev = next(iter(grads.values())).device if grads else "cpu"
+    v = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(v, op=dist.ReduceOp.SUM, group=group)
+    return grads, float(v.item())
+
+
 def gaussian_spot_array(shape, count, pitch, sigma):
     """Target weights of a centred count x count array of Gaussian spots (peak 1,
     standard deviation ``sigma`` samples, ``pitch`` samples apart) on a

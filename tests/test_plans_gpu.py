@@ -218,3 +218,35 @@ def test_plans_with_graph_capture_and_host_batch(plans_on):
     assert plans.stats()["hits"] >= hits0 + 2
     for o, r in zip(hout, refs):
         assert rel_l2(o, r) <= 1e-5
+
+
+def test_shutdown_after_real_work_frees_caches_and_library_stays_usable():
+    """osgpu_shutdown after plans, an encircled-energy merit and batched work:
+    the plan cache is emptied, the pooled scratch is trimmed (free device
+    memory does not drop), and later calls of every kind still work."""
+    import optics_studio_gb300 as og
+    from optics_studio_gb300 import _ffi
+    plans.clear()
+    plans.enable(1 << 30)
+    ob = band(seed=9)
+    first = gasm.propagate(to_gpu_band(ob), Z, gasm.AsmConfig(), "f32")
+    assert plans.stats()["plans"] == 1
+    obs = inv.Observation(["intensity"], [LAM], [(0.0, 0.0)], (N, N), (D, D),
+                          torch.from_numpy(np.abs(ob.samples)[None, None, None] ** 2).cuda())
+    ee = inv.EncircledEnergyMerit(100e-6)
+    v0 = ee.evaluate(obs)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    _ffi.check(og.lib().osgpu_shutdown())
+    free1 = torch.cuda.mem_get_info()[0]
+    assert plans.stats()["plans"] == 0 and plans.stats()["bytes"] == 0
+    assert free1 >= free0
+    # usable again: a plan is rebuilt, the merit re-sorts its order
+    again = gasm.propagate(to_gpu_band(ob), Z, gasm.AsmConfig(), "f32")
+    np.testing.assert_array_equal(first.samples, again.samples)
+    assert plans.stats()["builds"] >= 1
+    assert ee.evaluate(obs) == v0
+    plans.disable()
+    plans.clear()
+    plain = gasm.propagate(to_gpu_band(ob), Z, gasm.AsmConfig(), "f64")
+    assert rel_l2(plain.samples, oasm.propagate(ob, Z).samples) <= 1e-12
