@@ -20,7 +20,7 @@ SOURCES = ["prop_kernels.cu", "prop_fast.cu", "api.cu", "host_analysis.cpp", "no
            "inverse_kernels.cu", "gs_fast.cu"]
 HEADERS = ["fft_smem.cuh", "fft_reg.cuh", "elements.cuh", "prop_kernels.cuh", "osgpu_types.h",
            "host_analysis.h", "inverse_kernels.cuh",
-           "gs_fast.cuh"]
+           "gs_fast.cuh", "tma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                 "-I" + os.path.join(ROOT, "include")] + os.environ.get("OSGPU_NVCC_FLAGS", "").split()

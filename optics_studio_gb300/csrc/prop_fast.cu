@@ -14,6 +14,10 @@
 #include "fft_reg.cuh"
 #include "prop_kernels.cuh"
 #include "elements.cuh"
+#include "tma.cuh"
+
+#include <cudaTypedefs.h>
+#include <cstdint>
 
 namespace osgpu {
 
@@ -711,6 +715,121 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(Pro
   }
 }
 
+// Pass A, persistent, with the next tile's rows prefetched by bulk async
+// copies: for a complex64 input with a precomputed chain transmission, the
+// CTA (4 groups, one row each) walks 4-row tiles; the tile's 4 input rows
+// and 4 transmission rows (each a contiguous 4 nx-sample run) arrive in
+// shared memory through two untiled bulk copies (cp.async.bulk, one mbarrier
+// each).  The transmission run is consumed first (x t formed in place), so
+// the next tile's transmission is requested at once; the input run is free
+// after the last sub-transform has read it, and the next tile's input is
+// requested there, so both copies overlap the current tile's transforms.
+// The sub-transform tiles leave as in k_passA_tile (32-byte runs of the
+// column-major spectrum).  Every wait is bounded (status bit 8 on timeout).
+template <int M>
+__global__ void __launch_bounds__(4 * (M / 16), 1) k_passA_bulk(PropArgs a) {
+  constexpr int R = 4;
+  constexpr int T = M / 16;
+  constexpr int SBT = tile_stride<M>();
+  constexpr int NT = R * T;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int nx = a.nx, ny = a.ny, rx = a.ax.r;
+  const int n_tiles = ny / R;
+  const unsigned run_bytes = (unsigned)(R * nx) * 8u;
+  float2* xin = reinterpret_cast<float2*>(smem_raw);  // R rows of nx (input, then x t)
+  float2* trs = xin + R * M;                          // R rows of nx (transmission)
+  float2* tws = trs + R * M;
+  float2* bufs = tws + TwLay<M>::SIZE;
+  float2* tb = bufs + R * SBT;
+  float2* tq = tb + rx * T;
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(tq + rx * 16);  // [in, trans]
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  float2* buf = bufs + g * SBT;
+  float2* W = reinterpret_cast<float2*>(a.work);
+  const float2* gin = reinterpret_cast<const float2*>(a.in);
+  if (threadIdx.x == 0) {
+    tma::mbar_init(bar, 1);
+    tma::mbar_init(bar + 1, 1);
+  }
+  pdl_trigger();
+  copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
+  load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
+  __syncthreads();  // barriers initialised
+  // The transmission comes from the auxiliary stream, joined before this
+  // launch, so its first run is requested at once; the input may be the
+  // output of the kernel just before this one, so it waits for that kernel.
+  int tile = blockIdx.x;
+  if (tile < n_tiles && threadIdx.x == 0) {
+    tma::mbar_expect_tx(bar + 1, run_bytes);
+    tma::load_bulk(trs, a.trans + (size_t)tile * R * nx, run_bytes, bar + 1);
+  }
+  pdl_wait();  // the kernel before this one has completed and its memory is visible
+  if (tile < n_tiles && threadIdx.x == 0) {
+    tma::mbar_expect_tx(bar, run_bytes);
+    tma::load_bulk(xin, gin + (size_t)tile * R * nx, run_bytes, bar);
+  }
+  unsigned ph_in = 0, ph_tr = 0;
+  bool bad = false;
+  for (; tile < n_tiles; tile += gridDim.x) {
+    const bool arrived = tma::mbar_wait(bar + 1, ph_tr) && tma::mbar_wait(bar, ph_in);
+    if (!__syncthreads_and(arrived)) {
+      if (threadIdx.x == 0) {
+        if (a.status) atomicOr(a.status, 8);
+        tma::mbar_wait(bar + 1, ph_tr);
+        tma::mbar_wait(bar, ph_in);
+      }
+      return;
+    }
+    ph_in ^= 1u;
+    ph_tr ^= 1u;
+    // x t in place (R nx staged samples, 16 per thread when nx == M)
+    for (int e = threadIdx.x; e < R * nx; e += NT) {
+      const float2 x = xin[e];
+      bad = bad || !isfinite(x.x) || !isfinite(x.y);
+      xin[e] = cmul(x, trs[e]);
+    }
+    __syncthreads();  // the transmission run is consumed
+    const int nxt = tile + gridDim.x;
+    if (nxt < n_tiles && threadIdx.x == 0) {
+      tma::mbar_expect_tx(bar + 1, run_bytes);
+      tma::load_bulk(trs, a.trans + (size_t)nxt * R * nx, run_bytes, bar + 1);
+    }
+    const int iy0 = tile * R;
+    const float2* xr = xin + g * nx;
+    for (int s = 0; s < rx; ++s) {
+      const float2 wb = tb[s * T + tid];
+      float2 v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int j = tid + T * q;
+        float2 x = (j < nx) ? xr[j] : make_float2(0.f, 0.f);
+        if (s > 0) x = cmul(x, cmul(wb, tq[s * 16 + q]));
+        v[q] = x;
+      }
+      fft1s<M, false>(v, buf, tws, tid, 1 + g, T);
+      group_sync(1 + g, T);  // the transform's last reads of buf are done
+#pragma unroll
+      for (int q = 0; q < 16; ++q) buf[tid + T * q] = v[q];
+      __syncthreads();
+      if (s == rx - 1 && nxt < n_tiles && threadIdx.x == 0) {
+        // every group has read its row for the last time: the next input run
+        tma::mbar_expect_tx(bar, run_bytes);
+        tma::load_bulk(xin, gin + (size_t)nxt * R * nx, run_bytes, bar);
+      }
+      constexpr int HV = R / 2;
+      for (int h = threadIdx.x; h < HV * M; h += NT) {
+        const int p = h / HV, hf = h - p * HV;
+        float4* dst = reinterpret_cast<float4*>(W + (size_t)(rx * p + s) * ny + iy0) + hf;
+        const float2 r0 = bufs[2 * hf * SBT + p], r1 = bufs[(2 * hf + 1) * SBT + p];
+        *dst = make_float4(r0.x, r0.y, r1.x, r1.y);
+      }
+      __syncthreads();
+    }
+  }
+  if (a.status && bad) atomicOr(a.status, 1);
+}
+
 // Pass C on R-row tiles: the CTA stages each sub-transform's R-row tile of
 // the column-major spectrum through shared memory, read in runs
 // W[kx * ny + iy0 .. iy0 + R - 1] of 8 R bytes (with R = 4 the two lanes of a
@@ -802,6 +921,45 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// Pass C epilogue of one output row held by a group (samples tid + T q):
+// the adjoint element plane, the finiteness status, the field and the
+// optional intensities.
+template <int M, bool ADJ>
+__device__ __forceinline__ void pass_c_store(const PropArgs& a, const float2 (&acc)[16], int iy,
+                                             int tid) {
+  constexpr int T = M / 16;
+  const int nx = a.nx, ny = a.ny;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = tid + T * q;
+    if (j >= nx) continue;
+    float2 v = acc[q];
+    const size_t o = (size_t)iy * nx + j;
+    if (ADJ) {  // adjoint element plane (a.adj)
+      const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
+      if (a.trans && a.els.count == 1) {
+        // one element with its precomputed transmission t: v = t u,
+        // grad += -2 Im(conj(mu) v), mu <- conj(t) mu (adjoint_plane's steps)
+        const float2 t = __ldg(a.trans + o);
+        const float vr = u.x * t.x - u.y * t.y, vi = u.x * t.y + u.y * t.x;
+        if (a.adj_grad[0]) reinterpret_cast<float*>(a.adj_grad[0])[o] += -2.f * (v.x * vi + (-v.y) * vr);
+        const float nr = v.x * t.x - v.y * (-t.y), ni = v.x * (-t.y) + v.y * t.x;
+        v = make_float2(nr, ni);
+      } else {
+        adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x,
+                             v.y);
+      }
+    }
+    if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
+    if (a.out) {
+      if (a.out_c128) reinterpret_cast<double2*>(a.out)[o] = make_double2(v.x, v.y);
+      else reinterpret_cast<float2*>(a.out)[o] = v;
+    }
+    if (a.out_intensity) a.out_intensity[o] = v.x * v.x + v.y * v.y;
+    if (a.out_intensity64) a.out_intensity64[o] = (double)v.x * v.x + (double)v.y * v.y;
+  }
+}
+
 template <int M, bool ADJ>
 __global__ void __launch_bounds__(2 * (M / 16), 2) k_passC_pipe(PropArgs a) {
   constexpr int T = M / 16;
@@ -859,38 +1017,95 @@ __global__ void __launch_bounds__(2 * (M / 16), 2) k_passC_pipe(PropArgs a) {
         acc[q] = cadd(acc[q], y);
       }
     }
-    const int iy = 2 * tile + g;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int j = tid + T * q;
-      if (j >= nx) continue;
-      float2 v = acc[q];
-      const size_t o = (size_t)iy * nx + j;
-      if (ADJ) {  // adjoint element plane (a.adj)
-        const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
-        if (a.trans && a.els.count == 1) {
-          // one element with its precomputed transmission t: v = t u,
-          // grad += -2 Im(conj(mu) v), mu <- conj(t) mu (adjoint_plane's steps)
-          const float2 t = __ldg(a.trans + o);
-          const float vr = u.x * t.x - u.y * t.y, vi = u.x * t.y + u.y * t.x;
-          if (a.adj_grad[0]) reinterpret_cast<float*>(a.adj_grad[0])[o] += -2.f * (v.x * vi + (-v.y) * vr);
-          const float nr = v.x * t.x - v.y * (-t.y), ni = v.x * (-t.y) + v.y * t.x;
-          v = make_float2(nr, ni);
-        } else {
-          adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x,
-                               v.y);
-        }
-      }
-      if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
-      if (a.out) {
-        if (a.out_c128) reinterpret_cast<double2*>(a.out)[o] = make_double2(v.x, v.y);
-        else reinterpret_cast<float2*>(a.out)[o] = v;
-      }
-      if (a.out_intensity) a.out_intensity[o] = v.x * v.x + v.y * v.y;
-      if (a.out_intensity64) a.out_intensity64[o] = (double)v.x * v.x + (double)v.y * v.y;
-    }
+    pass_c_store<M, ADJ>(a, acc, 2 * tile + g, tid);
   }
   cp_async_wait_all();  // no copy outlives the CTA
+}
+
+// Pass C with TMA-staged tiles: the same persistent 2-row-tile walk as
+// k_passC_pipe, but each sub-transform's tile (2 rows x M spectral columns,
+// column-major spectrum) arrives through the tensor-memory accelerator: one
+// thread issues M / 256 three-dimensional box copies (iy: 2, s: 1, p: 256 of
+// the spectrum viewed as [p][s][iy]) into the staging buffer, completing an
+// mbarrier with the tile's bytes, while the groups transform the previous
+// tile.  The strided gather costs no load instructions, registers or LSU
+// issue slots in the threads.  Every wait is bounded: a tile that does not
+// arrive sets status bit 8 and the CTA leaves.
+template <int M, bool ADJ>
+__global__ void __launch_bounds__(2 * (M / 16), 2)
+    k_passC_tma(PropArgs a, const __grid_constant__ CUtensorMap wmap) {
+  constexpr int T = M / 16;
+  constexpr int SBT = tile_stride<M>();
+  constexpr int NT = 2 * T;
+  constexpr unsigned TILE_BYTES = (unsigned)M * 16u;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int ny = a.ny, rx = a.ax.r;
+  const int n_tiles = ny / 2;
+  float4* stage = reinterpret_cast<float4*>(smem_raw);  // column p: (row 0, row 1); 128-B aligned
+  float2* tws = reinterpret_cast<float2*>(stage + M);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  float2* tb = bufs + 2 * SBT;
+  float2* tq = tb + rx * T;
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(tq + rx * 16);
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  float2* buf = bufs + g * SBT;
+  if (threadIdx.x == 0) {
+    tma::prefetch_map(&wmap);
+    tma::mbar_init(bar, 1);
+  }
+  pdl_trigger();
+  copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
+  load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
+  pdl_wait();  // pass B's spectrum is complete
+  __syncthreads();  // the barrier is initialised
+  auto issue = [&](int tile, int s) {  // thread 0 only
+    tma::mbar_expect_tx(bar, TILE_BYTES);
+#pragma unroll 1
+    for (int b = 0; b < M / 256; ++b)
+      tma::load_3d(stage + 256 * b, &wmap, 2 * tile, s, 256 * b, bar);
+  };
+  unsigned phase = 0;
+  int tile = blockIdx.x;
+  if (tile < n_tiles && threadIdx.x == 0) issue(tile, 0);
+  for (; tile < n_tiles; tile += gridDim.x) {
+    float2 acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
+    for (int s = 0; s < rx; ++s) {
+      const bool arrived = tma::mbar_wait(bar, phase);
+      if (!__syncthreads_and(arrived)) {  // the whole CTA leaves together
+        if (threadIdx.x == 0) {
+          if (a.status) atomicOr(a.status, 8);
+          tma::mbar_wait(bar, phase);  // a late copy lands before the CTA's memory is reused
+        }
+        return;
+      }
+      phase ^= 1u;
+      float2 v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const float4 t = stage[tid + T * q];
+        v[q] = g ? make_float2(t.z, t.w) : make_float2(t.x, t.y);
+      }
+      __syncthreads();  // every group holds its row: the buffer takes the next tile
+      int ns = s + 1, nt = tile;
+      if (ns == rx) {
+        ns = 0;
+        nt = tile + gridDim.x;
+      }
+      if (nt < n_tiles && threadIdx.x == 0) issue(nt, ns);
+      fft1s<M, true>(v, buf, tws, tid, 1 + g, T);
+      const float2 wb = tb[s * T + tid];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float2 y = v[q];
+        if (s > 0) y = cmulc(y, cmul(wb, tq[s * 16 + q]));
+        acc[q] = cadd(acc[q], y);
+      }
+    }
+    pass_c_store<M, ADJ>(a, acc, 2 * tile + g, tid);
+  }
 }
 
 template <int M>
@@ -1017,9 +1232,45 @@ cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
   return launchB_mg<M, 1>(a, table, st);
 }
 
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+template <int M>
+size_t smem_abulk(int r) {
+  constexpr int T = M / 16;
+  return (8 * (size_t)M + (size_t)TwLay<M>::SIZE + 4 * (size_t)tile_stride<M>() +
+          (size_t)r * (T + 16)) * sizeof(float2) + 16;
+}
+
+template <int M>
+cudaError_t launch_A_bulk(const PropArgs& a, cudaStream_t st) {
+  const size_t smem = smem_abulk<M>(a.ax.r);
+  cudaError_t e = cudaFuncSetAttribute(k_passA_bulk<M>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int grid = std::min(a.ny / 4, sm_count());
+  ++launch_counter();
+  return launch_pdl(k_passA_bulk<M>, dim3(grid), dim3(4 * (M / 16)), smem, st, a);
+}
+
 template <int M>
 cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
   if constexpr (r4_ok<M>()) {
+    // persistent, bulk-copy prefetch: complex64 input with a precomputed
+    // chain transmission, 16-byte aligned 4-row runs
+    const char* be = getenv("OSGPU_PASSA_BULK");
+    if ((!be || atoi(be) != 0) && a.trans && !a.seed && !a.adj && !a.in_c128 && a.ny % 4 == 0 &&
+        reinterpret_cast<uintptr_t>(a.in) % 16 == 0 &&
+        reinterpret_cast<uintptr_t>(a.trans) % 16 == 0 && smem_abulk<M>(a.ax.r) <= kMaxSmemB)
+      return launch_A_bulk<M>(a, st);
     const char* e = getenv("OSGPU_PASSA_TILE");
     const int R = e ? atoi(e) : 4;
     if (R == 4 && a.ny % 4 == 0 && smem_tile<M, 4>(a.ax.r) <= kMaxSmemB)
@@ -1057,17 +1308,6 @@ size_t smem_cpipe(int r) {
           (size_t)r * (T + 16)) * sizeof(float2);
 }
 
-int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
-
 template <int M, bool ADJ>
 cudaError_t launch_C_pipe(const PropArgs& a, cudaStream_t st) {
   const size_t smem = smem_cpipe<M>(a.ax.r);
@@ -1081,8 +1321,43 @@ cudaError_t launch_C_pipe(const PropArgs& a, cudaStream_t st) {
 }
 
 template <int M>
+size_t smem_ctma(int r) {
+  constexpr int T = M / 16;
+  return (2 * (size_t)M + (size_t)TwLay<M>::SIZE + 2 * (size_t)tile_stride<M>() +
+          (size_t)r * (T + 16)) * sizeof(float2) + 16;
+}
+
+// Pass C through TMA when the tensor map of the spectrum can be encoded;
+// cudaErrorNotSupported tells the caller to take the cp.async kernel.
+template <int M, bool ADJ>
+cudaError_t launch_C_tma(const PropArgs& a, cudaStream_t st) {
+  const unsigned long long dims[3] = {(unsigned long long)a.ny, (unsigned long long)a.ax.r,
+                                      (unsigned long long)M};
+  const unsigned long long strides[2] = {(unsigned long long)a.ny * 8ull,
+                                         (unsigned long long)a.ax.r * a.ny * 8ull};
+  const unsigned box[3] = {2u, 1u, 256u};
+  CUtensorMap map;
+  if (!encode_map_3d_c64(&map, a.work, dims, strides, box)) return cudaErrorNotSupported;
+  const size_t smem = smem_ctma<M>(a.ax.r);
+  cudaError_t e = cudaFuncSetAttribute(k_passC_tma<M, ADJ>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int grid = std::min(a.ny / 2, 2 * sm_count());
+  ++launch_counter();
+  return launch_pdl(k_passC_tma<M, ADJ>, dim3(grid), dim3(2 * (M / 16)), smem, st, a, map);
+}
+
+template <int M>
 cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
   if constexpr (r4_ok<M>()) {
+    // persistent TMA-staged 2-row tiles (needs an even ny: 16-byte box starts)
+    const char* te = getenv("OSGPU_PASSC_TMA");
+    if ((!te || atoi(te) != 0) && a.ny % 2 == 0 && M >= 256 &&
+        reinterpret_cast<uintptr_t>(a.work) % 16 == 0 && smem_ctma<M>(a.ax.r) <= kMaxSmemB) {
+      const cudaError_t e =
+          a.adj ? launch_C_tma<M, true>(a, st) : launch_C_tma<M, false>(a, st);
+      if (e != cudaErrorNotSupported) return e;
+    }
     // persistent pipelined 2-row tiles: 0.120 -> 0.104 ms per 2048^2 band
     const char* pe = getenv("OSGPU_PASSC_PIPE");
     if ((!pe || atoi(pe) != 0) && a.ny % 2 == 0 && smem_cpipe<M>(a.ax.r) <= kMaxSmemB)
@@ -1112,6 +1387,29 @@ cudaError_t launch_stage(void* tw, cudaStream_t st) {
   ++launch_counter();
   k_stage_twiddles<M><<<(TwLay<M>::SIZE + 255) / 256, 256, 0, st>>>(reinterpret_cast<float2*>(tw));
   return cudaGetLastError();
+}
+
+bool encode_map_3d_c64(CUtensorMap* map, const void* base, const unsigned long long dims[3],
+                       const unsigned long long strides[2], const unsigned box[3]) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  if (!fn) return false;
+  const cuuint64_t gdim[3] = {dims[0], dims[1], dims[2]};
+  const cuuint64_t gstr[2] = {strides[0], strides[1]};
+  const cuuint32_t bdim[3] = {box[0], box[1], box[2]};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<void*>(base), gdim, gstr, bdim, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 bool reg_fft_size(int m) {
