@@ -767,6 +767,8 @@ def main():
     ap.add_argument("--no-gs", action="store_true")
     ap.add_argument("--no-ragged", action="store_true")
     ap.add_argument("--no-c2", action="store_true", help="no 1024^2 engine-sweep leg")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="built-in pass schedules instead of measured ones")
     ap.add_argument("--no-plans", action="store_true",
                     help="no kernel-spectrum plan legs (the batch with plans, the adjoint "
                          "leg's plans)")
@@ -804,6 +806,11 @@ def main():
     torch.cuda.set_stream(stream)
     sptr = C.c_void_p(stream.cuda_stream)
     assert sptr.value, "need a non-default CUDA stream"
+
+    if not args.no_autotune:
+        # measured pass schedules: the first (warm-up) batch of each geometry tunes it
+        from optics_studio_gb300 import tuning
+        tuning.enable()
 
     lat = doe_lattice()
     handle = C.c_void_p()
@@ -907,6 +914,9 @@ def main():
             "whole_step_hbm_gbs": all_bytes / prof_steps / (ms_step / 1e3) / 1e9,
             "kernel_stats_steps": prof_steps,
             "clocks": clk, "gpu_launches": int(launches)}
+    if not args.no_autotune:
+        from optics_studio_gb300 import tuning
+        line["schedules"] = tuning.schedules()
 
     # plain FP64 path on the same batch (device resident complex128)
     if not args.no_f64 and rank == 0:
@@ -1046,6 +1056,10 @@ def main():
     # single-plane engine sweep at 1024^2
     if not args.no_c2:
         line["c2"] = c2_leg(args)
+
+    if not args.no_autotune:  # every geometry the legs tuned (headline and ragged sizes)
+        from optics_studio_gb300 import tuning
+        line["schedules"] = tuning.schedules()
 
     # accuracy of band 0 against the f64 oracle + bounded CPU baseline
     if rank == 0 and not args.no_cpu_baseline:

@@ -583,6 +583,35 @@ int osgpu_asm_propagate_noalloc(const void* d_in, void* d_out, const osgpu_grid*
                                 const osgpu_asm_config* cfg, void* stream,
                                 osgpu_asm_report* report);
 
+/* ------------------------------------------------------------- autotuning */
+/* The counterpart of the reference's FftPlanner (src/propagation/fft.rs:41,53,
+ * built on every call there): a measured schedule of the f32 register-FFT
+ * passes per geometry.  Each pass has interchangeable kernel variants
+ * (pass A: bulk, tile4, tile2, g1, g2, g4; pass B: pair, g1, g2, g4; pass C:
+ * tma, pipe, tile2, tile4, g1, g2, g4 -- row tiles, persistent TMA/bulk-copy
+ * kernels, sub-transform groups per CTA) that compute the same transform.
+ * osgpu_autotune_asm times a synthetic batch of the geometry (one element
+ * plane, `lanes` 1: one item, 2: four items on the device batch's two lanes)
+ * under each variant of pass A, then B, then C, starting from the built-in
+ * defaults, and keeps the fastest; later f32 propagations of that geometry
+ * (m, r per axis, nx, ny, lanes) use it.  With osgpu_autotune_config(1) the
+ * device batch tunes every new geometry itself before its first run (not
+ * while its stream is being captured).  Off by default: the built-in
+ * defaults are used.  The environment variables OSGPU_SCHED_A / _B / _C
+ * (variant names) override both. */
+typedef struct {
+  uint32_t mx, rx, my, ry, nx, ny, lanes;
+  char pass_a[8], pass_b[8], pass_c[8];
+  double ms_default; /* synthetic batch under the built-in defaults */
+  double ms_best;    /* under the chosen schedule */
+} osgpu_schedule_info;
+
+int osgpu_autotune_config(int32_t enable);
+int osgpu_autotune_asm(const osgpu_grid* g, double z, const osgpu_asm_config* cfg, int32_t lanes,
+                       osgpu_schedule_info* out);
+int osgpu_autotune_list(osgpu_schedule_info* out, int32_t max_out, int32_t* n_out);
+int osgpu_autotune_clear(void);
+
 /* --------------------------------------------------------------- profiling */
 /* Per-kernel-class CUDA-event timing on the launching stream.  Between
  * osgpu_profile_begin and osgpu_profile_end every pass launch is bracketed by

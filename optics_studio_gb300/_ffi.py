@@ -161,6 +161,13 @@ class PlanStatsC(C.Structure):
                 ("builds", C.c_uint64)]
 
 
+class ScheduleInfoC(C.Structure):
+    _fields_ = [("mx", C.c_uint32), ("rx", C.c_uint32), ("my", C.c_uint32), ("ry", C.c_uint32),
+                ("nx", C.c_uint32), ("ny", C.c_uint32), ("lanes", C.c_uint32),
+                ("pass_a", C.c_char * 8), ("pass_b", C.c_char * 8), ("pass_c", C.c_char * 8),
+                ("ms_default", C.c_double), ("ms_best", C.c_double)]
+
+
 # (name, restype, argtypes) for every symbol of include/osgpu.h
 SIGNATURES = [
     ("osgpu_init", C.c_int, [C.c_int32]),
@@ -287,6 +294,12 @@ SIGNATURES = [
     ("osgpu_plan_cache_config", C.c_int, [C.c_int32, C.c_uint64]),
     ("osgpu_plan_cache_clear", C.c_int, []),
     ("osgpu_plan_cache_stats", C.c_int, [C.POINTER(PlanStatsC)]),
+    ("osgpu_autotune_config", C.c_int, [C.c_int32]),
+    ("osgpu_autotune_asm", C.c_int,
+     [C.POINTER(Grid), C.c_double, C.POINTER(AsmConfigC), C.c_int32, C.POINTER(ScheduleInfoC)]),
+    ("osgpu_autotune_list", C.c_int,
+     [C.POINTER(ScheduleInfoC), C.c_int32, C.POINTER(C.c_int32)]),
+    ("osgpu_autotune_clear", C.c_int, []),
     ("osgpu_profile_begin", C.c_int, []),
     ("osgpu_profile_end", C.c_int, [C.POINTER(KernelStatC), C.c_int32, C.POINTER(C.c_int32)]),
 ]

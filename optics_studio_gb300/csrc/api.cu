@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <array>
 #include <map>
 #include <mutex>
 #include <new>
@@ -94,6 +95,19 @@ struct Context {
   size_t plan_cap = 0, plan_bytes = 0;
   uint64_t plan_tick = 0, plan_hits = 0, plan_builds = 0;
   std::vector<KPlan> plans;
+  // measured schedules of the f32 register-FFT passes (osgpu_autotune_*),
+  // keyed by (m_x, r_x, m_y, r_y, nx, ny, lanes); off by default
+  struct Tuned {
+    Schedule s;
+    double ms_default, ms_best;
+  };
+  bool autotune = false;
+  bool tuning = false;    // a tuning run is in progress (its batches do not tune)
+  bool force_on = false;  // the tuner's forced schedule
+  Schedule force = {0, 0, 0};
+  int lane_mode = 1;      // lanes of the batch being run
+  std::map<std::array<int, 7>, Tuned> tuned;
+  uint64_t tunes = 0;
 };
 
 Context& ctx() {
@@ -713,6 +727,14 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
   a.adj_uin_c128 = j.adj_uin_c128;
   for (int q = 0; q < kMaxElements; ++q) a.adj_grad[q] = j.adj_grad[q];
   a.trans = is_d ? nullptr : j.trans;
+  if (!is_d) {  // schedule of the f32 passes: the tuner's forced one, else a measured one
+    if (c.force_on) {
+      a.sched = c.force;
+    } else if (!c.tuned.empty()) {
+      const auto it = c.tuned.find({a.ax.m, a.ax.r, a.ay.m, a.ay.r, a.nx, a.ny, c.lane_mode});
+      if (it != c.tuned.end()) a.sched = it->second.s;
+    }
+  }
   int rc;
   if ((rc = get_tw(c, a.ax.m, is_d, &a.tw_mx))) return rc;
   if ((rc = get_tw(c, a.ay.m, is_d, &a.tw_my))) return rc;
@@ -1329,6 +1351,9 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
   }
   return OSGPU_OK;
 }
+
+int tune_geometry(Context& c, const osgpu_grid& g, double z, const osgpu_asm_config& cfg,
+                  int lanes, cudaStream_t st);
 
 }  // namespace
 
@@ -2160,7 +2185,32 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
   // auxiliary stream for the per-item tables.  One lane while profiling
   // (per-kernel events) or when OSGPU_LANES=1.
   const char* lenv = getenv("OSGPU_LANES");
-  const int lanes = (n_items > 1 && !c.profiling && !(lenv && atoi(lenv) == 1)) ? 2 : 1;
+  // the schedule key keeps the lane count of the unprofiled run, so a
+  // profiled pass times the kernels that run otherwise
+  const int lanes_key = (n_items > 1 && !(lenv && atoi(lenv) == 1)) ? 2 : 1;
+  const int lanes = c.profiling ? 1 : lanes_key;
+  if (c.autotune && !c.tuning) {
+    // measure the pass schedule of every geometry not seen yet (not while the
+    // stream is being captured: tuning synchronises)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cap));
+    if (cap == cudaStreamCaptureStatusNone && f32)
+      for (int i = 0; i < n_items; ++i)
+        for (int s = 0; s < items[i].n_steps; ++s) {
+          if (items[i].steps[s].z_after == 0.0) continue;
+          osgpu_asm_config sc = *cfg;
+          sc.medium = items[i].steps[s].medium;
+          if ((rc = tune_geometry(c, items[i].grid, items[i].steps[s].z_after, sc, lanes_key,
+                                  st)))
+            return rc;
+        }
+  }
+  struct LaneMode {  // the schedule key of this batch's propagations
+    Context& c;
+    int old;
+    LaneMode(Context& c_, int l) : c(c_), old(c_.lane_mode) { c.lane_mode = l; }
+    ~LaneMode() { c.lane_mode = old; }
+  } lane_mode(c, lanes_key);
   cudaStream_t ls[2] = {st, nullptr};
   if (lanes == 2) {
     if (!c.lane2) CK(cudaStreamCreateWithFlags(&c.lane2, cudaStreamNonBlocking));
@@ -2210,6 +2260,163 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
   for (int l = lanes - 1; l >= 0; --l)
     if ((rc = aux[l].finish())) return join(rc);
   return join(OSGPU_OK);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Measured pass schedule of one f32 ASM geometry (the counterpart of the
+// reference's per-call FftPlanner, fft.rs:41,53, run once per geometry): a
+// synthetic batch of that geometry (`lanes` = 1: one item; 2: four items on
+// the two lanes, as a batch runs them) with one element plane, so the chain
+// transmission exists as in a beamline, is timed with CUDA events under each
+// candidate variant of pass A, then B, then C (coordinate descent from the
+// built-in defaults; a candidate must beat the current choice by 2 %).
+// Every variant computes the same transform; only the kernel differs.
+int tune_geometry(Context& c, const osgpu_grid& g, double z, const osgpu_asm_config& cfg,
+                  int lanes, cudaStream_t st) {
+  osgpu_asm_report r;
+  int rc = asm_resolve(g, z, cfg, r);
+  if (rc == -1) return OSGPU_OK;  // z == 0: nothing to propagate
+  if (rc > 0) return OSGPU_OK;    // the real call reports the error
+  const AxisPlan ax = make_axis((int)g.nx, (int)r.nx_pad), ay = make_axis((int)g.ny, (int)r.ny_pad);
+  if (ax.nst < 0 || ay.nst < 0 || !reg_fft_size(ax.m) || !reg_fft_size(ay.m)) return OSGPU_OK;
+  const std::array<int, 7> key = {ax.m, ax.r, ay.m, ay.r, (int)g.nx, (int)g.ny, lanes};
+  if (c.tuned.count(key)) return OSGPU_OK;
+  const int n_items = lanes == 2 ? 4 : 1;
+  const size_t n = g.nx * g.ny;
+  DBuf fin, fout;
+  CK(fin.alloc(n * 8, st));
+  CK(fout.alloc(n * 8 * n_items, st));
+  CK(cudaMemsetAsync(fin.p, 0, n * 8, st));
+  osgpu_element ap;
+  std::memset(&ap, 0, sizeof(ap));
+  ap.kind = OSGPU_EL_RECTANGULAR_APERTURE;
+  ap.stop = OSGPU_STOP_FIELD;
+  ap.a = ((double)g.nx - 1.0) / 2.0 * g.dx;
+  ap.b = ((double)g.ny - 1.0) / 2.0 * g.dy;
+  const osgpu_step step = {&ap, 1, z, cfg.medium};
+  std::vector<osgpu_trace_item> items(n_items);
+  for (int i = 0; i < n_items; ++i)
+    items[i] = osgpu_trace_item{fin.p, static_cast<char*>(fout.p) + i * n * 8, g, &step, 1};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  struct Guard {
+    Context& c;
+    cudaEvent_t a, b;
+    ~Guard() {
+      c.tuning = false;
+      c.force_on = false;
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } guard{c, e0, e1};
+  c.tuning = true;
+  auto measure = [&](const Schedule& s, double* ms) -> int {
+    c.force_on = true;
+    c.force = s;
+    int rc2 = osgpu_beamline_trace_batch_device(items.data(), n_items, &cfg, OSGPU_C64, st,
+                                                nullptr, 0);  // warm-up
+    if (rc2) return rc2;
+    CK(cudaEventRecord(e0, st));
+    for (int rep = 0; rep < 3; ++rep)
+      if ((rc2 = osgpu_beamline_trace_batch_device(items.data(), n_items, &cfg, OSGPU_C64, st,
+                                                   nullptr, 0)))
+        return rc2;
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t / 3.0;
+    return OSGPU_OK;
+  };
+  Schedule best = {0, 0, 0};
+  double t_best = 0.0;
+  if ((rc = measure(best, &t_best))) return rc;
+  const double t_default = t_best;
+  for (int pass = 0; pass < 3; ++pass)
+    for (int v = 1; v < sched_count(pass); ++v) {
+      Schedule cand = best;
+      (pass == 0 ? cand.a : pass == 1 ? cand.b : cand.c) = v;
+      double t = 0.0;
+      if ((rc = measure(cand, &t))) return rc;
+      if (t < 0.98 * t_best) {
+        best = cand;
+        t_best = t;
+      }
+    }
+  c.tuned[key] = Context::Tuned{best, t_default, t_best};
+  ++c.tunes;
+  return OSGPU_OK;
+}
+
+void fill_info(osgpu_schedule_info& o, const std::array<int, 7>& k, const Context::Tuned& t) {
+  std::memset(&o, 0, sizeof(o));
+  o.mx = k[0];
+  o.rx = k[1];
+  o.my = k[2];
+  o.ry = k[3];
+  o.nx = k[4];
+  o.ny = k[5];
+  o.lanes = k[6];
+  std::snprintf(o.pass_a, sizeof(o.pass_a), "%s", sched_name(0, t.s.a));
+  std::snprintf(o.pass_b, sizeof(o.pass_b), "%s", sched_name(1, t.s.b));
+  std::snprintf(o.pass_c, sizeof(o.pass_c), "%s", sched_name(2, t.s.c));
+  o.ms_default = t.ms_default;
+  o.ms_best = t.ms_best;
+}
+
+}  // namespace
+
+extern "C" {
+
+int osgpu_autotune_config(int32_t enable) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  c.autotune = enable != 0;
+  return OSGPU_OK;
+}
+
+int osgpu_autotune_asm(const osgpu_grid* g, double z, const osgpu_asm_config* cfg, int32_t lanes,
+                       osgpu_schedule_info* out) {
+  if (!g || !cfg || (lanes != 1 && lanes != 2)) return OSGPU_E_BAD_ARGUMENT;
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int rc;
+  if ((rc = ensure_init(c))) return rc;
+  if ((rc = tune_geometry(c, *g, z, *cfg, lanes, c.stream))) return rc;
+  osgpu_asm_report r;
+  if (asm_resolve(*g, z, *cfg, r) != 0) return OSGPU_E_BAD_ARGUMENT;
+  const AxisPlan ax = make_axis((int)g->nx, (int)r.nx_pad);
+  const AxisPlan ay = make_axis((int)g->ny, (int)r.ny_pad);
+  const auto it = c.tuned.find({ax.m, ax.r, ay.m, ay.r, (int)g->nx, (int)g->ny, lanes});
+  if (it == c.tuned.end()) {
+    set_err("geometry has no f32 register-FFT schedule to tune");
+    return OSGPU_E_UNSUPPORTED;
+  }
+  if (out) fill_info(*out, it->first, it->second);
+  return OSGPU_OK;
+}
+
+int osgpu_autotune_list(osgpu_schedule_info* out, int32_t max_out, int32_t* n_out) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  int n = 0;
+  for (const auto& kv : c.tuned) {
+    if (out && n < max_out) fill_info(out[n], kv.first, kv.second);
+    ++n;
+  }
+  if (n_out) *n_out = n;
+  return OSGPU_OK;
+}
+
+int osgpu_autotune_clear(void) {
+  Context& c = ctx();
+  std::lock_guard<std::recursive_mutex> lk(c.mu);
+  c.tuned.clear();
+  return OSGPU_OK;
 }
 
 // ------------------------------------------------------------ graphs

@@ -10,6 +10,7 @@
 // H(kx, |k_y|) for |k_y| <= Py/2 serves both halves of the column.
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "fft_reg.cuh"
 #include "prop_kernels.cuh"
@@ -1141,13 +1142,6 @@ size_t smem_v3(int kind, int r, int table) {
   return n * sizeof(float2);
 }
 
-int env_groups(const char* name, int dflt) {
-  const char* e = getenv(name);
-  if (!e) return dflt;
-  int g = atoi(e);
-  return (g == 1 || g == 2 || g == 4) ? g : dflt;
-}
-
 template <int M, int G>
 cudaError_t launchB_mg(const PropArgs& a, int use_table, cudaStream_t st) {
   const size_t smem = smem_v3<M, G>(1, a.ay.r, use_table);
@@ -1211,11 +1205,53 @@ size_t smem_pair(int r) {
           (size_t)r * (M / 2 + 1)) * sizeof(float2);
 }
 
+const char* const kNamesA[SA_N] = {"default", "bulk", "tile4", "tile2", "g1", "g2", "g4"};
+const char* const kNamesB[SB_N] = {"default", "pair", "g1", "g2", "g4"};
+const char* const kNamesC[SC_N] = {"default", "tma", "pipe", "tile2", "tile4", "g1", "g2", "g4"};
+
+// Variant forced by the environment (OSGPU_SCHED_A/_B/_C = name), else 0.
+int env_variant(const char* var, const char* const* names, int n) {
+  const char* e = getenv(var);
+  if (!e) return 0;
+  for (int v = 1; v < n; ++v)
+    if (!strcmp(e, names[v])) return v;
+  return 0;
+}
+
+template <int M>
+bool B_even(const PropArgs& a) {
+  return ((a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF) && a.h_mode == 1) ||
+         a.engine == ENG_KEVEN;
+}
+
+template <int M>
+int B_table(const PropArgs& a) {
+  return B_even<M>(a) && smem_v3<M, 1>(1, a.ay.r, 1) <= kMaxSmemB ? 1 : 0;
+}
+
+template <int M>
+bool B_ok(int v, const PropArgs& a) {
+  if (v == SB_PAIR)
+    return B_even<M>(a) && (a.ax.P % 2) == 0 && smem_pair<M>(a.ay.r) <= kMaxSmemB;
+  const int want = v == SB_G1 ? 1 : v == SB_G2 ? 2 : 4;
+  return pick_groups<M>(1, a.ay.r, B_table<M>(a), want) == want;
+}
+
+// Default: one CTA per mirror pair of columns for even transfer functions
+// (one H table for two columns), else the generic column kernel.
+template <int M>
+int B_default(const PropArgs& a) {
+  if (B_ok<M>(SB_PAIR, a)) return SB_PAIR;
+  const int g = pick_groups<M>(1, a.ay.r, B_table<M>(a), 2);
+  return g == 4 ? SB_G4 : g == 2 ? SB_G2 : SB_G1;
+}
+
 template <int M>
 cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
-  const bool even =
-      ((a.engine == ENG_ASM || a.engine == ENG_FRESNEL_TF) && a.h_mode == 1) || a.engine == ENG_KEVEN;
-  if (even && (a.ax.P % 2) == 0 && smem_pair<M>(a.ay.r) <= kMaxSmemB && !getenv("OSGPU_NO_PAIR")) {
+  int v = env_variant("OSGPU_SCHED_B", kNamesB, SB_N);
+  if (!v || !B_ok<M>(v, a)) v = a.sched.b;
+  if (!v || !B_ok<M>(v, a)) v = B_default<M>(a);
+  if (v == SB_PAIR) {
     const size_t smem = smem_pair<M>(a.ay.r);
     cudaError_t e = cudaFuncSetAttribute(k_passB_pair<M>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1224,11 +1260,9 @@ cudaError_t launch_B(const PropArgs& a, cudaStream_t st) {
     return launch_pdl(k_passB_pair<M>, dim3(a.ax.P / 2 + 1), dim3(Lay<M, 2>::THREADS), smem, st,
                       a);
   }
-  int table = even ? 1 : 0;
-  if (table && smem_v3<M, 1>(1, a.ay.r, 1) > kMaxSmemB) table = 0;
-  const int g = pick_groups<M>(1, a.ay.r, table, env_groups("OSGPU_GROUPS_B", 2));
-  if (g == 4) return launchB_mg<M, 4>(a, table, st);
-  if (g == 2) return launchB_mg<M, 2>(a, table, st);
+  const int table = B_table<M>(a);
+  if (v == SB_G4) return launchB_mg<M, 4>(a, table, st);
+  if (v == SB_G2) return launchB_mg<M, 2>(a, table, st);
   return launchB_mg<M, 1>(a, table, st);
 }
 
@@ -1262,25 +1296,43 @@ cudaError_t launch_A_bulk(const PropArgs& a, cudaStream_t st) {
 }
 
 template <int M>
-cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
-  if constexpr (r4_ok<M>()) {
-    // persistent, bulk-copy prefetch: complex64 input with a precomputed
-    // chain transmission, 16-byte aligned 4-row runs
-    const char* be = getenv("OSGPU_PASSA_BULK");
-    if ((!be || atoi(be) != 0) && a.trans && !a.seed && !a.adj && !a.in_c128 && a.ny % 4 == 0 &&
-        reinterpret_cast<uintptr_t>(a.in) % 16 == 0 &&
-        reinterpret_cast<uintptr_t>(a.trans) % 16 == 0 && smem_abulk<M>(a.ax.r) <= kMaxSmemB)
-      return launch_A_bulk<M>(a, st);
-    const char* e = getenv("OSGPU_PASSA_TILE");
-    const int R = e ? atoi(e) : 4;
-    if (R == 4 && a.ny % 4 == 0 && smem_tile<M, 4>(a.ax.r) <= kMaxSmemB)
-      return launch_A_tile<M, 4>(a, st);
-    if (R == 2 && a.ny % 2 == 0 && smem_tile<M, 2>(a.ax.r) <= kMaxSmemB)
-      return launch_A_tile<M, 2>(a, st);
+bool A_ok(int v, const PropArgs& a) {
+  if (v == SA_BULK || v == SA_TILE4 || v == SA_TILE2) {
+    if constexpr (!r4_ok<M>()) return false;
+    if (v == SA_BULK)
+      return a.trans && !a.seed && !a.adj && !a.in_c128 && a.ny % 4 == 0 &&
+             reinterpret_cast<uintptr_t>(a.in) % 16 == 0 &&
+             reinterpret_cast<uintptr_t>(a.trans) % 16 == 0 && smem_abulk<M>(a.ax.r) <= kMaxSmemB;
+    if (v == SA_TILE4) return a.ny % 4 == 0 && smem_tile<M, 4>(a.ax.r) <= kMaxSmemB;
+    return a.ny % 2 == 0 && smem_tile<M, 2>(a.ax.r) <= kMaxSmemB;
   }
-  const int g = pick_groups<M>(0, a.ax.r, 0, env_groups("OSGPU_GROUPS_A", 2));
-  if (g == 4) return launchA_mg<M, 4>(a, st);
-  if (g == 2) return launchA_mg<M, 2>(a, st);
+  const int want = v == SA_G1 ? 1 : v == SA_G2 ? 2 : 4;
+  return pick_groups<M>(0, a.ax.r, 0, want) == want;
+}
+
+// Default: 4-row tiles (measured best inside the two-lane batch, where the
+// persistent bulk kernel would hold every SM), else 2-row tiles, else the
+// generic row kernel with up to 2 sub-transform groups.
+template <int M>
+int A_default(const PropArgs& a) {
+  if (A_ok<M>(SA_TILE4, a)) return SA_TILE4;
+  if (A_ok<M>(SA_TILE2, a)) return SA_TILE2;
+  const int g = pick_groups<M>(0, a.ax.r, 0, 2);
+  return g == 4 ? SA_G4 : g == 2 ? SA_G2 : SA_G1;
+}
+
+template <int M>
+cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
+  int v = env_variant("OSGPU_SCHED_A", kNamesA, SA_N);
+  if (!v || !A_ok<M>(v, a)) v = a.sched.a;
+  if (!v || !A_ok<M>(v, a)) v = A_default<M>(a);
+  if constexpr (r4_ok<M>()) {
+    if (v == SA_BULK) return launch_A_bulk<M>(a, st);
+    if (v == SA_TILE4) return launch_A_tile<M, 4>(a, st);
+    if (v == SA_TILE2) return launch_A_tile<M, 2>(a, st);
+  }
+  if (v == SA_G4) return launchA_mg<M, 4>(a, st);
+  if (v == SA_G2) return launchA_mg<M, 2>(a, st);
   return launchA_mg<M, 1>(a, st);
 }
 
@@ -1348,35 +1400,51 @@ cudaError_t launch_C_tma(const PropArgs& a, cudaStream_t st) {
 }
 
 template <int M>
-cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
-  if constexpr (r4_ok<M>()) {
-    // persistent TMA-staged 2-row tiles (needs an even ny: 16-byte box starts)
-    const char* te = getenv("OSGPU_PASSC_TMA");
-    if ((!te || atoi(te) != 0) && a.ny % 2 == 0 && M >= 256 &&
-        reinterpret_cast<uintptr_t>(a.work) % 16 == 0 && smem_ctma<M>(a.ax.r) <= kMaxSmemB) {
-      const cudaError_t e =
-          a.adj ? launch_C_tma<M, true>(a, st) : launch_C_tma<M, false>(a, st);
-      if (e != cudaErrorNotSupported) return e;
-    }
-    // persistent pipelined 2-row tiles: 0.120 -> 0.104 ms per 2048^2 band
-    const char* pe = getenv("OSGPU_PASSC_PIPE");
-    if ((!pe || atoi(pe) != 0) && a.ny % 2 == 0 && smem_cpipe<M>(a.ax.r) <= kMaxSmemB)
-      return a.adj ? launch_C_pipe<M, true>(a, st) : launch_C_pipe<M, false>(a, st);
-    // 2-row tiles (2 CTAs per SM) measured fastest on the 2048^2 workload
-    // without the adjoint epilogue (0.126 -> 0.118 ms per band); the adjoint
-    // epilogue spills in the tile kernels, so it keeps the one-row kernel
-    const char* e = getenv("OSGPU_PASSC_TILE");
-    const int R = e ? atoi(e) : (a.adj ? 0 : 2);
-    if ((R == 2 || R == 4) && a.ny % R == 0) {
-      if (R == 4 && smem_ctile<M, 4, false>(a.ax.r) <= kMaxSmemB)
-        return a.adj ? launch_C_tile<M, 4, true>(a, st) : launch_C_tile<M, 4, false>(a, st);
-      if (R == 2 && smem_ctile<M, 2, false>(a.ax.r) <= kMaxSmemB)
-        return a.adj ? launch_C_tile<M, 2, true>(a, st) : launch_C_tile<M, 2, false>(a, st);
-    }
+bool C_ok(int v, const PropArgs& a) {
+  if (v == SC_TMA || v == SC_PIPE || v == SC_TILE2 || v == SC_TILE4) {
+    if constexpr (!r4_ok<M>()) return false;
+    if (v == SC_TMA)
+      return a.ny % 2 == 0 && reinterpret_cast<uintptr_t>(a.work) % 16 == 0 &&
+             smem_ctma<M>(a.ax.r) <= kMaxSmemB;
+    if (v == SC_PIPE) return a.ny % 2 == 0 && smem_cpipe<M>(a.ax.r) <= kMaxSmemB;
+    if (v == SC_TILE4) return a.ny % 4 == 0 && smem_ctile<M, 4, false>(a.ax.r) <= kMaxSmemB;
+    return a.ny % 2 == 0 && smem_ctile<M, 2, false>(a.ax.r) <= kMaxSmemB;
   }
-  const int g = pick_groups<M>(2, a.ax.r, 0, env_groups("OSGPU_GROUPS_C", 2));
-  if (g == 4) return launchC_mg<M, 4>(a, st);
-  if (g == 2) return launchC_mg<M, 2>(a, st);
+  const int want = v == SC_G1 ? 1 : v == SC_G2 ? 2 : 4;
+  return pick_groups<M>(2, a.ax.r, 0, want) == want;
+}
+
+// Default: the persistent TMA-staged kernel (0.095 -> 0.075 ms per 2048^2
+// band against the cp.async pipeline), else the cp.async pipeline, else the
+// generic row kernel.
+template <int M>
+int C_default(const PropArgs& a) {
+  if (C_ok<M>(SC_TMA, a)) return SC_TMA;
+  if (C_ok<M>(SC_PIPE, a)) return SC_PIPE;
+  const int g = pick_groups<M>(2, a.ax.r, 0, 2);
+  return g == 4 ? SC_G4 : g == 2 ? SC_G2 : SC_G1;
+}
+
+template <int M>
+cudaError_t launch_C(const PropArgs& a, cudaStream_t st) {
+  int v = env_variant("OSGPU_SCHED_C", kNamesC, SC_N);
+  if (!v || !C_ok<M>(v, a)) v = a.sched.c;
+  if (!v || !C_ok<M>(v, a)) v = C_default<M>(a);
+  if constexpr (r4_ok<M>()) {
+    if (v == SC_TMA) {
+      const cudaError_t e = a.adj ? launch_C_tma<M, true>(a, st) : launch_C_tma<M, false>(a, st);
+      if (e != cudaErrorNotSupported) return e;
+      v = SC_PIPE;  // the driver could not encode the tensor map
+    }
+    if (v == SC_PIPE && C_ok<M>(SC_PIPE, a))
+      return a.adj ? launch_C_pipe<M, true>(a, st) : launch_C_pipe<M, false>(a, st);
+    if (v == SC_TILE4)
+      return a.adj ? launch_C_tile<M, 4, true>(a, st) : launch_C_tile<M, 4, false>(a, st);
+    if (v == SC_TILE2)
+      return a.adj ? launch_C_tile<M, 2, true>(a, st) : launch_C_tile<M, 2, false>(a, st);
+  }
+  if (v == SC_G4) return launchC_mg<M, 4>(a, st);
+  if (v == SC_G2) return launchC_mg<M, 2>(a, st);
   return launchC_mg<M, 1>(a, st);
 }
 
@@ -1411,6 +1479,15 @@ bool encode_map_3d_c64(CUtensorMap* map, const void* base, const unsigned long l
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+const char* sched_name(int pass, int v) {
+  if (pass == 0 && v >= 0 && v < SA_N) return kNamesA[v];
+  if (pass == 1 && v >= 0 && v < SB_N) return kNamesB[v];
+  if (pass == 2 && v >= 0 && v < SC_N) return kNamesC[v];
+  return "?";
+}
+
+int sched_count(int pass) { return pass == 0 ? SA_N : pass == 1 ? SB_N : SC_N; }
 
 bool reg_fft_size(int m) {
   return m == 256 || m == 512 || m == 1024 || m == 2048 || m == 4096;

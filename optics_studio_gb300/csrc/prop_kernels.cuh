@@ -9,7 +9,22 @@ namespace osgpu {
 // Pointers are device pointers.  `T` is the arithmetic type (float/double);
 // complex buffers are float2/double2 (input/output may be complex128 while
 // the engine computes in f32: see in_c128/out_c128).
+// Kernel variants of the f32 register-FFT passes.  Every variant of a pass
+// computes the same transform; the schedule names one per pass (0: the
+// built-in default).  Environment overrides OSGPU_SCHED_A / _B / _C (variant
+// names below) take precedence; an ineligible choice falls back to the default.
+enum { SA_DEFAULT = 0, SA_BULK, SA_TILE4, SA_TILE2, SA_G1, SA_G2, SA_G4, SA_N };
+enum { SB_DEFAULT = 0, SB_PAIR, SB_G1, SB_G2, SB_G4, SB_N };
+enum { SC_DEFAULT = 0, SC_TMA, SC_PIPE, SC_TILE2, SC_TILE4, SC_G1, SC_G2, SC_G4, SC_N };
+struct Schedule {
+  int a, b, c;
+};
+// Variant names (index = enum value) of pass 0 (A), 1 (B), 2 (C).
+const char* sched_name(int pass, int v);
+int sched_count(int pass);
+
 struct PropArgs {
+  Schedule sched;  // host-side choice of pass variants (not read by kernels)
   int nx, ny;
   double dx, dy;
   AxisPlan ax, ay;

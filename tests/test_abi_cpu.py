@@ -47,6 +47,7 @@ STRUCTS = {
     "osgpu_gs_config": "GsConfigC", "osgpu_gs_record": "GsRecordC",
     "osgpu_gs_result": "GsResultC", "osgpu_gs_item": "GsItemC",
     "osgpu_host_trace_item": "HostTraceItemC", "osgpu_plan_stats": "PlanStatsC",
+    "osgpu_schedule_info": "ScheduleInfoC",
 }
 
 
