@@ -87,8 +87,12 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.first = threading.Event()
 
     def start(self):
+        """Starts sampling and returns once nvidia-smi delivers its first
+        sample (at most 5 s), so its start-up does not fall into the timed
+        region that follows."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
@@ -96,12 +100,14 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=5.0)
         except (OSError, FileNotFoundError):
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
 
     def stop(self):
         if not self.proc:
@@ -957,7 +963,7 @@ def main():
         def e2e_step():
             ffi.check(L.osgpu_beamline_trace_batch(hitems, NBANDS, cfg, ffi.F32, None, 0))
 
-        for _ in range(2):
+        for _ in range(3):
             e2e_step()
         barrier()
         nrep = max(1, min(args.steps, 10))

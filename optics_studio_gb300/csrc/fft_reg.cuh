@@ -153,6 +153,27 @@ __device__ __forceinline__ void dft16(float2* v) {
 
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
 
+// Twiddle powers w^q, q = 1..15, from w^1 and w^4 read from the table
+// (products of at most three table values, so within a few f32 ulps of the
+// table's own values): 2 shared-memory reads instead of 15.
+__device__ __forceinline__ void tw_powers16(float2 w1, float2 w4, float2 (&w)[16]) {
+  w[1] = w1;
+  w[2] = cmul(w1, w1);
+  w[3] = cmul(w[2], w1);
+  w[4] = w4;
+  w[5] = cmul(w4, w1);
+  w[6] = cmul(w4, w[2]);
+  w[7] = cmul(w4, w[3]);
+  w[8] = cmul(w4, w4);
+  w[9] = cmul(w[8], w1);
+  w[10] = cmul(w[8], w[2]);
+  w[11] = cmul(w[8], w[3]);
+  w[12] = cmul(w[8], w4);
+  w[13] = cmul(w[12], w1);
+  w[14] = cmul(w[12], w[2]);
+  w[15] = cmul(w[12], w[3]);
+}
+
 template <int M> struct Plan {
   static constexpr int T = M / 16;
   static constexpr int E = ilog2(M);
@@ -247,8 +268,17 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
     group_sync(bar_id, bar_count);
+#ifdef OSGPU_TW_REC
+    {
+      float2 w[16];
+      tw_powers16(tk[0], tk[3 * Ns], w);
+#pragma unroll
+      for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], w[q]);
+    }
+#else
 #pragma unroll
     for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tk[(q - 1) * Ns]);
+#endif
     dft16<INV>(v);
     const int base = (tid - k) * 16 + k;
     float2* bs = buf + (base + (base >> 4));
@@ -276,6 +306,19 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
       float2 u[RF];
 #pragma unroll
       for (int q = 0; q < RF; ++q) u[q] = bj[FP * q];
+#ifdef OSGPU_TW_REC
+      if (RF == 8) {  // w^2..w^7 from w^1: one table read instead of seven
+        const float2 w1 = tl[T * i];
+        const float2 w2 = cmul(w1, w1), w3 = cmul(w2, w1), w4 = cmul(w2, w2);
+        u[1] = twiddle<INV>(u[1], w1);
+        u[2] = twiddle<INV>(u[2], w2);
+        u[3] = twiddle<INV>(u[3], w3);
+        u[4] = twiddle<INV>(u[4], w4);
+        u[5] = twiddle<INV>(u[5], cmul(w4, w1));
+        u[6] = twiddle<INV>(u[6], cmul(w4, w2));
+        u[7] = twiddle<INV>(u[7], cmul(w4, w3));
+      } else
+#endif
 #pragma unroll
       for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], tl[(q - 1) * NSF + T * i]);
       if (RF == 2) dft2<INV>(u[0], u[1]);
