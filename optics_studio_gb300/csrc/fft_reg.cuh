@@ -236,6 +236,9 @@ __device__ __forceinline__ void group_sync(int id, int nthreads) {
 }
 
 // One transform of length M by the T = M/16 threads with local index tid.
+// TWREC: the middle stage's twiddles w^q from w^1 and w^4 and a final
+// radix-8 stage's from w^1 (cmul products, fewer shared-memory reads; pass B
+// uses it, where shared-memory wavefronts are the tighter resource).
 // buf: one padded shared buffer of Plan<M>::SMEM float2 owned by this
 // transform (padded index i + i/16 keeps the transposed stores conflict
 // free); tws: the stage-ordered twiddle table of TwLay<M> in shared memory.
@@ -243,7 +246,7 @@ __device__ __forceinline__ void group_sync(int id, int nthreads) {
 // and M/RF are multiples of 16, so pad(b + 16 c) = pad(b) + 17 c).  The
 // barrier (bar_id, bar_count) covers the threads of this transform, so the
 // groups of a CTA proceed independently.
-template <int M, bool INV>
+template <int M, bool INV, bool TWREC = false>
 __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2* tws, int tid,
                                       int bar_id, int bar_count) {
   using P = Plan<M>;
@@ -268,17 +271,15 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = bl[TP * q];
     group_sync(bar_id, bar_count);
-#ifdef OSGPU_TW_REC
-    {
+    if constexpr (TWREC) {
       float2 w[16];
       tw_powers16(tk[0], tk[3 * Ns], w);
 #pragma unroll
       for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], w[q]);
-    }
-#else
+    } else {
 #pragma unroll
-    for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tk[(q - 1) * Ns]);
-#endif
+      for (int q = 1; q < 16; ++q) v[q] = twiddle<INV>(v[q], tk[(q - 1) * Ns]);
+    }
     dft16<INV>(v);
     const int base = (tid - k) * 16 + k;
     float2* bs = buf + (base + (base >> 4));
@@ -306,8 +307,7 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
       float2 u[RF];
 #pragma unroll
       for (int q = 0; q < RF; ++q) u[q] = bj[FP * q];
-#ifdef OSGPU_TW_REC
-      if (RF == 8) {  // w^2..w^7 from w^1: one table read instead of seven
+      if (TWREC && RF == 8) {  // w^2..w^7 from w^1: one table read instead of seven
         const float2 w1 = tl[T * i];
         const float2 w2 = cmul(w1, w1), w3 = cmul(w2, w1), w4 = cmul(w2, w2);
         u[1] = twiddle<INV>(u[1], w1);
@@ -318,7 +318,6 @@ __device__ __forceinline__ void fft1s(float2 (&v)[16], float2* buf, const float2
         u[6] = twiddle<INV>(u[6], cmul(w4, w2));
         u[7] = twiddle<INV>(u[7], cmul(w4, w3));
       } else
-#endif
 #pragma unroll
       for (int q = 1; q < RF; ++q) u[q] = twiddle<INV>(u[q], tl[(q - 1) * NSF + T * i]);
       if (RF == 2) dft2<INV>(u[0], u[1]);

@@ -387,13 +387,13 @@ __global__ void __launch_bounds__(Lay<M, 2>::THREADS, Lay<M, 2>::MINB)
       if (t > 0) x = cmul(x, cmul(wb, tq[t * 16 + q]));
       v[q] = x;
     }
-    fft1s<M, false>(v, buf, tws, tid, BAR_ID, BAR_N);
+    fft1s<M, false, true>(v, buf, tws, tid, BAR_ID, BAR_N);
     const int hb_lo = t * U + tid;
     const int hb_hi = (t == 0) ? M - tid : (ry - t) * U + M - 1 - tid;
 #pragma unroll
     for (int q = 0; q < 16; ++q)
       v[q] = cmul(v[q], (q < 8) ? htab[hb_lo + T * q] : htab[hb_hi - T * q]);
-    fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
+    fft1s<M, true, true>(v, buf, tws, tid, BAR_ID, BAR_N);
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       float2 y = v[q];
