@@ -321,6 +321,59 @@ int AuxTables::fork(Context& c, cudaStream_t compute, bool second) {
   return OSGPU_OK;
 }
 
+// Two lanes for a batch of independent items: the caller's stream and a
+// second stream forked from it (joined back by join()), each with its own
+// auxiliary stream for the per-item tables.  Item i runs on lane i % n, so one
+// item's passes fill the SMs another's leave idle at the ends of their
+// grids.  One lane for a single item, while profiling (per-kernel events) or
+// with OSGPU_LANES=1.
+struct Lanes {
+  int n = 1;
+  cudaStream_t ls[2] = {nullptr, nullptr};
+  AuxTables aux[2];
+  bool forked = false;
+  static int want(const Context& c, int n_items) {
+    const char* e = getenv("OSGPU_LANES");
+    return (n_items > 1 && !c.profiling && !(e && atoi(e) == 1)) ? 2 : 1;
+  }
+  int fork(Context& c, cudaStream_t st, int lanes) {
+    n = lanes;
+    ls[0] = st;
+    if (n == 2) {
+      if (!c.lane2) CK(cudaStreamCreateWithFlags(&c.lane2, cudaStreamNonBlocking));
+      ls[1] = c.lane2;
+      cudaEvent_t fk = nullptr;
+      CK(cudaEventCreateWithFlags(&fk, cudaEventDisableTiming));
+      CK(cudaEventRecord(fk, st));
+      CK(cudaStreamWaitEvent(ls[1], fk, 0));
+      cudaEventDestroy(fk);
+      forked = true;
+    }
+    int rc;
+    for (int l = 0; l < n; ++l)
+      if ((rc = aux[l].fork(c, ls[l], l == 1))) return rc;
+    return OSGPU_OK;
+  }
+  int finish() {
+    int rc;
+    for (int l = n - 1; l >= 0; --l)
+      if ((rc = aux[l].finish())) return rc;
+    return OSGPU_OK;
+  }
+  // the second lane's work joins the caller's stream (also on error paths)
+  void join() {
+    if (!forked) return;
+    cudaEvent_t jn = nullptr;
+    if (cudaEventCreateWithFlags(&jn, cudaEventDisableTiming) == cudaSuccess) {
+      cudaEventRecord(jn, ls[1]);
+      cudaStreamWaitEvent(ls[0], jn, 0);
+      cudaEventDestroy(jn);
+    }
+    forked = false;
+  }
+  ~Lanes() { join(); }
+};
+
 int build_elements(Context& c, const osgpu_element* els, int n, const osgpu_grid& g,
                    Elements& E, cudaStream_t st) {
   std::memset(&E.list, 0, sizeof(E.list));
@@ -759,7 +812,7 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
   } else if (j.engine == ENG_KSEP) {
     o_hx = carve(Px * es);
     o_hy = carve(Py * es);
-    o_tmp = carve(2 * (Px + Py) * 16);
+    o_tmp = carve(3 * (Px + Py) * 16);
   } else if (j.engine == ENG_KSPEC) {
     o_ks = carve(Px * Py * es);
     o_tmp = carve((2 * Px * Py + Px + Py) * 16);
@@ -2178,17 +2231,11 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
       return OSGPU_E_BAD_ARGUMENT;
     if (it.grid.nx == 0 || it.grid.ny == 0) return OSGPU_E_EMPTY_GRID;
   }
-  // Items are independent: two lanes (the caller's stream and a second
-  // stream forked from it and joined back at the end) take alternate items,
-  // so one item's passes fill the SMs that the other's leave idle at the
-  // ends of their grids.  Each lane has its own scratch and its own
-  // auxiliary stream for the per-item tables.  One lane while profiling
-  // (per-kernel events) or when OSGPU_LANES=1.
+  // Items are independent: they alternate over two lanes (Lanes).  The
+  // schedule key keeps the lane count of the unprofiled run, so a profiled
+  // pass times the kernels that run otherwise.
   const char* lenv = getenv("OSGPU_LANES");
-  // the schedule key keeps the lane count of the unprofiled run, so a
-  // profiled pass times the kernels that run otherwise
   const int lanes_key = (n_items > 1 && !(lenv && atoi(lenv) == 1)) ? 2 : 1;
-  const int lanes = c.profiling ? 1 : lanes_key;
   if (c.autotune && !c.tuning) {
     // measure the pass schedule of every geometry not seen yet (not while the
     // stream is being captured: tuning synchronises)
@@ -2211,35 +2258,12 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
     LaneMode(Context& c_, int l) : c(c_), old(c_.lane_mode) { c.lane_mode = l; }
     ~LaneMode() { c.lane_mode = old; }
   } lane_mode(c, lanes_key);
-  cudaStream_t ls[2] = {st, nullptr};
-  if (lanes == 2) {
-    if (!c.lane2) CK(cudaStreamCreateWithFlags(&c.lane2, cudaStreamNonBlocking));
-    ls[1] = c.lane2;
-    cudaEvent_t fk = nullptr;
-    CK(cudaEventCreateWithFlags(&fk, cudaEventDisableTiming));
-    CK(cudaEventRecord(fk, st));
-    CK(cudaStreamWaitEvent(ls[1], fk, 0));
-    cudaEventDestroy(fk);
-  }
-  AuxTables aux[2];
-  for (int l = 0; l < lanes; ++l)
-    if ((rc = aux[l].fork(c, ls[l], l == 1))) return rc;
-  // on an error return the second lane is still joined back into `st`
-  auto join = [&](int rc0) {
-    if (lanes == 2) {
-      cudaEvent_t jn = nullptr;
-      if (cudaEventCreateWithFlags(&jn, cudaEventDisableTiming) == cudaSuccess) {
-        cudaEventRecord(jn, ls[1]);
-        cudaStreamWaitEvent(st, jn, 0);
-        cudaEventDestroy(jn);
-      }
-    }
-    return rc0;
-  };
+  Lanes lanes;
+  if ((rc = lanes.fork(c, st, Lanes::want(c, n_items)))) return rc;
   for (int i = 0; i < n_items; ++i) {
     const osgpu_trace_item& it = items[i];
-    AuxTables& ax = aux[i % lanes];
-    if ((rc = ax.begin())) return join(rc);
+    AuxTables& ax = lanes.aux[i % lanes.n];
+    if ((rc = ax.begin())) return rc;
     std::vector<Elements> E;
     std::vector<osgpu_asm_report> R;
     rc = prepare_trace(c, nullptr, 0, it.grid, it.steps, it.n_steps, *cfg, f32, E, R, ax.ax);
@@ -2248,18 +2272,18 @@ int osgpu_beamline_trace_batch_device(const osgpu_trace_item* items, int32_t n_i
         reports[(size_t)i * reports_stride + s] = R[s];
     if (rc) {
       set_err("batch item %d: %s", i, t_err);
-      return join(rc);
+      return rc;
     }
-    if ((rc = ax.ready())) return join(rc);
+    if ((rc = ax.ready())) return rc;
     std::vector<Elements>& Ei = ax.take(E);
     if ((rc = run_trace(c, it.d_in, c128, it.d_out, c128, it.grid, it.steps, it.n_steps, Ei, R,
-                        *cfg, f32, ls[i % lanes])))
-      return join(rc);
-    if ((rc = ax.end())) return join(rc);
+                        *cfg, f32, lanes.ls[i % lanes.n])))
+      return rc;
+    if ((rc = ax.end())) return rc;
   }
-  for (int l = lanes - 1; l >= 0; --l)
-    if ((rc = aux[l].finish())) return join(rc);
-  return join(OSGPU_OK);
+  rc = lanes.finish();
+  lanes.join();
+  return rc;
 }
 
 }  // extern "C"
@@ -2548,10 +2572,12 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
       record = true;
     }
   }
-  AuxTables aux;
-  if ((rc = aux.fork(c, st))) return rc;
+  Lanes lanes;  // frames write their own planes and intensities: independent
+  if ((rc = lanes.fork(c, st, Lanes::want(c, n_frames)))) return rc;
   for (int f = 0; f < n_frames; ++f) {
     const osgpu_frame& fr = frames[f];
+    AuxTables& aux = lanes.aux[f % lanes.n];
+    const cudaStream_t lst = lanes.ls[f % lanes.n];
     if ((rc = aux.begin())) return rc;
     std::vector<Elements> E0;
     std::vector<osgpu_asm_report> R;
@@ -2569,19 +2595,21 @@ int osgpu_render_batch_device(const osgpu_frame* frames, int32_t n_frames,
     if ((rc = make_chains(fr.steps, fr.n_steps, E, f32, ch))) return rc;
     const size_t pl = (fr.grid.nx * fr.grid.ny * es + 255) & ~(size_t)255;
     DBuf work;
-    if (!record) CK(work.alloc(pl, st));
+    if (!record) CK(work.alloc(pl, lst));
     char* base = record ? reinterpret_cast<char*>(tape->buf) + tape->off[f] : nullptr;
     auto plane = [&](int k) -> void* {
       return record ? static_cast<void*>(base + (size_t)k * pl) : work.p;
     };
-    if ((rc = forward_frame(c, fr, E, R, ch, *cfg, f32, c128, plane, record, st))) return rc;
+    if ((rc = forward_frame(c, fr, E, R, ch, *cfg, f32, c128, plane, record, lst))) return rc;
     if ((rc = aux.end())) return rc;
   }
   if (record) {
     tape->valid = 1;
     tape->dtype = dtype;
   }
-  return aux.finish();
+  rc = lanes.finish();
+  lanes.join();
+  return rc;
 }
 
 int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
@@ -2614,11 +2642,28 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
   cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   const int f32 = dtype == OSGPU_C64, c128 = dtype == OSGPU_C128;
   const size_t es = c128 ? 16 : 8;
-  AuxTables aux;
-  if ((rc = aux.fork(c, st))) return rc;
+  const size_t rs = c128 ? 8 : 4;  // bytes per gradient value
+  Lanes lanes;
+  if ((rc = lanes.fork(c, st, Lanes::want(c, n_frames)))) return rc;
+  // Frames accumulate into shared gradient arrays (grid_gradient's sum), so
+  // the second lane accumulates into zeroed scratch copies of them, added to
+  // the caller's arrays once both lanes are done.
+  std::map<void*, size_t> gsize;  // caller's gradient array -> values
+  std::map<void*, DBuf> gscr;  // caller's array -> lane-2 scratch
+  auto lane_grad = [&](void* p, size_t n) -> int {
+    if (!p || gscr.count(p)) return OSGPU_OK;
+    DBuf& b = gscr[p];
+    CK(b.alloc(n * rs, lanes.ls[1]));
+    CK(cudaMemsetAsync(b.p, 0, n * rs, lanes.ls[1]));
+    gsize[p] = n;
+    return OSGPU_OK;
+  };
   for (int f = 0; f < n_frames; ++f) {
     const osgpu_frame& fr = frames[f];
     const osgpu_grid& g = fr.grid;
+    const int lane = f % lanes.n;
+    AuxTables& aux = lanes.aux[lane];
+    st = lanes.ls[lane];
     if ((rc = aux.begin())) return rc;
     std::vector<Elements> E0;
     std::vector<osgpu_asm_report> R;
@@ -2648,9 +2693,15 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
     auto uin = [&](int k) -> const void* {
       return k == 0 ? fr.d_source : static_cast<const void*>(base + (size_t)(k - 1) * pl);
     };
+    if (lane == 1)
+      for (const Chain& cn : ch)
+        for (int q = 0; q < cn.list.count; ++q)
+          if (fr.d_grad && (rc = lane_grad(fr.d_grad[cn.flat[q]], g.nx * g.ny))) return rc;
     auto grads = [&](const Chain& cn, void** out) {
-      for (int q = 0; q < kMaxElements; ++q)
-        out[q] = (q < cn.list.count && fr.d_grad) ? fr.d_grad[cn.flat[q]] : nullptr;
+      for (int q = 0; q < kMaxElements; ++q) {
+        void* p = (q < cn.list.count && fr.d_grad) ? fr.d_grad[cn.flat[q]] : nullptr;
+        out[q] = (p && lane == 1) ? gscr[p].p : p;
+      }
     };
     const int seed_f64 = c128;
     DBuf mu;
@@ -2702,7 +2753,14 @@ int osgpu_push_back_batch_device(const osgpu_frame* frames, int32_t n_frames,
     }
     if ((rc = aux.end())) return rc;
   }
-  return aux.finish();
+  st = lanes.ls[0];
+  if ((rc = lanes.finish())) return rc;
+  lanes.join();
+  for (auto& kv : gscr) {  // the second lane's sums into the caller's arrays
+    CK(launch_add_real(kv.first, kv.second.p, c128, gsize[kv.first], st));
+    kv.second.s = st;  // freed after the add, in the caller's stream order
+  }
+  return OSGPU_OK;
 }
 
 namespace {

@@ -651,6 +651,15 @@ __global__ void k_plane_wave(void* out, int c128, int nx, int ny, double dx, dou
   }
 }
 
+// dst[k] += src[k] (real arrays of one dtype)
+__global__ void k_add_real(void* dst, const void* src, int f64, uint64_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    if (f64) reinterpret_cast<double*>(dst)[k] += reinterpret_cast<const double*>(src)[k];
+    else reinterpret_cast<float*>(dst)[k] += reinterpret_cast<const float*>(src)[k];
+  }
+}
+
 __global__ void k_fill(void* out, int c128, size_t n, double re, double im) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
        k += (size_t)gridDim.x * blockDim.x)
@@ -694,6 +703,12 @@ cudaError_t launch_adjoint_seed_plane(const void* uin, int uin_c128, const Eleme
   else
     k_adjoint_seed_plane<double><<<red_blocks(n), kRedThreads, 0, st>>>(
         uin, uin_c128, els, grads, seed, seed_f64, scale, nx, ny, dx, dy, mu_out, mu_c128);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add_real(void* dst, const void* src, int f64, uint64_t n, cudaStream_t st) {
+  OSGPU_LAUNCH;
+  k_add_real<<<red_blocks(n), kRedThreads, 0, st>>>(dst, src, f64, n);
   return cudaGetLastError();
 }
 

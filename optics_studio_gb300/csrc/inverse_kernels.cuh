@@ -81,6 +81,8 @@ cudaError_t launch_adjoint_seed_plane(const void* uin, int uin_c128, const Eleme
                                       const AdjGrads& grads, const void* seed, int seed_f64,
                                       double scale, int nx, int ny, double dx, double dy,
                                       void* mu_out, int mu_c128, int f32, cudaStream_t st);
+// dst[k] += src[k] over n real values (f64 or f32)
+cudaError_t launch_add_real(void* dst, const void* src, int f64, uint64_t n, cudaStream_t st);
 // Scratch (device) needed by the reductions below for n_frames frames.
 size_t reduce_scratch_bytes(int n_frames);
 // out[f] = sum over win of frame f (f = 0..nf-1)

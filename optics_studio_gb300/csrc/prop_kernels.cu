@@ -837,15 +837,25 @@ __device__ __forceinline__ double dft_coord(int i, int n, double d) {
 
 // Direct length-n DFT of one row (used for the two 1-D chirp spectra of the
 // separable Fresnel kernel; O(n^2) once per (lambda, z, grid)).
-__global__ void k_chirp_dft(int n, double d, double A, const double2* tw, double2* out,
-                            double pre_re, double pre_im) {
+// chirp[j] = e^{i A x_j^2} at the DFT-order coordinates (computed once, not
+// per output bin)
+__global__ void k_chirp_vals(int n, double d, double A, double2* chirp) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double x = dft_coord(j, n, d);
+  double s, c;
+  sincos(__dmul_rn(A, __dmul_rn(x, x)), &s, &c);
+  chirp[j] = make_double2(c, s);
+}
+
+__global__ void k_chirp_dft(int n, const double2* __restrict__ chirp, const double2* tw,
+                            double2* out, double pre_re, double pre_im) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   double sr = 0.0, si = 0.0;
   for (int j = 0; j < n; ++j) {
-    const double x = dft_coord(j, n, d);
-    double s, c;
-    sincos(__dmul_rn(A, __dmul_rn(x, x)), &s, &c);
+    const double2 cs = __ldg(chirp + j);
+    const double c = cs.x, s = cs.y;
     const double2 w = tw[(int)(((long long)j * k) % n)];
     sr += c * w.x - s * w.y;
     si += c * w.y + s * w.x;
@@ -867,12 +877,14 @@ __global__ void k_cast_c128(const double2* src, void* dst, size_t n) {
 // h = pref e^{i pi (x^2+y^2)/(lam z)} (reference fresnel.rs:312-338).
 template <typename T>
 cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp, cudaStream_t st) {
-  // tmp: (Px + Py) double2 twiddles + (Px + Py) double2 results
+  // tmp: (Px + Py) double2 twiddles, results and chirp samples each
   const int Px = a.ax.P, Py = a.ay.P;
   double2* twx = reinterpret_cast<double2*>(tmp);
   double2* twy = twx + Px;
   double2* ox = twy + Py;
   double2* oy = ox + Px;
+  double2* cx = oy + Py;
+  double2* cy = cx + Px;
   cudaError_t e = launch_twiddles(twx, Px, 1, st);
   if (e != cudaSuccess) return e;
   e = launch_twiddles(twy, Py, 1, st);
@@ -886,9 +898,13 @@ cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp
   const double pr = sin(kz) / lz * (a.dx * a.dy) * a.scale;
   const double pi_ = -cos(kz) / lz * (a.dx * a.dy) * a.scale;
   COUNT_LAUNCH();
-  k_chirp_dft<<<(Px + 127) / 128, 128, 0, st>>>(Px, a.dx, A, twx, ox, pr, pi_);
+  k_chirp_vals<<<(Px + 127) / 128, 128, 0, st>>>(Px, a.dx, A, cx);
   COUNT_LAUNCH();
-  k_chirp_dft<<<(Py + 127) / 128, 128, 0, st>>>(Py, a.dy, A, twy, oy, 1.0, 0.0);
+  k_chirp_vals<<<(Py + 127) / 128, 128, 0, st>>>(Py, a.dy, A, cy);
+  COUNT_LAUNCH();
+  k_chirp_dft<<<(Px + 127) / 128, 128, 0, st>>>(Px, cx, twx, ox, pr, pi_);
+  COUNT_LAUNCH();
+  k_chirp_dft<<<(Py + 127) / 128, 128, 0, st>>>(Py, cy, twy, oy, 1.0, 0.0);
   COUNT_LAUNCH();
   k_cast_c128<T><<<(Px + 255) / 256, 256, 0, st>>>(ox, hx, Px);
   COUNT_LAUNCH();
