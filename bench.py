@@ -438,7 +438,7 @@ def ragged_leg(args, stream):
     L = og.lib()
     rng = np.random.default_rng(RAGGED_SEED)
     arr = (ffi.TraceItemC * RAGGED_ITEMS)()
-    keep, samples, pads = [], 0, []
+    keep, samples = [], 0
     cfg = ffi.AsmConfigC(2.0, 1, 1, 8.0, 1.0)
     for i in range(RAGGED_ITEMS):
         n = int(rng.choice([256, 512, 1024, 2048]))
@@ -453,10 +453,6 @@ def ragged_leg(args, stream):
         keep += [tin, tout, steps]
         arr[i] = ffi.TraceItemC(tin.data_ptr(), tout.data_ptr(), ffi.Grid(n, n, DX, DX, lam),
                                 steps, 1)
-        rep = ffi.AsmReportC()
-        ffi.check(L.osgpu_asm_sampling_report(C.byref(ffi.Grid(n, n, DX, DX, lam)), z,
-                                              C.byref(cfg), C.byref(rep)))
-        pads.append(int(rep.nx_pad))
         samples += n * n
     sptr = C.c_void_p(stream.cuda_stream)
     g = C.c_void_p()
@@ -484,9 +480,22 @@ def ragged_leg(args, stream):
     sides = {}
     for i in range(RAGGED_ITEMS):
         sides[int(arr[i].grid.nx)] = sides.get(int(arr[i].grid.nx), 0) + 1
+    # padded size of every item after the strict densification ladder (the
+    # reports of one batch call), for the algorithmic bytes
+    reps = (ffi.AsmReportC * RAGGED_ITEMS)()
+    ffi.check(L.osgpu_beamline_trace_batch_device(arr, RAGGED_ITEMS, cfg, ffi.C64, sptr, reps, 1))
+    torch.cuda.synchronize()
+    padded = [int(reps[i].nx_pad) for i in range(RAGGED_ITEMS)]
+    nbytes = sum(prop_bytes(int(arr[i].grid.nx), padded[i]) for i in range(RAGGED_ITEMS))
+    peak, src = hbm_peak()
+    achieved = nbytes / (ms_graph / 1e3) / 1e9
     return {"value": RAGGED_ITEMS / (ms_graph / 1e3), "unit": "propagations/s",
             "ms_per_batch_graph": ms_graph, "ms_per_batch_direct": ms_direct,
-            "items": RAGGED_ITEMS, "sides": sides, "padded_sides": sorted(set(pads)),
+            "roofline": {"bound": "hbm", "bytes_per_batch": nbytes, "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": src,
+                         "note": "s (2 n^2 + 4 n P) per item at its strict padded size P"},
+            "items": RAGGED_ITEMS, "sides": sides, "padded_sides": sorted(set(padded)),
             "workload": "64 ASM items, side {256..2048}, z log-uniform 1 mm-1 m, Gaussian waist "
                         "50-500 um, dx 3 um, 450-650 nm, complex64, one captured CUDA graph"}
 
