@@ -2104,11 +2104,14 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   }
   const int f32 = precision == OSGPU_F32;
   const cudaStream_t cs = c.stream, si = c.copy_in, so = c.copy_out;
-  // two device slots each way; the copy streams run ahead of the compute stream
+  // Items alternate over the compute lanes (Lanes); each lane has two device
+  // slots each way, and the copy streams run ahead of the compute lanes.
   // f32: complex64 slots beside the complex128 ones; the conversions run on
   // the copy streams, so the passes read and write complex64
-  DBuf din[2], dout[2], din64[2], dout64[2];
-  for (int k = 0; k < 2; ++k) {
+  const int n_lanes = Lanes::want(c, n_items);
+  const int S = 2 * n_lanes;  // slot of item i: i % S, lane: i % n_lanes
+  DBuf din[4], dout[4], din64[4], dout64[4];
+  for (int k = 0; k < S; ++k) {
     CK(din[k].alloc(max_n * 16, cs));
     CK(dout[k].alloc(max_n * 16, cs));
     if (f32) {
@@ -2118,21 +2121,23 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   }
   CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), cs));
   CK(cudaStreamSynchronize(cs));  // slots allocated before the copy streams use them
-  // element tables of item i on the auxiliary stream, overlapped with item i - 1
-  AuxTables aux;
-  if ((rc = aux.fork(c, cs))) return rc;
-  cudaEvent_t ev_in[2], ev_comp[2], ev_out[2];
-  for (int k = 0; k < 2; ++k) {
+  // element tables of item i on the lane's auxiliary stream, overlapped with item i - lanes
+  Lanes lanes;
+  if ((rc = lanes.fork(c, cs, n_lanes))) return rc;
+  cudaEvent_t ev_in[4], ev_comp[4], ev_out[4];
+  for (int k = 0; k < S; ++k) {
     CK(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_comp[k], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_out[k], cudaEventDisableTiming));
   }
   auto release = [&]() {
     cudaStreamSynchronize(si);
-    cudaStreamSynchronize(aux.ax);
-    cudaStreamSynchronize(cs);
+    for (int l = 0; l < lanes.n; ++l) {
+      cudaStreamSynchronize(lanes.aux[l].ax);
+      cudaStreamSynchronize(lanes.ls[l]);
+    }
     cudaStreamSynchronize(so);
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < S; ++k) {
       cudaEventDestroy(ev_in[k]);
       cudaEventDestroy(ev_comp[k]);
       cudaEventDestroy(ev_out[k]);
@@ -2140,7 +2145,10 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   };
   for (int i = 0; i < n_items; ++i) {
     const osgpu_host_trace_item& it = items[i];
-    const int k = i & 1;
+    const int k = i % S;
+    const int l = i % lanes.n;
+    AuxTables& aux = lanes.aux[l];
+    const cudaStream_t ls = lanes.ls[l];
     const size_t bytes = (size_t)(it.grid.nx * it.grid.ny) * 16;
     if ((rc = aux.begin())) {
       release();
@@ -2164,24 +2172,24 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
     }
     std::vector<Elements>& Ei = aux.take(E);
     cudaError_t e = cudaSuccess;
-    if (i >= 2) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - 2
+    if (i >= S) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - S
     if (e == cudaSuccess) e = cudaMemcpyAsync(din[k].p, it.in, bytes, cudaMemcpyHostToDevice, si);
     if (e == cudaSuccess && f32) e = launch_c128_to_c64(din[k].p, din64[k].p, bytes / 16, si);
     if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], si);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_in[k], 0);
-    if (e == cudaSuccess && i >= 2) e = cudaStreamWaitEvent(cs, ev_out[k], 0);  // out slot drained
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ls, ev_in[k], 0);
+    if (e == cudaSuccess && i >= S) e = cudaStreamWaitEvent(ls, ev_out[k], 0);  // out slot drained
     if (e != cudaSuccess) {
       release();
       return cuda_fail(e, "batch copy in");
     }
     if ((rc = f32 ? run_trace(c, din64[k].p, 0, dout64[k].p, 0, it.grid, it.steps, it.n_steps,
-                              Ei, R, *cfg, f32, cs)
+                              Ei, R, *cfg, f32, ls)
                   : run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, Ei, R,
-                              *cfg, f32, cs))) {
+                              *cfg, f32, ls))) {
       release();
       return rc;
     }
-    e = cudaEventRecord(ev_comp[k], cs);
+    e = cudaEventRecord(ev_comp[k], ls);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(so, ev_comp[k], 0);
     if (e == cudaSuccess && f32) e = launch_c64_to_c128(dout64[k].p, dout[k].p, bytes / 16, so);
     if (e == cudaSuccess) e = cudaMemcpyAsync(it.out, dout[k].p, bytes, cudaMemcpyDeviceToHost, so);
@@ -2195,10 +2203,11 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
       return cuda_fail(e, "batch copy out");
     }
   }
-  if ((rc = aux.finish())) {
+  if ((rc = lanes.finish())) {
     release();
     return rc;
   }
+  lanes.join();
   int status = 0;
   cudaError_t e = cudaStreamSynchronize(so);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, cs);
