@@ -1314,6 +1314,8 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
   a.hi = (float)cfg.hi;
   a.wrap = (cfg.hi - cfg.lo >= 2.0 * PI) ? 1 : 0;
   a.intensity_only = 0;
+  a.w_base = base + o_W;
+  a.w_stride = per;
   const double bytes_cols = (double)n * (2 * 8 + 4) * n_items;
   const double bytes_rows = (double)n * (2 * 8 + 4 + 4 + 4 + 1) * n_items;
   {
@@ -1378,6 +1380,15 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
     }
   }
   CK(cudaStreamSynchronize(st));
+  {  // a row pass whose staged inputs never arrived marked its items
+    std::vector<GsState> hf(n_items);
+    CK(cudaMemcpy(hf.data(), S, sizeof(GsState) * n_items, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n_items; ++i)
+      if (hf[i].fault) {
+        set_err("GS item %d: a staged row-pass input did not arrive (bounded wait ran out)", i);
+        return OSGPU_E_CUDA;
+      }
+  }
   for (int i = 0; i < n_items; ++i) {
     osgpu_gs_item& it = items[i];
     const GsState& h = hs[i];

@@ -16,10 +16,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "fft_reg.cuh"
 #include "gs_fast.cuh"
 #include "inverse_kernels.cuh"
+#include "tma.cuh"
 
 namespace osgpu {
 
@@ -171,63 +173,25 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
   }
 }
 
+// One row unit of the fused GS row pass after its inputs are in place (v:
+// the group's spectrum row when iterating, ph / am: its phase and amplitude
+// samples tid + T q): inverse row FFT, conj(pre), the DOE-plane update, the
+// next mask and pre, forward row FFT, the spectrum tile written back.
 template <int M, int G>
-__global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
-    k_gs_rows(const GsFastItem* __restrict__ items, GsFastArgs a, int iterate, int n_items) {
+__device__ __forceinline__ void gs_row_unit(const GsFastItem& it, const GsFastArgs& a,
+                                            int iterate, int iy0, int g, int tid,
+                                            float2 (&v)[16], float (&ph)[16],
+                                            const float (&am)[16], float2* buf, float2* bufs,
+                                            const float2* tws, double* red, int blk) {
   constexpr int T = M / 16;
-  constexpr int NB = M / G;  // CTAs' worth of rows per item
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* tws = reinterpret_cast<float2*>(smem_raw);
-  float2* bufs = tws + TwLay<M>::SIZE;
-  double* red = reinterpret_cast<double*>(bufs + G * GsLay<M, G>::SB);
-  const int g = threadIdx.x / T, tid = threadIdx.x - g * T;
+  constexpr int NB = M / G;
+  constexpr bool kTile = (G == 4) && (T % 32 == 0);
   const int BAR_ID = (T % 32 == 0) ? 1 + g : 1;
   const int BAR_N = (T % 32 == 0) ? T : GsLay<M, G>::THREADS;
-  float2* buf = bufs + g * GsLay<M, G>::SB;
-  {  // stage-ordered table stored behind the M-point table
-    const float2* twm = reinterpret_cast<const float2*>(a.tw);
-    for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
-  }
-  // persistent: the CTA walks (item, row block) units, the twiddles loaded once
-  for (int u = blockIdx.x; u < NB * n_items; u += gridDim.x) {
-  const GsFastItem& it = items[u / NB];
-  const int blk = u - (u / NB) * NB;
-  if (iterate && it.state->stop) continue;
-  const int iy0 = blk * G, iy = iy0 + g;
+  const int iy = iy0 + g;
   const float2 py = __ldg(it.pry + iy);
   float* __restrict__ prow = it.phase + (size_t)iy * M;
-  // 4-row tiles: the spectrum moves through the groups' exchange buffers in
-  // 32-byte runs W[kx * M + iy0 .. iy0 + 3] (one sector per request)
-  constexpr bool kTile = (G == 4) && (T % 32 == 0);
-  float2 v[16];
-  float ph[16], am[16];
   float d2 = 0.f;
-  if (iterate) {
-    if (kTile) {
-      // the two lanes of a pair read the two 16-byte halves of one 32-byte run
-      constexpr int SB = GsLay<M, G>::SB;
-      for (int h = threadIdx.x; h < 2 * M; h += blockDim.x) {
-        const int p = h >> 1, hf = h & 1;
-        const float4 a0 = reinterpret_cast<const float4*>(it.W + (size_t)p * M + iy0)[hf];
-        bufs[2 * hf * SB + p] = make_float2(a0.x, a0.y);
-        bufs[(2 * hf + 1) * SB + p] = make_float2(a0.z, a0.w);
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < 16; ++q) v[q] = it.W[(size_t)(tid + T * q) * M + iy];
-    }
-  }
-  // per-sample inputs issued before the transform (no store precedes them)
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    ph[q] = prow[tid + T * q];
-    am[q] = __ldg(it.amask + (size_t)iy * M + tid + T * q);
-  }
-  __syncthreads();
-  if (iterate && kTile) {
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = buf[tid + T * q];
-  }
   if (iterate) {
     fft1s<M, true>(v, buf, tws, tid, BAR_ID, BAR_N);
   }
@@ -273,7 +237,158 @@ __global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
     for (int q = 0; q < 16; ++q) it.W[(size_t)(tid + T * q) * M + iy] = v[q];
   }
   if (iterate) cta_sum(d2, it.part_row, 0, red, blk, NB);
+  (void)NB;
+}
+
+template <int M, int G>
+__global__ void __launch_bounds__(GsLay<M, G>::THREADS, GsLay<M, G>::MINB)
+    k_gs_rows(const GsFastItem* __restrict__ items, GsFastArgs a, int iterate, int n_items) {
+  constexpr int T = M / 16;
+  constexpr int NB = M / G;  // CTAs' worth of rows per item
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  double* red = reinterpret_cast<double*>(bufs + G * GsLay<M, G>::SB);
+  const int g = threadIdx.x / T, tid = threadIdx.x - g * T;
+  float2* buf = bufs + g * GsLay<M, G>::SB;
+  {  // stage-ordered table stored behind the M-point table
+    const float2* twm = reinterpret_cast<const float2*>(a.tw);
+    for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
+  }
+  // persistent: the CTA walks (item, row block) units, the twiddles loaded once
+  for (int u = blockIdx.x; u < NB * n_items; u += gridDim.x) {
+  const GsFastItem& it = items[u / NB];
+  const int blk = u - (u / NB) * NB;
+  if (iterate && it.state->stop) continue;
+  const int iy0 = blk * G, iy = iy0 + g;
+  const float* prow = it.phase + (size_t)iy * M;
+  // 4-row tiles: the spectrum moves through the groups' exchange buffers in
+  // 32-byte runs W[kx * M + iy0 .. iy0 + 3] (one sector per request)
+  constexpr bool kTile = (G == 4) && (T % 32 == 0);
+  float2 v[16];
+  float ph[16], am[16];
+  if (iterate) {
+    if (kTile) {
+      // the two lanes of a pair read the two 16-byte halves of one 32-byte run
+      constexpr int SB = GsLay<M, G>::SB;
+      for (int h = threadIdx.x; h < 2 * M; h += blockDim.x) {
+        const int p = h >> 1, hf = h & 1;
+        const float4 a0 = reinterpret_cast<const float4*>(it.W + (size_t)p * M + iy0)[hf];
+        bufs[2 * hf * SB + p] = make_float2(a0.x, a0.y);
+        bufs[(2 * hf + 1) * SB + p] = make_float2(a0.z, a0.w);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = it.W[(size_t)(tid + T * q) * M + iy];
+    }
+  }
+  // per-sample inputs issued before the transform (no store precedes them)
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    ph[q] = prow[tid + T * q];
+    am[q] = __ldg(it.amask + (size_t)iy * M + tid + T * q);
+  }
+  __syncthreads();
+  if (iterate && kTile) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = buf[tid + T * q];
+  }
+  gs_row_unit<M, G>(it, a, iterate, iy0, g, tid, v, ph, am, buf, bufs, tws, red, blk);
   __syncthreads();  // the next unit's tile gather rewrites the exchange buffers
+  }
+}
+
+// The row pass with its inputs staged by the tensor-memory accelerator: the
+// same persistent walk over (item, 4-row block) units as k_gs_rows (G = 4),
+// but the next unit's inputs arrive in shared memory while the current one
+// is transformed -- its 4-row tile of the column-major spectrum (M / 256
+// three-dimensional box copies, iy 4 x kx 256 x item 1, of the spectra viewed
+// as [item][kx][ky]) and its 4 phase and 4 amplitude rows (two contiguous
+// bulk copies), completing one mbarrier.  Every wait is bounded (status bit
+// of the item's state on timeout: the CTA leaves as a whole).
+template <int M>
+__global__ void __launch_bounds__(GsLay<M, 4>::THREADS, 1)
+    k_gs_rows_tma(const GsFastItem* __restrict__ items, GsFastArgs a, int iterate, int n_items,
+                  const __grid_constant__ CUtensorMap wmap) {
+  constexpr int G = 4;
+  constexpr int T = M / 16;
+  constexpr int NB = M / G;
+  constexpr int SB = GsLay<M, G>::SB;
+  extern __shared__ __align__(128) unsigned char smem_gs_tma[];
+  float4* stw = reinterpret_cast<float4*>(smem_gs_tma);            // [kx][4 rows]: 2 float4 per kx
+  float* stp = reinterpret_cast<float*>(stw + 2 * M);           // 4 phase rows
+  float* sta = stp + 4 * M;                                     // 4 amplitude rows
+  float2* tws = reinterpret_cast<float2*>(sta + 4 * M);
+  float2* bufs = tws + TwLay<M>::SIZE;
+  double* red = reinterpret_cast<double*>(bufs + G * SB);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(red + 32);
+  const int g = threadIdx.x / T, tid = threadIdx.x - g * T;
+  float2* buf = bufs + g * SB;
+  const unsigned rows_bytes = 4u * M * 4u;
+  const unsigned bytes = (iterate ? (unsigned)M * 32u : 0u) + 2u * rows_bytes;
+  if (threadIdx.x == 0) {
+    tma::prefetch_map(&wmap);
+    tma::mbar_init(bar, 1);
+  }
+  {  // stage-ordered table stored behind the M-point table
+    const float2* twm = reinterpret_cast<const float2*>(a.tw);
+    for (int i = threadIdx.x; i < TwLay<M>::SIZE; i += blockDim.x) tws[i] = __ldg(twm + M + i);
+  }
+  __syncthreads();  // the barrier is initialised
+  auto issue = [&](int u) {  // thread 0: the inputs of unit u
+    const int item = u / NB, iy0 = (u - item * NB) * G;
+    const GsFastItem& it = items[item];
+    tma::mbar_expect_tx(bar, bytes);
+    if (iterate)
+#pragma unroll 1
+      for (int b = 0; b < M / 256; ++b) tma::load_3d(stw + 2 * 256 * b, &wmap, iy0, 256 * b, item, bar);
+    tma::load_bulk(stp, it.phase + (size_t)iy0 * M, rows_bytes, bar);
+    tma::load_bulk(sta, it.amask + (size_t)iy0 * M, rows_bytes, bar);
+  };
+  unsigned phase = 0;
+  int u = blockIdx.x;
+  if (u < NB * n_items && threadIdx.x == 0) issue(u);
+  for (; u < NB * n_items; u += gridDim.x) {
+    const GsFastItem& it = items[u / NB];
+    const int blk = u - (u / NB) * NB;
+    const int iy0 = blk * G;
+    const bool arrived = tma::mbar_wait(bar, phase);
+    if (!__syncthreads_and(arrived)) {
+      if (threadIdx.x == 0) {
+        it.state->fault = 1;  // reported by the host after the loop
+        it.state->stop = 1;
+        tma::mbar_wait(bar, phase);  // a late copy lands before the CTA's memory is reused
+      }
+      return;
+    }
+    phase ^= 1u;
+    float2 v[16];
+    float ph[16], am[16];
+    if (iterate) {
+      for (int h = threadIdx.x; h < 2 * M; h += blockDim.x) {
+        const int p = h >> 1, hf = h & 1;
+        const float4 a0 = stw[2 * p + hf];
+        bufs[2 * hf * SB + p] = make_float2(a0.x, a0.y);
+        bufs[(2 * hf + 1) * SB + p] = make_float2(a0.z, a0.w);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      ph[q] = stp[g * M + tid + T * q];
+      am[q] = sta[g * M + tid + T * q];
+    }
+    __syncthreads();  // the staging buffers are consumed: the next unit's inputs
+    const int nu = u + gridDim.x;
+    if (nu < NB * n_items && threadIdx.x == 0) issue(nu);
+    const bool stopped = iterate && it.state->stop;
+    if (!stopped) {
+      if (iterate) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) v[q] = buf[tid + T * q];
+      }
+      gs_row_unit<M, G>(it, a, iterate, iy0, g, tid, v, ph, am, buf, bufs, tws, red, blk);
+    }
+    __syncthreads();  // the next unit's tile rewrites the exchange buffers
   }
 }
 
@@ -311,9 +426,40 @@ cudaError_t launch_cols(const GsFastItem* items, int n_items, const GsFastArgs& 
 }
 
 template <int M>
+size_t gs_rows_tma_smem() {
+  return (size_t)M * 32 + 2 * (size_t)4 * M * 4 + GsLay<M, 4>::SMEM + 16;
+}
+
+template <int M>
 cudaError_t launch_rows(const GsFastItem* items, int n_items, const GsFastArgs& a, int iterate,
                         cudaStream_t st) {
   constexpr int G = (M / 16 * kGR <= 512) ? kGR : 512 / (M / 16);
+  if constexpr (G == 4 && (M / 16) % 32 == 0) {
+    const char* te = getenv("OSGPU_GS_TMA");
+    if ((!te || atoi(te) != 0) && a.w_base && a.w_stride % 16 == 0 &&
+        gs_rows_tma_smem<M>() <= 232448) {
+      const unsigned long long dims[3] = {(unsigned long long)M, (unsigned long long)M,
+                                          (unsigned long long)n_items};
+      const unsigned long long strides[2] = {(unsigned long long)M * 8ull, a.w_stride};
+      const unsigned box[3] = {4u, 256u, 1u};
+      CUtensorMap map;
+      if (encode_map_3d_c64(&map, a.w_base, dims, strides, box)) {
+        const size_t smem = gs_rows_tma_smem<M>();
+        cudaError_t e = cudaFuncSetAttribute(
+            k_gs_rows_tma<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int units = (M / 4) * n_items;
+        const int grid = std::max(1, std::min(units, std::max(1, sms)));
+        ++launch_counter();
+        k_gs_rows_tma<M><<<grid, GsLay<M, 4>::THREADS, smem, st>>>(items, a, iterate, n_items,
+                                                                  map);
+        return cudaGetLastError();
+      }
+    }
+  }
   using L = GsLay<M, G>;
   cudaError_t e = cudaFuncSetAttribute(k_gs_rows<M, G>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM);

@@ -33,6 +33,10 @@ struct GsFastArgs {
   float beta_f, beta_p, lo, hi;
   int wrap;        // hi - lo >= 2 pi (encode_bounds wraps instead of clamping)
   int intensity_only;  // column pass: forward transform and |U|^2 only
+  // every item's W lies at w_base + i w_stride bytes (one allocation; the row
+  // kernel's tensor map of the spectra); null: the row kernel gathers directly
+  const void* w_base;
+  unsigned long long w_stride;
 };
 
 bool gs_fast_size(int m);

@@ -27,6 +27,7 @@ struct GsState {
   int stop;      // converged or iteration cap reached: later kernels return
   int converged;
   int iterations;
+  int fault;     // a staged input of this item never arrived (bounded wait ran out)
 };
 // One history record (layout of osgpu_gs_record).
 struct GsRecordDev {

@@ -733,11 +733,11 @@ __global__ void __launch_bounds__(4 * (M / 16), 1) k_passA_bulk(PropArgs a) {
   constexpr int T = M / 16;
   constexpr int SBT = tile_stride<M>();
   constexpr int NT = R * T;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_abulk[];
   const int nx = a.nx, ny = a.ny, rx = a.ax.r;
   const int n_tiles = ny / R;
   const unsigned run_bytes = (unsigned)(R * nx) * 8u;
-  float2* xin = reinterpret_cast<float2*>(smem_raw);  // R rows of nx (input, then x t)
+  float2* xin = reinterpret_cast<float2*>(smem_abulk);  // R rows of nx (input, then x t)
   float2* trs = xin + R * M;                          // R rows of nx (transmission)
   float2* tws = trs + R * M;
   float2* bufs = tws + TwLay<M>::SIZE;
@@ -967,7 +967,7 @@ __global__ void __launch_bounds__(2 * (M / 16), 2) k_passC_pipe(PropArgs a) {
   constexpr int SBT = tile_stride<M>();
   constexpr int NT = 2 * T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nx = a.nx, ny = a.ny, rx = a.ax.r;
+  const int ny = a.ny, rx = a.ax.r;
   const int n_tiles = ny / 2;
   float2* tws = reinterpret_cast<float2*>(smem_raw);
   float2* bufs = tws + TwLay<M>::SIZE;
@@ -1039,10 +1039,10 @@ __global__ void __launch_bounds__(2 * (M / 16), 2)
   constexpr int SBT = tile_stride<M>();
   constexpr int NT = 2 * T;
   constexpr unsigned TILE_BYTES = (unsigned)M * 16u;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_ctma[];
   const int ny = a.ny, rx = a.ax.r;
   const int n_tiles = ny / 2;
-  float4* stage = reinterpret_cast<float4*>(smem_raw);  // column p: (row 0, row 1); 128-B aligned
+  float4* stage = reinterpret_cast<float4*>(smem_ctma);  // column p: (row 0, row 1); 128-B aligned
   float2* tws = reinterpret_cast<float2*>(stage + M);
   float2* bufs = tws + TwLay<M>::SIZE;
   float2* tb = bufs + 2 * SBT;
@@ -1487,7 +1487,10 @@ const char* sched_name(int pass, int v) {
   return "?";
 }
 
-int sched_count(int pass) { return pass == 0 ? SA_N : pass == 1 ? SB_N : SC_N; }
+int sched_count(int pass) {
+  if (pass == 0) return (int)SA_N;
+  return pass == 1 ? (int)SB_N : (int)SC_N;
+}
 
 bool reg_fft_size(int m) {
   return m == 256 || m == 512 || m == 1024 || m == 2048 || m == 4096;

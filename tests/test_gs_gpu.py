@@ -218,3 +218,23 @@ def test_gs_fused_matches_generic_path_and_patience(monkeypatch):
         assert f.converged == g.converged
         for hf, hg in zip(f.history, g.history):
             assert hf["merit"] == pytest.approx(hg["merit"], rel=1e-4)
+
+
+def test_gs_row_pass_tma_staging_matches_direct_gather(monkeypatch):
+    """The fused row pass with its inputs staged by TMA (spectrum tiles, phase
+    and amplitude rows of the next unit prefetched) computes exactly what the
+    direct-gather row pass computes: identical merit histories and phases."""
+    n = 512
+    u, tamp, init, z = inputs_fraunhofer(n, seed=12)
+    probs = lambda: [fraunhofer_problem(n, u, tamp, init, z, 6),
+                     fraunhofer_problem(n, u, tamp * 0.8, init, z, 6)]
+    monkeypatch.delenv("OSGPU_GS_TMA", raising=False)
+    staged = ggs.run_batch(probs())
+    monkeypatch.setenv("OSGPU_GS_TMA", "0")
+    direct = ggs.run_batch(probs())
+    for s, d in zip(staged, direct):
+        assert [h["merit"] for h in s.history] == [h["merit"] for h in d.history]
+        assert torch.equal(s.phase, d.phase)
+    want = oracle_fraunhofer(n, u, tamp, init, z, 6)
+    for hg, hw in zip(staged[0].history, want.history):
+        assert hg["merit"] == pytest.approx(hw.merit, rel=1e-4)
