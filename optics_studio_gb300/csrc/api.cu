@@ -2116,19 +2116,16 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
   const int f32 = precision == OSGPU_F32;
   const cudaStream_t cs = c.stream, si = c.copy_in, so = c.copy_out;
   // Items alternate over the compute lanes (Lanes); each lane has two device
-  // slots each way, and the copy streams run ahead of the compute lanes.
-  // f32: complex64 slots beside the complex128 ones; the conversions run on
-  // the copy streams, so the passes read and write complex64
+  // slots each way, and the copy streams run ahead of the compute lanes.  The
+  // slots hold the caller's complex128 samples; the f32 engine converts on
+  // its first pass's loads and its last pass's stores (the same roundings as
+  // a separate conversion, without its extra pass over the field)
   const int n_lanes = Lanes::want(c, n_items);
   const int S = 2 * n_lanes;  // slot of item i: i % S, lane: i % n_lanes
-  DBuf din[4], dout[4], din64[4], dout64[4];
+  DBuf din[4], dout[4];
   for (int k = 0; k < S; ++k) {
     CK(din[k].alloc(max_n * 16, cs));
     CK(dout[k].alloc(max_n * 16, cs));
-    if (f32) {
-      CK(din64[k].alloc(max_n * 8, cs));
-      CK(dout64[k].alloc(max_n * 8, cs));
-    }
   }
   CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), cs));
   CK(cudaStreamSynchronize(cs));  // slots allocated before the copy streams use them
@@ -2185,7 +2182,6 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
     cudaError_t e = cudaSuccess;
     if (i >= S) e = cudaStreamWaitEvent(si, ev_comp[k], 0);  // slot k read by item i - S
     if (e == cudaSuccess) e = cudaMemcpyAsync(din[k].p, it.in, bytes, cudaMemcpyHostToDevice, si);
-    if (e == cudaSuccess && f32) e = launch_c128_to_c64(din[k].p, din64[k].p, bytes / 16, si);
     if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], si);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ls, ev_in[k], 0);
     if (e == cudaSuccess && i >= S) e = cudaStreamWaitEvent(ls, ev_out[k], 0);  // out slot drained
@@ -2193,16 +2189,13 @@ int osgpu_beamline_trace_batch(const osgpu_host_trace_item* items, int32_t n_ite
       release();
       return cuda_fail(e, "batch copy in");
     }
-    if ((rc = f32 ? run_trace(c, din64[k].p, 0, dout64[k].p, 0, it.grid, it.steps, it.n_steps,
-                              Ei, R, *cfg, f32, ls)
-                  : run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, Ei, R,
-                              *cfg, f32, ls))) {
+    if ((rc = run_trace(c, din[k].p, 1, dout[k].p, 1, it.grid, it.steps, it.n_steps, Ei, R,
+                        *cfg, f32, ls))) {
       release();
       return rc;
     }
     e = cudaEventRecord(ev_comp[k], ls);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(so, ev_comp[k], 0);
-    if (e == cudaSuccess && f32) e = launch_c64_to_c128(dout64[k].p, dout[k].p, bytes / 16, so);
     if (e == cudaSuccess) e = cudaMemcpyAsync(it.out, dout[k].p, bytes, cudaMemcpyDeviceToHost, so);
     if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], so);
     if (e == cudaSuccess && (rc = aux.end())) {
