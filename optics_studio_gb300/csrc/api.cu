@@ -1322,14 +1322,38 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
     ProfScope ps(c, st, PC_GS_ROWS, bytes_rows);
     CK(launch_gs_rows(DI, n_items, a, 0, st));
   }
+  // The loop state is copied to pinned host memory after every chunk of
+  // iterations, and the host looks at the copy of the chunk before the one
+  // just queued, so the GPU always has a chunk of work ahead of the check
+  // (one extra chunk after every item has stopped: its kernels return at
+  // once for stopped items).
   constexpr int kChunk = 8;
+  struct Pinned {
+    GsState* p = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    ~Pinned() {
+      if (p) cudaFreeHost(p);
+      for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+    }
+  } pin;
+  CK(cudaMallocHost(&pin.p, sizeof(GsState) * 2 * n_items));
+  CK(cudaEventCreateWithFlags(&pin.ev[0], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&pin.ev[1], cudaEventDisableTiming));
+  int pending = -1;
   for (int k = 0; k < max_it; ++k) {
     if (k > 0 && k % kChunk == 0) {
-      CK(cudaMemcpyAsync(hs.data(), S, sizeof(GsState) * n_items, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      bool all = true;
-      for (auto& h : hs) all = all && h.stop;
-      if (all) break;
+      const int b = (k / kChunk) & 1;
+      CK(cudaMemcpyAsync(pin.p + (size_t)b * n_items, S, sizeof(GsState) * n_items,
+                         cudaMemcpyDeviceToHost, st));
+      CK(cudaEventRecord(pin.ev[b], st));
+      if (pending >= 0) {
+        CK(cudaEventSynchronize(pin.ev[pending]));
+        bool all = true;
+        for (int i = 0; i < n_items; ++i) all = all && pin.p[(size_t)pending * n_items + i].stop;
+        if (all) break;
+      }
+      pending = b;
     }
     {
       ProfScope ps(c, st, PC_GS_COLS, bytes_cols);
