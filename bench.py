@@ -685,26 +685,39 @@ def gs_leg(args, stream):
         import optics_studio_gb300 as og
         from optics_studio_gb300 import _ffi as ffi
         L = og.lib()
-        ffi.check(L.osgpu_profile_begin())
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         sols = ggs.run_batch(probs, stream)
         e1.record(stream)
         torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        its = sum(s.iterations for s in sols)
+        # per-kernel device times from a separate profiled call of the same
+        # batch cut to 20 iterations (events around every launch)
+        ffi.check(L.osgpu_profile_begin())
+        ggs.run_batch(problems("f32", range(n_t), 20), stream)
+        torch.cuda.synchronize()
         stats = (ffi.KernelStatC * 16)()
         nst = C.c_int32()
         ffi.check(L.osgpu_profile_end(stats, 16, C.byref(nst)))
-        ms = e0.elapsed_time(e1)
-        its = sum(s.iterations for s in sols)
         kst = {stats[i].name.decode(): {"launches": int(stats[i].launches),
-                                        "total_ms": stats[i].total_ms, "bytes": stats[i].bytes}
+                                        "total_ms": stats[i].total_ms, "bytes": stats[i].bytes,
+                                        "ms_per_launch": stats[i].total_ms / max(1, stats[i].launches)}
                for i in range(nst.value)}
         eff32, uni32 = spot_metrics(sols[0].target_intensity.double().cpu().numpy(),
                                     targets[0][1])
+        peak, src = hbm_peak()
+        gs_bytes = N * N * (8 * 8 + 16)  # per target-iteration: n^2 (8 s + 16), s = 8
         out = {"value": its / (ms / 1e3), "unit": "target-iterations/s", "ms_total": ms,
                "targets": n_t, "iterations_per_target": n_it,
-               "workload": GS_WORKLOAD, "dtype": "f32", "kernels": kst,
+               "workload": GS_WORKLOAD, "dtype": "f32",
+               "kernels_profiled_20_iterations": kst,
+               "roofline": {"bound": "hbm", "bytes_per_target_iteration": gs_bytes,
+                            "achieved": its * gs_bytes / (ms / 1e3) / 1e9, "peak": peak,
+                            "unit": "GB/s", "peak_source": src,
+                            "frac": its * gs_bytes / (ms / 1e3) / 1e9 / peak,
+                            "note": "whole call (set-up, 200 iterations, read-back) timed"},
                "target0": {"efficiency": eff32, "uniformity": uni32}}
         if not args.no_f64:
             t0 = time.perf_counter()
