@@ -58,6 +58,13 @@ WORKLOAD = ("32 bands 450-650 nm x 2048^2, dx 3 um, [16-level DOE, square apertu
             "thin lens f 100 mm, ASM z 100 mm], padded 8192^2")
 
 
+def workload_config(world):
+    """The `config` object of both arms' lines (the same workload)."""
+    return {"workload": WORKLOAD, "bands_per_gpu": NBANDS, "grid": N, "padded": 8192,
+            "l2": "inputs larger than L2 (1 GiB field batch + 134 MB spectrum per band)",
+            "parallelism": f"replicas x{world}"}
+
+
 def set_bands(n):
     global NBANDS, LAMS
     NBANDS = n
@@ -765,7 +772,8 @@ def reference_arm(args):
             "steps_requested": args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "step": f"{workers} bands, one per worker process"},
+            "config": workload_config(world),
+            "step": f"{workers} bands, one per worker process",
             "cpu_baseline": {"value": val, "unit": "propagations/s", "cores": workers,
                              "kind": "port",
                              "sample": f"bands 0-{workers - 1} of the 32 per step (one band per "
@@ -930,9 +938,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "bands_per_gpu": NBANDS, "grid": N, "padded": 8192,
-                       "l2": "inputs larger than L2 (1 GiB field batch + 134 MB spectrum per band)",
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(world),
             "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": traffic_src, "peak_source": peak_src,
