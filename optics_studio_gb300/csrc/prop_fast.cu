@@ -604,27 +604,14 @@ __host__ __device__ constexpr int tile_stride() {
   return Plan<M>::SMEM + 4;
 }
 
+// The R input rows iy0 .. iy0 + R - 1 of a row-tile kernel (R T threads),
+// each sample through the per-sample stage, into xin[r * M + j] (zero past
+// nx).  Loads are batched, then one status check (returns true when a
+// sample is not finite).
 template <int M, int R>
-__global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(PropArgs a) {
-  constexpr int T = M / 16;
-  constexpr int SBT = tile_stride<M>();
-  constexpr int NT = R * T;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nx = a.nx, ny = a.ny, rx = a.ax.r;
-  float2* tws = reinterpret_cast<float2*>(smem_raw);
-  float2* xin = tws + TwLay<M>::SIZE;  // R rows of M
-  float2* bufs = xin + R * M;
-  float2* tb = bufs + R * SBT;
-  float2* tq = tb + rx * T;
-  const int g = threadIdx.x / T;
-  const int tid = threadIdx.x - g * T;
-  const int iy0 = blockIdx.x * R;
-  float2* buf = bufs + g * SBT;
-  float2* W = reinterpret_cast<float2*>(a.work);
-  pdl_trigger();
-  copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
-  load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
-  // inputs of the R rows: loads batched, then one status check
+__device__ __forceinline__ bool pass_a_tile_inputs(const PropArgs& a, float2* xin, int iy0) {
+  constexpr int NT = R * (M / 16);
+  const int nx = a.nx;
   constexpr int KS = R * M / NT;  // 16 samples per thread
   static_assert(KS <= 32, "sample mask is 32 bits");
   bool bad = false;
@@ -685,6 +672,30 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(Pro
 #pragma unroll
     for (int k = 0; k < KS; ++k) xin[threadIdx.x + k * NT] = xs[k];
   }
+  return bad;
+}
+
+template <int M, int R>
+__global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(PropArgs a) {
+  constexpr int T = M / 16;
+  constexpr int SBT = tile_stride<M>();
+  constexpr int NT = R * T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ny = a.ny, rx = a.ax.r;
+  float2* tws = reinterpret_cast<float2*>(smem_raw);
+  float2* xin = tws + TwLay<M>::SIZE;  // R rows of M
+  float2* bufs = xin + R * M;
+  float2* tb = bufs + R * SBT;
+  float2* tq = tb + rx * T;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  const int iy0 = blockIdx.x * R;
+  float2* buf = bufs + g * SBT;
+  float2* W = reinterpret_cast<float2*>(a.work);
+  pdl_trigger();
+  copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
+  load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
+  const bool bad = pass_a_tile_inputs<M, R>(a, xin, iy0);
   if (a.status && bad) atomicOr(a.status, 1);
   pdl_wait();  // the kernel before this one has completed (its workspace is ours to write)
   __syncthreads();
@@ -714,6 +725,73 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passA_tile(Pro
     }
     __syncthreads();
   }
+}
+
+// Pass A on 4-row tiles whose sub-transform tiles leave through TMA tensor
+// stores: the CTA assembles tile s in shared memory in the spectrum's own
+// order (p-major, the 4 rows of one kx adjacent: 32 bytes) and one thread
+// stores it as M/256 boxes (iy 4 x s 1 x p 256) of the 3-D view
+// (iy, s, p) -> W[(rx p + s) ny + iy].  The stores run in the async proxy
+// while the CTA transforms the next sub-transform; the staging buffer is
+// reused only after the previous tile's stores have read it.
+template <int M>
+__global__ void __launch_bounds__(4 * (M / 16), 1)
+    k_passA_tstore(PropArgs a, const __grid_constant__ CUtensorMap wmap) {
+  constexpr int R = 4;
+  constexpr int T = M / 16;
+  constexpr int SBT = tile_stride<M>();
+  constexpr int NT = R * T;
+  extern __shared__ __align__(128) unsigned char smem_atst[];
+  const int rx = a.ax.r;
+  float2* stage = reinterpret_cast<float2*>(smem_atst);  // M x R, p-major
+  float2* tws = stage + R * M;
+  float2* xin = tws + TwLay<M>::SIZE;  // R rows of M
+  float2* bufs = xin + R * M;
+  float2* tb = bufs + R * SBT;
+  float2* tq = tb + rx * T;
+  const int g = threadIdx.x / T;
+  const int tid = threadIdx.x - g * T;
+  const int iy0 = blockIdx.x * R;
+  float2* buf = bufs + g * SBT;
+  if (threadIdx.x == 0) tma::prefetch_map(&wmap);
+  pdl_trigger();
+  copy_stage_twiddles<M>(tws, reinterpret_cast<const float2*>(a.tw_mx), threadIdx.x, NT);
+  load_ptw(tb, tq, reinterpret_cast<const float2*>(a.tw_Px), rx, T);
+  const bool bad = pass_a_tile_inputs<M, R>(a, xin, iy0);
+  if (a.status && bad) atomicOr(a.status, 1);
+  pdl_wait();  // the kernel before this one has completed (its workspace is ours to write)
+  __syncthreads();
+  const float2* xr = xin + g * M;
+  for (int s = 0; s < rx; ++s) {
+    const float2 wb = tb[s * T + tid];
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      float2 x = xr[tid + T * q];
+      if (s > 0) x = cmul(x, cmul(wb, tq[s * 16 + q]));
+      v[q] = x;
+    }
+    fft1s<M, false>(v, buf, tws, tid, 1 + g, T);
+    group_sync(1 + g, T);  // the transform's last reads of buf are done
+#pragma unroll
+    for (int q = 0; q < 16; ++q) buf[tid + T * q] = v[q];
+    if (threadIdx.x == 0) tma::bulk_wait_read();  // the previous tile has left the stage
+    __syncthreads();
+    // stage[4 p + r] = row r's bin p: 16 bytes (two rows) per lane, dense
+    for (int h = threadIdx.x; h < 2 * M; h += NT) {
+      const int p = h >> 1, hf = h & 1;
+      const float2 r0 = bufs[2 * hf * SBT + p], r1 = bufs[(2 * hf + 1) * SBT + p];
+      reinterpret_cast<float4*>(stage)[h] = make_float4(r0.x, r0.y, r1.x, r1.y);
+    }
+    tma::fence_async_shared();  // this thread's stage writes, before the stores read them
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll 1
+      for (int b = 0; b < M / 256; ++b) tma::store_3d(&wmap, stage + b * 256 * R, iy0, s, 256 * b);
+      tma::bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) tma::bulk_wait_all();  // the last tile is written before the CTA leaves
 }
 
 // Pass A, persistent, with the next tile's rows prefetched by bulk async
@@ -1205,7 +1283,8 @@ size_t smem_pair(int r) {
           (size_t)r * (M / 2 + 1)) * sizeof(float2);
 }
 
-const char* const kNamesA[SA_N] = {"default", "bulk", "tile4", "tile2", "g1", "g2", "g4"};
+const char* const kNamesA[SA_N] = {"default", "bulk", "tile4", "tile2", "g1", "g2", "g4",
+                                    "tstore"};
 const char* const kNamesB[SB_N] = {"default", "pair", "g1", "g2", "g4"};
 const char* const kNamesC[SC_N] = {"default", "tma", "pipe", "tile2", "tile4", "g1", "g2", "g4"};
 
@@ -1296,7 +1375,34 @@ cudaError_t launch_A_bulk(const PropArgs& a, cudaStream_t st) {
 }
 
 template <int M>
+size_t smem_atstore(int r) {
+  return smem_tile<M, 4>(r) + 4 * (size_t)M * sizeof(float2);
+}
+
+// cudaErrorNotSupported when the tensor map cannot be encoded (the caller
+// then takes the 4-row tile kernel).
+template <int M>
+cudaError_t launch_A_tstore(const PropArgs& a, cudaStream_t st) {
+  const unsigned long long dims[3] = {(unsigned long long)a.ny, (unsigned long long)a.ax.r,
+                                      (unsigned long long)M};
+  const unsigned long long strides[2] = {(unsigned long long)a.ny * 8ull,
+                                         (unsigned long long)a.ax.r * a.ny * 8ull};
+  const unsigned box[3] = {4u, 1u, 256u};
+  CUtensorMap map;
+  if (!encode_map_3d_c64(&map, a.work, dims, strides, box)) return cudaErrorNotSupported;
+  const size_t smem = smem_atstore<M>(a.ax.r);
+  cudaError_t e = cudaFuncSetAttribute(k_passA_tstore<M>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ++launch_counter();
+  return launch_pdl(k_passA_tstore<M>, dim3(a.ny / 4), dim3(4 * (M / 16)), smem, st, a, map);
+}
+
+template <int M>
 bool A_ok(int v, const PropArgs& a) {
+  if (v == SA_TSTORE)
+    return r4_ok<M>() && a.ny % 4 == 0 && reinterpret_cast<uintptr_t>(a.work) % 16 == 0 &&
+           smem_atstore<M>(a.ax.r) <= kMaxSmemB;
   if (v == SA_BULK || v == SA_TILE4 || v == SA_TILE2) {
     if constexpr (!r4_ok<M>()) return false;
     if (v == SA_BULK)
@@ -1327,6 +1433,11 @@ cudaError_t launch_A(const PropArgs& a, cudaStream_t st) {
   if (!v || !A_ok<M>(v, a)) v = a.sched.a;
   if (!v || !A_ok<M>(v, a)) v = A_default<M>(a);
   if constexpr (r4_ok<M>()) {
+    if (v == SA_TSTORE) {
+      const cudaError_t e = launch_A_tstore<M>(a, st);
+      if (e != cudaErrorNotSupported) return e;
+      v = SA_TILE4;
+    }
     if (v == SA_BULK) return launch_A_bulk<M>(a, st);
     if (v == SA_TILE4) return launch_A_tile<M, 4>(a, st);
     if (v == SA_TILE2) return launch_A_tile<M, 2>(a, st);

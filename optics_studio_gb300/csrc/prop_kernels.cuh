@@ -13,7 +13,7 @@ namespace osgpu {
 // computes the same transform; the schedule names one per pass (0: the
 // built-in default).  Environment overrides OSGPU_SCHED_A / _B / _C (variant
 // names below) take precedence; an ineligible choice falls back to the default.
-enum { SA_DEFAULT = 0, SA_BULK, SA_TILE4, SA_TILE2, SA_G1, SA_G2, SA_G4, SA_N };
+enum { SA_DEFAULT = 0, SA_BULK, SA_TILE4, SA_TILE2, SA_G1, SA_G2, SA_G4, SA_TSTORE, SA_N };
 enum { SB_DEFAULT = 0, SB_PAIR, SB_G1, SB_G2, SB_G4, SB_N };
 enum { SC_DEFAULT = 0, SC_TMA, SC_PIPE, SC_TILE2, SC_TILE4, SC_G1, SC_G2, SC_G4, SC_N };
 struct Schedule {

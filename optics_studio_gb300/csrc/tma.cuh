@@ -80,6 +80,42 @@ __device__ __forceinline__ void load_bulk(void* dst, const void* src, unsigned b
       : "memory");
 }
 
+// 3-D tiled TMA store of one box from shared memory to coordinates
+// (c0, c1, c2), tracked by the issuing thread's bulk-async group.  The
+// writers of the box must have run fence_async_shared() and a barrier with
+// the issuing thread first; coordinates are never negative, and c0 *
+// element size is a multiple of 16 bytes.
+__device__ __forceinline__ void store_3d(const CUtensorMap* map, const void* src, int c0, int c1,
+                                         int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+          reinterpret_cast<unsigned long long>(map)),
+      "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(src))
+      : "memory");
+}
+
+// Close the issuing thread's current group of bulk stores.
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// Until every committed store group of this thread has read its shared-memory
+// source (the source may then be overwritten).
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+// Until every committed store group of this thread has completed its writes.
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// Order this thread's generic-proxy shared-memory writes before later
+// async-proxy (TMA) reads of them.
+__device__ __forceinline__ void fence_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<unsigned long long>(map))
                : "memory");

@@ -32,7 +32,7 @@ from optics_studio_gb300.propagation.asm import AsmConfig  # noqa: E402
 N, D, LAM, Z = 512, 3e-6, 532e-9, 2e-3
 HALF = 0.6e-3
 VARIANTS = {
-    "OSGPU_SCHED_A": ["bulk", "tile4", "tile2", "g1", "g2", "g4"],
+    "OSGPU_SCHED_A": ["bulk", "tstore", "tile4", "tile2", "g1", "g2", "g4"],
     "OSGPU_SCHED_B": ["pair", "g1", "g2", "g4"],
     "OSGPU_SCHED_C": ["tma", "pipe", "tile2", "tile4", "g1", "g2", "g4"],
 }
