@@ -36,6 +36,36 @@ struct Acc {
   __device__ __forceinline__ double value() const { return s + c; }
 };
 
+// Per-thread partial of a sum of f32 products for the f32 engine's
+// reductions, kept as an unevaluated pair hi + lo of f32 values: each product
+// is split exactly (TwoProduct by FMA) and added to hi by TwoSum (Knuth), the
+// rounding errors collecting in lo (the Dot2 scheme of Ogita, Rump and
+// Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005).
+// The partial is as accurate as an FP64 sum of the exact products (relative
+// error ~n 2^-48 for n terms) while every operation runs on the FP32 pipe;
+// the pairs are then folded by the compensated FP64 Acc.  Explicit _rn
+// intrinsics keep the compiler from contracting the error terms.
+struct AccF {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);  // a b - p exactly
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));  // hi + p - s
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+  }
+  // another partial: hi by TwoSum, the rounding error and both lo into lo
+  __device__ __forceinline__ void add(float ohi, float olo) {
+    const float s = __fadd_rn(hi, ohi);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(ohi, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, olo));
+  }
+};
+
 __device__ __forceinline__ Acc shfl_down(const Acc& a, int d) {
   Acc b;
   b.s = __shfl_down_sync(0xffffffffu, a.s, d);
@@ -49,6 +79,40 @@ __device__ Acc block_fold(Acc a) {
   for (int d = 16; d > 0; d >>= 1) a.add(shfl_down(a, d));
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) {
+    ss[w] = a.s;
+    sc[w] = a.c;
+  }
+  __syncthreads();
+  Acc r;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kRedThreads / 32; ++i) {
+      Acc o;
+      o.s = ss[i];
+      o.c = sc[i];
+      r.add(o);
+    }
+  }
+  __syncthreads();
+  return r;
+}
+
+// Block fold of one AccF per thread: the warp's partials combine on the
+// FP32 pipe (AccF::add, five shuffle levels), then each warp's pair enters
+// the compensated FP64 fold once.  The result is valid in thread 0.
+__device__ Acc block_fold_f32(AccF t) {
+  for (int d = 16; d > 0; d >>= 1) {
+    const float ohi = __shfl_down_sync(0xffffffffu, t.hi, d);
+    const float olo = __shfl_down_sync(0xffffffffu, t.lo, d);
+    t.add(ohi, olo);
+  }
+  Acc a;
+  if ((threadIdx.x & 31) == 0) {
+    a.add((double)t.hi);
+    a.add((double)t.lo);
+  }
+  __shared__ double ss[kRedThreads / 32], sc[kRedThreads / 32];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
     ss[w] = a.s;
     sc[w] = a.c;
   }
@@ -196,19 +260,63 @@ __global__ void k_weighted_sums(const void* obs, int f64, uint64_t len, const vo
   const int f = blockIdx.y;
   const size_t base = (size_t)f * len;
   Acc a;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
-       k += (size_t)gridDim.x * blockDim.x) {
-    const double wk = ld_real(w, f64, k);
-    if (wk != 0.0) a.add(wk * ld_real(obs, f64, base + k));
+  // RU grid-stride steps per pass, all loads of a pass issued before its sums
+  // (the terms are added in the plain grid-stride order)
+  constexpr int RU = 4;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if (!f64) {  // f32 frames and weights: FP32-pipe partials (AccF), FP64 fold
+    const float* wf = static_cast<const float*>(w);
+    const float* of = static_cast<const float*>(obs) + base;
+    AccF t;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len; k += RU * stride) {
+      float wv[RU], ov[RU];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) {
+        const size_t kk = k + u * stride;
+        wv[u] = kk < len ? wf[kk] : 0.f;
+        ov[u] = kk < len ? of[kk] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < RU; ++u)
+        if (wv[u] != 0.f) t.add_prod(wv[u], ov[u]);
+    }
+    write_part(part, f, block_fold_f32(t));
+    return;
+  } else {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len; k += RU * stride) {
+      double wv[RU], ov[RU];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) {
+        const size_t kk = k + u * stride;
+        wv[u] = kk < len ? ld_real(w, f64, kk) : 0.0;
+        ov[u] = kk < len ? ld_real(obs, f64, base + kk) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < RU; ++u)
+        if (wv[u] != 0.0) a.add(wv[u] * ov[u]);
+    }
   }
   write_part(part, f, block_fold(a));
 }
 
-// seed_f[k] = coef[f] w[k]
+// seed_f[k] = coef[f] w[k].  For f32 seeds the FP64 coefficient is split into
+// two f32 parts (c = ch + cl to ~2^-48) and the product formed on the FP32
+// pipe, ch w + cl w, then rounded once to f32.
 __global__ void k_weighted_seed(void* seed, int f64, uint64_t len, const void* w,
                                 const double* coef) {
   const int f = blockIdx.y;
   const double c = coef[f];
+  if (!f64) {
+    const float ch = (float)c, cl = (float)(c - (double)ch);
+    const float* wf = static_cast<const float*>(w);
+    float* sf = static_cast<float*>(seed) + (size_t)f * len;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
+         k += (size_t)gridDim.x * blockDim.x) {
+      const float wk = wf[k];
+      sf[k] = __fmaf_rn(cl, wk, __fmul_rn(ch, wk));
+    }
+    return;
+  }
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < len;
        k += (size_t)gridDim.x * blockDim.x)
     st_real(seed, f64, (size_t)f * len + k, c * ld_real(w, f64, k));
@@ -341,17 +449,34 @@ __global__ void k_power(const void* u, int c128, uint64_t n, double* part) {
 // Sum of squares of a real vector.
 __global__ void k_sumsq(const void* g, int f64, uint64_t n, double* part) {
   Acc a;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
-       k += (size_t)gridDim.x * blockDim.x) {
-    const double v = ld_real(g, f64, k);
-    a.add(v * v);
+  if (!f64) {  // f32 vector: FP32-pipe partials (AccF), FP64 fold
+    const float* gf = static_cast<const float*>(g);
+    constexpr int RU = 4;  // loads of RU grid-stride steps in flight together
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    AccF t;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += RU * stride) {
+      float v[RU];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) v[u] = k + u * stride < n ? gf[k + u * stride] : 0.f;
+#pragma unroll
+      for (int u = 0; u < RU; ++u) t.add_prod(v[u], v[u]);
+    }
+    write_part(part, 0, block_fold_f32(t));
+    return;
+  } else {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x) {
+      const double v = ld_real(g, f64, k);
+      a.add(v * v);
+    }
   }
   write_part(part, 0, block_fold(a));
 }
 
-// Final fold of nb partial pairs per frame: out[f] = compensated sum.
+// Final fold of nb partial pairs per frame: out[f] = compensated sum (one
+// block per frame).
 __global__ void k_fold_parts(const double* part, int nb, int nf, double* out) {
-  for (int f = 0; f < nf; ++f) {
+  for (int f = blockIdx.x; f < nf; f += gridDim.x) {
     Acc a;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
       Acc o;
@@ -671,6 +796,16 @@ int red_blocks(uint64_t n) {
   return (int)(b < 1216 ? (b ? b : 1) : 1216);  // <= 8 per SM on 152 SMs
 }
 
+// Blocks for a reduction whose per-thread partials run on the FP32 pipe
+// (AccF, folded by block_fold_f32): about 64 terms per thread (with 4 steps'
+// loads in flight per thread, enough to cover the memory latency), so that
+// the per-block fold (barriers and a short serial FP64 tail in thread 0;
+// the GPU's FP64 rate is a small fraction of its FP32 rate) is amortised.
+int red_blocks_f32(uint64_t n) {
+  const uint64_t b = (n + 64 * kRedThreads - 1) / (64 * kRedThreads);
+  return (int)(b < 1216 ? (b ? b : 1) : 1216);  // the partials' scratch holds 1216 per frame
+}
+
 }  // namespace
 
 #define OSGPU_LAUNCH ++launch_counter()
@@ -723,7 +858,7 @@ cudaError_t launch_window_sums(const void* obs, int f64, int nf, uint64_t len,
   OSGPU_LAUNCH;
   k_window_sums<<<dim3(nb, nf), kRedThreads, 0, st>>>(obs, f64, len, win, scratch);
   OSGPU_LAUNCH;
-  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, nb, nf, out);
+  k_fold_parts<<<nf, kRedThreads, 0, st>>>(scratch, nb, nf, out);
   return cudaGetLastError();
 }
 
@@ -736,11 +871,11 @@ cudaError_t launch_window_seed(void* seed, int f64, int nf, uint64_t len,
 
 cudaError_t launch_weighted_sums(const void* obs, int f64, int nf, uint64_t len, const void* w,
                                  double* scratch, double* out, cudaStream_t st) {
-  const int nb = red_blocks(len);
+  const int nb = f64 ? red_blocks(len) : red_blocks_f32(len);
   OSGPU_LAUNCH;
   k_weighted_sums<<<dim3(nb, nf), kRedThreads, 0, st>>>(obs, f64, len, w, scratch);
   OSGPU_LAUNCH;
-  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, nb, nf, out);
+  k_fold_parts<<<nf, kRedThreads, 0, st>>>(scratch, nb, nf, out);
   return cudaGetLastError();
 }
 
@@ -776,7 +911,7 @@ cudaError_t launch_ee(const void* obs, int f64, int nx, int ny, double dx, doubl
   k_ee_sums<<<blocks, kRedThreads, 0, st>>>(obs, f64, nx, ny, dx, dy, radius, nb, ns, band,
                                             scene, scratch);
   OSGPU_LAUNCH;
-  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 2, out);
+  k_fold_parts<<<2, kRedThreads, 0, st>>>(scratch, blocks, 2, out);
   if (seed) {
     OSGPU_LAUNCH;
     k_ee_seed<<<dim3(blocks, nb * ns), kRedThreads, 0, st>>>(seed, f64, nx, ny, dx, dy, radius,
@@ -976,7 +1111,7 @@ cudaError_t launch_psf_moments(const void* img, int f64, int nx, int ny, double 
   OSGPU_LAUNCH;
   k_psf_moments<<<blocks, kRedThreads, 0, st>>>(img, f64, nx, ny, dx, dy, scratch);
   OSGPU_LAUNCH;
-  k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 2, out2);
+  k_fold_parts<<<2, kRedThreads, 0, st>>>(scratch, blocks, 2, out2);
   return cudaGetLastError();
 }
 
@@ -1015,10 +1150,11 @@ cudaError_t launch_adam(double* x, float* x32, const void* g, int g_f64, double*
                         cudaStream_t st) {
   const int blocks = red_blocks(n);
   if (p.clip) {
+    const int sb = g_f64 ? blocks : red_blocks_f32(n);
     OSGPU_LAUNCH;
-    k_sumsq<<<blocks, kRedThreads, 0, st>>>(g, g_f64, n, scratch);
+    k_sumsq<<<sb, kRedThreads, 0, st>>>(g, g_f64, n, scratch);
     OSGPU_LAUNCH;
-    k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, blocks, 1, norm2);
+    k_fold_parts<<<1, kRedThreads, 0, st>>>(scratch, sb, 1, norm2);
   }
   OSGPU_LAUNCH;
   k_adam<<<blocks, kRedThreads, 0, st>>>(x, x32, g, g_f64, m, v, n, p, norm2);

@@ -1000,6 +1000,31 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// The adjoint epilogue's inputs of output row iy (forward field, element
+// transmission, gradient accumulator) requested into L2 at the start of the
+// row's tile, one prefetch per 128-byte line, so that pass_c_store finds
+// them there after the row's sub-transforms.
+template <int M, bool ADJ>
+__device__ __forceinline__ void pass_c_prefetch(const PropArgs& a, int iy, int tid) {
+  if (!ADJ || !a.trans || a.els.count != 1) return;
+  constexpr int T = M / 16;
+  const int nx = a.nx;
+  const int ue = a.adj_uin_c128 ? 8 : 16;  // samples per 128-byte line of the field
+  const float* grad = reinterpret_cast<const float*>(a.adj_grad[0]);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = tid + T * q;
+    if (j >= nx) continue;
+    const size_t o = (size_t)iy * nx + j;
+    if (j % ue == 0) {
+      const char* pu = static_cast<const char*>(a.adj_uin) + o * (a.adj_uin_c128 ? 16 : 8);
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(pu));
+    }
+    if (j % 16 == 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.trans + o));
+    if (grad && j % 32 == 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(grad + o));
+  }
+}
+
 // Pass C epilogue of one output row held by a group (samples tid + T q):
 // the adjoint element plane, the finiteness status, the field and the
 // optional intensities.
@@ -1008,26 +1033,60 @@ __device__ __forceinline__ void pass_c_store(const PropArgs& a, const float2 (&a
                                              int tid) {
   constexpr int T = M / 16;
   const int nx = a.nx, ny = a.ny;
+  if (ADJ && a.trans && a.els.count == 1) {
+    // one element with its precomputed transmission t: v = t u,
+    // grad += -2 Im(conj(mu) v), mu <- conj(t) mu (adjoint_plane's steps).
+    // The loads of 8 samples go out together, ahead of their stores (a
+    // store may alias a later load, so the compiler keeps them in order).
+    float* grad = reinterpret_cast<float*>(a.adj_grad[0]);
+    constexpr int CH = 8;
+#pragma unroll
+    for (int c0 = 0; c0 < 16; c0 += CH) {
+      float2 u[CH], t[CH];
+      float gv[CH];
+#pragma unroll
+      for (int k = 0; k < CH; ++k) {
+        const int j = tid + T * (c0 + k);
+        const size_t o = (size_t)iy * nx + j;
+        u[k] = t[k] = make_float2(0.f, 0.f);
+        gv[k] = 0.f;
+        if (j < nx) {
+          u[k] = ld_in(a.adj_uin, a.adj_uin_c128, o);
+          t[k] = __ldg(a.trans + o);
+          if (grad) gv[k] = grad[o];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < CH; ++k) {
+        const int j = tid + T * (c0 + k);
+        if (j >= nx) continue;
+        const size_t o = (size_t)iy * nx + j;
+        float2 v = acc[c0 + k];
+        const float vr = u[k].x * t[k].x - u[k].y * t[k].y;
+        const float vi = u[k].x * t[k].y + u[k].y * t[k].x;
+        if (grad) grad[o] = gv[k] + -2.f * (v.x * vi + (-v.y) * vr);
+        const float nr = v.x * t[k].x - v.y * (-t[k].y), ni = v.x * (-t[k].y) + v.y * t[k].x;
+        v = make_float2(nr, ni);
+        if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
+        if (a.out) {
+          if (a.out_c128) reinterpret_cast<double2*>(a.out)[o] = make_double2(v.x, v.y);
+          else reinterpret_cast<float2*>(a.out)[o] = v;
+        }
+        if (a.out_intensity) a.out_intensity[o] = v.x * v.x + v.y * v.y;
+        if (a.out_intensity64) a.out_intensity64[o] = (double)v.x * v.x + (double)v.y * v.y;
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int j = tid + T * q;
     if (j >= nx) continue;
     float2 v = acc[q];
     const size_t o = (size_t)iy * nx + j;
-    if (ADJ) {  // adjoint element plane (a.adj)
+    if (ADJ) {  // adjoint element plane (a.adj), general chain
       const float2 u = ld_in(a.adj_uin, a.adj_uin_c128, o);
-      if (a.trans && a.els.count == 1) {
-        // one element with its precomputed transmission t: v = t u,
-        // grad += -2 Im(conj(mu) v), mu <- conj(t) mu (adjoint_plane's steps)
-        const float2 t = __ldg(a.trans + o);
-        const float vr = u.x * t.x - u.y * t.y, vi = u.x * t.y + u.y * t.x;
-        if (a.adj_grad[0]) reinterpret_cast<float*>(a.adj_grad[0])[o] += -2.f * (v.x * vi + (-v.y) * vr);
-        const float nr = v.x * t.x - v.y * (-t.y), ni = v.x * (-t.y) + v.y * t.x;
-        v = make_float2(nr, ni);
-      } else {
-        adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x,
-                             v.y);
-      }
+      adjoint_plane<float>(a.els, a.adj_grad, j, iy, nx, ny, a.dx, a.dy, o, u.x, u.y, v.x, v.y);
     }
     if (a.status && (!isfinite(v.x) || !isfinite(v.y))) atomicOr(a.status, 2);
     if (a.out) {
@@ -1068,6 +1127,7 @@ __global__ void __launch_bounds__(2 * (M / 16), 2) k_passC_pipe(PropArgs a) {
   int tile = blockIdx.x;
   if (tile < n_tiles) issue(tile, 0);
   for (; tile < n_tiles; tile += gridDim.x) {
+    pass_c_prefetch<M, ADJ>(a, 2 * tile + g, tid);
     float2 acc[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
@@ -1148,6 +1208,7 @@ __global__ void __launch_bounds__(2 * (M / 16), 2)
   int tile = blockIdx.x;
   if (tile < n_tiles && threadIdx.x == 0) issue(tile, 0);
   for (; tile < n_tiles; tile += gridDim.x) {
+    pass_c_prefetch<M, ADJ>(a, 2 * tile + g, tid);
     float2 acc[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.f, 0.f);
