@@ -257,6 +257,30 @@ def adjoint_setup(precision, bands):
 ADJ_STEPS = 500  # Adam steps of the inverse-design run (plan builds amortised over them)
 
 
+class nvtx_range:
+    """NVTX push/pop range around a timed region (a no-op unless a profiler
+    listens), so that `ncu --nvtx --nvtx-include "<name>/"` selects exactly the
+    launches of that region."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        import torch
+        try:
+            torch.cuda.nvtx.range_push(self.name)
+            self.on = True
+        except Exception:
+            self.on = False
+        return self
+
+    def __exit__(self, *exc):
+        if self.on:
+            import torch
+            torch.cuda.nvtx.range_pop()
+        return False
+
+
 def hbm_peak():
     """Measured HBM copy bandwidth (GB/s) of this GPU pool, else the fallback."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -371,8 +395,9 @@ def adjoint_leg(args, stream):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(nsteps):
-            g, val = step()
+        with nvtx_range("adjoint_timed"):
+            for _ in range(nsteps):
+                g, val = step()
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / nsteps
@@ -695,7 +720,8 @@ def gs_leg(args, stream):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        sols = ggs.run_batch(probs, stream)
+        with nvtx_range("gs_timed"):
+            sols = ggs.run_batch(probs, stream)
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -873,8 +899,9 @@ def main():
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        run_batch(og, ffi, items, ffi.C64, sptr)
+    with nvtx_range("prop_timed"):
+        for _ in range(args.steps):
+            run_batch(og, ffi, items, ffi.C64, sptr)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
