@@ -108,6 +108,12 @@ struct Context {
   int lane_mode = 1;      // lanes of the batch being run
   std::map<std::array<int, 7>, Tuned> tuned;
   uint64_t tunes = 0;
+  // pinned copies of the fused GS loop state (two chunks) and their events,
+  // kept between calls: a pinned allocation and free per call (the free
+  // synchronises the device) cost more than the loop's own host work
+  GsState* gs_pin = nullptr;
+  size_t gs_pin_bytes = 0;
+  cudaEvent_t gs_ev[2] = {nullptr, nullptr};
 };
 
 Context& ctx() {
@@ -1328,29 +1334,28 @@ int gs_fused(Context& c, osgpu_gs_item* items, int n_items, const osgpu_gs_confi
   // (one extra chunk after every item has stopped: its kernels return at
   // once for stopped items).
   constexpr int kChunk = 8;
-  struct Pinned {
-    GsState* p = nullptr;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    ~Pinned() {
-      if (p) cudaFreeHost(p);
-      for (cudaEvent_t e : ev)
-        if (e) cudaEventDestroy(e);
-    }
-  } pin;
-  CK(cudaMallocHost(&pin.p, sizeof(GsState) * 2 * n_items));
-  CK(cudaEventCreateWithFlags(&pin.ev[0], cudaEventDisableTiming));
-  CK(cudaEventCreateWithFlags(&pin.ev[1], cudaEventDisableTiming));
+  const size_t pin_need = sizeof(GsState) * 2 * n_items;
+  if (c.gs_pin_bytes < pin_need) {  // grows only; the previous call's copies have completed
+    if (c.gs_pin) CK(cudaFreeHost(c.gs_pin));
+    c.gs_pin = nullptr;
+    c.gs_pin_bytes = 0;
+    CK(cudaMallocHost(&c.gs_pin, pin_need));
+    c.gs_pin_bytes = pin_need;
+  }
+  for (cudaEvent_t& e : c.gs_ev)
+    if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  GsState* pin = c.gs_pin;
   int pending = -1;
   for (int k = 0; k < max_it; ++k) {
     if (k > 0 && k % kChunk == 0) {
       const int b = (k / kChunk) & 1;
-      CK(cudaMemcpyAsync(pin.p + (size_t)b * n_items, S, sizeof(GsState) * n_items,
+      CK(cudaMemcpyAsync(pin + (size_t)b * n_items, S, sizeof(GsState) * n_items,
                          cudaMemcpyDeviceToHost, st));
-      CK(cudaEventRecord(pin.ev[b], st));
+      CK(cudaEventRecord(c.gs_ev[b], st));
       if (pending >= 0) {
-        CK(cudaEventSynchronize(pin.ev[pending]));
+        CK(cudaEventSynchronize(c.gs_ev[pending]));
         bool all = true;
-        for (int i = 0; i < n_items; ++i) all = all && pin.p[(size_t)pending * n_items + i].stop;
+        for (int i = 0; i < n_items; ++i) all = all && pin[(size_t)pending * n_items + i].stop;
         if (all) break;
       }
       pending = b;
@@ -1576,6 +1581,13 @@ int osgpu_shutdown(void) {
   c.plan_bytes = 0;
   if (c.ee.d) cudaFree(c.ee.d);
   c.ee = Context::EeOrder();
+  if (c.gs_pin) cudaFreeHost(c.gs_pin);
+  c.gs_pin = nullptr;
+  c.gs_pin_bytes = 0;
+  for (cudaEvent_t& e : c.gs_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
   cudaMemPool_t pool;
   CK(cudaDeviceGetDefaultMemPool(&pool, c.device));
   CK(cudaMemPoolTrimTo(pool, 0));  // scratch returned by the stream-ordered frees
