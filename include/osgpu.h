@@ -587,9 +587,10 @@ int osgpu_asm_propagate_noalloc(const void* d_in, void* d_out, const osgpu_grid*
 /* The counterpart of the reference's FftPlanner (src/propagation/fft.rs:41,53,
  * built on every call there): a measured schedule of the f32 register-FFT
  * passes per geometry.  Each pass has interchangeable kernel variants
- * (pass A: bulk, tile4, tile2, g1, g2, g4; pass B: pair, g1, g2, g4; pass C:
- * tma, pipe, tile2, tile4, g1, g2, g4 -- row tiles, persistent TMA/bulk-copy
- * kernels, sub-transform groups per CTA) that compute the same transform.
+ * (pass A: bulk, tstore, tile4, tile2, g1, g2, g4; pass B: pair, g1, g2, g4;
+ * pass C: tma, pipe, tile2, tile4, g1, g2, g4 -- row tiles, persistent
+ * TMA/bulk-copy kernels, TMA tensor stores, sub-transform groups per CTA) that
+ * compute the same transform.
  * osgpu_autotune_asm times a synthetic batch of the geometry (one element
  * plane, `lanes` 1: one item, 2: four items on the device batch's two lanes)
  * under each variant of pass A, then B, then C, starting from the built-in
