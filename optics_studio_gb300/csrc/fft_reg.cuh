@@ -237,8 +237,8 @@ __device__ __forceinline__ void group_sync(int id, int nthreads) {
 
 // One transform of length M by the T = M/16 threads with local index tid.
 // TWREC: the middle stage's twiddles w^q from w^1 and w^4 and a final
-// radix-8 stage's from w^1 (cmul products, fewer shared-memory reads; pass B
-// uses it, where shared-memory wavefronts are the tighter resource).
+// radix-8 stage's from w^1 (cmul products, fewer shared-memory reads; passes
+// B and C use it, where shared-memory wavefronts are the tighter resource).
 // buf: one padded shared buffer of Plan<M>::SMEM float2 owned by this
 // transform (padded index i + i/16 keeps the transposed stores conflict
 // free); tws: the stage-ordered twiddle table of TwLay<M> in shared memory.

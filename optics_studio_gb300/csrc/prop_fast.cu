@@ -957,7 +957,7 @@ __global__ void __launch_bounds__(R * (M / 16), R == 4 ? 1 : 2) k_passC_tile(Pro
       const int j = tid + T * q;
       v[q] = buf[j + (j >> 4)];
     }
-    fft1s<M, true>(v, buf, tws, tid, 1 + g, T);
+    fft1s<M, true, true>(v, buf, tws, tid, 1 + g, T);
     const float2 wb = tb[s * T + tid];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
@@ -1147,7 +1147,9 @@ __global__ void __launch_bounds__(2 * (M / 16), 2) k_passC_pipe(PropArgs a) {
         nt = tile + gridDim.x;
       }
       if (nt < n_tiles) issue(nt, ns);
-      fft1s<M, true>(v, buf, tws, tid, 1 + g, T);
+      // twiddles by products (TWREC): fewer shared-memory loads, so the pass
+      // leaves more of the LSU to the other lane's co-resident pass-B CTAs
+      fft1s<M, true, true>(v, buf, tws, tid, 1 + g, T);
       const float2 wb = tb[s * T + tid];
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
@@ -1235,7 +1237,9 @@ __global__ void __launch_bounds__(2 * (M / 16), 2)
         nt = tile + gridDim.x;
       }
       if (nt < n_tiles && threadIdx.x == 0) issue(nt, ns);
-      fft1s<M, true>(v, buf, tws, tid, 1 + g, T);
+      // twiddles by products (TWREC): fewer shared-memory loads, so the pass
+      // leaves more of the LSU to the other lane's co-resident pass-B CTAs
+      fft1s<M, true, true>(v, buf, tws, tid, 1 + g, T);
       const float2 wb = tb[s * T + tid];
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
