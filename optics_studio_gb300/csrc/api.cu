@@ -2379,14 +2379,19 @@ int tune_geometry(Context& c, const osgpu_grid& g, double z, const osgpu_asm_con
   struct Guard {
     Context& c;
     cudaEvent_t a, b;
+    bool plans_on;
     ~Guard() {
       c.tuning = false;
       c.force_on = false;
+      c.plans_on = plans_on;
       cudaEventDestroy(a);
       cudaEventDestroy(b);
     }
-  } guard{c, e0, e1};
+  } guard{c, e0, e1, c.plans_on};
   c.tuning = true;
+  // the synthetic batch runs the padded passes of the key's geometry (with
+  // kernel-spectrum plans on, its propagations would run another geometry)
+  c.plans_on = false;
   auto measure = [&](const Schedule& s, double* ms) -> int {
     c.force_on = true;
     c.force = s;
