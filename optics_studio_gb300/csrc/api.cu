@@ -1024,8 +1024,17 @@ int run_fraun(Context& c, const osgpu_grid& g, double z, const osgpu_fraunhofer_
   if ((rc = get_tw(c, a.ax.m, is_d, &a.tw_mx))) return rc;
   if ((rc = get_tw(c, a.ay.m, is_d, &a.tw_my))) return rc;
   DBuf ws;
-  CK(ws.alloc((size_t)a.nx * a.ny * es, st));
+  const size_t work_bytes = ((size_t)a.nx * a.ny * es + 255) & ~(size_t)255;
+  const size_t tab_bytes = is_d ? 0 : 2 * ((size_t)a.nx + a.ny) * sizeof(float2);
+  CK(ws.alloc(work_bytes + tab_bytes, st));
   a.work = ws.p;
+  if (!is_d) {  // the f32 engine's per-axis phase tables behind the spectrum
+    float2* t = reinterpret_cast<float2*>(static_cast<char*>(ws.p) + work_bytes);
+    a.tpx = t;
+    a.tqx = t + a.nx;
+    a.tpy = t + 2 * a.nx;
+    a.tqy = t + 2 * a.nx + a.ny;
+  }
   a.in = d_in;
   a.in_c128 = in_c128;
   a.out = d_out;

@@ -10,6 +10,7 @@
 // crop (a circular shift of the input by o followed by a shift of the
 // output by -o leaves a circular convolution unchanged), so the support
 // starts at index 0 here.
+#include <algorithm>
 #include <cstdio>
 #include "prop_kernels.cuh"
 #include "fft_smem.cuh"
@@ -848,19 +849,43 @@ __global__ void k_chirp_vals(int n, double d, double A, double2* chirp) {
   chirp[j] = make_double2(c, s);
 }
 
-__global__ void k_chirp_dft(int n, const double2* __restrict__ chirp, const double2* tw,
-                            double2* out, double pre_re, double pre_im) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+// One block of kChirpThreads per output bin k: thread t sums the terms
+// j = t, t + kChirpThreads, ... with the twiddle index (j k) mod n advanced
+// by a conditional subtraction (no division in the loop), then the block
+// adds the partial sums (FP64 throughout).
+constexpr int kChirpThreads = 128;
+
+__global__ void __launch_bounds__(kChirpThreads)
+    k_chirp_dft(int n, const double2* __restrict__ chirp, const double2* __restrict__ tw,
+                double2* out, double pre_re, double pre_im) {
+  const int k = blockIdx.x, t = threadIdx.x;
+  int idx = (int)(((long long)t * k) % n);
+  const int step = (int)(((long long)kChirpThreads * k) % n);
   double sr = 0.0, si = 0.0;
-  for (int j = 0; j < n; ++j) {
+  for (int j = t; j < n; j += kChirpThreads) {
     const double2 cs = __ldg(chirp + j);
-    const double c = cs.x, s = cs.y;
-    const double2 w = tw[(int)(((long long)j * k) % n)];
-    sr += c * w.x - s * w.y;
-    si += c * w.y + s * w.x;
+    const double2 w = __ldg(tw + idx);
+    sr += cs.x * w.x - cs.y * w.y;
+    si += cs.x * w.y + cs.y * w.x;
+    idx += step;
+    if (idx >= n) idx -= n;
   }
-  out[k] = make_double2(sr * pre_re - si * pre_im, sr * pre_im + si * pre_re);
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, o);
+    si += __shfl_down_sync(0xffffffffu, si, o);
+  }
+  __shared__ double2 part[kChirpThreads / 32];
+  if ((t & 31) == 0) part[t >> 5] = make_double2(sr, si);
+  __syncthreads();
+  if (t == 0) {
+    sr = part[0].x;
+    si = part[0].y;
+    for (int w = 1; w < kChirpThreads / 32; ++w) {
+      sr += part[w].x;
+      si += part[w].y;
+    }
+    out[k] = make_double2(sr * pre_re - si * pre_im, sr * pre_im + si * pre_re);
+  }
 }
 
 template <typename T>
@@ -902,9 +927,9 @@ cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp
   COUNT_LAUNCH();
   k_chirp_vals<<<(Py + 127) / 128, 128, 0, st>>>(Py, a.dy, A, cy);
   COUNT_LAUNCH();
-  k_chirp_dft<<<(Px + 127) / 128, 128, 0, st>>>(Px, cx, twx, ox, pr, pi_);
+  k_chirp_dft<<<Px, kChirpThreads, 0, st>>>(Px, cx, twx, ox, pr, pi_);
   COUNT_LAUNCH();
-  k_chirp_dft<<<(Py + 127) / 128, 128, 0, st>>>(Py, cy, twy, oy, 1.0, 0.0);
+  k_chirp_dft<<<Py, kChirpThreads, 0, st>>>(Py, cy, twy, oy, 1.0, 0.0);
   COUNT_LAUNCH();
   k_cast_c128<T><<<(Px + 255) / 256, 256, 0, st>>>(ox, hx, Px);
   COUNT_LAUNCH();
@@ -1157,6 +1182,60 @@ __device__ __forceinline__ void fraun_post(const FraunArgs& a, int ix, int iy, i
   fi = ti * w;
 }
 
+// The f32 engine's per-axis tables of the pre and post factors (FP64, the
+// reference's formulas, rounded once to f32):
+//   tpx[ix] = e^{i px(ix)},  tpy[iy] = e^{i py(iy)} e^{i ry(iy)}          (fraun_pre)
+//   tqx[mx] = quad (dx dy) e^{i pi dxp(ix)^2 / (lam z)} e^{i px'(mx)},
+//   tqy[my] = e^{i pi dyp(iy)^2 / (lam z)} e^{i py'(my)}                 (fraun_post)
+// with (ix, iy) the output sample of the bin (mx, my) (the mirror map for
+// z < 0, its own inverse): the chirp e^{i pi (dxp^2 + dyp^2) / (lam z)}
+// factors into its two axes.
+__global__ void k_fraun_tables(FraunArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double cx = a.cxc, cy = a.cyc;
+  const double sgn = a.z > 0.0 ? 1.0 : -1.0;
+  const double lz = __dmul_rn(a.lam, a.z);
+  if (i < a.nx) {
+    const double xi = __dmul_rn(__dsub_rn((double)i, cx), a.dx);
+    const double px = __dmul_rn(2.0 * M_PI, __dadd_rn(__ddiv_rn(__dmul_rn(cx, (double)i), (double)a.nx),
+                                                      __dmul_rn(a.f_s, xi)));
+    double s, c;
+    sincos(px, &s, &c);
+    a.tpx[i] = make_float2((float)c, (float)s);
+    const int ix = (int)rint(sgn * ((double)i - cx) + cx);  // output sample of bin mx = i
+    const double dxp = __dsub_rn(__dmul_rn(__dsub_rn((double)ix, cx), a.dxo), a.xs);
+    const double ch = __ddiv_rn(__dmul_rn(M_PI, __dmul_rn(dxp, dxp)), lz);
+    const double pp = __ddiv_rn(__dmul_rn(__dmul_rn(2.0 * M_PI, cx), __dsub_rn((double)i, cx)), (double)a.nx);
+    double s1, c1, s2, c2;
+    sincos(ch, &s1, &c1);
+    sincos(pp, &s2, &c2);
+    const double qr = a.quad_re * c1 - a.quad_im * s1, qi = a.quad_re * s1 + a.quad_im * c1;
+    const double w = __dmul_rn(a.dx, a.dy);
+    a.tqx[i] = make_float2((float)((qr * c2 - qi * s2) * w), (float)((qr * s2 + qi * c2) * w));
+  }
+  if (i < a.ny) {
+    const double eta = __dmul_rn(__dsub_rn((double)i, cy), a.dy);
+    const double py = __ddiv_rn(__dmul_rn(__dmul_rn(2.0 * M_PI, cy), (double)i), (double)a.ny);
+    const double ry = __dmul_rn(__dmul_rn(2.0 * M_PI, a.g_s), eta);
+    double s1, c1, s2, c2;
+    sincos(py, &s1, &c1);
+    sincos(ry, &s2, &c2);
+    a.tpy[i] = make_float2((float)(c1 * c2 - s1 * s2), (float)(c1 * s2 + s1 * c2));
+    const int iy = (int)rint(sgn * ((double)i - cy) + cy);
+    const double dyp = __dsub_rn(__dmul_rn(__dsub_rn((double)iy, cy), a.dyo), a.ys);
+    const double ch = __ddiv_rn(__dmul_rn(M_PI, __dmul_rn(dyp, dyp)), lz);
+    const double pp = __ddiv_rn(__dmul_rn(__dmul_rn(2.0 * M_PI, cy), __dsub_rn((double)i, cy)), (double)a.ny);
+    double s3, c3, s4, c4;
+    sincos(ch, &s3, &c3);
+    sincos(pp, &s4, &c4);
+    a.tqy[i] = make_float2((float)(c3 * c4 - s3 * s4), (float)(c3 * s4 + s3 * c4));
+  }
+}
+
+__device__ __forceinline__ float2 fcmul(float2 p, float2 q) {
+  return make_float2(p.x * q.x - p.y * q.y, p.x * q.y + p.y * q.x);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_fraunA(FraunArgs a, int rows) {
   using V = cx<T>;
@@ -1180,14 +1259,27 @@ __global__ void __launch_bounds__(kThreads) k_fraunA(FraunArgs a, int rows) {
       if (a.status && nonfinite2(re, im)) atomicOr(a.status, 1);
       if (!a.adjoint) {
         if (a.els.count) apply_elements_exact(a.els, j, iy, nx, ny, a.dx, a.dy, re, im);
-        fraun_pre<T>(a, j, iy, re, im);
+        if constexpr (sizeof(T) == 4) {
+          const float2 f = fcmul(a.tpy[iy], a.tpx[j]);
+          const float xr = (float)re, xi = (float)im;
+          re = xr * f.x - xi * f.y;
+          im = xr * f.y + xi * f.x;
+        } else {
+          fraun_pre<T>(a, j, iy, re, im);
+        }
       } else {
         // adjoint: far-field sample (ix = j, iy) came from DFT bin (mx, my);
         // multiply conj(factor) and place it at its bin index mx.
         const int mx = (int)rint(sgn * ((double)j - a.cxc) + a.cxc);
         const int my = (int)rint(sgn * ((double)iy - a.cyc) + a.cyc);
         double fr, fi;
-        fraun_post(a, j, iy, mx, my, fr, fi);
+        if constexpr (sizeof(T) == 4) {
+          const float2 f = fcmul(a.tqx[mx], a.tqy[my]);
+          fr = f.x;
+          fi = f.y;
+        } else {
+          fraun_post(a, j, iy, mx, my, fr, fi);
+        }
         const double r2 = re * fr + im * fi, i2 = im * fr - re * fi;  // * conj(f)
         re = r2;
         im = i2;
@@ -1236,7 +1328,13 @@ __global__ void __launch_bounds__(kThreads) k_fraunB(FraunArgs a) {
       const int ix = (int)rint(sgn * ((double)kx - a.cxc) + a.cxc);
       const int iy = (int)rint(sgn * ((double)p - a.cyc) + a.cyc);
       double fr, fi;
-      fraun_post(a, ix, iy, kx, p, fr, fi);
+      if constexpr (sizeof(T) == 4) {
+        const float2 f = fcmul(a.tqx[kx], a.tqy[p]);
+        fr = f.x;
+        fi = f.y;
+      } else {
+        fraun_post(a, ix, iy, kx, p, fr, fi);
+      }
       const double r2 = fr * re - fi * im, i2 = fr * im + fi * re;
       re = r2;
       im = i2;
@@ -1244,7 +1342,14 @@ __global__ void __launch_bounds__(kThreads) k_fraunB(FraunArgs a) {
       oy = iy;
     } else {
       // spatial sample (ix = kx, iy = p): multiply conj(pre)
-      fraun_pre<T>(a, kx, p, re, im);
+      if constexpr (sizeof(T) == 4) {
+        const float2 f = fcmul(a.tpy[p], a.tpx[kx]);
+        const float xr = (float)re, xi = (float)im;
+        re = xr * f.x + xi * f.y;
+        im = xi * f.x - xr * f.y;
+      } else {
+        fraun_pre<T>(a, kx, p, re, im);
+      }
       ox = kx;
       oy = p;
     }
@@ -1260,6 +1365,14 @@ template <typename T>
 cudaError_t launch_fraunhofer(const FraunArgs& a, cudaStream_t st) {
   const int is_d = sizeof(T) == 8;
   const size_t es = is_d ? 16 : 8;
+  if (!is_d) {
+    if (!a.tpx || !a.tpy || !a.tqx || !a.tqy) return cudaErrorInvalidValue;
+    const int nt = std::max(a.nx, a.ny);
+    COUNT_LAUNCH();
+    k_fraun_tables<<<(nt + 127) / 128, 128, 0, st>>>(a);
+    cudaError_t e0 = cudaGetLastError();
+    if (e0 != cudaSuccess) return e0;
+  }
   int rows = 16;
   while (rows > 1 && 2 * ((size_t)a.ax.m + 1) * rows * es > kSmemBudgetRows) rows /= 2;
   size_t smem = 2 * ((size_t)a.ax.m + 1) * rows * es;

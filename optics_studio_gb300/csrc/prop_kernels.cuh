@@ -109,6 +109,10 @@ struct FraunArgs {
   double quad_re, quad_im;  // e^{ikz}/(i lam z)
   int adjoint;         // 1: exact adjoint of the forward operator
   int* status;
+  // f32 engine: the separable phase factors as per-axis tables (FP64 values
+  // rounded to f32, launch_fraunhofer fills them): pre = tpx[ix] tpy[iy],
+  // post = tqx[mx] tqy[my] for the source bin (mx, my); null for FP64
+  float2 *tpx, *tpy, *tqx, *tqy;
 };
 
 template <typename T> cudaError_t launch_asm_prep(const PropArgs& a, void* tables, cudaStream_t st);
