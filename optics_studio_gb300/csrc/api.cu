@@ -851,6 +851,10 @@ int run_prop(Context& c, const PropJob& j0, cudaStream_t st) {
       set_err("kernel-spectrum build of %zux%zu exceeds the shared-memory plan", Px, Py);
       return OSGPU_E_UNSUPPORTED;
     }
+    if (!is_d) {  // the f32 build transforms with the f32 passes and tables
+      if ((rc = get_tw(c, (int)Px, 0, &b.tw_mx))) return rc;
+      if ((rc = get_tw(c, (int)Py, 0, &b.tw_my))) return rc;
+    }
     ProfScope ps(c, st, PC_KSPEC, 0.0);
     CK(launch_rs_kspec<T>(b, base + o_ks, base + o_tmp, st));
     a.kspec = base + o_ks;

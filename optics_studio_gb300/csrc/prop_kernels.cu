@@ -958,11 +958,64 @@ __global__ void k_rs_kernel(int Px, int Py, double dx, double dy, double lam, do
   h[idx] = make_double2((pr * c - pi_ * s) * w, (pr * s + pi_ * c) * w);
 }
 
+// f32 engine: the same kernel samples with r and the phase s k r in FP64,
+// the phase reduced to [-pi, pi] by a two-constant Cody-Waite step
+// (2 pi = hi + lo, each product by FMA), and the amplitude, obliquity and
+// e^{i phase} in f32.
+__global__ void k_rs_kernel_f32(int Px, int Py, double dx, double dy, double sk, double z,
+                                float2* h) {
+  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (idx >= (size_t)Px * Py) return;
+  const int ix = (int)(idx % Px), iy = (int)(idx / Px);
+  const double x = dft_coord(ix, Px, dx), y = dft_coord(iy, Py, dy);
+  const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+  const double ph = __dmul_rn(sk, r);
+  const double q = rint(__dmul_rn(ph, 0.15915494309189533577));
+  const double red = fma(-q, 2.4492935982947064e-16, fma(-q, 6.283185307179586232, ph));
+  float s, c;
+  sincosf((float)red, &s, &c);
+  const float rf = (float)r;
+  const float amp = (float)fabs(z) / (6.2831853071795865f * rf * rf);
+  const float pr = amp / rf, pi_ = -amp * (float)sk;
+  const float w = (float)(dx * dy);
+  h[idx] = make_float2((pr * c - pi_ * s) * w, (pr * s + pi_ * c) * w);
+}
+
 template <typename T>
 cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStream_t st) {
-  // tmp64 holds: h (Px*Py double2) then the column-major work (Px*Py double2)
-  // then twiddles (Px + Py double2); `a` carries full-support axis plans.
+  // FP64: tmp64 holds h (Px*Py double2), then the column-major work (Px*Py
+  // double2), then twiddles (Px + Py double2); `a` carries full-support axis
+  // plans.  f32: h and the work as float2 in the same space, and the f32
+  // twiddle tables of Px and Py come with `a` (tw_mx, tw_my).
   const int Px = a.ax.P, Py = a.ay.P;
+  const size_t n = (size_t)Px * Py;
+  if (sizeof(T) == 4) {
+    if (!a.tw_mx || !a.tw_my) return cudaErrorInvalidValue;
+    float2* hf = reinterpret_cast<float2*>(tmp64);
+    const double sg = a.z > 0.0 ? 1.0 : -1.0;
+    COUNT_LAUNCH();
+    k_rs_kernel_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        Px, Py, a.dx, a.dy, sg * (2.0 * M_PI / a.lam), a.z, hf);
+    PropArgs b = a;
+    b.nx = Px;
+    b.ny = Py;
+    b.in = hf;
+    b.in_c128 = 0;
+    b.work = hf + n;
+    b.tw_Px = a.tw_mx;
+    b.tw_Py = a.tw_my;
+    b.els.count = 0;
+    b.trans = nullptr;
+    b.seed = nullptr;
+    b.adj = 0;
+    b.out_intensity = nullptr;
+    b.out_intensity64 = nullptr;
+    b.engine = ENG_IDENTITY;
+    b.sched = Schedule{0, 0, 0};
+    cudaError_t e = launch_passA<float>(b, st);
+    if (e != cudaSuccess) return e;
+    return launch_passB_impl<float>(b, 1, kspec, st);
+  }
   double2* h = reinterpret_cast<double2*>(tmp64);
   double2* work = h + (size_t)Px * Py;
   double2* twx = work + (size_t)Px * Py;
@@ -971,7 +1024,6 @@ cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStr
   if (e != cudaSuccess) return e;
   e = launch_twiddles(twy, Py, 1, st);
   if (e != cudaSuccess) return e;
-  const size_t n = (size_t)Px * Py;
   COUNT_LAUNCH();
   k_rs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Px, Py, a.dx, a.dy, a.lam, a.z, h);
   PropArgs b = a;
