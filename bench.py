@@ -603,8 +603,9 @@ def c2_leg(args):
         for prec in ("f64", "f32"):
             fn(band, prec)  # warm-up: twiddle tables, kernel attributes
             t0 = time.perf_counter()
-            for _ in range(reps):
-                r = fn(band, prec)
+            with nvtx_range(f"c2_{prec}"):
+                for _ in range(reps):
+                    r = fn(band, prec)
             dt = (time.perf_counter() - t0) / reps
             results[(name, prec)] = r.samples
             # device time of the kernels of one call (events on the launching stream)

@@ -939,11 +939,12 @@ cudaError_t launch_fresnel_ksep(const PropArgs& a, void* hx, void* hy, void* tmp
 
 // RS-I kernel samples in DFT order, dx dy folded in (reference
 // rayleigh_sommerfeld.rs:228-235, 277-301).
+// (2-D grid: x over a row, blockIdx.y the row.)
 __global__ void k_rs_kernel(int Px, int Py, double dx, double dy, double lam, double z,
                             double2* h) {
-  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (idx >= (size_t)Px * Py) return;
-  const int ix = (int)(idx % Px), iy = (int)(idx / Px);
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y;
+  if (ix >= Px) return;
+  const size_t idx = (size_t)iy * Px + ix;
   const double x = dft_coord(ix, Px, dx), y = dft_coord(iy, Py, dy);
   const double k = __ddiv_rn(2.0 * M_PI, lam);
   const double sg = z > 0.0 ? 1.0 : -1.0;
@@ -961,14 +962,21 @@ __global__ void k_rs_kernel(int Px, int Py, double dx, double dy, double lam, do
 // f32 engine: the same kernel samples with r and the phase s k r in FP64,
 // the phase reduced to [-pi, pi] by a two-constant Cody-Waite step
 // (2 pi = hi + lo, each product by FMA), and the amplitude, obliquity and
-// e^{i phase} in f32.
+// e^{i phase} in f32.  r = sqrt(s) from the f32 square root r0 of s and one
+// Newton step in FP64, r = r0 + (s - r0^2) / (2 r0): r0^2 is exact in FP64
+// (24-bit operands) and the step takes the relative error from 2^-24 to
+// about 2^-49, so the phase k r (~1e5 rad) keeps ~1e-9 rad with a few FP64
+// operations instead of an FP64 square root.
 __global__ void k_rs_kernel_f32(int Px, int Py, double dx, double dy, double sk, double z,
                                 float2* h) {
-  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (idx >= (size_t)Px * Py) return;
-  const int ix = (int)(idx % Px), iy = (int)(idx / Px);
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y;
+  if (ix >= Px) return;
+  const size_t idx = (size_t)iy * Px + ix;
   const double x = dft_coord(ix, Px, dx), y = dft_coord(iy, Py, dy);
-  const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+  const double sq = fma(x, x, fma(y, y, z * z));
+  const float r0 = sqrtf((float)sq);
+  const double e = fma(-(double)r0, (double)r0, sq);
+  const double r = fma(e, (double)(0.5f / r0), (double)r0);
   const double ph = __dmul_rn(sk, r);
   const double q = rint(__dmul_rn(ph, 0.15915494309189533577));
   const double red = fma(-q, 2.4492935982947064e-16, fma(-q, 6.283185307179586232, ph));
@@ -994,7 +1002,7 @@ cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStr
     float2* hf = reinterpret_cast<float2*>(tmp64);
     const double sg = a.z > 0.0 ? 1.0 : -1.0;
     COUNT_LAUNCH();
-    k_rs_kernel_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+    k_rs_kernel_f32<<<dim3((Px + 255) / 256, Py), 256, 0, st>>>(
         Px, Py, a.dx, a.dy, sg * (2.0 * M_PI / a.lam), a.z, hf);
     PropArgs b = a;
     b.nx = Px;
@@ -1025,7 +1033,7 @@ cudaError_t launch_rs_kspec(const PropArgs& a, void* kspec, void* tmp64, cudaStr
   e = launch_twiddles(twy, Py, 1, st);
   if (e != cudaSuccess) return e;
   COUNT_LAUNCH();
-  k_rs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Px, Py, a.dx, a.dy, a.lam, a.z, h);
+  k_rs_kernel<<<dim3((Px + 255) / 256, Py), 256, 0, st>>>(Px, Py, a.dx, a.dy, a.lam, a.z, h);
   PropArgs b = a;
   b.nx = Px;
   b.ny = Py;
