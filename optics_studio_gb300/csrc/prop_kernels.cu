@@ -529,7 +529,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_passA(PropArgs a, int rows) {
   using V = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int m = a.ax.m, r = a.ax.r, P = a.ax.P, nx = a.nx, ny = a.ny;
+  const int m = a.ax.m, r = a.ax.r, nx = a.nx, ny = a.ny;
   const int ld = m + 1;
   V* bufA = reinterpret_cast<V*>(smem_raw);
   V* bufB = bufA + (size_t)rows * ld;
@@ -765,7 +765,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_passC(PropArgs a, int rows) {
   using V = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int m = a.ax.m, r = a.ax.r, P = a.ax.P, nx = a.nx, ny = a.ny;
+  const int m = a.ax.m, r = a.ax.r, nx = a.nx, ny = a.ny;
   const int ld = m + 1;
   V* bufA = reinterpret_cast<V*>(smem_raw);
   V* bufB = bufA + (size_t)rows * ld;
